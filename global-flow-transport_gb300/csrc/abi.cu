@@ -1,0 +1,652 @@
+// extern "C" entry points of libgft.so (declared in include/gft.h): argument
+// checks with the reference ops' error classes, camera set-up and dispatch to
+// the launchers.  No entry point allocates device memory or synchronises.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gft.h"
+#include "gft_internal.h"
+
+namespace gft {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+// column-major 16 floats -> row-major double 4x4 (the column-vector matrix)
+static void mat_from_flat(const float* m16, double a[4][4]) {
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) a[r][c] = (double)m16[c * 4 + r];
+}
+static void matmul4(const double a[4][4], const double b[4][4], double o[4][4]) {
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += a[r][k] * b[k][c];
+            o[r][c] = s;
+        }
+}
+// Gauss-Jordan with partial pivoting; a singular matrix yields non-finite entries.
+static void inverse4(const double a_in[4][4], double inv[4][4]) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? a_in[r][c] : (c - 4 == r ? 1.0 : 0.0);
+    for (int col = 0; col < 4; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (piv != col)
+            for (int c = 0; c < 8; ++c) std::swap(a[piv][c], a[col][c]);
+        const double d = a[col][col];
+        for (int c = 0; c < 8; ++c) a[col][c] /= d;
+        for (int r = 0; r < 4; ++r) {
+            if (r == col) continue;
+            const double f = a[r][col];
+            for (int c = 0; c < 8; ++c) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[r][c] = a[r][c + 4];
+}
+static Mat4 to_mat4(const double a[4][4]) {
+    Mat4 m;
+    m.r0 = make_float4((float)a[0][0], (float)a[0][1], (float)a[0][2], (float)a[0][3]);
+    m.r1 = make_float4((float)a[1][0], (float)a[1][1], (float)a[1][2], (float)a[1][3]);
+    m.r2 = make_float4((float)a[2][0], (float)a[2][1], (float)a[2][2], (float)a[2][3]);
+    m.r3 = make_float4((float)a[3][0], (float)a[3][1], (float)a[3][2], (float)a[3][3]);
+    return m;
+}
+
+static CamX make_cam(const float* M, const float* V, const float* P, const float* F) {
+    double m[4][4], v[4][4], p[4][4], mv[4][4], mvi[4][4], pi[4][4];
+    mat_from_flat(M, m);
+    mat_from_flat(V, v);
+    mat_from_flat(P, p);
+    matmul4(v, m, mv);
+    inverse4(mv, mvi);
+    inverse4(p, pi);
+    CamX c;
+    c.mv = to_mat4(mv);
+    c.mv_inv = to_mat4(mvi);
+    c.p = to_mat4(p);
+    c.p_inv = to_mat4(pi);
+    c.near_ = F[0];
+    c.far_ = F[1];
+    c.p22 = (float)p[2][2];
+    c.p23 = (float)p[2][3];
+    return c;
+}
+
+std::vector<Pair> make_pairs(const float* M, int num_m, const float* V, const float* P, const float* F,
+                             int num_cameras, int batch, bool separate) {
+    static const float eye[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    std::vector<Pair> out;
+    const int nv = separate ? num_cameras : 1;
+    for (int b = 0; b < batch; ++b) {
+        const float* mb = (M == nullptr) ? eye : M + 16 * (num_m == 1 ? 0 : b);
+        for (int vi = 0; vi < nv; ++vi) {
+            const int c = separate ? vi : b;
+            Pair p;
+            p.cam = make_cam(mb, V + 16 * c, P + 16 * c, F + 6 * c);
+            p.in_batch = b;
+            p.out_slot = b * nv + vi;
+            p.camera = c;
+            out.push_back(p);
+        }
+    }
+    return out;
+}
+
+std::vector<PairTable> make_tables(const std::vector<Pair>& pairs) {
+    std::vector<PairTable> out;
+    for (size_t i = 0; i < pairs.size(); i += MAX_PAIRS) {
+        PairTable t;
+        std::memset(&t, 0, sizeof(t));
+        t.pair_base = (int)i;
+        t.n = (int)std::min<size_t>(MAX_PAIRS, pairs.size() - i);
+        for (int k = 0; k < t.n; ++k) {
+            t.cam[k] = pairs[i + k].cam;
+            t.in_batch[k] = pairs[i + k].in_batch;
+            t.out_slot[k] = pairs[i + k].out_slot;
+        }
+        out.push_back(t);
+    }
+    return out;
+}
+
+}  // namespace gft
+
+using namespace gft;
+
+namespace {
+
+gft_status fail(gft_status s, const std::string& msg) {
+    set_error(msg);
+    return s;
+}
+
+bool grid_shape_ok(const int64_t* s, std::string& why) {
+    if (s == nullptr) {
+        why = "shape pointer is NULL";
+        return false;
+    }
+    for (int i = 0; i < 5; ++i)
+        if (s[i] <= 0) {
+            why = "Invalid input shape (NDHWC): all dimensions must be positive";
+            return false;
+        }
+    if (s[1] > INT32_MAX || s[2] > INT32_MAX || s[3] > INT32_MAX) {
+        why = "grid dimension too large";
+        return false;
+    }
+    return true;
+}
+
+bool channels_ok(int64_t c) { return c == 1 || c == 2 || c == 4; }
+
+Dims dims_of(const int64_t* s) { return Dims{(int)s[3], (int)s[2], (int)s[1]}; }
+
+gft_status check_cameras(const float* M, int num_m, int64_t batch, const float* V, const float* P, const float* F,
+                         int num_cameras, int separate) {
+    if (V == nullptr || P == nullptr || F == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "camera arrays must not be NULL");
+    if (num_cameras <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "camera batch size mismatch");
+    if (M == nullptr || num_m != batch) return fail(GFT_ERR_INVALID_ARGUMENT, "model matrix batch size mismatch");
+    if (!separate && num_cameras != batch)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "camera batch must match data batch when not using global sampling.");
+    return GFT_OK;
+}
+
+bool enum_in(int v, int lo, int hi) { return v >= lo && v <= hi; }
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" {
+
+const char* gft_last_error(void) { return g_last_error.c_str(); }
+
+const char* gft_version(void) { return "gft-gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- raymarch
+gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                       const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                       const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                       const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
+                                       int32_t blending_mode, int32_t separate_camera_batch, float* output,
+                                       void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
+    if (!enum_in(interpolation, 0, 3)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid filter mode");
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
+    if (!enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid input dtype");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
+                                  separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (input == nullptr || output == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    RaymarchArgs a;
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.D = output_shape[0];
+    a.H = output_shape[1];
+    a.W = output_shape[2];
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.blend = blending_mode;
+    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                                  separate_camera_batch != 0);
+    a.n_slots = (int)pairs.size();
+    if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_raymarch_grid_transform_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
+                                                       int32_t separate_camera_batch, int32_t grad_mode) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why) || grad_mode == GFT_GRAD_EXACT) return 0;
+    const size_t nvox = (size_t)input_shape[1] * input_shape[2] * input_shape[3];
+    const size_t pairs = (size_t)input_shape[0] * (separate_camera_batch ? (size_t)std::max(num_cameras, 1) : 1);
+    return align256(sizeof(float) * nvox * input_shape[4] * pairs) + align256(sizeof(float) * nvox * pairs);
+}
+
+gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                            const float* output, const float* output_grad, const float* matrix_m,
+                                            int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                            const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+                                            int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                            int32_t separate_camera_batch, int32_t grad_mode, float* input_grad,
+                                            void* workspace, size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
+    if (interpolation != GFT_FILTER_LINEAR)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "gradient supports LINEAR interpolation only");
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
+    if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
+                                  separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (!input || !output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras,
+                                                                        separate_camera_batch, grad_mode);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    RaymarchArgs a;
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.D = output_shape[0];
+    a.H = output_shape[1];
+    a.W = output_shape[2];
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.blend = blending_mode;
+    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                                  separate_camera_batch != 0);
+    a.n_slots = (int)pairs.size();
+    float* buf = nullptr;
+    float* cnt = nullptr;
+    if (need > 0) {
+        const size_t nvox = (size_t)voxels(a.din);
+        buf = reinterpret_cast<float*>(workspace);
+        cnt = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) +
+                                       align256(sizeof(float) * nvox * a.C * pairs.size()));
+    }
+    if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, input_grad, buf, cnt,
+                             as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+// ---------------------------------------------------------------- resample
+static size_t mip_ws_bytes(const int64_t* s, int mip, int num) {
+    if (mip == GFT_MIP_NONE) return 0;
+    const int L = usable_mip_levels(dims_of(s), num);
+    return sizeof(float) * mip_workspace_floats(dims_of(s), L, (int)s[4]) * (size_t)s[0];
+}
+
+size_t gft_sample_grid_transform_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return 0;
+    return mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+}
+
+static bool build_batch_mips(const void* input, int dtype, const int64_t* s, int mip, int num, void* ws,
+                             std::vector<MipSet>& sets, cudaStream_t st) {
+    const int N = (int)s[0], C = (int)s[4];
+    const Dims d = dims_of(s);
+    const int L = (mip == GFT_MIP_NONE) ? 0 : usable_mip_levels(d, num);
+    const size_t per = mip_workspace_floats(d, L, C);
+    sets.resize(N);
+    const size_t esz = dtype == GFT_DTYPE_BF16 ? 2 : 4;
+    for (int b = 0; b < N; ++b) {
+        const void* base = reinterpret_cast<const char*>(input) + (size_t)b * voxels(d) * C * esz;
+        if (!launch_build_mips(base, dtype, C, d, L, reinterpret_cast<float*>(ws) + per * b, st, &sets[b]))
+            return false;
+    }
+    return true;
+}
+
+gft_status gft_sample_grid_transform(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                     const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                     const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                     const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
+                                     int32_t mipmapping, int32_t num_mipmaps, float mip_bias,
+                                     int32_t coordinate_mode, float cell_center_offset,
+                                     int32_t separate_camera_batch, float* output, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
+    if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(mipmapping, 0, 2) ||
+        !enum_in(input_dtype, 0, 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (!(coordinate_mode == 0 || coordinate_mode == 1 || coordinate_mode == 3 || coordinate_mode == 4))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid coordinate_mode");
+    if (num_mipmaps <= 0 && mipmapping != GFT_MIP_NONE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "when using mipmaps num_mipmaps must be larger than 0.");
+    if (cell_center_offset != 0.5f)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid cell center offset for given coordinate mode.");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
+                                  separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "mip workspace too small");
+    std::vector<MipSet> sets;
+    if (!build_batch_mips(input, input_dtype, input_shape, mipmapping, num_mipmaps, workspace, sets, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    SampleArgs a;
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.dout = Dims{output_shape[2], output_shape[1], output_shape[0]};
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.mip_mode = mipmapping;
+    a.levels = sets.empty() ? 0 : sets[0].levels;
+    a.mip_bias = mip_bias;
+    a.cco = cell_center_offset;
+    a.coord_mode = coordinate_mode;
+    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                                  separate_camera_batch != 0);
+    if (!launch_sample_transform_fwd(a, pairs, sets.data(), output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_sample_grid_transform_grad_workspace_size(const int64_t input_shape[5]) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return 0;
+    return align256(sizeof(unsigned int) * (size_t)input_shape[1] * input_shape[2] * input_shape[3]);
+}
+
+gft_status gft_sample_grid_transform_grad(const int64_t input_shape[5], const float* output_grad,
+                                          const int64_t output_grad_shape[6], const float* matrix_m, int32_t num_m,
+                                          const float* matrix_v, const float* matrix_p, const float* frustum,
+                                          int32_t num_cameras, int32_t interpolation, int32_t boundary,
+                                          int32_t coordinate_mode, float cell_center_offset,
+                                          int32_t separate_camera_batch, int32_t grad_mode, float* input_grad,
+                                          void* workspace, size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (output_grad_shape == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "output_grad shape is NULL");
+    for (int i = 0; i < 6; ++i)
+        if (output_grad_shape[i] <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid output_grads shape (NVDHWC)");
+    if (output_grad_shape[0] != input_shape[0])
+        return fail(GFT_ERR_INVALID_ARGUMENT, "output_grads batch size does not match input batch size.");
+    if (output_grad_shape[5] != input_shape[4]) return fail(GFT_ERR_INVALID_ARGUMENT, "channel mismatch");
+    if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(grad_mode, 0, 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (!(coordinate_mode == 0 || coordinate_mode == 1 || coordinate_mode == 3 || coordinate_mode == 4))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid coordinate_mode");
+    if (cell_center_offset != 0.5f)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid cell center offset for given coordinate mode.");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
+                                  separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (output_grad_shape[1] != (separate_camera_batch ? num_cameras : 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "output_grads views size does not match cameras.");
+    if (!output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_sample_grid_transform_grad_workspace_size(input_shape);
+    if (grad_mode == GFT_GRAD_REFERENCE && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "sample count workspace too small");
+    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, (int)input_shape[0],
+                                  separate_camera_batch != 0);
+    const Dims dout{(int)output_grad_shape[4], (int)output_grad_shape[3], (int)output_grad_shape[2]};
+    if (!launch_sample_transform_bwd((int)input_shape[0], (int)input_shape[4], dims_of(input_shape), dout, boundary,
+                                     coordinate_mode, cell_center_offset, pairs, output_grad,
+                                     grad_mode == GFT_GRAD_EXACT, input_grad,
+                                     reinterpret_cast<unsigned int*>(workspace), as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_sample_grid_lut_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return 0;
+    return mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+}
+
+static gft_status check_lut(const int64_t* input_shape, const int64_t* lookup_shape, int separate) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (!grid_shape_ok(lookup_shape, why) || lookup_shape[4] != 4)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid lut shape (NDHWC) with C=4");
+    if (!separate && lookup_shape[0] != input_shape[0])
+        return fail(GFT_ERR_INVALID_ARGUMENT, "camera batch must match data batch when not using global sampling.");
+    return GFT_OK;
+}
+
+gft_status gft_sample_grid_lut(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                               const float* lookup, const int64_t lookup_shape[5], int32_t interpolation,
+                               int32_t boundary, int32_t mipmapping, int32_t num_mipmaps, float mip_bias,
+                               float cell_center_offset, int32_t separate_camera_batch, int32_t relative_coords,
+                               int32_t normalized_coords, float* output, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+    gft_status st = check_lut(input_shape, lookup_shape, separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(mipmapping, 0, 2) ||
+        !enum_in(input_dtype, 0, 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (num_mipmaps <= 0 && mipmapping != GFT_MIP_NONE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "when using mipmaps num_mipmaps must be larger than 0.");
+    if (normalized_coords && cell_center_offset != 0.5f)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid cell center offset must be 0.5 when using normalized coordinates.");
+    if (!input || !lookup || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "mip workspace too small");
+    std::vector<MipSet> sets;
+    if (!build_batch_mips(input, input_dtype, input_shape, mipmapping, num_mipmaps, workspace, sets, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    LutArgs a;
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.dout = dims_of(lookup_shape);
+    a.n_lut = (int)lookup_shape[0];
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.mip_mode = mipmapping;
+    a.levels = sets.empty() ? 0 : sets[0].levels;
+    a.mip_bias = mip_bias;
+    a.cco = cell_center_offset;
+    a.separate = separate_camera_batch;
+    a.relative = relative_coords;
+    a.normalized = normalized_coords;
+    if (!launch_lut_fwd(a, lookup, sets.data(), output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_sample_grid_lut_grad_workspace_size(const int64_t input_shape[5]) {
+    return gft_sample_grid_transform_grad_workspace_size(input_shape);
+}
+
+gft_status gft_sample_grid_lut_grad(const float* input, const int64_t input_shape[5], const float* output_grad,
+                                    const float* lookup, const int64_t lookup_shape[5], int32_t interpolation,
+                                    int32_t boundary, float cell_center_offset, int32_t separate_camera_batch,
+                                    int32_t relative_coords, int32_t normalized_coords, int32_t grad_mode,
+                                    float* input_grad, float* lookup_grad, void* workspace, size_t workspace_bytes,
+                                    void* stream) {
+    gft_status st = check_lut(input_shape, lookup_shape, separate_camera_batch);
+    if (st != GFT_OK) return st;
+    if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(grad_mode, 0, 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (normalized_coords && cell_center_offset != 0.5f)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "Invalid cell center offset must be 0.5 when using normalized coordinates.");
+    if (!input || !lookup || !output_grad || !input_grad || !lookup_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_sample_grid_lut_grad_workspace_size(input_shape);
+    if (grad_mode == GFT_GRAD_REFERENCE && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "sample count workspace too small");
+    LutArgs a;
+    a.input = input;
+    a.dtype = 0;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.dout = dims_of(lookup_shape);
+    a.n_lut = (int)lookup_shape[0];
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.mip_mode = 0;
+    a.levels = 0;
+    a.mip_bias = 0.f;
+    a.cco = cell_center_offset;
+    a.separate = separate_camera_batch;
+    a.relative = relative_coords;
+    a.normalized = normalized_coords;
+    if (!launch_lut_bwd(a, input, lookup, output_grad, grad_mode == GFT_GRAD_EXACT, input_grad, lookup_grad,
+                        reinterpret_cast<unsigned int*>(workspace), as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_lod_transform(const int32_t input_shape[3], const float* matrix_mv, const float* matrix_p,
+                             const float* frustum, int32_t num, const int32_t output_shape[3],
+                             int32_t inverse_transform, float* output, void* stream) {
+    if (!input_shape || !output_shape || input_shape[0] < 1 || input_shape[1] < 1 || input_shape[2] < 1 ||
+        output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive");
+    if (!matrix_mv || !matrix_p || !frustum || num <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "camera batch size mismatch");
+    if (!output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const auto pairs = make_pairs(nullptr, 1, matrix_mv, matrix_p, frustum, num, num, false);
+    const Dims din{input_shape[2], input_shape[1], input_shape[0]};
+    const Dims dout{output_shape[2], output_shape[1], output_shape[0]};
+    if (!launch_lod_transform(din, dout, pairs, inverse_transform != 0, output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+// ---------------------------------------------------------------- blend
+gft_status gft_reduce_grid_blend(const float* input, const int64_t input_shape[5], int32_t blending_mode,
+                                 int32_t keep_dims, float* output, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blending mode");
+    if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_blend_fwd(input, (int)input_shape[0], (int)input_shape[4], dims_of(input_shape), blending_mode,
+                          keep_dims != 0, output, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_reduce_grid_blend_grad(const float* output_grad, const float* output, const float* input,
+                                      const int64_t input_shape[5], int32_t blending_mode, int32_t keep_dims,
+                                      int32_t grad_mode, float* input_grad, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    // ReduceGridBlendGrad accepts BEER_LAMBERT, ALPHA and ADDITIVE (reduce_blend.cc:41)
+    if (!(blending_mode == GFT_BLEND_BEER_LAMBERT || blending_mode == GFT_BLEND_ALPHA ||
+          blending_mode == GFT_BLEND_ADDITIVE))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blending mode");
+    if (!enum_in(grad_mode, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (!output_grad || !output || !input || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_blend_bwd(output_grad, output, input, (int)input_shape[0], (int)input_shape[4], dims_of(input_shape),
+                          blending_mode, keep_dims != 0, grad_mode == GFT_GRAD_EXACT, input_grad, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+// ---------------------------------------------------------------- advect
+size_t gft_advect_workspace_size(const int64_t density_shape[5], int32_t order) {
+    std::string why;
+    if (!grid_shape_ok(density_shape, why) || order != 2) return 0;
+    return align256(sizeof(float) * (size_t)density_shape[1] * density_shape[2] * density_shape[3] * density_shape[4]);
+}
+
+static gft_status check_advect(const int64_t* s, const float* vx, const float* vy, const float* vz, int order,
+                               int clamp, int boundary) {
+    std::string why;
+    if (!grid_shape_ok(s, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(s[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (order != 1 && order != 2) return fail(GFT_ERR_INVALID_ARGUMENT, "Unsupported warp order");
+    if (!enum_in(clamp, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid clamp");
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    if (!vx || !vy || !vz) return fail(GFT_ERR_INVALID_ARGUMENT, "velocity pointer is NULL");
+    return GFT_OK;
+}
+
+gft_status gft_advect(const void* density, int32_t density_dtype, const int64_t density_shape[5], const float* vel_x,
+                      const float* vel_y, const float* vel_z, float dt, int32_t order, int32_t clamp,
+                      int32_t boundary, float* output, void* workspace, size_t workspace_bytes, void* stream) {
+    gft_status st = check_advect(density_shape, vel_x, vel_y, vel_z, order, clamp, boundary);
+    if (st != GFT_OK) return st;
+    if (!enum_in(density_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (!density || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_advect_workspace_size(density_shape, order);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "advect workspace too small");
+    AdvectArgs a;
+    a.density = density;
+    a.dtype = density_dtype;
+    a.N = (int)density_shape[0];
+    a.C = (int)density_shape[4];
+    a.d = dims_of(density_shape);
+    a.vx = vel_x;
+    a.vy = vel_y;
+    a.vz = vel_z;
+    a.dt = dt;
+    a.order = order;
+    a.clamp = clamp;
+    a.boundary = boundary;
+    if (!launch_advect_fwd(a, output, reinterpret_cast<float*>(workspace), as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t order) {
+    std::string why;
+    if (!grid_shape_ok(density_shape, why)) return 0;
+    const size_t nv = (size_t)density_shape[1] * density_shape[2] * density_shape[3];
+    const size_t C = (size_t)density_shape[4];
+    return align256(sizeof(float) * (nv * (4 * C + 3)) + sizeof(unsigned int) * 2 * nv);
+}
+
+gft_status gft_advect_grad(const float* density, const int64_t density_shape[5], const float* vel_x,
+                           const float* vel_y, const float* vel_z, float dt, int32_t order, int32_t clamp,
+                           int32_t boundary, int32_t grad_mode, const float* output_grad, float* density_grad,
+                           float* vel_x_grad, float* vel_y_grad, float* vel_z_grad, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+    gft_status st = check_advect(density_shape, vel_x, vel_y, vel_z, order, clamp, boundary);
+    if (st != GFT_OK) return st;
+    if (!enum_in(grad_mode, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (!density || !output_grad || !density_grad || !vel_x_grad || !vel_y_grad || !vel_z_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_advect_grad_workspace_size(density_shape, order);
+    if (workspace == nullptr || workspace_bytes < need) return fail(GFT_ERR_WORKSPACE, "advect gradient workspace too small");
+    AdvectArgs a;
+    a.density = density;
+    a.dtype = 0;
+    a.N = (int)density_shape[0];
+    a.C = (int)density_shape[4];
+    a.d = dims_of(density_shape);
+    a.vx = vel_x;
+    a.vy = vel_y;
+    a.vz = vel_z;
+    a.dt = dt;
+    a.order = order;
+    a.clamp = clamp;
+    a.boundary = boundary;
+    if (!launch_advect_bwd(a, grad_mode == GFT_GRAD_EXACT, output_grad, density_grad, vel_x_grad, vel_y_grad,
+                           vel_z_grad, reinterpret_cast<float*>(workspace), as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+}  // extern "C"

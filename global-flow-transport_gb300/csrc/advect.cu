@@ -1,0 +1,390 @@
+// Fused advection of a density grid by a staggered velocity grid
+// (VelocityGrid.warp, data_structures.py:870-905) and its adjoint.
+//
+// The reference builds lut = -dt * centered(v) with TF ops and calls
+// SampleGridLut up to four times (forward, back, MIN, MAX) plus TF elementwise
+// ops.  Here the staggered -> centred average is folded into the lookup and
+// MacCormack runs in two passes: (1) the semi-Lagrangian value, (2) the back
+// lookup of (1), the correction and the MC_SMOOTH clamp, with the MIN/MAX of
+// the forward footprint taken from the same 8 gathers as the forward value.
+#include "gft_internal.h"
+
+namespace gft {
+
+constexpr int AD_THREADS = 256;
+constexpr int CLAMP_NONE = 0, CLAMP_MC_SMOOTH = 1, CLAMP_NEGATIVE = 2;
+
+// lut = -dt * centred velocity at voxel (x, y, z) (centered, data_structures.py:819-833)
+__device__ __forceinline__ float3 lut_at(const float* __restrict__ vx, const float* __restrict__ vy,
+                                         const float* __restrict__ vz, Dims d, int x, int y, int z, float dt) {
+    const int64_t ix = ((int64_t)z * d.y + y) * (d.x + 1) + x;
+    const int64_t iy = ((int64_t)z * (d.y + 1) + y) * d.x + x;
+    const int64_t iz = ((int64_t)z * d.y + y) * d.x + x;
+    const float cx = (__ldg(vx + ix + 1) + __ldg(vx + ix)) * 0.5f;
+    const float cy = (__ldg(vy + iy + d.x) + __ldg(vy + iy)) * 0.5f;
+    const float cz = (__ldg(vz + iz + (int64_t)d.x * d.y) + __ldg(vz + iz)) * 0.5f;
+    return make_float3(cx * (-dt), cy * (-dt), cz * (-dt));
+}
+
+__device__ __forceinline__ void unflat(int64_t v, Dims d, int& x, int& y, int& z) {
+    x = (int)(v % d.x);
+    y = (int)((v / d.x) % d.y);
+    z = (int)(v / ((int64_t)d.x * d.y));
+}
+
+// Trilinear value plus the MIN/MAX of the lookup op (read3DMin/Max) from one
+// set of 8 corner reads.
+template <int C, typename S, int BM>
+__device__ __forceinline__ void fetch_linear_minmax(const S* __restrict__ g, Dims d, float px, float py, float pz,
+                                                    Vec<C>& val, Vec<C>& mn, Vec<C>& mx) {
+    if constexpr (BM == BM_BORDER) {
+        if (!border_inside(px, py, pz, d)) {
+            val = mn = mx = vzero<C>();
+            return;
+        }
+    }
+    const Corners c = corners<BM>(px, py, pz, d);
+    const bool ok[8] = {c.vx0 && c.vy0 && c.vz0, c.vx1 && c.vy0 && c.vz0, c.vx0 && c.vy1 && c.vz0,
+                        c.vx1 && c.vy1 && c.vz0, c.vx0 && c.vy0 && c.vz1, c.vx1 && c.vy0 && c.vz1,
+                        c.vx0 && c.vy1 && c.vz1, c.vx1 && c.vy1 && c.vz1};
+    const int xs[8] = {c.x0, c.x1, c.x0, c.x1, c.x0, c.x1, c.x0, c.x1};
+    const int ys[8] = {c.y0, c.y0, c.y1, c.y1, c.y0, c.y0, c.y1, c.y1};
+    const int zs[8] = {c.z0, c.z0, c.z0, c.z0, c.z1, c.z1, c.z1, c.z1};
+    Vec<C> v[8];
+    bool all_ok = true;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = read_corner<C, S, BM>(g, d, xs[k], ys[k], zs[k], ok[k]);
+        all_ok = all_ok && ok[k];
+    }
+    const Vec<C> v0 = vlerp(vlerp(v[0], v[1], c.wx), vlerp(v[2], v[3], c.wx), c.wy);
+    const Vec<C> v1 = vlerp(vlerp(v[4], v[5], c.wx), vlerp(v[6], v[7], c.wx), c.wy);
+    val = vlerp(v0, v1, c.wz);
+    mn = vfill<C>(all_ok ? REF_FLOAT_MAX : 0.f);
+    mx = vfill<C>(all_ok ? -REF_FLOAT_MAX : 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (BM != BM_BORDER || ok[k]) {
+            mn = vmin(mn, v[k]);
+            mx = vmax(mx, v[k]);
+        }
+    }
+}
+
+template <int C>
+__device__ __forceinline__ Vec<C> vmax0(Vec<C> a) {
+#pragma unroll
+    for (int i = 0; i < C; ++i) a.v[i] = fmaxf(a.v[i], 0.f);
+    return a;
+}
+
+// Pass 1 / semi-Lagrangian: out = d(x + lut(x))
+template <int C, typename S, int BM>
+__global__ void __launch_bounds__(AD_THREADS)
+    k_adv_sl(const S* __restrict__ d, Dims dm, const float* __restrict__ vx, const float* __restrict__ vy,
+             const float* __restrict__ vz, float dt, bool negative, float* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= voxels(dm)) return;
+    int x, y, z;
+    unflat(t, dm, x, y, z);
+    const float3 l = lut_at(vx, vy, vz, dm, x, y, z, dt);
+    Vec<C> r = fetch_linear<C, S, BM>(d, dm, l.x + (float)x, l.y + (float)y, l.z + (float)z);
+    if (negative) r = vmax0(r);
+    store<C>(out, t, r);
+}
+
+// Pass 2 / MacCormack: corr = fwd + 0.5*(d - fwd(x - lut)), MC_SMOOTH keeps fwd
+// where corr leaves [min, max] of the forward footprint.
+template <int C, typename S, int BM>
+__global__ void __launch_bounds__(AD_THREADS)
+    k_adv_mc(const S* __restrict__ d, const float* __restrict__ fwd, Dims dm, const float* __restrict__ vx,
+             const float* __restrict__ vy, const float* __restrict__ vz, float dt, int clamp, float* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= voxels(dm)) return;
+    int x, y, z;
+    unflat(t, dm, x, y, z);
+    const float3 l = lut_at(vx, vy, vz, dm, x, y, z, dt);
+    Vec<C> f, mn, mx;
+    fetch_linear_minmax<C, S, BM>(d, dm, l.x + (float)x, l.y + (float)y, l.z + (float)z, f, mn, mx);
+    const Vec<C> back = fetch_linear<C, float, BM>(fwd, dm, -l.x + (float)x, -l.y + (float)y, -l.z + (float)z);
+    const Vec<C> dv = Load<C, S>::at(d, t);
+    Vec<C> r;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        float corr = f.v[i] + 0.5f * (dv.v[i] - back.v[i]);
+        if (clamp == CLAMP_MC_SMOOTH && (corr < mn.v[i] || corr > mx.v[i])) corr = f.v[i];
+        if (clamp == CLAMP_NEGATIVE) corr = fmaxf(corr, 0.f);
+        r.v[i] = corr;
+    }
+    store<C>(out, t, r);
+}
+
+template <int C, typename S>
+static bool adv_fwd_c(const AdvectArgs& a, float* out, float* ws, cudaStream_t s) {
+    const int64_t nv = voxels(a.d);
+    const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
+    for (int b = 0; b < a.N; ++b) {
+        const S* db = reinterpret_cast<const S*>(a.density) + (size_t)b * nv * C;
+        float* ob = out + (size_t)b * nv * C;
+        if (a.order == 1) {
+            const bool neg = a.clamp == CLAMP_NEGATIVE;
+            switch (a.boundary) {
+                case BM_BORDER: k_adv_sl<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+                case BM_CLAMP: k_adv_sl<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+                default: k_adv_sl<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+            }
+        } else {
+            switch (a.boundary) {
+                case BM_BORDER:
+                    k_adv_sl<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    break;
+                case BM_CLAMP:
+                    k_adv_sl<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    break;
+                default:
+                    k_adv_sl<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    break;
+            }
+        }
+        if (!cuda_ok(cudaGetLastError(), "advect launch")) return false;
+    }
+    return true;
+}
+
+bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s) {
+    if (a.dtype == 0) {
+        if (a.C == 4) return adv_fwd_c<4, float>(a, out, ws, s);
+        if (a.C == 2) return adv_fwd_c<2, float>(a, out, ws, s);
+        return adv_fwd_c<1, float>(a, out, ws, s);
+    }
+    if (a.C == 4) return adv_fwd_c<4, __nv_bfloat16>(a, out, ws, s);
+    if (a.C == 2) return adv_fwd_c<2, __nv_bfloat16>(a, out, ws, s);
+    return adv_fwd_c<1, __nv_bfloat16>(a, out, ws, s);
+}
+
+// ---- adjoint ---------------------------------------------------------------------
+// Stage B (MacCormack only): route the output gradient through the MC_SMOOTH
+// `where` (TF semantics: each branch gets the gradient where selected, none to
+// min/max), store the direct density term 0.5*g_corr, scatter the back-lookup
+// gradient -0.5*g_corr into the fwd adjoint and accumulate the lookup gradient
+// of the back lookup (whose lut is -lut).
+template <int C, int BM, int COUNT>
+__global__ void __launch_bounds__(AD_THREADS)
+    k_adv_bwd_back(const float* __restrict__ d, const float* __restrict__ fwd, Dims dm, const float* __restrict__ vx,
+                   const float* __restrict__ vy, const float* __restrict__ vz, float dt, int clamp,
+                   const float* __restrict__ dy, float* __restrict__ gd, float* __restrict__ gfwd_sc,
+                   unsigned int* __restrict__ cnt2, float* __restrict__ gdir, float* __restrict__ glut) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= voxels(dm)) return;
+    int x, y, z;
+    unflat(t, dm, x, y, z);
+    const float3 l = lut_at(vx, vy, vz, dm, x, y, z, dt);
+    Vec<C> f, mn, mx;
+    fetch_linear_minmax<C, float, BM>(d, dm, l.x + (float)x, l.y + (float)y, l.z + (float)z, f, mn, mx);
+    const float bx = -l.x + (float)x, by = -l.y + (float)y, bz = -l.z + (float)z;
+    const Vec<C> back = fetch_linear<C, float, BM>(fwd, dm, bx, by, bz);
+    const Vec<C> dv = loadf<C>(d, t);
+    Vec<C> g = loadf<C>(dy, t);
+    Vec<C> gcorr, gback;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        const float corr = f.v[i] + 0.5f * (dv.v[i] - back.v[i]);
+        bool oob = false;
+        if (clamp == CLAMP_MC_SMOOTH) oob = corr < mn.v[i] || corr > mx.v[i];
+        if (clamp == CLAMP_NEGATIVE && !(corr >= 0.f)) g.v[i] = 0.f;
+        gcorr.v[i] = oob ? 0.f : g.v[i];
+        gback.v[i] = -0.5f * gcorr.v[i];
+    }
+    store<C>(gd, t, vscale(gcorr, 0.5f));
+    store<C>(gdir, t, g);
+    scatter_linear<C, BM, COUNT>(gfwd_sc, cnt2, dm, bx, by, bz, gback);
+    Vec<C> ddx, ddy, ddz;
+    fetch_grad<C, BM>(fwd, dm, bx, by, bz, ddx, ddy, ddz);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        sx += gback.v[i] * ddx.v[i];
+        sy += gback.v[i] * ddy.v[i];
+        sz += gback.v[i] * ddz.v[i];
+    }
+    float* gl = glut + t * 3;
+    gl[0] -= sx;
+    gl[1] -= sy;
+    gl[2] -= sz;
+}
+
+// Stage C: fwd adjoint = direct term + (normalised) back-lookup scatter; scatter
+// it into the density through the forward lookup and accumulate that lookup's
+// gradient.  first_order: the fwd adjoint is the output gradient itself.
+template <int C, int BM, int COUNT>
+__global__ void __launch_bounds__(AD_THREADS)
+    k_adv_bwd_fwd(const float* __restrict__ d, Dims dm, const float* __restrict__ vx, const float* __restrict__ vy,
+                  const float* __restrict__ vz, float dt, bool first_order, bool negative,
+                  const float* __restrict__ gdir, const float* __restrict__ gfwd_sc,
+                  const unsigned int* __restrict__ cnt2, float* __restrict__ gd_sc, unsigned int* __restrict__ cnt3,
+                  float* __restrict__ glut) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= voxels(dm)) return;
+    int x, y, z;
+    unflat(t, dm, x, y, z);
+    const float3 l = lut_at(vx, vy, vz, dm, x, y, z, dt);
+    const float px = l.x + (float)x, py = l.y + (float)y, pz = l.z + (float)z;
+    Vec<C> gf = loadf<C>(gdir, t);
+    if (first_order) {
+        if (negative) {
+            const Vec<C> f = fetch_linear<C, float, BM>(d, dm, px, py, pz);
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+                if (!(f.v[i] >= 0.f)) gf.v[i] = 0.f;
+        }
+    } else {
+        Vec<C> sc = loadf<C>(gfwd_sc, t);
+        if (COUNT) {
+            const unsigned int n = cnt2[t];
+            if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+        }
+        gf = vadd(gf, sc);
+    }
+    scatter_linear<C, BM, COUNT>(gd_sc, cnt3, dm, px, py, pz, gf);
+    Vec<C> ddx, ddy, ddz;
+    fetch_grad<C, BM>(d, dm, px, py, pz, ddx, ddy, ddz);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        sx += gf.v[i] * ddx.v[i];
+        sy += gf.v[i] * ddy.v[i];
+        sz += gf.v[i] * ddz.v[i];
+    }
+    float* gl = glut + t * 3;
+    gl[0] += sx;
+    gl[1] += sy;
+    gl[2] += sz;
+}
+
+// Stage D: density gradient = direct term + (normalised) forward-lookup scatter.
+template <int C, bool NORM>
+__global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restrict__ gd_sc,
+                                  const unsigned int* __restrict__ cnt3, int64_t nv) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv) return;
+    Vec<C> sc = loadf<C>(gd_sc, t);
+    if (NORM) {
+        const unsigned int n = cnt3[t];
+        if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+    }
+    store<C>(gd, t, vadd(loadf<C>(gd, t), sc));
+}
+
+// Velocity gradient: g_centred = -dt * g_lut, then the adjoint of the face
+// average (each face receives half of both adjacent cells).
+__global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, float dt, float* __restrict__ gvx,
+                                   float* __restrict__ gvy, float* __restrict__ gvz) {
+    const int64_t nx = (int64_t)(dm.x + 1) * dm.y * dm.z;
+    const int64_t ny = (int64_t)dm.x * (dm.y + 1) * dm.z;
+    const int64_t nz = (int64_t)dm.x * dm.y * (dm.z + 1);
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float h = -0.5f * dt;
+    if (t < nx) {
+        const int i = (int)(t % (dm.x + 1));
+        const int64_t r = t / (dm.x + 1);  // z*H + y
+        float a = 0.f;
+        if (i > 0) a += glut[(r * dm.x + i - 1) * 3 + 0];
+        if (i < dm.x) a += glut[(r * dm.x + i) * 3 + 0];
+        gvx[t] = h * a;
+        return;
+    }
+    t -= nx;
+    if (t < ny) {
+        const int x = (int)(t % dm.x);
+        const int j = (int)((t / dm.x) % (dm.y + 1));
+        const int z = (int)(t / ((int64_t)dm.x * (dm.y + 1)));
+        float a = 0.f;
+        if (j > 0) a += glut[((((int64_t)z * dm.y) + j - 1) * dm.x + x) * 3 + 1];
+        if (j < dm.y) a += glut[((((int64_t)z * dm.y) + j) * dm.x + x) * 3 + 1];
+        gvy[t] = h * a;
+        return;
+    }
+    t -= ny;
+    if (t < nz) {
+        const int64_t plane = (int64_t)dm.x * dm.y;
+        const int64_t k = t / plane;
+        const int64_t xy = t - k * plane;
+        float a = 0.f;
+        if (k > 0) a += glut[((k - 1) * plane + xy) * 3 + 2];
+        if (k < dm.z) a += glut[(k * plane + xy) * 3 + 2];
+        gvz[t] = h * a;
+    }
+}
+
+template <int C, int BM, int COUNT>
+static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float* gvx, float* gvy, float* gvz,
+                         float* ws, cudaStream_t s) {
+    const int64_t nv = voxels(a.d);
+    const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
+    const size_t vc = (size_t)nv * C;
+    float* fwd = ws;
+    float* gfwd_sc = fwd + vc;
+    float* gdir = gfwd_sc + vc;
+    float* gd_sc = gdir + vc;
+    float* glut = gd_sc + vc;
+    unsigned int* cnt2 = reinterpret_cast<unsigned int*>(glut + (size_t)nv * 3);
+    unsigned int* cnt3 = cnt2 + nv;
+    if (!cuda_ok(cudaMemsetAsync(glut, 0, sizeof(float) * nv * 3, s), "zero lookup gradient")) return false;
+    const float* dens = reinterpret_cast<const float*>(a.density);
+    for (int b = 0; b < a.N; ++b) {
+        const float* db = dens + (size_t)b * vc;
+        const float* dyb = dy + (size_t)b * vc;
+        float* gdb = gd + (size_t)b * vc;
+        if (!cuda_ok(cudaMemsetAsync(gd_sc, 0, sizeof(float) * vc, s), "zero scatter")) return false;
+        if (COUNT && !cuda_ok(cudaMemsetAsync(cnt3, 0, sizeof(unsigned int) * nv, s), "zero counter")) return false;
+        if (a.order == 2) {
+            if (!cuda_ok(cudaMemsetAsync(gfwd_sc, 0, sizeof(float) * vc, s), "zero scatter")) return false;
+            if (COUNT && !cuda_ok(cudaMemsetAsync(cnt2, 0, sizeof(unsigned int) * nv, s), "zero counter")) return false;
+            k_adv_sl<C, float, BM><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
+            k_adv_bwd_back<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
+                                                                      dyb, gdb, gfwd_sc, cnt2, gdir, glut);
+            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
+                                                                     gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut);
+        } else {
+            if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
+            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
+                                                                     a.clamp == CLAMP_NEGATIVE, dyb, nullptr,
+                                                                     nullptr, gd_sc, cnt3, glut);
+        }
+        k_adv_bwd_density<C, COUNT != 0><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
+        if (!cuda_ok(cudaGetLastError(), "advect gradient launch")) return false;
+    }
+    const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
+                          (int64_t)a.d.x * a.d.y * (a.d.z + 1);
+    k_adv_bwd_velocity<<<(unsigned)((nstag + AD_THREADS - 1) / AD_THREADS), AD_THREADS, 0, s>>>(glut, a.d, a.dt, gvx,
+                                                                                                 gvy, gvz);
+    return cuda_ok(cudaGetLastError(), "velocity gradient launch");
+}
+
+template <int C>
+static bool adv_bwd_c(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy, float* gvz,
+                      float* ws, cudaStream_t s) {
+    switch (a.boundary) {
+        case BM_BORDER:
+            return exact ? adv_bwd_impl<C, BM_BORDER, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_BORDER, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+        case BM_CLAMP:
+            return exact ? adv_bwd_impl<C, BM_CLAMP, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_CLAMP, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+        default:
+            return exact ? adv_bwd_impl<C, BM_WRAP, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_WRAP, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+    }
+}
+
+bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
+                       float* gvz, float* ws, cudaStream_t s) {
+    if (a.C == 4) return adv_bwd_c<4>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
+    if (a.C == 2) return adv_bwd_c<2>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
+    return adv_bwd_c<1>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
+}
+
+}  // namespace gft

@@ -1,0 +1,121 @@
+// Host-side declarations shared by the kernel translation units and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "gft_common.cuh"
+
+namespace gft {
+
+// Up to this many (input batch, camera) pairs travel by value in one launch's
+// parameter block; more pairs are split into several launches.
+constexpr int MAX_PAIRS = 16;
+
+struct PairTable {
+    CamX cam[MAX_PAIRS];
+    int in_batch[MAX_PAIRS];  // batch slice of the input grid
+    int out_slot[MAX_PAIRS];  // slot in the output's [N * V] leading dims
+    int pair_base;            // global index of pair 0 of this launch
+    int n;                    // pairs in this launch
+};
+
+// One (input batch, camera) pair of a launcher loop (e.g. raymarch_grid.cu.cc:262-291).
+struct Pair {
+    CamX cam;
+    int in_batch;
+    int out_slot;
+    int camera;
+};
+
+// Builds the (batch, camera) pairs with MV = V*M and the inverses computed in
+// double on the host.  separate_camera_batch=false pairs batch b with camera b.
+std::vector<Pair> make_pairs(const float* M, int num_m, const float* V, const float* P, const float* F,
+                             int num_cameras, int batch, bool separate_camera_batch);
+std::vector<PairTable> make_tables(const std::vector<Pair>& pairs);
+
+// Mip pyramid of one batch slice: level 0 is the input, levels 1..L live in a
+// workspace as fp32 (dims >> m per level).
+constexpr int MAX_MIPS = 15;
+struct MipSet {
+    const float* lvl[MAX_MIPS + 1];
+    Dims dims[MAX_MIPS + 1];
+    int levels;  // L
+};
+int usable_mip_levels(Dims d, int num_mips);
+size_t mip_workspace_floats(Dims d, int levels, int C);
+
+// error helpers
+void set_error(const std::string& msg);
+bool cuda_ok(cudaError_t e, const char* what);
+
+// launchers ------------------------------------------------------------------
+struct RaymarchArgs {
+    const void* input;
+    int dtype;
+    int N, C;
+    Dims din;
+    int D, H, W;
+    int filter, boundary, blend;
+    int n_slots;  // output slots = N * (separate ? V : 1)
+};
+bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
+bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
+                         const float* dout, bool exact, float* grad, float* ws_buf, float* ws_cnt,
+                         cudaStream_t s);
+
+bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, float* ws, cudaStream_t s,
+                       MipSet* set_out);
+
+struct SampleArgs {
+    const void* input;
+    int dtype;
+    int N, C;
+    Dims din, dout;
+    int filter, boundary, mip_mode, levels;
+    float mip_bias, cco;
+    int coord_mode;
+};
+bool launch_sample_transform_fwd(const SampleArgs& a, const std::vector<Pair>& pairs, const MipSet* mips_per_batch,
+                                 float* out, cudaStream_t s);
+bool launch_sample_transform_bwd(int N, int C, Dims din, Dims dout, int boundary, int coord_mode, float cco,
+                                 const std::vector<Pair>& pairs, const float* dy, bool exact, float* grad,
+                                 unsigned int* count, cudaStream_t s);
+
+struct LutArgs {
+    const void* input;
+    int dtype;
+    int N, C;
+    Dims din, dout;
+    int n_lut;  // V
+    int filter, boundary, mip_mode, levels;
+    float mip_bias, cco;
+    int separate, relative, normalized;
+};
+bool launch_lut_fwd(const LutArgs& a, const float* lut, const MipSet* mips_per_batch, float* out, cudaStream_t s);
+bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, const float* dy, bool exact,
+                    float* grad, float* lut_grad, unsigned int* count, cudaStream_t s);
+bool launch_lod_transform(Dims din, Dims dout, const std::vector<Pair>& pairs, bool inverse, float* out,
+                          cudaStream_t s);
+
+bool launch_blend_fwd(const float* in, int N, int C, Dims d, int mode, bool keep_dims, float* out, cudaStream_t s);
+bool launch_blend_bwd(const float* dy, const float* y, const float* x, int N, int C, Dims d, int mode,
+                      bool keep_dims, bool exact, float* gx, cudaStream_t s);
+
+struct AdvectArgs {
+    const void* density;
+    int dtype;
+    int N, C;
+    Dims d;
+    const float *vx, *vy, *vz;
+    float dt;
+    int order, clamp, boundary;
+};
+bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s);
+bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
+                       float* gvz, float* ws, cudaStream_t s);
+
+}  // namespace gft

@@ -1,0 +1,513 @@
+// Resampling ops: mip pyramid, SampleGridTransform (+ scatter adjoint),
+// SampleGridLut (+ adjoint) and LodTransform.
+//
+// Semantics: resample_grid.cu.cc (kGenerateMip3D :46-72, kSample3D :240-252,
+// kSampleGrid3DLuT :465-484, kScatter3DGradients :841-861,
+// kScatterLuT3DGradients :1051-1081, kComputeLoD3D :1288-1300) and the
+// sampler of sampling.hpp.  All cameras of a batch slice run in one launch;
+// per-camera transforms travel in the launch parameters.
+#include "gft_internal.h"
+
+namespace gft {
+
+constexpr int RS_THREADS = 256;
+
+// ---- mips --------------------------------------------------------------------
+// Level m+1 = 2x2x2 mean of level m, dims >> 1, averaging z pairs, then y, then
+// x as kGenerateMip3D does.
+template <int C, typename S>
+__global__ void k_mip_level(const S* __restrict__ src, Dims ds, float* __restrict__ dst, Dims dd) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= voxels(dd)) return;
+    const int x = (int)(t % dd.x);
+    const int y = (int)((t / dd.x) % dd.y);
+    const int z = (int)(t / ((int64_t)dd.x * dd.y));
+    Vec<C> c[2];
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx) {
+        const int sx = 2 * x + dx;
+        const Vec<C> a = vscale(vadd(Load<C, S>::at(src, flat3(sx, 2 * y, 2 * z, ds)),
+                                     Load<C, S>::at(src, flat3(sx, 2 * y, 2 * z + 1, ds))), 0.5f);
+        const Vec<C> b = vscale(vadd(Load<C, S>::at(src, flat3(sx, 2 * y + 1, 2 * z, ds)),
+                                     Load<C, S>::at(src, flat3(sx, 2 * y + 1, 2 * z + 1, ds))), 0.5f);
+        c[dx] = vscale(vadd(a, b), 0.5f);
+    }
+    store<C>(dst, t, vscale(vadd(c[0], c[1]), 0.5f));
+}
+
+int usable_mip_levels(Dims d, int num_mips) {
+    int L = num_mips < 0 ? 0 : num_mips;
+    if (L > MAX_MIPS) L = MAX_MIPS;
+    for (int m = 1; m <= L; ++m) {
+        if ((int64_t)(d.x >> m) * (d.y >> m) * (d.z >> m) <= 0) return m - 1;
+    }
+    return L;
+}
+
+size_t mip_workspace_floats(Dims d, int levels, int C) {
+    size_t n = 0;
+    for (int m = 1; m <= levels; ++m) {
+        const size_t v = (size_t)(d.x >> m) * (d.y >> m) * (d.z >> m) * C;
+        n += (v + 63) & ~size_t(63);  // 256 B aligned levels
+    }
+    return n;
+}
+
+template <int C>
+static void mip_launch(const void* src, int dtype, Dims ds, float* dst, Dims dd, cudaStream_t s) {
+    const int64_t n = voxels(dd);
+    const unsigned blocks = (unsigned)((n + RS_THREADS - 1) / RS_THREADS);
+    if (dtype == 0)
+        k_mip_level<C, float><<<blocks, RS_THREADS, 0, s>>>((const float*)src, ds, dst, dd);
+    else
+        k_mip_level<C, __nv_bfloat16><<<blocks, RS_THREADS, 0, s>>>((const __nv_bfloat16*)src, ds, dst, dd);
+}
+
+bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, float* ws, cudaStream_t s,
+                       MipSet* set) {
+    set->levels = levels;
+    set->lvl[0] = (const float*)input;  // reinterpreted by the sampler according to dtype
+    set->dims[0] = d;
+    float* p = ws;
+    const void* src = input;
+    int src_dtype = dtype;
+    for (int m = 1; m <= levels; ++m) {
+        const Dims dm{d.x >> m, d.y >> m, d.z >> m};
+        if (C == 4) mip_launch<4>(src, src_dtype, set->dims[m - 1], p, dm, s);
+        else if (C == 2) mip_launch<2>(src, src_dtype, set->dims[m - 1], p, dm, s);
+        else mip_launch<1>(src, src_dtype, set->dims[m - 1], p, dm, s);
+        if (!cuda_ok(cudaGetLastError(), "mip generation launch")) return false;
+        set->lvl[m] = p;
+        set->dims[m] = dm;
+        src = p;
+        src_dtype = 0;
+        const size_t v = (size_t)voxels(dm) * C;
+        p += (v + 63) & ~size_t(63);
+    }
+    return true;
+}
+
+// Sampler2::sample3D / Sampling::sample3D with mips (sampling.hpp:551-620, 690-712).
+// Level 0 is read with the storage type S, coarser levels are fp32.
+template <int C, typename S, int BM>
+__device__ __forceinline__ Vec<C> read_level(int filter, const MipSet& ms, int m, float3 p, float cco) {
+    const float sc = (float)(1 << m);
+    const float px = p.x / sc - cco, py = p.y / sc - cco, pz = p.z / sc - cco;
+    if (m == 0) return fetch<C, S, BM, false>(filter, reinterpret_cast<const S*>(ms.lvl[0]), ms.dims[0], px, py, pz);
+    return fetch<C, float, BM, false>(filter, ms.lvl[m], ms.dims[m], px, py, pz);
+}
+
+template <int C, typename S, int BM>
+__device__ __forceinline__ Vec<C> sample_mip(int filter, int mip_mode, const MipSet& ms, float4 pos, float bias,
+                                             float cco) {
+    const float3 p = make_float3(pos.x, pos.y, pos.z);
+    if (mip_mode == MIP_NONE) return read_level<C, S, BM>(filter, ms, 0, p, cco);
+    const int L = ms.levels;
+    const float lod = fminf(fmaxf(pos.w + bias, 0.f), (float)L);
+    const int lf = min((int)(lod + (mip_mode == MIP_NEAREST ? 0.5f : 0.f)), L);
+    Vec<C> data = read_level<C, S, BM>(filter, ms, lf, p, cco);
+    if (mip_mode == MIP_LINEAR) {
+        const int lc = min((int)ceilf(lod), L);
+        if (lc > lf) data = vlerp(data, read_level<C, S, BM>(filter, ms, lc, p, cco), lod - floorf(lod));
+    }
+    return data;
+}
+
+// ---- SampleGridTransform -------------------------------------------------------
+constexpr int CM_LINDEPTH = 0, CM_LINDEPTH_REVERSE = 1, CM_TRANSFORM = 3, CM_TRANSFORM_REVERSE = 4;
+
+__device__ __forceinline__ float3 map_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv) {
+    switch (cm) {
+        case CM_LINDEPTH: return idx_to_os_lindepth(c, idx, dout_inv);
+        case CM_TRANSFORM: return idx_to_os(c, idx, dout_inv);
+        case CM_LINDEPTH_REVERSE: return os_to_idx_lindepth(c, idx, din);
+        default: return os_to_idx(c, idx, din);
+    }
+}
+
+// samplePos3D<CM, MIP> (sampling.hpp:58-136): position and LOD from forward
+// differences; forward modes use Jacobian rows, reverse modes its columns.
+__device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv,
+                                             bool lod) {
+    const float3 p = map_pos(c, cm, idx, din, dout_inv);
+    if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
+    const float3 ex = map_pos(c, cm, make_float3(idx.x + 1.f, idx.y, idx.z), din, dout_inv);
+    const float3 ey = map_pos(c, cm, make_float3(idx.x, idx.y + 1.f, idx.z), din, dout_inv);
+    const float3 ez = map_pos(c, cm, make_float3(idx.x, idx.y, idx.z + 1.f), din, dout_inv);
+    const float3 dx = make_float3(p.x - ex.x, p.y - ex.y, p.z - ex.z);
+    const float3 dy = make_float3(p.x - ey.x, p.y - ey.y, p.z - ey.z);
+    const float3 dz = make_float3(p.x - ez.x, p.y - ez.y, p.z - ez.z);
+    float px, py, pz;
+    if (cm == CM_LINDEPTH || cm == CM_TRANSFORM) {
+        px = sqrtf(dx.x * dx.x + dy.x * dy.x + dz.x * dz.x);
+        py = sqrtf(dx.y * dx.y + dy.y * dy.y + dz.y * dz.y);
+        pz = sqrtf(dx.z * dx.z + dy.z * dy.z + dz.z * dz.z);
+    } else {
+        px = sqrtf(dx.x * dx.x + dx.y * dx.y + dx.z * dx.z);
+        py = sqrtf(dy.x * dy.x + dy.y * dy.y + dy.z * dy.z);
+        pz = sqrtf(dz.x * dz.x + dz.y * dz.y + dz.z * dz.z);
+    }
+    const float dm = fmaxf(px, fmaxf(py, pz));
+    return make_float4(p.x, p.y, p.z, fmaxf(0.f, log2f(dm)));
+}
+
+template <int C, typename S, int BM>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_sample_transform(Dims dout, int filter, int mip_mode, float bias, float cco, int cm, const MipSet ms,
+                       float* __restrict__ out, const __grid_constant__ PairTable tab) {
+    const int64_t nv = voxels(dout);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv * tab.n) return;
+    const int p = (int)(t / nv);
+    const int64_t v = t - (int64_t)p * nv;
+    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
+    const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
+    const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
+                                  mip_mode != MIP_NONE);
+    Vec<C> r;
+    if ((filter == F_LINEAR || filter == F_NEAREST) && (BM == BM_BORDER || BM == BM_CLAMP))
+        r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
+    else
+        r = vzero<C>();
+    store<C>(out, (int64_t)tab.out_slot[p] * nv + v, r);
+}
+
+template <int C, typename S>
+static void st_fwd(int bm, unsigned blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
+                   const PairTable& t) {
+    switch (bm) {
+        case BM_BORDER:
+            k_sample_transform<C, S, BM_BORDER><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
+                                                                             a.cco, a.coord_mode, ms, out, t);
+            break;
+        case BM_CLAMP:
+            k_sample_transform<C, S, BM_CLAMP><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
+                                                                            a.cco, a.coord_mode, ms, out, t);
+            break;
+        default:
+            k_sample_transform<C, S, BM_WRAP><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
+                                                                           a.cco, a.coord_mode, ms, out, t);
+            break;
+    }
+}
+
+bool launch_sample_transform_fwd(const SampleArgs& a, const std::vector<Pair>& pairs, const MipSet* mips,
+                                 float* out, cudaStream_t s) {
+    const int64_t nv = voxels(a.dout);
+    for (int b = 0; b < a.N; ++b) {
+        std::vector<Pair> pb;
+        for (const Pair& p : pairs)
+            if (p.in_batch == b) pb.push_back(p);
+        for (const PairTable& t : make_tables(pb)) {
+            const unsigned blocks = (unsigned)((nv * t.n + RS_THREADS - 1) / RS_THREADS);
+            if (a.dtype == 0) {
+                if (a.C == 4) st_fwd<4, float>(a.boundary, blocks, s, a, mips[b], out, t);
+                else if (a.C == 2) st_fwd<2, float>(a.boundary, blocks, s, a, mips[b], out, t);
+                else st_fwd<1, float>(a.boundary, blocks, s, a, mips[b], out, t);
+            } else {
+                if (a.C == 4) st_fwd<4, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
+                else if (a.C == 2) st_fwd<2, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
+                else st_fwd<1, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
+            }
+            if (!cuda_ok(cudaGetLastError(), "sample transform launch")) return false;
+        }
+    }
+    return true;
+}
+
+// Scatter adjoint (kScatter3DGradients): trilinear scatter of dy at the
+// sampling position, +1 per reached corner on the uint32 counter.
+template <int C, int BM, int COUNT>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_sample_transform_bwd(Dims din, Dims dout, int cm, float cco, const float* __restrict__ dy,
+                           float* __restrict__ grad, unsigned int* __restrict__ count,
+                           const __grid_constant__ PairTable tab) {
+    const int64_t nv = voxels(dout);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv * tab.n) return;
+    const int p = (int)(t / nv);
+    const int64_t v = t - (int64_t)p * nv;
+    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const float3 dinf = make_float3((float)din.x, (float)din.y, (float)din.z);
+    const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
+    const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), dinf, dinv, false);
+    const Vec<C> g = loadf<C>(dy, (int64_t)tab.out_slot[p] * nv + v);
+    scatter_linear<C, BM, COUNT>(grad, count, din, pos.x - cco, pos.y - cco, pos.z - cco, g);
+}
+
+// grad /= count where count > 0; the counter is reset (kNormalize3DGradients<T,true>).
+template <int C>
+__global__ void k_normalize_count(float* __restrict__ grad, unsigned int* __restrict__ count, int64_t nv) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv) return;
+    const unsigned int n = count[t];
+    if (n > 0) {
+        const float w = 1.0f / (float)n;
+        store<C>(grad, t, vscale(loadf<C>(grad, t), w));
+        count[t] = 0;
+    }
+}
+
+template <int C>
+static void normalize_launch(float* grad, unsigned int* count, int64_t nv, cudaStream_t s) {
+    k_normalize_count<C><<<(unsigned)((nv + RS_THREADS - 1) / RS_THREADS), RS_THREADS, 0, s>>>(grad, count, nv);
+}
+static void normalize_any(int C, float* grad, unsigned int* count, int64_t nv, cudaStream_t s) {
+    if (C == 4) normalize_launch<4>(grad, count, nv, s);
+    else if (C == 2) normalize_launch<2>(grad, count, nv, s);
+    else normalize_launch<1>(grad, count, nv, s);
+}
+
+template <int C, int COUNT>
+static void stb_launch(int bm, unsigned blocks, cudaStream_t s, Dims din, Dims dout, int cm, float cco,
+                       const float* dy, float* grad, unsigned int* count, const PairTable& t) {
+    switch (bm) {
+        case BM_BORDER:
+            k_sample_transform_bwd<C, BM_BORDER, COUNT><<<blocks, RS_THREADS, 0, s>>>(din, dout, cm, cco, dy, grad, count, t);
+            break;
+        case BM_CLAMP:
+            k_sample_transform_bwd<C, BM_CLAMP, COUNT><<<blocks, RS_THREADS, 0, s>>>(din, dout, cm, cco, dy, grad, count, t);
+            break;
+        default:
+            k_sample_transform_bwd<C, BM_WRAP, COUNT><<<blocks, RS_THREADS, 0, s>>>(din, dout, cm, cco, dy, grad, count, t);
+            break;
+    }
+}
+
+bool launch_sample_transform_bwd(int N, int C, Dims din, Dims dout, int boundary, int coord_mode, float cco,
+                                 const std::vector<Pair>& pairs, const float* dy, bool exact, float* grad,
+                                 unsigned int* count, cudaStream_t s) {
+    const int64_t nvi = voxels(din), nvo = voxels(dout);
+    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvi * C * N, s), "zero gradient")) return false;
+    if (!exact && !cuda_ok(cudaMemsetAsync(count, 0, sizeof(unsigned int) * nvi, s), "zero counter")) return false;
+    for (int b = 0; b < N; ++b) {
+        std::vector<Pair> pb;
+        for (const Pair& p : pairs)
+            if (p.in_batch == b) pb.push_back(p);
+        float* gb = grad + (size_t)b * nvi * C;
+        for (const PairTable& t : make_tables(pb)) {
+            const unsigned blocks = (unsigned)((nvo * t.n + RS_THREADS - 1) / RS_THREADS);
+            if (exact) {
+                if (C == 4) stb_launch<4, 0>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+                else if (C == 2) stb_launch<2, 0>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+                else stb_launch<1, 0>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+            } else {
+                if (C == 4) stb_launch<4, 1>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+                else if (C == 2) stb_launch<2, 1>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+                else stb_launch<1, 1>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
+            }
+            if (!cuda_ok(cudaGetLastError(), "sample transform gradient launch")) return false;
+        }
+        if (!exact) {
+            normalize_any(C, gb, count, nvi, s);
+            if (!cuda_ok(cudaGetLastError(), "normalize launch")) return false;
+        }
+    }
+    return true;
+}
+
+// ---- SampleGridLut -------------------------------------------------------------
+struct LutK {
+    Dims dout;
+    int n_cam;      // cameras handled by this launch
+    int cam0;       // first lookup index (separate) or the batch index
+    int slot0;      // first output slot
+    int filter, mip_mode;
+    float bias, cco;
+    int relative, normalized;
+};
+
+__device__ __forceinline__ float4 lut_pos(const float* __restrict__ lut, int cam, int64_t v, int x, int y, int z,
+                                          const LutK& k) {
+    float4 p = __ldg(reinterpret_cast<const float4*>(lut) + (int64_t)cam * voxels(k.dout) + v);
+    if (k.normalized) {
+        p.x *= (float)k.dout.x;
+        p.y *= (float)k.dout.y;
+        p.z *= (float)k.dout.z;
+    }
+    if (k.relative) {
+        p.x += (float)x;
+        p.y += (float)y;
+        p.z += (float)z;
+    }
+    return p;
+}
+
+template <int C, typename S, int BM>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_lut_fwd(const float* __restrict__ lut, const LutK k, const MipSet ms, float* __restrict__ out) {
+    const int64_t nv = voxels(k.dout);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv * k.n_cam) return;
+    const int c = (int)(t / nv);
+    const int64_t v = t - (int64_t)c * nv;
+    const int x = (int)(v % k.dout.x), y = (int)((v / k.dout.x) % k.dout.y), z = (int)(v / ((int64_t)k.dout.x * k.dout.y));
+    const float4 pos = lut_pos(lut, k.cam0 + c, v, x, y, z, k);
+    const Vec<C> r = sample_mip<C, S, BM>(k.filter, k.mip_mode, ms, pos, k.bias, k.cco);
+    store<C>(out, (int64_t)(k.slot0 + c) * nv + v, r);
+}
+
+template <int C, typename S>
+static void lut_fwd_launch(int bm, unsigned blocks, cudaStream_t s, const float* lut, const LutK& k,
+                           const MipSet& ms, float* out) {
+    switch (bm) {
+        case BM_BORDER: k_lut_fwd<C, S, BM_BORDER><<<blocks, RS_THREADS, 0, s>>>(lut, k, ms, out); break;
+        case BM_CLAMP: k_lut_fwd<C, S, BM_CLAMP><<<blocks, RS_THREADS, 0, s>>>(lut, k, ms, out); break;
+        default: k_lut_fwd<C, S, BM_WRAP><<<blocks, RS_THREADS, 0, s>>>(lut, k, ms, out); break;
+    }
+}
+
+static LutK make_lutk(const LutArgs& a, int b) {
+    LutK k;
+    k.dout = a.dout;
+    k.n_cam = a.separate ? a.n_lut : 1;
+    k.cam0 = a.separate ? 0 : b;
+    k.slot0 = a.separate ? b * a.n_lut : b;
+    k.filter = a.filter;
+    k.mip_mode = a.mip_mode;
+    k.bias = a.mip_bias;
+    k.cco = a.cco;
+    k.relative = a.relative;
+    k.normalized = a.normalized;
+    return k;
+}
+
+bool launch_lut_fwd(const LutArgs& a, const float* lut, const MipSet* mips, float* out, cudaStream_t s) {
+    const int64_t nv = voxels(a.dout);
+    for (int b = 0; b < a.N; ++b) {
+        const LutK k = make_lutk(a, b);
+        const unsigned blocks = (unsigned)((nv * k.n_cam + RS_THREADS - 1) / RS_THREADS);
+        if (a.dtype == 0) {
+            if (a.C == 4) lut_fwd_launch<4, float>(a.boundary, blocks, s, lut, k, mips[b], out);
+            else if (a.C == 2) lut_fwd_launch<2, float>(a.boundary, blocks, s, lut, k, mips[b], out);
+            else lut_fwd_launch<1, float>(a.boundary, blocks, s, lut, k, mips[b], out);
+        } else {
+            if (a.C == 4) lut_fwd_launch<4, __nv_bfloat16>(a.boundary, blocks, s, lut, k, mips[b], out);
+            else if (a.C == 2) lut_fwd_launch<2, __nv_bfloat16>(a.boundary, blocks, s, lut, k, mips[b], out);
+            else lut_fwd_launch<1, __nv_bfloat16>(a.boundary, blocks, s, lut, k, mips[b], out);
+        }
+        if (!cuda_ok(cudaGetLastError(), "sample lut launch")) return false;
+    }
+    return true;
+}
+
+// kScatterLuT3DGradients: lookup gradient (LINEAR only, written) and trilinear
+// input-gradient scatter for every filter mode.
+template <int C, int BM, int COUNT>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_lut_bwd(const float* __restrict__ in, Dims din, const float* __restrict__ lut, const LutK k,
+              const float* __restrict__ dy, float* __restrict__ grad, float* __restrict__ lut_grad,
+              unsigned int* __restrict__ count) {
+    const int64_t nv = voxels(k.dout);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv * k.n_cam) return;
+    const int c = (int)(t / nv);
+    const int64_t v = t - (int64_t)c * nv;
+    const int x = (int)(v % k.dout.x), y = (int)((v / k.dout.x) % k.dout.y), z = (int)(v / ((int64_t)k.dout.x * k.dout.y));
+    const float4 pos = lut_pos(lut, k.cam0 + c, v, x, y, z, k);
+    const float px = pos.x - k.cco, py = pos.y - k.cco, pz = pos.z - k.cco;
+    const Vec<C> g = loadf<C>(dy, (int64_t)(k.slot0 + c) * nv + v);
+    if (k.filter == F_LINEAR) {
+        Vec<C> ddx, ddy, ddz;
+        fetch_grad<C, BM>(in, din, px, py, pz, ddx, ddy, ddz);
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            sx += g.v[i] * ddx.v[i];
+            sy += g.v[i] * ddy.v[i];
+            sz += g.v[i] * ddz.v[i];
+        }
+        reinterpret_cast<float4*>(lut_grad)[(int64_t)(k.cam0 + c) * nv + v] = make_float4(sx, sy, sz, 0.f);
+    }
+    scatter_linear<C, BM, COUNT>(grad, count, din, px, py, pz, g);
+}
+
+template <int C, int COUNT>
+static void lut_bwd_launch(int bm, unsigned blocks, cudaStream_t s, const float* in, Dims din, const float* lut,
+                           const LutK& k, const float* dy, float* grad, float* lut_grad, unsigned int* count) {
+    switch (bm) {
+        case BM_BORDER:
+            k_lut_bwd<C, BM_BORDER, COUNT><<<blocks, RS_THREADS, 0, s>>>(in, din, lut, k, dy, grad, lut_grad, count);
+            break;
+        case BM_CLAMP:
+            k_lut_bwd<C, BM_CLAMP, COUNT><<<blocks, RS_THREADS, 0, s>>>(in, din, lut, k, dy, grad, lut_grad, count);
+            break;
+        default:
+            k_lut_bwd<C, BM_WRAP, COUNT><<<blocks, RS_THREADS, 0, s>>>(in, din, lut, k, dy, grad, lut_grad, count);
+            break;
+    }
+}
+
+bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, const float* dy, bool exact,
+                    float* grad, float* lut_grad, unsigned int* count, cudaStream_t s) {
+    const int64_t nvi = voxels(a.din), nvo = voxels(a.dout);
+    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvi * a.C * a.N, s), "zero gradient")) return false;
+    if (!cuda_ok(cudaMemsetAsync(lut_grad, 0, sizeof(float) * 4 * nvo * a.n_lut, s), "zero lookup gradient"))
+        return false;
+    if (!exact && !cuda_ok(cudaMemsetAsync(count, 0, sizeof(unsigned int) * nvi, s), "zero counter")) return false;
+    for (int b = 0; b < a.N; ++b) {
+        const LutK k = make_lutk(a, b);
+        const float* inb = input + (size_t)b * nvi * a.C;
+        float* gb = grad + (size_t)b * nvi * a.C;
+        const unsigned blocks = (unsigned)((nvo * k.n_cam + RS_THREADS - 1) / RS_THREADS);
+        if (exact) {
+            if (a.C == 4) lut_bwd_launch<4, 0>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+            else if (a.C == 2) lut_bwd_launch<2, 0>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+            else lut_bwd_launch<1, 0>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+        } else {
+            if (a.C == 4) lut_bwd_launch<4, 1>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+            else if (a.C == 2) lut_bwd_launch<2, 1>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+            else lut_bwd_launch<1, 1>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
+        }
+        if (!cuda_ok(cudaGetLastError(), "sample lut gradient launch")) return false;
+        if (!exact) {
+            normalize_any(a.C, gb, count, nvi, s);
+            if (!cuda_ok(cudaGetLastError(), "normalize launch")) return false;
+        }
+    }
+    return true;
+}
+
+// ---- LodTransform ----------------------------------------------------------------
+// calcLoD (sampling.hpp:18-56): central differences, rows of the Jacobian.
+__global__ void __launch_bounds__(RS_THREADS)
+    k_lod_transform(Dims din, Dims dout, int cm, float* __restrict__ out, const __grid_constant__ PairTable tab) {
+    const int64_t nv = voxels(dout);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nv * tab.n) return;
+    const int p = (int)(t / nv);
+    const int64_t v = t - (int64_t)p * nv;
+    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const float3 dinf = make_float3((float)din.x, (float)din.y, (float)din.z);
+    const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
+    const CamX& c = tab.cam[p];
+    const float3 idx = make_float3(x + 0.5f, y + 0.5f, z + 0.5f);
+    const float3 pos = map_pos(c, cm, idx, dinf, dinv);
+    float3 d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float3 e = make_float3(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
+        const float3 m = map_pos(c, cm, make_float3(idx.x - e.x, idx.y - e.y, idx.z - e.z), dinf, dinv);
+        const float3 q = map_pos(c, cm, make_float3(idx.x + e.x, idx.y + e.y, idx.z + e.z), dinf, dinv);
+        d[a] = make_float3((m.x - q.x) * 0.5f, (m.y - q.y) * 0.5f, (m.z - q.z) * 0.5f);
+    }
+    const float px = sqrtf(d[0].x * d[0].x + d[1].x * d[1].x + d[2].x * d[2].x);
+    const float py = sqrtf(d[0].y * d[0].y + d[1].y * d[1].y + d[2].y * d[2].y);
+    const float pz = sqrtf(d[0].z * d[0].z + d[1].z * d[1].z + d[2].z * d[2].z);
+    const float lod = fmaxf(0.f, log2f(fmaxf(px, fmaxf(py, pz))));
+    reinterpret_cast<float4*>(out)[(int64_t)tab.out_slot[p] * nv + v] = make_float4(pos.x, pos.y, pos.z, lod);
+}
+
+bool launch_lod_transform(Dims din, Dims dout, const std::vector<Pair>& pairs, bool inverse, float* out,
+                          cudaStream_t s) {
+    const int64_t nv = voxels(dout);
+    for (const PairTable& t : make_tables(pairs)) {
+        const unsigned blocks = (unsigned)((nv * t.n + RS_THREADS - 1) / RS_THREADS);
+        k_lod_transform<<<blocks, RS_THREADS, 0, s>>>(din, dout, inverse ? CM_LINDEPTH_REVERSE : CM_LINDEPTH, out, t);
+        if (!cuda_ok(cudaGetLastError(), "lod transform launch")) return false;
+    }
+    return true;
+}
+
+}  // namespace gft

@@ -1,0 +1,110 @@
+"""ctypes binding of libgft.so (include/gft.h).
+
+The library is the only compute path: importing this module fails loudly when
+the shared object has not been built, and every call raises on a non-OK status.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libgft.so')
+
+# gft_status -> exception, mirroring TF's InvalidArgument / Unimplemented / Internal
+OK, ERR_INVALID_ARGUMENT, ERR_UNIMPLEMENTED, ERR_CUDA, ERR_WORKSPACE = 0, 1, 2, 3, 4
+
+
+class GftError(RuntimeError):
+    pass
+
+
+class GftInvalidArgument(GftError, ValueError):
+    pass
+
+
+class GftUnimplemented(GftError, NotImplementedError):
+    pass
+
+
+class GftCudaError(GftError):
+    pass
+
+
+_EXC = {ERR_INVALID_ARGUMENT: GftInvalidArgument, ERR_UNIMPLEMENTED: GftUnimplemented,
+        ERR_CUDA: GftCudaError, ERR_WORKSPACE: GftError}
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_F = ctypes.c_float
+_SZ = ctypes.c_size_t
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_I32P = ctypes.POINTER(ctypes.c_int32)
+
+# name -> (restype, argtypes)
+_SIGS = {
+    'gft_last_error': (ctypes.c_char_p, []),
+    'gft_version': (ctypes.c_char_p, []),
+    'gft_raymarch_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
+                                           _I32, _I32, _I32, _I32, _P, _P]),
+    'gft_raymarch_grid_transform_grad_workspace_size': (_SZ, [_I64P, _I32, _I32, _I32]),
+    'gft_raymarch_grid_transform_grad': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
+                                                _I32, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_sample_grid_transform_workspace_size': (_SZ, [_I64P, _I32, _I32]),
+    'gft_sample_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
+                                         _I32, _I32, _I32, _I32, _F, _I32, _F, _I32, _P, _P, _SZ, _P]),
+    'gft_sample_grid_transform_grad_workspace_size': (_SZ, [_I64P]),
+    'gft_sample_grid_transform_grad': (_I32, [_I64P, _P, _I64P, _P, _I32, _P, _P, _P, _I32,
+                                              _I32, _I32, _I32, _F, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_sample_grid_lut_workspace_size': (_SZ, [_I64P, _I32, _I32]),
+    'gft_sample_grid_lut': (_I32, [_P, _I32, _I64P, _P, _I64P, _I32, _I32, _I32, _I32, _F, _F,
+                                   _I32, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_sample_grid_lut_grad_workspace_size': (_SZ, [_I64P]),
+    'gft_sample_grid_lut_grad': (_I32, [_P, _I64P, _P, _P, _I64P, _I32, _I32, _F, _I32, _I32, _I32, _I32,
+                                        _P, _P, _P, _SZ, _P]),
+    'gft_lod_transform': (_I32, [_I32P, _P, _P, _P, _I32, _I32P, _I32, _P, _P]),
+    'gft_reduce_grid_blend': (_I32, [_P, _I64P, _I32, _I32, _P, _P]),
+    'gft_reduce_grid_blend_grad': (_I32, [_P, _P, _P, _I64P, _I32, _I32, _I32, _P, _P]),
+    'gft_advect_workspace_size': (_SZ, [_I64P, _I32]),
+    'gft_advect': (_I32, [_P, _I32, _I64P, _P, _P, _P, _F, _I32, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_advect_grad_workspace_size': (_SZ, [_I64P, _I32]),
+    'gft_advect_grad': (_I32, [_P, _I64P, _P, _P, _P, _F, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P,
+                               _P, _SZ, _P]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Loads libgft.so once; raises ImportError when it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError('libgft.so is not built (%s); run `python build.py` in the package directory '
+                          'or __graft_entry__.build()' % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def check(status, what):
+    if status != OK:
+        msg = load().gft_last_error().decode(errors='replace')
+        raise _EXC.get(status, GftError)('%s: %s' % (what, msg))
+
+
+def i64(vals):
+    vals = [int(v) for v in vals]
+    return (ctypes.c_int64 * len(vals))(*vals)
+
+
+def i32(vals):
+    vals = [int(v) for v in vals]
+    return (ctypes.c_int32 * len(vals))(*vals)

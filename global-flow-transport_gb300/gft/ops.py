@@ -1,0 +1,533 @@
+"""PyTorch-facing ops over libgft.so with the reference op signatures.
+
+Each forward op mirrors one TensorFlow op of the reference
+(phitest/render/cuda/ops_loader.py:11-85): same argument names, attribute
+strings and output layouts; the gradient ops are registered as the autograd
+backward exactly as ops_loader.py registers them with TF.  Tensors are CUDA
+tensors (NDHWC, fp32, or bf16 storage where noted); matrices and frustum
+parameters are host arrays as in the reference (HostMemory inputs).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+FILTER = {'NEAREST': 0, 'LINEAR': 1, 'MIN': 2, 'MAX': 3}
+BOUNDARY = {'BORDER': 0, 'CLAMP': 1, 'WRAP': 2}
+MIP = {'NONE': 0, 'NEAREST': 1, 'LINEAR': 2}
+BLEND = {'BEER_LAMBERT': 0, 'BEER_LAMBERT_EXCLUSIVE': 1, 'ALPHA': 2, 'ALPHA_ADDITIVE': 3, 'ADDITIVE': 4}
+COORD = {'TRANSFORM_LINDEPTH': 0, 'TRANSFORM_LINDEPTH_REVERSE': 1, 'TRANSFORM': 3, 'TRANSFORM_REVERSE': 4}
+GRAD = {'REFERENCE': 0, 'EXACT': 1}
+CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
+
+_state = {'grad_mode': 'REFERENCE'}
+
+
+def set_grad_mode(mode):
+    """'REFERENCE' (default): gradients normalised like the reference ops;
+    'EXACT': true adjoints of the forward ops."""
+    mode = mode.upper()
+    if mode not in GRAD:
+        raise ValueError(mode)
+    _state['grad_mode'] = mode
+
+
+def get_grad_mode():
+    return _state['grad_mode']
+
+
+class grad_mode:
+    """Context manager switching the gradient mode."""
+
+    def __init__(self, mode):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = get_grad_mode()
+        set_grad_mode(self.mode)
+
+    def __exit__(self, *a):
+        set_grad_mode(self.prev)
+
+
+def _enum(table, v, what):
+    if isinstance(v, bytes):
+        v = v.decode()
+    if isinstance(v, str):
+        key = v.upper()
+        if key not in table:
+            raise _lib.GftInvalidArgument('invalid %s %r' % (what, v))
+        return table[key]
+    return int(v)
+
+
+def _host(x, tail):
+    if isinstance(x, torch.Tensor):
+        x = x.detach().cpu().numpy()
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    if a.shape == tail:
+        a = a[None]
+    if a.shape[1:] != tail:
+        raise _lib.GftInvalidArgument('expected shape %s or (K,)+%s, got %s' % (tail, tail, a.shape))
+    return a
+
+
+def _mats(m):
+    a = _host(m, (4, 4))
+    return a, a.shape[0]
+
+
+def _frustum(f):
+    a = _host(f, (6,))
+    return a, a.shape[0]
+
+
+def _p(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    return ctypes.c_void_p(a.data_ptr())
+
+
+def _cuda(t, name, dtypes=(torch.float32,)):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise _lib.GftInvalidArgument('%s must be a CUDA tensor' % name)
+    if t.dtype not in dtypes:
+        raise _lib.GftInvalidArgument('%s must have dtype in %s, got %s' % (name, dtypes, t.dtype))
+    return t.contiguous()
+
+
+def _dtype_code(t):
+    return 1 if t.dtype == torch.bfloat16 else 0
+
+
+def _stream(dev):
+    return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+
+def _workspace(nbytes, dev):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=dev)
+
+
+def _shape3(s):
+    s = [int(v) for v in (s.tolist() if isinstance(s, (np.ndarray, torch.Tensor)) else s)]
+    if len(s) != 3:
+        raise _lib.GftInvalidArgument('Invalid output_shape')
+    return s
+
+
+def _storage(x, storage_dtype):
+    if storage_dtype is None or storage_dtype == x.dtype:
+        return x
+    return x.to(storage_dtype)
+
+
+# ------------------------------------------------------------------ raymarch
+def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate):
+    lib = _lib.load()
+    D, H, W = out_shape
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, npj = _mats(P)
+    Fh, nf = _frustum(F)
+    if not (nv == npj == nf):
+        raise _lib.GftInvalidArgument('camera batch size mismatch')
+    N, C = x.shape[0], x.shape[4]
+    out = torch.empty((N, nv if separate else 1, H, W, C), dtype=torch.float32, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform(_p(x), _dtype_code(x), _lib.i64(x.shape), _p(Mh), nm, _p(Vh), _p(Ph),
+                                             _p(Fh), nv, _lib.i32(out_shape), interp, boundary, blend, int(separate),
+                                             _p(out), _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransform')
+    return out
+
+
+def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode):
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, _ = _mats(P)
+    Fh, _ = _frustum(F)
+    shape = _lib.i64(x.shape)
+    grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    ws_n = lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode)
+    ws = _workspace(ws_n, x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_grad(_p(x), _dtype_code(x), shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
+                                                  _p(Ph), _p(Fh), nv, _lib.i32(out_shape), interp, boundary, blend,
+                                                  int(separate), gmode, _p(grad), _p(ws), ws.numel(),
+                                                  _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformGrad')
+    return grad
+
+
+class _Raymarch(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype):
+        xs = _storage(x, storage_dtype)
+        y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate)
+        ctx.save_for_backward(xs, y)
+        ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate)
+        ctx.in_dtype = x.dtype
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        xs, y = ctx.saved_tensors
+        M, V, P, F, out_shape, interp, boundary, blend, separate = ctx.args
+        g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
+                          GRAD[get_grad_mode()])
+        return (g.to(ctx.in_dtype),) + (None,) * 10
+
+
+def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
+                            interpolation='LINEAR', boundary='BORDER', blending_mode='BEER_LAMBERT',
+                            keep_dims=False, separate_camera_batch=True, storage_dtype=None):
+    """RaymarchGridTransform: [N,D,H,W,C] -> [N,V,H,W,C] ([N,V,1,H,W,C] with keep_dims).
+    ``storage_dtype=torch.bfloat16`` stores the sampled grid in bf16 (fp32 math)."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    if x.dim() != 5 or x.shape[4] > 4:
+        raise _lib.GftInvalidArgument('Invalid input shape (NDHWC): %s' % (tuple(x.shape),))
+    out_shape = _shape3(output_shape)
+    y = _Raymarch.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, out_shape,
+                        _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                        _enum(BLEND, blending_mode, 'blending_mode'), bool(separate_camera_batch), storage_dtype)
+    return y.unsqueeze(2) if keep_dims else y
+
+
+def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
+                                 output_shape, interpolation='LINEAR', boundary='BORDER',
+                                 blending_mode='BEER_LAMBERT', keep_dims=False, separate_camera_batch=True):
+    """RaymarchGridTransformGrad (raymarch_grid.cc:56-76)."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    y = _cuda(output, 'output')
+    dy = _cuda(output_grad, 'output_grad')
+    if keep_dims:
+        y, dy = y.squeeze(2), dy.squeeze(2)
+    if tuple(y.shape) != tuple(dy.shape):
+        raise _lib.GftInvalidArgument('Shapes of output grid and output gradients must match')
+    return _raymarch_bwd(x, y.contiguous(), dy.contiguous(), matrix_m, matrix_v, matrix_p, frustum_params,
+                         _shape3(output_shape), _enum(FILTER, interpolation, 'interpolation'),
+                         _enum(BOUNDARY, boundary, 'boundary'), _enum(BLEND, blending_mode, 'blending_mode'),
+                         bool(separate_camera_batch), GRAD[get_grad_mode()])
+
+
+# ------------------------------------------------------------------ SampleGridTransform
+def _sample_transform_fwd(x, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco, separate):
+    lib = _lib.load()
+    Do, Ho, Wo = out_shape
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, npj = _mats(P)
+    Fh, nf = _frustum(F)
+    if not (nv == npj == nf):
+        raise _lib.GftInvalidArgument('camera batch size mismatch')
+    N, C = x.shape[0], x.shape[4]
+    shape = _lib.i64(x.shape)
+    out = torch.empty((N, nv if separate else 1, Do, Ho, Wo, C), dtype=torch.float32, device=x.device)
+    ws = _workspace(lib.gft_sample_grid_transform_workspace_size(shape, mip, num_mips), x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_sample_grid_transform(_p(x), _dtype_code(x), shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
+                                           _lib.i32(out_shape), interp, boundary, mip, int(num_mips), float(bias),
+                                           coord, float(cco), int(separate), _p(out), _p(ws), ws.numel(),
+                                           _stream(x.device))
+    _lib.check(st, 'SampleGridTransform')
+    return out
+
+
+def _sample_transform_bwd(in_shape, dy, M, V, P, F, interp, boundary, coord, cco, separate, gmode, device):
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, _ = _mats(P)
+    Fh, _ = _frustum(F)
+    shape = _lib.i64(in_shape)
+    grad = torch.empty(tuple(in_shape), dtype=torch.float32, device=device)
+    ws = _workspace(lib.gft_sample_grid_transform_grad_workspace_size(shape), device)
+    with torch.cuda.device(device):
+        st = lib.gft_sample_grid_transform_grad(shape, _p(dy), _lib.i64(dy.shape), _p(Mh), nm, _p(Vh), _p(Ph),
+                                                _p(Fh), nv, interp, boundary, coord, float(cco), int(separate),
+                                                gmode, _p(grad), _p(ws), ws.numel(), _stream(device))
+    _lib.check(st, 'SampleGridTransformGrad')
+    return grad
+
+
+class _SampleTransform(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco, separate,
+                storage_dtype):
+        xs = _storage(x, storage_dtype)
+        y = _sample_transform_fwd(xs, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco,
+                                  separate)
+        ctx.args = (tuple(x.shape), M, V, P, F, interp, boundary, mip, coord, cco, separate)
+        ctx.in_dtype = x.dtype
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        in_shape, M, V, P, F, interp, boundary, mip, coord, cco, separate = ctx.args
+        if mip != MIP['NONE']:
+            # the registered gradient op only accepts mipmapping NONE (resample_grid.cc:73)
+            raise _lib.GftInvalidArgument('SampleGridTransformGrad: mipmapping must be NONE')
+        g = _sample_transform_bwd(in_shape, _cuda(dy, 'output_grad'), M, V, P, F, interp, boundary, coord, cco,
+                                  separate, GRAD[get_grad_mode()], dy.device)
+        return (g.to(ctx.in_dtype),) + (None,) * 14
+
+
+def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
+                          interpolation='LINEAR', boundary='BORDER', mipmapping='NONE', num_mipmaps=0, mip_bias=0.0,
+                          coordinate_mode='TRANSFORM_LINDEPTH', cell_center_offset=0.5, separate_camera_batch=True,
+                          storage_dtype=None):
+    """SampleGridTransform: [N,D,H,W,C] -> [N, V (or 1), Do, Ho, Wo, C]."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    if x.dim() != 5 or x.shape[4] > 4:
+        raise _lib.GftInvalidArgument('Invalid input shape (NDHWC): %s' % (tuple(x.shape),))
+    return _SampleTransform.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, _shape3(output_shape),
+                                  _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                                  _enum(MIP, mipmapping, 'mipmapping'), int(num_mipmaps), float(mip_bias),
+                                  _enum(COORD, coordinate_mode, 'coordinate_mode'), float(cell_center_offset),
+                                  bool(separate_camera_batch), storage_dtype)
+
+
+def sample_grid_transform_grad(input, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
+                               interpolation='LINEAR', boundary='BORDER', mipmapping='NONE', num_mipmaps=0,
+                               mip_bias=0.0, coordinate_mode='TRANSFORM_LINDEPTH', cell_center_offset=0.5,
+                               separate_camera_batch=True):
+    """SampleGridTransformGrad (resample_grid.cc:64-84): trilinear scatter adjoint."""
+    if _enum(MIP, mipmapping, 'mipmapping') != MIP['NONE']:
+        raise _lib.GftInvalidArgument('SampleGridTransformGrad: mipmapping must be NONE')
+    dy = _cuda(output_grad, 'output_grad')
+    if dy.dim() != 6:
+        raise _lib.GftInvalidArgument('Invalid output_grads shape (NVDHWC)')
+    return _sample_transform_bwd(tuple(input.shape), dy, matrix_m, matrix_v, matrix_p, frustum_params,
+                                 _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                                 _enum(COORD, coordinate_mode, 'coordinate_mode'), float(cell_center_offset),
+                                 bool(separate_camera_batch), GRAD[get_grad_mode()], dy.device)
+
+
+# ------------------------------------------------------------------ SampleGridLut
+def _lut_fwd(x, lut, interp, boundary, mip, num_mips, bias, cco, separate, relative, normalized):
+    lib = _lib.load()
+    N, C = x.shape[0], x.shape[4]
+    V = lut.shape[0]
+    shape = _lib.i64(x.shape)
+    out = torch.empty((N, V if separate else 1) + tuple(lut.shape[1:4]) + (C,), dtype=torch.float32,
+                      device=x.device)
+    ws = _workspace(lib.gft_sample_grid_lut_workspace_size(shape, mip, num_mips), x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_sample_grid_lut(_p(x), _dtype_code(x), shape, _p(lut), _lib.i64(lut.shape), interp, boundary,
+                                     mip, int(num_mips), float(bias), float(cco), int(separate), int(relative),
+                                     int(normalized), _p(out), _p(ws), ws.numel(), _stream(x.device))
+    _lib.check(st, 'SampleGridLut')
+    return out
+
+
+def _lut_bwd(x, lut, dy, interp, boundary, cco, separate, relative, normalized, gmode):
+    lib = _lib.load()
+    shape = _lib.i64(x.shape)
+    gx = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    glut = torch.empty(lut.shape, dtype=torch.float32, device=x.device)
+    ws = _workspace(lib.gft_sample_grid_lut_grad_workspace_size(shape), x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_sample_grid_lut_grad(_p(x), shape, _p(dy), _p(lut), _lib.i64(lut.shape), interp, boundary,
+                                          float(cco), int(separate), int(relative), int(normalized), gmode, _p(gx),
+                                          _p(glut), _p(ws), ws.numel(), _stream(x.device))
+    _lib.check(st, 'SampleGridLutGrad')
+    return gx, glut
+
+
+class _SampleLut(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, lut, interp, boundary, mip, num_mips, bias, cco, separate, relative, normalized,
+                storage_dtype):
+        xs = _storage(x, storage_dtype)
+        y = _lut_fwd(xs, lut, interp, boundary, mip, num_mips, bias, cco, separate, relative, normalized)
+        ctx.save_for_backward(x, lut)
+        ctx.args = (interp, boundary, mip, cco, separate, relative, normalized)
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        x, lut = ctx.saved_tensors
+        interp, boundary, mip, cco, separate, relative, normalized = ctx.args
+        if mip != MIP['NONE']:
+            raise _lib.GftInvalidArgument('SampleGridLutGrad: mipmapping must be NONE')
+        gx, glut = _lut_bwd(x.float(), lut, _cuda(dy, 'output_grad'), interp, boundary, cco, separate, relative,
+                            normalized, GRAD[get_grad_mode()])
+        return (gx.to(x.dtype), glut) + (None,) * 10
+
+
+def sample_grid_lut(input, lookup, interpolation='LINEAR', boundary='BORDER', mipmapping='NONE', num_mipmaps=0,
+                    mip_bias=0.0, coordinate_mode='LOOKUP', cell_center_offset=0.0, separate_camera_batch=True,
+                    relative_coords=True, normalized_coords=False, storage_dtype=None):
+    """SampleGridLut: input [N,D,H,W,C], lookup [V,Do,Ho,Wo,4] -> [N, V (or 1), Do, Ho, Wo, C]."""
+    if str(coordinate_mode).upper() != 'LOOKUP':
+        raise _lib.GftInvalidArgument('Invalid coorindate_mode')
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    lut = _cuda(lookup, 'lookup')
+    if x.dim() != 5 or lut.dim() != 5 or lut.shape[4] != 4:
+        raise _lib.GftInvalidArgument('Invalid lut shape (NDHWC) with C=4')
+    return _SampleLut.apply(x, lut, _enum(FILTER, interpolation, 'interpolation'),
+                            _enum(BOUNDARY, boundary, 'boundary'), _enum(MIP, mipmapping, 'mipmapping'),
+                            int(num_mipmaps), float(mip_bias), float(cell_center_offset),
+                            bool(separate_camera_batch), bool(relative_coords), bool(normalized_coords), storage_dtype)
+
+
+def sample_grid_lut_grad(input, output_grad, lookup, interpolation='LINEAR', boundary='BORDER', mipmapping='NONE',
+                         num_mipmaps=0, mip_bias=0.0, coordinate_mode='LOOKUP', cell_center_offset=0.0,
+                         separate_camera_batch=True, relative_coords=True, normalized_coords=False):
+    """SampleGridLutGrad: returns (input_grad, lookup_grad)."""
+    if _enum(MIP, mipmapping, 'mipmapping') != MIP['NONE']:
+        raise _lib.GftInvalidArgument('SampleGridLutGrad: mipmapping must be NONE')
+    x = _cuda(input, 'input')
+    return _lut_bwd(x, _cuda(lookup, 'lookup'), _cuda(output_grad, 'output_grad'),
+                    _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                    float(cell_center_offset), bool(separate_camera_batch), bool(relative_coords),
+                    bool(normalized_coords), GRAD[get_grad_mode()])
+
+
+def lod_transform(input_shape, matrix_mv, matrix_p, frustum_params, output_shape, inverse_transform=False,
+                  device=None):
+    """LodTransform: [V, Do, Ho, Wo, 4] of sampling positions and LOD."""
+    lib = _lib.load()
+    dev = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
+    MVh, n = _mats(matrix_mv)
+    Ph, npj = _mats(matrix_p)
+    Fh, nf = _frustum(frustum_params)
+    if not (n == npj == nf):
+        raise _lib.GftInvalidArgument('camera batch size mismatch')
+    ins, outs = _shape3(input_shape), _shape3(output_shape)
+    out = torch.empty((n,) + tuple(outs) + (4,), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        st = lib.gft_lod_transform(_lib.i32(ins), _p(MVh), _p(Ph), _p(Fh), n, _lib.i32(outs), int(inverse_transform),
+                                   _p(out), _stream(dev))
+    _lib.check(st, 'LodTransform')
+    return out
+
+
+# ------------------------------------------------------------------ ReduceGridBlend
+def _blend_fwd(x, mode, keep):
+    lib = _lib.load()
+    N, D, H, W, C = x.shape
+    out = torch.empty((N, D, H, W, C) if keep else (N, H, W, C), dtype=torch.float32, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_reduce_grid_blend(_p(x), _lib.i64(x.shape), mode, int(keep), _p(out), _stream(x.device))
+    _lib.check(st, 'ReduceGridBlend')
+    return out
+
+
+def _blend_bwd(dy, y, x, mode, keep, gmode):
+    lib = _lib.load()
+    gx = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_reduce_grid_blend_grad(_p(dy), _p(y), _p(x), _lib.i64(x.shape), mode, int(keep), gmode, _p(gx),
+                                            _stream(x.device))
+    _lib.check(st, 'ReduceGridBlendGrad')
+    return gx
+
+
+class _Blend(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, mode, keep):
+        y = _blend_fwd(x, mode, keep)
+        ctx.save_for_backward(x, y)
+        ctx.args = (mode, keep)
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        x, y = ctx.saved_tensors
+        mode, keep = ctx.args
+        return _blend_bwd(_cuda(dy, 'output_grad'), y, x, mode, keep, GRAD[get_grad_mode()]), None, None
+
+
+def reduce_grid_blend(input, blending_mode='BEER_LAMBERT', keep_dims=False):
+    """ReduceGridBlend: [N,D,H,W,C] -> [N,H,W,C] or [N,D,H,W,C] (keep_dims)."""
+    x = _cuda(input, 'input')
+    if x.dim() != 5 or x.shape[4] > 4:
+        raise _lib.GftInvalidArgument('Invalid input shape')
+    return _Blend.apply(x, _enum(BLEND, blending_mode, 'blending_mode'), bool(keep_dims))
+
+
+def reduce_grid_blend_grad(output_grad, output, input, blending_mode='BEER_LAMBERT', keep_dims=False):
+    """ReduceGridBlendGrad (reduce_blend.cc:37-48)."""
+    dy = _cuda(output_grad, 'output_grad')
+    y = _cuda(output, 'output')
+    if tuple(dy.shape) != tuple(y.shape):
+        raise _lib.GftInvalidArgument('Mismatch between output gradients and output shape')
+    return _blend_bwd(dy, y, _cuda(input, 'input'), _enum(BLEND, blending_mode, 'blending_mode'), bool(keep_dims),
+                      GRAD[get_grad_mode()])
+
+
+# ------------------------------------------------------------------ advection
+def _advect_fwd(d, vx, vy, vz, dt, order, clamp, boundary):
+    lib = _lib.load()
+    shape = _lib.i64(d.shape)
+    out = torch.empty(d.shape, dtype=torch.float32, device=d.device)
+    ws = _workspace(lib.gft_advect_workspace_size(shape, order), d.device)
+    with torch.cuda.device(d.device):
+        st = lib.gft_advect(_p(d), _dtype_code(d), shape, _p(vx), _p(vy), _p(vz), float(dt), order, clamp, boundary,
+                            _p(out), _p(ws), ws.numel(), _stream(d.device))
+    _lib.check(st, 'advect')
+    return out
+
+
+def _advect_bwd(d, vx, vy, vz, dy, dt, order, clamp, boundary, gmode):
+    lib = _lib.load()
+    shape = _lib.i64(d.shape)
+    gd = torch.empty(d.shape, dtype=torch.float32, device=d.device)
+    gvx, gvy, gvz = (torch.empty(v.shape, dtype=torch.float32, device=d.device) for v in (vx, vy, vz))
+    ws = _workspace(lib.gft_advect_grad_workspace_size(shape, order), d.device)
+    with torch.cuda.device(d.device):
+        st = lib.gft_advect_grad(_p(d), shape, _p(vx), _p(vy), _p(vz), float(dt), order, clamp, boundary, gmode,
+                                 _p(dy), _p(gd), _p(gvx), _p(gvy), _p(gvz), _p(ws), ws.numel(), _stream(d.device))
+    _lib.check(st, 'advect gradient')
+    return gd, gvx, gvy, gvz
+
+
+def _vel_component(v, name, expect):
+    v = _cuda(v, name)
+    if v.numel() != int(np.prod(expect)):
+        raise _lib.GftInvalidArgument('Invalid shape of velocity %s component: %s, expected %s'
+                                      % (name, tuple(v.shape), expect))
+    return v
+
+
+class _Advect(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, d, vx, vy, vz, dt, order, clamp, boundary, storage_dtype):
+        ds = _storage(d, storage_dtype)
+        y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary)
+        ctx.save_for_backward(d, vx, vy, vz)
+        ctx.args = (dt, order, clamp, boundary)
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        d, vx, vy, vz = ctx.saved_tensors
+        dt, order, clamp, boundary = ctx.args
+        gd, gvx, gvy, gvz = _advect_bwd(d.float().contiguous(), vx, vy, vz, _cuda(dy, 'output_grad'), dt, order,
+                                        clamp, boundary, GRAD[get_grad_mode()])
+        return gd.to(d.dtype), gvx.view_as(vx), gvy.view_as(vy), gvz.view_as(vz), None, None, None, None, None
+
+
+def advect(density, vel_x, vel_y, vel_z, dt=1.0, order=1, clamp='NONE', boundary='CLAMP', storage_dtype=None):
+    """VelocityGrid.warp fused: density [N,D,H,W,C] advected by the staggered
+    velocity x [..,D,H,W+1,1], y [..,D,H+1,W,1], z [..,D+1,H,W,1] (leading batch
+    dims of the components must be 1).  order 1 semi-Lagrangian, 2 MacCormack;
+    clamp NONE / MC_SMOOTH / NEGATIVE."""
+    d = _cuda(density, 'density', (torch.float32, torch.bfloat16))
+    if d.dim() != 5:
+        raise _lib.GftInvalidArgument('density must be 5D (NDHWC)')
+    _, D, H, W, _ = d.shape
+    vx = _vel_component(vel_x, 'x', (D, H, W + 1))
+    vy = _vel_component(vel_y, 'y', (D, H + 1, W))
+    vz = _vel_component(vel_z, 'z', (D + 1, H, W))
+    c = str(clamp).upper()
+    if c == 'MC':
+        raise NotImplementedError('MIM and MAX warp sampling have wrong gradients.')
+    return _Advect.apply(d, vx, vy, vz, float(dt), int(order), _enum(CLAMP, c, 'clamp'),
+                         _enum(BOUNDARY, boundary, 'boundary'), storage_dtype)

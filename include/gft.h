@@ -1,0 +1,194 @@
+/*
+ * gft.h -- C ABI of the GB300 render + advect hot path (libgft.so).
+ *
+ * Every entry point replaces one op of the reference's TensorFlow custom-op
+ * libraries (phitest/render/cuda/src/{resample_grid,reduce_blend,raymarch_grid}.cc)
+ * with the same inputs, attributes and output layout, as plain pointers:
+ *
+ *   - tensors are NDHWC, channel counts C in {1, 2, 4} (C == 3 is rejected as in
+ *     resample_grid.cc:330-331);
+ *   - tensor data pointers are DEVICE pointers; the caller allocates every
+ *     output, gradient and workspace buffer (query sizes with *_workspace_size);
+ *   - 4x4 matrices and frustum parameters are HOST pointers (the reference
+ *     declares them HostMemory, resample_grid.cc:1070-1105): 16 floats read
+ *     column-major, i.e. numpy ``matrix.transpose()`` flattened, as
+ *     phitest/render/renderer.py:108-111 passes them; frustum = [near, far,
+ *     left, right, top, bottom] (camera.py:61-62);
+ *   - ``stream`` is a cudaStream_t (NULL = legacy default stream); every call is
+ *     stream-ordered, never synchronises the device, allocates no device memory
+ *     and keeps no per-call global state, so calls are re-entrant and can be
+ *     captured into CUDA graphs;
+ *   - every function returns a gft_status and never exits the process; the
+ *     message of the last failure on the calling thread is gft_last_error().
+ *
+ * Enum values equal the reference's (sampling_settings_v2.hpp:9-10,
+ * sampling_settings.hpp:14-18 and :56-65, blending_settings.hpp:6-12).
+ */
+#ifndef GFT_H
+#define GFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef enum {
+    GFT_OK = 0,
+    GFT_ERR_INVALID_ARGUMENT = 1, /* TF errors::InvalidArgument */
+    GFT_ERR_UNIMPLEMENTED = 2,    /* TF errors::Unimplemented */
+    GFT_ERR_CUDA = 3,             /* TF errors::Internal after a CUDA failure */
+    GFT_ERR_WORKSPACE = 4         /* workspace missing or too small */
+} gft_status;
+
+typedef enum { GFT_FILTER_NEAREST = 0, GFT_FILTER_LINEAR = 1, GFT_FILTER_MIN = 2, GFT_FILTER_MAX = 3 } gft_filter;
+typedef enum { GFT_BOUNDARY_BORDER = 0, GFT_BOUNDARY_CLAMP = 1, GFT_BOUNDARY_WRAP = 2 } gft_boundary;
+typedef enum { GFT_MIP_NONE = 0, GFT_MIP_NEAREST = 1, GFT_MIP_LINEAR = 2 } gft_mip;
+typedef enum {
+    GFT_BLEND_BEER_LAMBERT = 0,
+    GFT_BLEND_BEER_LAMBERT_EXCLUSIVE = 1,
+    GFT_BLEND_ALPHA = 2,
+    GFT_BLEND_ALPHA_ADDITIVE = 3,
+    GFT_BLEND_ADDITIVE = 4
+} gft_blend;
+typedef enum {
+    GFT_COORD_TRANSFORM_LINDEPTH = 0,
+    GFT_COORD_TRANSFORM_LINDEPTH_REVERSE = 1,
+    GFT_COORD_TRANSFORM = 3,
+    GFT_COORD_TRANSFORM_REVERSE = 4
+} gft_coord;
+/* Storage type of density-like inputs; all arithmetic is fp32. */
+typedef enum { GFT_DTYPE_F32 = 0, GFT_DTYPE_BF16 = 1 } gft_dtype;
+/* GFT_GRAD_REFERENCE reproduces the reference's gradient normalisations
+ * (per-voxel sample count for resample/lookup, resample_grid.cu.cc:814-832;
+ * per-camera sum of trilinear weights for raymarch, raymarch_grid.cu.cc:519-568).
+ * GFT_GRAD_EXACT returns the true adjoint of the forward op. */
+typedef enum { GFT_GRAD_REFERENCE = 0, GFT_GRAD_EXACT = 1 } gft_grad_mode;
+/* MacCormack clamp of VelocityGrid.warp (data_structures.py:870-905). */
+typedef enum { GFT_CLAMP_NONE = 0, GFT_CLAMP_MC_SMOOTH = 1, GFT_CLAMP_NEGATIVE = 2 } gft_clamp;
+
+const char* gft_last_error(void);
+const char* gft_version(void);
+
+/* ---- RaymarchGridTransform (raymarch_grid.cc:28-52, launcher raymarch_grid.cu.cc:222-294) ----
+ * input  [N, D, H, W, C] (input_dtype storage)
+ * matrix_m num_m x 16 (num_m == N), matrix_v / matrix_p num_cameras x 16, frustum num_cameras x 6
+ * output_shape = (depth samples, height, width)
+ * output [N, separate_camera_batch ? num_cameras : 1, height, width, C] fp32 */
+gft_status gft_raymarch_grid_transform(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
+    float* output, void* stream);
+
+/* ---- RaymarchGridTransformGrad (raymarch_grid.cc:56-76, launcher raymarch_grid.cu.cc:451-574) ----
+ * output / output_grad are the forward result and its gradient (same shape as the
+ * forward output); input_grad [N, D, H, W, C] fp32 is overwritten.
+ * LINEAR interpolation only (raymarch_grid.cc:65). */
+size_t gft_raymarch_grid_transform_grad_workspace_size(
+    const int64_t input_shape[5], int32_t num_cameras, int32_t separate_camera_batch, int32_t grad_mode);
+gft_status gft_raymarch_grid_transform_grad(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* output, const float* output_grad,
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
+    int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- SampleGridTransform (resample_grid.cc:23-61, :268-447; launcher resample_grid.cu.cc:289-438) ----
+ * output [N, separate_camera_batch ? num_cameras : 1, Do, Ho, Wo, C] fp32.
+ * The workspace holds the mip pyramid (empty without mips). */
+size_t gft_sample_grid_transform_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps);
+gft_status gft_sample_grid_transform(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t mipmapping, int32_t num_mipmaps, float mip_bias,
+    int32_t coordinate_mode, float cell_center_offset, int32_t separate_camera_batch,
+    float* output, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- SampleGridTransformGrad (resample_grid.cc:64-84, :469-625; launcher resample_grid.cu.cc:863-1018) ----
+ * Trilinear scatter adjoint (no mips, as the reference op).  output_grad
+ * [N, V or 1, Do, Ho, Wo, C]; input_grad [N, D, H, W, C] overwritten. */
+size_t gft_sample_grid_transform_grad_workspace_size(const int64_t input_shape[5]);
+gft_status gft_sample_grid_transform_grad(
+    const int64_t input_shape[5], const float* output_grad, const int64_t output_grad_shape[6],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras,
+    int32_t interpolation, int32_t boundary, int32_t coordinate_mode, float cell_center_offset,
+    int32_t separate_camera_batch, int32_t grad_mode,
+    float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- SampleGridLut (resample_grid.cc:86-109, :650-802; launcher resample_grid.cu.cc:498-660) ----
+ * lookup [V, Do, Ho, Wo, 4] fp32 (x, y, z, LOD); output [N, V or 1, Do, Ho, Wo, C] fp32. */
+size_t gft_sample_grid_lut_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps);
+gft_status gft_sample_grid_lut(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* lookup, const int64_t lookup_shape[5],
+    int32_t interpolation, int32_t boundary, int32_t mipmapping, int32_t num_mipmaps, float mip_bias,
+    float cell_center_offset, int32_t separate_camera_batch, int32_t relative_coords, int32_t normalized_coords,
+    float* output, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- SampleGridLutGrad (resample_grid.cc:113-134, :828-979; launcher resample_grid.cu.cc:1083-1251) ----
+ * input_grad [N, D, H, W, C] and lookup_grad [V, Do, Ho, Wo, 4] overwritten. */
+size_t gft_sample_grid_lut_grad_workspace_size(const int64_t input_shape[5]);
+gft_status gft_sample_grid_lut_grad(
+    const float* input, const int64_t input_shape[5], const float* output_grad,
+    const float* lookup, const int64_t lookup_shape[5],
+    int32_t interpolation, int32_t boundary, float cell_center_offset,
+    int32_t separate_camera_batch, int32_t relative_coords, int32_t normalized_coords, int32_t grad_mode,
+    float* input_grad, float* lookup_grad, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- LodTransform (resample_grid.cc:136-154, :986-1064; kComputeLoD3D resample_grid.cu.cc:1288-1363) ----
+ * output [num, Do, Ho, Wo, 4]: sampling position (xyz) and LOD (w). */
+gft_status gft_lod_transform(
+    const int32_t input_shape[3], const float* matrix_mv, const float* matrix_p, const float* frustum,
+    int32_t num, const int32_t output_shape[3], int32_t inverse_transform, float* output, void* stream);
+
+/* ---- ReduceGridBlend / ReduceGridBlendGrad (reduce_blend.cc:23-48; reduce_blend.cu.cc:34-244) ----
+ * input [N, D, H, W, C]; output [N, D, H, W, C] (keep_dims) or [N, H, W, C]. */
+gft_status gft_reduce_grid_blend(
+    const float* input, const int64_t input_shape[5], int32_t blending_mode, int32_t keep_dims,
+    float* output, void* stream);
+gft_status gft_reduce_grid_blend_grad(
+    const float* output_grad, const float* output, const float* input, const int64_t input_shape[5],
+    int32_t blending_mode, int32_t keep_dims, int32_t grad_mode, float* input_grad, void* stream);
+
+/* ---- Fused advection (VelocityGrid.warp, data_structures.py:870-905) ----
+ * The reference composes it from SampleGridLut calls (renderer.py:445-460) on
+ * lut = -dt * centered(v) (:819-833, :864-868); here one fused pass per stage.
+ * density [N, D, H, W, C] (density_dtype); velocity components fp32 staggered
+ * x [D, H, W+1], y [D, H+1, W], z [D+1, H, W] (shared by the N batch slices);
+ * order 1 = semi-Lagrangian, 2 = MacCormack; boundary of the lookups. */
+size_t gft_advect_workspace_size(const int64_t density_shape[5], int32_t order);
+gft_status gft_advect(
+    const void* density, int32_t density_dtype, const int64_t density_shape[5],
+    const float* vel_x, const float* vel_y, const float* vel_z, float dt,
+    int32_t order, int32_t clamp, int32_t boundary,
+    float* output, void* workspace, size_t workspace_bytes, void* stream);
+/* Gradient of gft_advect w.r.t. density and the staggered velocity components,
+ * all overwritten.  In GFT_GRAD_REFERENCE mode each lookup's input gradient is
+ * divided by its per-voxel sample count as the reference SampleGridLutGrad does. */
+size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t order);
+gft_status gft_advect_grad(
+    const float* density, const int64_t density_shape[5],
+    const float* vel_x, const float* vel_y, const float* vel_z, float dt,
+    int32_t order, int32_t clamp, int32_t boundary, int32_t grad_mode,
+    const float* output_grad,
+    float* density_grad, float* vel_x_grad, float* vel_y_grad, float* vel_z_grad,
+    void* workspace, size_t workspace_bytes, void* stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GFT_H */

@@ -1,0 +1,276 @@
+"""CUDA path (libgft.so via gft.ops) vs the FP64 oracle on small seeded cases.
+
+Tolerances: forward rel-L2 <= 1e-5 (fp32 storage) and <= 1e-2 (bf16 storage);
+gradients rel-L2 <= 1e-4 (fp32 atomics change only the summation order).
+"""
+import numpy as np
+import pytest
+import torch
+
+from scene_utils import rel_l2, scene, small_grid
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = 1e-5
+BF16_TOL = 1e-2
+GRAD_TOL = 1e-4
+
+BLENDS = ['BEER_LAMBERT', 'ALPHA', 'ALPHA_ADDITIVE', 'ADDITIVE']
+BOUNDS = ['BORDER', 'CLAMP', 'WRAP']
+
+
+@pytest.fixture(scope='module')
+def ops():
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from gft import ops as _ops
+    return _ops
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def np_(t):
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+# ------------------------------------------------------------------ raymarch
+@pytest.mark.parametrize('C', [1, 2, 4])
+@pytest.mark.parametrize('blend', BLENDS)
+@pytest.mark.parametrize('boundary', BOUNDS)
+def test_raymarch_forward(ops, C, blend, boundary):
+    from oracle import raymarch as RM
+    from oracle import blend as OB
+    from oracle import sampling as OS
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), C, 11) * 0.4
+    y = ops.raymarch_grid_transform(cuda(x), M, V, P, F, (13, 9, 11), 'LINEAR', boundary, blend)
+    ref = RM.raymarch_fwd(x, M, V, P, F, (13, 9, 11), OS.LINEAR, BOUNDS.index(boundary),
+                          getattr(OB, blend))
+    assert y.shape == ref.shape
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+@pytest.mark.parametrize('filt', ['NEAREST', 'MIN', 'MAX'])
+@pytest.mark.parametrize('boundary', ['CLAMP', 'WRAP'])
+def test_raymarch_forward_filters(ops, filt, boundary):
+    from oracle import raymarch as RM
+    from oracle import blend as OB
+    _, _, M, V, P, F = scene((10, 14, 12), 2, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 12) * 0.4
+    y = ops.raymarch_grid_transform(cuda(x), M, V, P, F, (13, 9, 11), filt, boundary, 'ADDITIVE')
+    ref = RM.raymarch_fwd(x, M, V, P, F, (13, 9, 11), ['NEAREST', 'LINEAR', 'MIN', 'MAX'].index(filt),
+                          BOUNDS.index(boundary), OB.ADDITIVE)
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+@pytest.mark.parametrize('C', [1, 4])
+@pytest.mark.parametrize('blend', BLENDS)
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_backward(ops, C, blend, boundary, mode):
+    from oracle import raymarch as RM
+    from oracle import blend as OB
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), C, 13) * 0.4
+    rng = np.random.default_rng(14)
+    dy = rng.standard_normal((1, 3, 9, 11, C)).astype(np.float32)
+    xt = cuda(x).requires_grad_(True)
+    with ops.grad_mode(mode):
+        y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11), 'LINEAR', boundary, blend)
+        y.backward(cuda(dy))
+    ref = RM.raymarch_bwd(x, np_(y), dy, M, V, P, F, (13, 9, 11), BOUNDS.index(boundary),
+                          getattr(OB, blend), exact=(mode == 'EXACT'))
+    assert rel_l2(np_(xt.grad), ref) <= GRAD_TOL
+
+
+def test_raymarch_not_separate_batch(ops):
+    from oracle import raymarch as RM
+    _, _, M, V, P, F = scene((8, 9, 7), 2, (9, 6, 5))
+    x = np.concatenate([small_grid((8, 9, 7), 4, 1), small_grid((8, 9, 7), 4, 2)], 0) * 0.3
+    M2 = np.concatenate([M, M], 0)
+    y = ops.raymarch_grid_transform(cuda(x), M2, V, P, F, (9, 6, 5), separate_camera_batch=False)
+    ref = RM.raymarch_fwd(x, M2, V, P, F, (9, 6, 5), separate_camera_batch=False)
+    assert y.shape == (2, 1, 6, 5, 4)
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+def test_raymarch_bf16_storage(ops):
+    from oracle import raymarch as RM
+    _, _, M, V, P, F = scene((10, 14, 12), 2, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 15) * 0.4
+    y = ops.raymarch_grid_transform(cuda(x), M, V, P, F, (13, 9, 11), storage_dtype=torch.bfloat16)
+    ref = RM.raymarch_fwd(x, M, V, P, F, (13, 9, 11))
+    assert rel_l2(np_(y), ref) <= BF16_TOL
+
+
+# ------------------------------------------------------------------ SampleGridLut
+@pytest.mark.parametrize('C', [1, 2, 4])
+@pytest.mark.parametrize('filt', ['NEAREST', 'LINEAR', 'MIN', 'MAX'])
+@pytest.mark.parametrize('boundary', BOUNDS)
+def test_lut_forward(ops, C, filt, boundary):
+    from oracle import resample as R
+    rng = np.random.default_rng(20)
+    x = small_grid((8, 9, 7), C, 21)
+    lut = np.concatenate([rng.standard_normal((2, 6, 5, 4, 3)) * 2.0, np.zeros((2, 6, 5, 4, 1))], -1).astype(np.float32)
+    y = ops.sample_grid_lut(cuda(x), cuda(lut), filt, boundary)
+    ref = R.sample_grid_lut(x, lut, ['NEAREST', 'LINEAR', 'MIN', 'MAX'].index(filt), BOUNDS.index(boundary))
+    assert y.shape == ref.shape
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+@pytest.mark.parametrize('mip', ['NEAREST', 'LINEAR'])
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+def test_lut_forward_mips(ops, mip, boundary):
+    from oracle import resample as R
+    from oracle import sampling as OS
+    rng = np.random.default_rng(22)
+    x = small_grid((16, 18, 14), 2, 23)
+    lut = np.concatenate([rng.random((1, 7, 6, 5, 3)) * [14, 18, 16], rng.random((1, 7, 6, 5, 1)) * 3.5],
+                         -1).astype(np.float32)
+    y = ops.sample_grid_lut(cuda(x), cuda(lut), 'LINEAR', boundary, mip, 3, 0.25, relative_coords=False,
+                            cell_center_offset=0.5)
+    ref = R.sample_grid_lut(x, lut, OS.LINEAR, BOUNDS.index(boundary), ['NONE', 'NEAREST', 'LINEAR'].index(mip), 3,
+                            0.25, 0.5, relative=False)
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+@pytest.mark.parametrize('C', [1, 4])
+@pytest.mark.parametrize('filt', ['LINEAR', 'NEAREST'])
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_lut_backward(ops, C, filt, boundary, mode):
+    from oracle import resample as R
+    rng = np.random.default_rng(24)
+    x = small_grid((8, 9, 7), C, 25)
+    lut = np.concatenate([rng.standard_normal((2, 8, 9, 7, 3)) * 1.5, np.zeros((2, 8, 9, 7, 1))], -1).astype(np.float32)
+    dy = rng.standard_normal((1, 2, 8, 9, 7, C)).astype(np.float32)
+    xt = cuda(x).requires_grad_(True)
+    lt = cuda(lut).requires_grad_(True)
+    with ops.grad_mode(mode):
+        y = ops.sample_grid_lut(xt, lt, filt, boundary)
+        y.backward(cuda(dy))
+    gx, gl = R.sample_grid_lut_grad(x, dy, lut, ['NEAREST', 'LINEAR'].index(filt), BOUNDS.index(boundary),
+                                    exact=(mode == 'EXACT'))
+    assert rel_l2(np_(xt.grad), gx) <= GRAD_TOL
+    if filt == 'LINEAR':
+        assert rel_l2(np_(lt.grad), gl) <= GRAD_TOL
+    else:
+        assert np.all(np_(lt.grad) == 0)
+
+
+# ------------------------------------------------------------------ SampleGridTransform
+CMS = ['TRANSFORM_LINDEPTH', 'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM', 'TRANSFORM_REVERSE']
+
+
+def _transform_case(cm):
+    from oracle import transforms as OT
+    shape, res = (10, 14, 12), (13, 9, 11)
+    _, _, M, V, P, F = scene(shape, 2, res)
+    if cm in ('TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_REVERSE'):
+        in_shape, out_shape = res, shape
+    else:
+        in_shape, out_shape = shape, res
+    return M, V, P, F, in_shape, out_shape, [OT.LINDEPTH, OT.LINDEPTH_REVERSE, OT.TRANSFORM, OT.TRANSFORM_REVERSE][CMS.index(cm)]
+
+
+@pytest.mark.parametrize('cm', CMS)
+@pytest.mark.parametrize('filt', ['NEAREST', 'LINEAR'])
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+@pytest.mark.parametrize('mip', ['NONE', 'NEAREST', 'LINEAR'])
+def test_sample_transform_forward(ops, cm, filt, boundary, mip):
+    from oracle import resample as R
+    M, V, P, F, in_shape, out_shape, ocm = _transform_case(cm)
+    x = small_grid(in_shape, 2, 30)
+    y = ops.sample_grid_transform(cuda(x), M, V, P, F, out_shape, filt, boundary, mip, 2 if mip != 'NONE' else 0,
+                                  0.3, cm)
+    ref = R.sample_grid_transform(x, M, V, P, F, out_shape, ['NEAREST', 'LINEAR'].index(filt),
+                                  ['BORDER', 'CLAMP'].index(boundary), ['NONE', 'NEAREST', 'LINEAR'].index(mip),
+                                  2 if mip != 'NONE' else 0, 0.3, ocm)
+    assert y.shape == ref.shape
+    if filt == 'NEAREST' or mip == 'NEAREST':
+        # Nearest cell / nearest level are step functions of the position: cells whose
+        # fp32 position sits on a rounding tie may pick the neighbour the fp64 oracle
+        # does not.  Bound the fraction of such cells; all others must agree.
+        bad = np.any(np.abs(np_(y) - ref) > 1e-5, axis=-1)
+        assert bad.mean() <= 0.02
+        assert rel_l2(np_(y)[~bad], ref[~bad]) <= FWD_TOL
+    else:
+        assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+@pytest.mark.parametrize('cm', CMS)
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_sample_transform_backward(ops, cm, boundary, mode):
+    from oracle import resample as R
+    M, V, P, F, in_shape, out_shape, ocm = _transform_case(cm)
+    x = small_grid(in_shape, 4, 31)
+    rng = np.random.default_rng(32)
+    dy = rng.standard_normal((1, 2) + tuple(out_shape) + (4,)).astype(np.float32)
+    with ops.grad_mode(mode):
+        g = ops.sample_grid_transform_grad(cuda(x), cuda(dy), M, V, P, F, 'LINEAR', boundary,
+                                           coordinate_mode=cm)
+    ref = R.sample_grid_transform_grad(x, dy, M, V, P, F, BOUNDS.index(boundary), ocm, exact=(mode == 'EXACT'))
+    assert rel_l2(np_(g), ref) <= GRAD_TOL
+
+
+def test_lod_transform(ops):
+    from oracle import resample as R
+    _, cams, M, V, P, F = scene((10, 14, 12), 2, (13, 9, 11))
+    MV = np.stack([M[0] @ V[i] for i in range(2)]).astype(np.float32)  # (V @ M)^T
+    for inv in (False, True):
+        ins, outs = ((10, 14, 12), (13, 9, 11)) if not inv else ((13, 9, 11), (10, 14, 12))
+        y = ops.lod_transform(ins, MV, P, F, outs, inv)
+        ref = R.lod_transform(ins, MV, P, F, outs, inv)
+        assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
+# ------------------------------------------------------------------ ReduceGridBlend
+@pytest.mark.parametrize('C', [1, 2, 4])
+@pytest.mark.parametrize('blend', BLENDS)
+@pytest.mark.parametrize('keep', [False, True])
+def test_blend(ops, C, blend, keep):
+    from oracle import blend as OB
+    x = small_grid((9, 7, 6), C, 40) * 0.3
+    y = ops.reduce_grid_blend(cuda(x), blend, keep)
+    ref = OB.reduce_grid_blend(x, getattr(OB, blend), keep)
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+    if blend == 'ALPHA_ADDITIVE':
+        return
+    rng = np.random.default_rng(41)
+    dy = rng.standard_normal(ref.shape).astype(np.float32)
+    for mode in ('REFERENCE', 'EXACT'):
+        with ops.grad_mode(mode):
+            g = ops.reduce_grid_blend_grad(cuda(dy), y, cuda(x), blend, keep)
+        gref = OB.reduce_grid_blend_grad(dy, np_(y), x, getattr(OB, blend), keep, exact=(mode == 'EXACT'))
+        assert rel_l2(np_(g), gref) <= GRAD_TOL
+
+
+# ------------------------------------------------------------------ advection
+@pytest.mark.parametrize('order,clamp', [(1, 'NONE'), (2, 'NONE'), (2, 'MC_SMOOTH'), (1, 'NEGATIVE'), (2, 'NEGATIVE')])
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_advect(ops, order, clamp, boundary, mode):
+    from oracle import advect as OA
+    rng = np.random.default_rng(50)
+    D, H, W = 9, 10, 8
+    d = small_grid((D, H, W), 1, 51, positive=(clamp != 'NEGATIVE'))
+    vx = (rng.standard_normal((1, D, H, W + 1, 1)) * 0.8).astype(np.float32)
+    vy = (rng.standard_normal((1, D, H + 1, W, 1)) * 0.8).astype(np.float32)
+    vz = (rng.standard_normal((1, D + 1, H, W, 1)) * 0.8).astype(np.float32)
+    dt = 1.3
+    bi = BOUNDS.index(boundary)
+    dtn = cuda(d).requires_grad_(True)
+    vs = [cuda(v).requires_grad_(True) for v in (vx, vy, vz)]
+    with ops.grad_mode(mode):
+        y = ops.advect(dtn, *vs, dt=dt, order=order, clamp=clamp, boundary=boundary)
+        go = rng.standard_normal(d.shape).astype(np.float32)
+        y.backward(cuda(go))
+    ref = OA.warp(d[0], vx[0], vy[0], vz[0], dt, order, clamp, bi)
+    assert rel_l2(np_(y)[0], ref) <= FWD_TOL
+    gd, gvx, gvy, gvz = OA.warp_grad(d[0], vx[0], vy[0], vz[0], go[0], dt, order, clamp, bi, exact=(mode == 'EXACT'))
+    assert rel_l2(np_(dtn.grad)[0], gd) <= GRAD_TOL
+    for got, want in zip(vs, (gvx, gvy, gvz)):
+        assert rel_l2(np_(got.grad)[0], want) <= GRAD_TOL
