@@ -1,0 +1,342 @@
+"""Benchmark: fwd+bwd render + advect iterations per second on one GB300.
+
+Workload (default ``cfg2``, the multi-view frame configuration): plume density
+128x227x128 advected one MacCormack step (MC_SMOOTH, CLAMP) by a staggered
+curl-noise velocity field, spot light with a 256x196x196 shadow frustum (3 mip
+levels, inverse-resampling gradients), 5 perspective views of 480x270 with 192
+depth samples, fused Beer-Lambert raymarch, L2 image loss against seeded target
+renders; one step = forward + backward to the previous density and all three
+velocity components.  Synthetic seeded data stand in for ScalarFlow.
+
+Arms:
+  default            this repo: batched kernels, whole step in one CUDA graph
+  --impl reference   the FP64 NumPy port of the reference ops on the host cores
+                     (the reference's ops are CUDA-only TensorFlow kernels)
+
+One JSON line on stdout (rank 0).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, 'global-flow-transport_gb300')
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = 'fwd+bwd render+advect iters/s'
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index, out_path=None):
+        self.idx = gpu_index
+        self.out_path = out_path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.idx), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+            if self.out_path:
+                with open(self.out_path, 'w') as f:
+                    f.write('\n'.join(self.lines) + '\n')
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for l in getattr(self, 'lines', []):
+            f = [x.strip() for x in l.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        sm.sort()
+        return {'sm_mhz': sm[len(sm) // 2] if sm else None, 'sm_max_mhz': mx, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def _ddp():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def bench_ours(args):
+    import numpy as np
+    import torch
+    from gft import _lib, ops
+    from gft.pipeline import RenderAdvectStep
+
+    ws, rank, local = _ddp()
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    lib = _lib.load()
+    storage = torch.bfloat16 if args.storage == 'bf16' else None
+    ops.set_grad_mode(args.grad_mode)
+
+    step = RenderAdvectStep(args.config, dev, storage_dtype=storage, mode='batched')
+    inputs = step.make_inputs(frame=rank)
+    step.setup_static(inputs)
+    n0 = lib.gft_launch_count()
+    step.capture(warmup=args.warmup)
+    launches_per_step = (lib.gft_launch_count() - n0) // (args.warmup + 1)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, k, flush_l2=True):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for i in range(k):
+            if flush_l2:
+                flush.fill_(float(i))
+            evs[i][0].record()
+            fn()
+            evs[i][1].record()
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    # ---- timed region: graph replays, L2 flushed between steps -------------
+    for _ in range(args.warmup):
+        step.replay()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local, os.path.join(ROOT, 'gpurun_out', 'bench_clocks.csv') if args.save_clocks else None) as cs:
+        t_wall0 = time.perf_counter()
+        times = timed(step.replay, args.steps)
+        t_wall = time.perf_counter() - t_wall0
+    ms = float(np.mean(times))
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    loss_val = float(step.g_loss.item())
+
+    result = {}
+    if rank == 0 and not args.quick:
+        result = extras(args, step, dev, timed, storage, inputs, ms)
+    clocks = cs.summary()
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+    value = ws * 1000.0 / ms
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'iters/s', 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32' if storage is None else 'bf16-storage/f32',
+        'data': 'synthetic (seeded plume + curl-noise velocity; ScalarFlow absent)',
+        'config': {'workload': '%s: density %s, MacCormack advect, spot-light shadow %s (%d mips), %d views %dx%d x%d '
+                               'samples, L2 image loss, fwd+bwd' % (args.config, 'x'.join(map(str, step.shape)),
+                                                                   'x'.join(map(str, step.shadow_res)), step.rs.num_mips,
+                                                                   len(step.cams), step.res[1], step.res[2],
+                                                                   step.res[0]),
+                   'grad_mode': args.grad_mode, 'cuda_graph': True,
+                   'l2': 'flushed between timed steps (write of 258 MB)', 'parallelism': 'replicas' if ws > 1 else 'single'},
+        'gpu_launches': int(launches_per_step * args.steps),
+        'launches_per_step': int(launches_per_step),
+        'loss': loss_val,
+        'wall_s_timed': t_wall,
+        'clocks': clocks,
+    }
+    line.update(result)
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def extras(args, step, dev, timed, storage, inputs, ms):
+    """e2e through the public API, the plain per-op path, per-kernel roofline
+    and the CPU baseline."""
+    import numpy as np
+    import torch
+    from gft import ops
+    from gft.pipeline import RenderAdvectStep
+    out = {}
+    # ---- e2e: pinned host inputs -> device, graph step, loss -> host ----------
+    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+            (('d', inputs['d_prev']), ('vx', inputs['vx'][None]), ('vy', inputs['vy'][None]),
+             ('vz', inputs['vz'][None]), ('t', inputs['target']))}
+    dsts = {'d': step.s_d, 'vx': step.s_vx, 'vy': step.s_vy, 'vz': step.s_vz, 't': step.s_t}
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    loss_host = torch.empty(1, dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        with torch.no_grad():
+            for k, v in host.items():
+                dsts[k].copy_(v, non_blocking=True)
+        loss, _ = step.replay()
+        loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
+
+    k = max(3, args.steps // 2)
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        e2e_step()
+        torch.cuda.current_stream().synchronize()
+        float(loss_host[0])
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / k
+    out['e2e'] = {'value': 1000.0 / e2e_ms, 'unit': 'iters/s', 'h2d_bytes_per_step': int(h2d),
+                  'd2h_bytes_per_step': 4, 'ms_per_step': e2e_ms}
+
+    # ---- plain: per-camera launches, composed advection, no graph -----------
+    plain = RenderAdvectStep(args.config, dev, storage_dtype=None, mode='plain')
+    plain.setup_static(inputs)
+    for _ in range(2):
+        plain.run_static()
+    torch.cuda.synchronize()
+    pt = timed(plain.run_static, max(3, args.steps // 3))
+    out['plain'] = {'value': 1000.0 / float(np.mean(pt)), 'unit': 'iters/s', 'ms_per_step': float(np.mean(pt)),
+                    'what': 'same step, one raymarch launch per camera, advection from 4 SampleGridLut calls + '
+                            'elementwise ops, no CUDA graph'}
+    out['batched_vs_plain'] = out['plain']['ms_per_step'] / ms
+    del plain
+
+    # ---- per-kernel timing of the dominant ops (roofline) -------------------
+    out.update(kernel_roofline(step, dev, timed))
+
+    # ---- CPU baseline ------------------------------------------------------------
+    if not args.no_cpu:
+        try:
+            from oracle import cpu_step
+            out['cpu_baseline'] = cpu_step.time_step(step, inputs, budget_s=args.cpu_budget, workers=1)
+        except Exception as e:  # the baseline is reported, not required
+            out['cpu_baseline'] = {'error': repr(e)}
+    return out
+
+
+def kernel_roofline(step, dev, timed):
+    """Times the raymarch forward and backward launches (the dominant kernels)
+    alone with CUDA events on their stream and converts the algorithmic bytes
+    per launch into GB/s against the measured HBM peak."""
+    import numpy as np
+    import torch
+    from gft import ops
+    peak, src = _peaks()
+    with torch.no_grad():
+        d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
+        light = d * (step.shadow(d) * step.falloff_col + step.ambient)
+        data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
+    D, H, W = step.res
+    V = len(step.cams)
+    fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True)
+    y = fwd()
+    dy = torch.randn_like(y) * 1e-3
+    bwd = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                    ops.GRAD[ops.get_grad_mode()])
+    for _ in range(2):
+        fwd()
+        bwd()
+    tf = float(np.median(timed(fwd, 7)))
+    tb = float(np.median(timed(bwd, 7)))
+    nvox = int(np.prod(step.shape))
+    s = 4
+    pix = V * H * W
+    bytes_fwd = nvox * 4 * s + pix * 4 * 4
+    bytes_bwd = nvox * 4 * s + 2 * pix * 4 * 4 + 2 * nvox * 4 * 4
+    samples = pix * D
+    kern = {
+        'raymarch_fwd': {'ms': tf, 'alg_bytes': bytes_fwd, 'GBps': bytes_fwd / tf / 1e6,
+                         'gather_GBps': samples * 8 * 16 / tf / 1e6, 'samples_per_s': samples / tf * 1e3},
+        'raymarch_bwd': {'ms': tb, 'alg_bytes': bytes_bwd, 'GBps': bytes_bwd / tb / 1e6,
+                         'gather_GBps': samples * 8 * 16 / tb / 1e6, 'samples_per_s': samples / tb * 1e3},
+    }
+    dom = 'raymarch_bwd' if tb >= tf else 'raymarch_fwd'
+    k = kern[dom]
+    return {'roofline': {'kernel': dom, 'bound': 'hbm', 'achieved': k['GBps'], 'peak': peak, 'unit': 'GB/s',
+                         'frac': k['GBps'] / peak, 'peak_source': src, 'traffic': None,
+                         'note': 'algorithmic bytes = compulsory unique traffic; the grid is L2-resident, so the '
+                                 'binding resource is L1/L2 gather throughput (gather_GBps)'},
+            'kernels': kern}
+
+
+def bench_reference(args):
+    """The reference's own implementation of the path is CUDA-only TensorFlow
+    ops; its CPU stand-in is the FP64 NumPy port in oracle/, timed on a bounded
+    sample of the same workload with all host cores."""
+    ws, rank, _ = _ddp()
+    if rank != 0:
+        return
+    from oracle import cpu_step
+    workers = os.cpu_count() or 1
+    res = cpu_step.time_step(None, None, budget_s=args.cpu_budget, workers=workers, config=args.config)
+    v = res['value']
+    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'iters/s', 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1000.0 / v if v else None, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': args.config + ' (same step as the GPU arm)'},
+            'cpu_baseline': res,
+            'e2e': {'value': v, 'unit': 'iters/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--config', default='cfg2')
+    ap.add_argument('--storage', default='f32', choices=['f32', 'bf16'])
+    ap.add_argument('--grad-mode', default='REFERENCE', choices=['REFERENCE', 'EXACT'])
+    ap.add_argument('--quick', action='store_true', help='only the timed graph replays')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cpu-budget', type=float, default=20.0)
+    ap.add_argument('--save-clocks', action='store_true')
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == 'reference':
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,6 +1,7 @@
 // extern "C" entry points of libgft.so (declared in include/gft.h): argument
 // checks with the reference ops' error classes, camera set-up and dispatch to
 // the launchers.  No entry point allocates device memory or synchronises.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -20,6 +21,13 @@ bool cuda_ok(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return true;
     set_error(std::string(what) + ": " + cudaGetErrorString(e));
     return false;
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+
+bool launched(int n, const char* what) {
+    g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed);
+    return cuda_ok(cudaGetLastError(), what);
 }
 
 // column-major 16 floats -> row-major double 4x4 (the column-vector matrix)
@@ -178,6 +186,8 @@ extern "C" {
 const char* gft_last_error(void) { return g_last_error.c_str(); }
 
 const char* gft_version(void) { return "gft-gb300 0.1 (sm_103a)"; }
+
+unsigned long long gft_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------- raymarch
 gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, const int64_t input_shape[5],

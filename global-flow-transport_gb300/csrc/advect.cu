@@ -149,7 +149,7 @@ static bool adv_fwd_c(const AdvectArgs& a, float* out, float* ws, cudaStream_t s
                     break;
             }
         }
-        if (!cuda_ok(cudaGetLastError(), "advect launch")) return false;
+        if (!launched(a.order == 1 ? 1 : 2, "advect launch")) return false;
     }
     return true;
 }
@@ -355,13 +355,13 @@ static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float*
                                                                      nullptr, gd_sc, cnt3, glut);
         }
         k_adv_bwd_density<C, COUNT != 0><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
-        if (!cuda_ok(cudaGetLastError(), "advect gradient launch")) return false;
+        if (!launched(a.order == 2 ? 4 : 2, "advect gradient launch")) return false;
     }
     const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
                           (int64_t)a.d.x * a.d.y * (a.d.z + 1);
     k_adv_bwd_velocity<<<(unsigned)((nstag + AD_THREADS - 1) / AD_THREADS), AD_THREADS, 0, s>>>(glut, a.d, a.dt, gvx,
                                                                                                  gvy, gvz);
-    return cuda_ok(cudaGetLastError(), "velocity gradient launch");
+    return launched(1, "velocity gradient launch");
 }
 
 template <int C>

@@ -68,7 +68,7 @@ bool launch_blend_fwd(const float* in, int N, int C, Dims d, int mode, bool keep
     if (C == 4) fwd_launch<4>(keep_dims, blocks, s, in, N, d, mode, out);
     else if (C == 2) fwd_launch<2>(keep_dims, blocks, s, in, N, d, mode, out);
     else fwd_launch<1>(keep_dims, blocks, s, in, N, d, mode, out);
-    return cuda_ok(cudaGetLastError(), "reduce blend launch");
+    return launched(1, "reduce blend launch");
 }
 
 template <int C>
@@ -85,7 +85,7 @@ bool launch_blend_bwd(const float* dy, const float* y, const float* x, int N, in
     if (C == 4) bwd_launch<4>(keep_dims, blocks, s, dy, y, x, N, d, mode, exact, gx);
     else if (C == 2) bwd_launch<2>(keep_dims, blocks, s, dy, y, x, N, d, mode, exact, gx);
     else bwd_launch<1>(keep_dims, blocks, s, dy, y, x, N, d, mode, exact, gx);
-    return cuda_ok(cudaGetLastError(), "reduce blend gradient launch");
+    return launched(1, "reduce blend gradient launch");
 }
 
 }  // namespace gft

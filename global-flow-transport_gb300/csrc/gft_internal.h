@@ -51,6 +51,9 @@ size_t mip_workspace_floats(Dims d, int levels, int C);
 // error helpers
 void set_error(const std::string& msg);
 bool cuda_ok(cudaError_t e, const char* what);
+// Records n kernel launches in the process-wide launch counter and checks the
+// launch status.
+bool launched(int n, const char* what);
 
 // launchers ------------------------------------------------------------------
 struct RaymarchArgs {

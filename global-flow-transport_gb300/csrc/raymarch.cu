@@ -148,7 +148,7 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
             else if (a.C == 2) fwd_dispatch_bm<2, __nv_bfloat16>(grid, block, s, a, out, t);
             else fwd_dispatch_bm<1, __nv_bfloat16>(grid, block, s, a, out, t);
         }
-        if (!cuda_ok(cudaGetLastError(), "raymarch forward launch")) return false;
+        if (!launched(1, "raymarch forward launch")) return false;
     }
     return true;
 }
@@ -199,7 +199,7 @@ bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
             else if (a.C == 2) bwd_dispatch_bm<2, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
             else bwd_dispatch_bm<1, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
         }
-        if (!cuda_ok(cudaGetLastError(), "raymarch backward launch")) return false;
+        if (!launched(1, "raymarch backward launch")) return false;
     }
     if (!exact) {
         // pairs are ordered batch-major with the same count per batch
@@ -210,7 +210,7 @@ bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
         if (a.C == 4) k_raymarch_normalize<4><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
         else if (a.C == 2) k_raymarch_normalize<2><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
         else k_raymarch_normalize<1><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
-        if (!cuda_ok(cudaGetLastError(), "raymarch normalize launch")) return false;
+        if (!launched(1, "raymarch normalize launch")) return false;
     }
     return true;
 }

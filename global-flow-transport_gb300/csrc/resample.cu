@@ -76,7 +76,7 @@ bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, 
         if (C == 4) mip_launch<4>(src, src_dtype, set->dims[m - 1], p, dm, s);
         else if (C == 2) mip_launch<2>(src, src_dtype, set->dims[m - 1], p, dm, s);
         else mip_launch<1>(src, src_dtype, set->dims[m - 1], p, dm, s);
-        if (!cuda_ok(cudaGetLastError(), "mip generation launch")) return false;
+        if (!launched(1, "mip generation launch")) return false;
         set->lvl[m] = p;
         set->dims[m] = dm;
         src = p;
@@ -210,7 +210,7 @@ bool launch_sample_transform_fwd(const SampleArgs& a, const std::vector<Pair>& p
                 else if (a.C == 2) st_fwd<2, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
                 else st_fwd<1, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
             }
-            if (!cuda_ok(cudaGetLastError(), "sample transform launch")) return false;
+            if (!launched(1, "sample transform launch")) return false;
         }
     }
     return true;
@@ -297,11 +297,11 @@ bool launch_sample_transform_bwd(int N, int C, Dims din, Dims dout, int boundary
                 else if (C == 2) stb_launch<2, 1>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
                 else stb_launch<1, 1>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
             }
-            if (!cuda_ok(cudaGetLastError(), "sample transform gradient launch")) return false;
+            if (!launched(1, "sample transform gradient launch")) return false;
         }
         if (!exact) {
             normalize_any(C, gb, count, nvi, s);
-            if (!cuda_ok(cudaGetLastError(), "normalize launch")) return false;
+            if (!launched(1, "normalize launch")) return false;
         }
     }
     return true;
@@ -387,7 +387,7 @@ bool launch_lut_fwd(const LutArgs& a, const float* lut, const MipSet* mips, floa
             else if (a.C == 2) lut_fwd_launch<2, __nv_bfloat16>(a.boundary, blocks, s, lut, k, mips[b], out);
             else lut_fwd_launch<1, __nv_bfloat16>(a.boundary, blocks, s, lut, k, mips[b], out);
         }
-        if (!cuda_ok(cudaGetLastError(), "sample lut launch")) return false;
+        if (!launched(1, "sample lut launch")) return false;
     }
     return true;
 }
@@ -460,10 +460,10 @@ bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, cons
             else if (a.C == 2) lut_bwd_launch<2, 1>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
             else lut_bwd_launch<1, 1>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
         }
-        if (!cuda_ok(cudaGetLastError(), "sample lut gradient launch")) return false;
+        if (!launched(1, "sample lut gradient launch")) return false;
         if (!exact) {
             normalize_any(a.C, gb, count, nvi, s);
-            if (!cuda_ok(cudaGetLastError(), "normalize launch")) return false;
+            if (!launched(1, "normalize launch")) return false;
         }
     }
     return true;
@@ -505,7 +505,7 @@ bool launch_lod_transform(Dims din, Dims dout, const std::vector<Pair>& pairs, b
     for (const PairTable& t : make_tables(pairs)) {
         const unsigned blocks = (unsigned)((nv * t.n + RS_THREADS - 1) / RS_THREADS);
         k_lod_transform<<<blocks, RS_THREADS, 0, s>>>(din, dout, inverse ? CM_LINDEPTH_REVERSE : CM_LINDEPTH, out, t);
-        if (!cuda_ok(cudaGetLastError(), "lod transform launch")) return false;
+        if (!launched(1, "lod transform launch")) return false;
     }
     return true;
 }

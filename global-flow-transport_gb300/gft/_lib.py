@@ -43,6 +43,7 @@ _I32P = ctypes.POINTER(ctypes.c_int32)
 _SIGS = {
     'gft_last_error': (ctypes.c_char_p, []),
     'gft_version': (ctypes.c_char_p, []),
+    'gft_launch_count': (ctypes.c_ulonglong, []),
     'gft_raymarch_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                            _I32, _I32, _I32, _I32, _P, _P]),
     'gft_raymarch_grid_transform_grad_workspace_size': (_SZ, [_I64P, _I32, _I32, _I32]),

@@ -1,0 +1,220 @@
+"""One differentiable render + advect iteration of the global-transport
+reconstruction, built on gft.ops (the path of Renderer.render_density,
+SpotLight.grid_lighting and VelocityGrid.warp of the reference).
+
+    d      = warp(d_prev, v)                    MacCormack + MC_SMOOTH, CLAMP
+    shadow = exp(-shift(cumsum(sample(d))))     light frustum, LINDEPTH, mips
+    light  = d * (back_project(shadow) * falloff * c * i + ambient)
+    img    = raymarch(concat(light, d) * depth_step, cameras)   BEER_LAMBERT
+    loss   = mean((img.rgb + bkg * exp(-img.a) - target)^2)
+
+``batched``: all cameras in one raymarch launch, fused advection, and the
+whole forward + backward captured in one CUDA graph.  ``plain``: the
+reference's launch structure -- one raymarch launch per camera, advection
+composed from four SampleGridLut calls plus elementwise ops, no graph.
+All constants are device tensors created up front so the step is capturable.
+"""
+import numpy as np
+import torch
+
+from . import ops
+from . import synthetic as syn
+from phitest.render.lighting import SpotLight
+from phitest.render.transform import Transform
+
+
+class RenderSettings:
+    """The Renderer fields the shadow pass reads (renderer.py:64-88)."""
+
+    def __init__(self, num_mips=3):
+        self.filter_mode = 'LINEAR'
+        self.boundary_mode = 'BORDER'
+        self.mip_mode = 'LINEAR'
+        self.num_mips = num_mips
+        self.mip_bias = 0.0
+        self.gradient_mip_bias_add = 0.0
+        self.blend_mode = 'BEER_LAMBERT'
+
+
+CONFIGS = {
+    # configs[1]: multi-view frame, 5 views 480x270, 192 samples, 3 mips, spot light + shadow volume
+    'cfg2': dict(grid=(128, 227, 128), views=5, image=(480, 270), samples=192, mips=3,
+                 shadow=(256, 196, 196), seed=2000),
+    # configs[0]-sized case for quick runs / CPU timing
+    'cfg1': dict(grid=(64, 64, 64), views=1, image=(128, 128), samples=64, mips=3,
+                 shadow=(64, 64, 64), seed=1000),
+}
+
+
+class RenderAdvectStep:
+    def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched'):
+        cfg = CONFIGS[config] if isinstance(config, str) else config
+        self.cfg = cfg
+        self.dev = torch.device(device)
+        self.storage_dtype = storage_dtype
+        self.mode = mode
+        D, H, W = cfg['grid']
+        self.shape = (D, H, W)
+        Hi, Wi = cfg['image']
+        self.res = (cfg['samples'], Hi, Wi)
+        self.gt = syn.grid_transform(self.shape)
+        self.cams = syn.arc_cameras(cfg['views'], self.res, radius=2.5, fov=30.0)
+        self.M = syn.model_matrix(self.gt)
+        self.V, self.P, self.F = syn.camera_params(self.cams)
+        self.depth_step = float(self.cams[0].depth_step)
+        # spot light with shadow volume + ambient (lighting set-up of reconstruct_sequence.py:696-705)
+        self.spot = SpotLight(Transform(translation=[0, 0, 2.0], parent=Transform(rotation_deg=[-40, 0, 0])),
+                              intensity=0.85, cast_shadows=True, shadow_clip=[0.85, 3.15], range_scale=0.825,
+                              angle_deg=60.0, shadow_resolution=list(cfg['shadow']), cone_mask=False)
+        self.ambient = 0.64
+        self.rs = RenderSettings(cfg['mips'])
+        self.Vs, self.Ps, self.Fs = syn.camera_params([self.spot.shadow_cam])
+        self.shadow_step = float(self.spot.shadow_cam.depth_step)
+        self.shadow_res = tuple(cfg['shadow'])
+        fall = self.spot.falloff(_Holder(self.gt), self.dev)  # [D,H,W,1]
+        col = torch.tensor(self.spot.c * np.float32(self.spot.i), dtype=torch.float32, device=self.dev)
+        self.falloff_col = (fall * col)[None].contiguous()  # [1,D,H,W,3]
+        self.bkg = torch.tensor([0.0, 0.5, 1.0], dtype=torch.float32, device=self.dev)
+        self.graph = None
+
+    # --------------------------------------------------------------- inputs
+    def make_inputs(self, frame=0, target_seed_offset=7):
+        """Seeded density (previous frame), staggered velocity and target images
+        (rendered from a perturbed plume with the same path)."""
+        seed = self.cfg['seed'] + frame
+        d_prev = syn.plume_density(self.shape, seed, frame)
+        vx, vy, vz = syn.curl_velocity(self.shape, seed + 500)
+        with torch.no_grad():
+            dt = torch.from_numpy(syn.plume_density(self.shape, seed + target_seed_offset, frame + 1)).to(self.dev)
+            tgt = self.render(dt)[..., :3].contiguous()
+        return dict(d_prev=d_prev, vx=vx[0], vy=vy[0], vz=vz[0], target=tgt.cpu().numpy())
+
+    # --------------------------------------------------------------- pieces
+    def advect(self, d_prev, vx, vy, vz):
+        if self.mode == 'plain':
+            return advect_composed(d_prev, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP')
+        return ops.advect(d_prev, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP',
+                          storage_dtype=self.storage_dtype)
+
+    def shadow(self, d):
+        from phitest.render.renderer import _InverseSampleGrad
+        sh = _InverseSampleGrad.apply(d * self.shadow_step, self.M, self.Vs, self.Ps, self.Fs, self.shadow_res,
+                                      'TRANSFORM_LINDEPTH', 'TRANSFORM_LINDEPTH_REVERSE', self.rs, None)
+        sh = ops.reduce_grid_blend(sh[0], 'BEER_LAMBERT', keep_dims=True)
+        sh = torch.cat([torch.zeros_like(sh[:, :1]), sh[:, :-1]], dim=1)  # BORDER shift
+        tr = torch.exp(-sh)
+        trv = _InverseSampleGrad.apply(tr, self.M, self.Vs, self.Ps, self.Fs, self.shape,
+                                       'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_LINDEPTH', self.rs, None)
+        return trv[0]  # [1,D,H,W,1]
+
+    def render(self, d):
+        light = d * (self.shadow(d) * self.falloff_col + self.ambient)
+        data = torch.cat([light, d], dim=-1) * self.depth_step
+        if self.mode == 'plain':
+            imgs = [ops.raymarch_grid_transform(data, self.M, self.V[i:i + 1], self.P[i:i + 1], self.F[i:i + 1],
+                                                self.res) for i in range(len(self.V))]
+            img = torch.cat(imgs, dim=1)
+        else:
+            img = ops.raymarch_grid_transform(data, self.M, self.V, self.P, self.F, self.res,
+                                              storage_dtype=self.storage_dtype)
+        return img[0]  # [V,H,W,4]
+
+    def loss(self, d_prev, vx, vy, vz, target):
+        d = self.advect(d_prev, vx, vy, vz)
+        img = self.render(d)
+        rgb = img[..., :3] + self.bkg * torch.exp(-img[..., 3:])
+        return torch.mean((rgb - target) ** 2)
+
+    def step(self, d_prev, vx, vy, vz, target):
+        """Forward + backward; returns (loss, (g_d_prev, g_vx, g_vy, g_vz))."""
+        loss = self.loss(d_prev, vx, vy, vz, target)
+        grads = torch.autograd.grad(loss, [d_prev, vx, vy, vz])
+        return loss, grads
+
+    # --------------------------------------------------------------- graphs
+    def setup_static(self, inputs):
+        dev = self.dev
+        self.s_d = torch.from_numpy(inputs['d_prev']).to(dev).requires_grad_(True)
+        self.s_vx = torch.from_numpy(inputs['vx'][None]).to(dev).requires_grad_(True)
+        self.s_vy = torch.from_numpy(inputs['vy'][None]).to(dev).requires_grad_(True)
+        self.s_vz = torch.from_numpy(inputs['vz'][None]).to(dev).requires_grad_(True)
+        self.s_t = torch.from_numpy(inputs['target']).to(dev)
+        return (self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
+
+    def capture(self, warmup=3):
+        """Captures step() on the static inputs into one CUDA graph."""
+        args = (self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self.step(*args)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        torch.cuda.synchronize(self.dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.g_loss, self.g_grads = self.step(*args)
+        torch.cuda.synchronize(self.dev)
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+        return self.g_loss, self.g_grads
+
+    def run_static(self):
+        if self.graph is not None:
+            return self.replay()
+        return self.step(self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
+
+
+class _Holder:
+    """GridTransform view used for the falloff computation."""
+
+    def __init__(self, gt):
+        self.gt = gt
+        self.grid_size = gt.grid_size
+
+    def cell_size_world(self):
+        return self.gt.cell_size_world()
+
+    def grid_size_world(self):
+        return self.gt.grid_size_world()
+
+    def get_inverse_transform(self):
+        return self.gt.get_inverse_transform()
+
+
+def centered_lut(vx, vy, vz, dt):
+    """lut = -dt * centred velocity with a zero LOD channel (data_structures.py:819-868,
+    renderer.py:449-455), from staggered [1,D,H,W+1,1], [1,D,H+1,W,1], [1,D+1,H,W,1]."""
+    cx = (vx[:, :, :, 1:] + vx[:, :, :, :-1]) * 0.5
+    cy = (vy[:, :, 1:] + vy[:, :, :-1]) * 0.5
+    cz = (vz[:, 1:] + vz[:, :-1]) * 0.5
+    v = torch.cat([cx, cy, cz], dim=-1) * (-dt)
+    return torch.nn.functional.pad(v, (0, 1))
+
+
+def advect_composed(d, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP'):
+    """VelocityGrid.warp as the reference composes it (data_structures.py:870-905):
+    SampleGridLut calls and elementwise ops.  Velocity components carry a leading
+    batch dim of 1 ([1,D,H,W+1,1], ...)."""
+    lut = centered_lut(vx, vy, vz, dt)
+
+    def look(x, l, filt='LINEAR'):
+        return ops.sample_grid_lut(x, l, filt, boundary, separate_camera_batch=False, relative_coords=True)[:, 0]
+
+    fwd = look(d, lut)
+    if order == 1:
+        out = fwd
+    else:
+        back = look(fwd, -lut)
+        corr = fwd + 0.5 * (d - back)
+        if clamp in ('MC', 'MC_SMOOTH'):
+            mn = look(d, lut, 'MIN')
+            mx = look(d, lut, 'MAX')
+            oob = torch.logical_or(corr < mn, corr > mx)
+            corr = torch.where(oob, fwd, corr)
+        out = corr
+    if clamp == 'NEGATIVE':
+        out = torch.clamp_min(out, 0)
+    return out

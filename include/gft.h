@@ -74,6 +74,8 @@ typedef enum { GFT_CLAMP_NONE = 0, GFT_CLAMP_MC_SMOOTH = 1, GFT_CLAMP_NEGATIVE =
 
 const char* gft_last_error(void);
 const char* gft_version(void);
+/* Kernels this library has launched in the process so far (all threads). */
+unsigned long long gft_launch_count(void);
 
 /* ---- RaymarchGridTransform (raymarch_grid.cc:28-52, launcher raymarch_grid.cu.cc:222-294) ----
  * input  [N, D, H, W, C] (input_dtype storage)
