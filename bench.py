@@ -297,6 +297,41 @@ def kernel_roofline(step, dev, timed):
             'kernels': kern}
 
 
+def kernel_only(args):
+    """Runs one op of the cfg workload ``args.repeat`` times without a graph
+    (for ncu captures of a single kernel)."""
+    import torch
+    from gft import ops
+    from gft.pipeline import RenderAdvectStep
+    dev = torch.device('cuda', 0)
+    ops.set_grad_mode(args.grad_mode)
+    step = RenderAdvectStep(args.config, dev, mode='batched')
+    inputs = step.make_inputs()
+    step.setup_static(inputs)
+    with torch.no_grad():
+        d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
+        light = d * (step.shadow(d) * step.falloff_col + step.ambient)
+        data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
+        y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True)
+        dy = torch.randn_like(y) * 1e-3
+    gm = ops.GRAD[ops.get_grad_mode()]
+    fns = {
+        'raymarch_fwd': lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True),
+        'raymarch_bwd': lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0,
+                                                  True, gm),
+        'advect_fwd': lambda: ops._advect_fwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
+                                              step.s_vz.detach(), 1.0, 2, 1, 1),
+        'advect_bwd': lambda: ops._advect_bwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
+                                              step.s_vz.detach(), torch.ones_like(d), 1.0, 2, 1, 1, gm),
+        'shadow_fwd': lambda: step.shadow(d),
+    }
+    fn = fns[args.kernel_only]
+    for _ in range(args.repeat):
+        fn()
+    torch.cuda.synchronize()
+    print(json.dumps({'kernel_only': args.kernel_only, 'repeat': args.repeat, 'ok': True}))
+
+
 def bench_reference(args):
     """The reference's own implementation of the path is CUDA-only TensorFlow
     ops; its CPU stand-in is the FP64 NumPy port in oracle/, timed on a bounded
@@ -330,9 +365,15 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-budget', type=float, default=20.0)
     ap.add_argument('--save-clocks', action='store_true')
+    ap.add_argument('--kernel-only', default=None,
+                    choices=['raymarch_fwd', 'raymarch_bwd', 'advect_fwd', 'advect_bwd', 'shadow_fwd'],
+                    help='run one op of the workload --repeat times (profiling)')
+    ap.add_argument('--repeat', type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    if args.impl == 'reference':
+    if args.kernel_only:
+        kernel_only(args)
+    elif args.impl == 'reference':
         bench_reference(args)
     else:
         bench_ours(args)
