@@ -7,6 +7,10 @@
 // MacCormack runs in two passes: (1) the semi-Lagrangian value, (2) the back
 // lookup of (1), the correction and the MC_SMOOTH clamp, with the MIN/MAX of
 // the forward footprint taken from the same 8 gathers as the forward value.
+#include <mutex>
+#include <string>
+
+#include "../../include/gft.h"
 #include "gft_internal.h"
 
 namespace gft {
@@ -387,4 +391,97 @@ bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* 
     return adv_bwd_c<1>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
 }
 
+// ---- allocation-free advection ---------------------------------------------------
+// gft_advect_noalloc keeps the intermediate semi-Lagrangian grid of MacCormack
+// in this fixed device array instead of a caller-provided workspace.  It holds
+// NOALLOC_MAX_ELEMENTS floats (16 MiB); every device that loads the library
+// keeps it until the process exits.  Host code cannot pass the array's name to a
+// kernel (on the host it is only a stand-in symbol), so its device address is
+// looked up once per device with cudaGetSymbolAddress.
+constexpr size_t NOALLOC_MAX_ELEMENTS = size_t(1) << 22;
+static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_MAX_ELEMENTS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_scratch on the current device; the lookup runs on
+// the first call per device and is cached.
+static bool noalloc_scratch(float** out) {
+    int dev = -1;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        set_error("gft_advect_noalloc: device ordinal out of range");
+        return false;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)"))
+            return false;
+        g_noalloc_ptr[dev] = reinterpret_cast<float*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return true;
+}
+
 }  // namespace gft
+
+extern "C" {
+
+size_t gft_advect_noalloc_max_elements(void) { return gft::NOALLOC_MAX_ELEMENTS; }
+
+gft_status gft_advect_noalloc(const void* density, int32_t density_dtype, const int64_t density_shape[5],
+                              const float* vel_x, const float* vel_y, const float* vel_z, float dt, int32_t order,
+                              int32_t clamp, int32_t boundary, float* output, void* stream) {
+    using namespace gft;
+    if (density_shape == nullptr) {
+        set_error("density shape is NULL");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < 5; ++i)
+        if (density_shape[i] <= 0) {
+            set_error("Invalid input shape (NDHWC): all dimensions must be positive");
+            return GFT_ERR_INVALID_ARGUMENT;
+        }
+    const int64_t C = density_shape[4];
+    if (!(C == 1 || C == 2 || C == 4)) {
+        set_error("Only 1,2 and 4 Channel supported.");
+        return GFT_ERR_UNIMPLEMENTED;
+    }
+    if ((order != 1 && order != 2) || clamp < 0 || clamp > 2 || boundary < 0 || boundary > 2 ||
+        (density_dtype != GFT_DTYPE_F32 && density_dtype != GFT_DTYPE_BF16)) {
+        set_error("gft_advect_noalloc: invalid order, clamp, boundary or dtype");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
+    if (!density || !vel_x || !vel_y || !vel_z || !output) {
+        set_error("tensor pointer is NULL");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
+    const double elems = (double)density_shape[1] * (double)density_shape[2] * (double)density_shape[3] * (double)C;
+    if (order == 2 && elems > (double)NOALLOC_MAX_ELEMENTS) {
+        set_error("gft_advect_noalloc: D*H*W*C = " + std::to_string((long long)elems) +
+                  " exceeds the built-in scratch of " + std::to_string((long long)NOALLOC_MAX_ELEMENTS) +
+                  " floats; use gft_advect with a workspace");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
+    float* scratch = nullptr;
+    if (order == 2 && !noalloc_scratch(&scratch)) return GFT_ERR_CUDA;
+    AdvectArgs a;
+    a.density = density;
+    a.dtype = density_dtype;
+    a.N = (int)density_shape[0];
+    a.C = (int)C;
+    a.d = Dims{(int)density_shape[3], (int)density_shape[2], (int)density_shape[1]};
+    a.vx = vel_x;
+    a.vy = vel_y;
+    a.vz = vel_z;
+    a.dt = dt;
+    a.order = order;
+    a.clamp = clamp;
+    a.boundary = boundary;
+    if (!launch_advect_fwd(a, output, scratch, reinterpret_cast<cudaStream_t>(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+}  // extern "C"

@@ -174,6 +174,27 @@ gft_status gft_advect(
     const float* vel_x, const float* vel_y, const float* vel_z, float dt,
     int32_t order, int32_t clamp, int32_t boundary,
     float* output, void* workspace, size_t workspace_bytes, void* stream);
+/* Allocation-free variant of gft_advect.  No counterpart in the reference.
+ * For callers that cannot hand the library device memory: hosts whose device
+ * memory belongs to an allocator they cannot call from the advection call site
+ * (a plugin host or foreign-language runtime without a device allocator, or a
+ * fixed-budget real-time loop that forbids new allocations).  Same arguments as
+ * gft_advect minus the workspace; the MacCormack intermediate lives in a static
+ * device array of gft_advect_noalloc_max_elements() floats (16 MiB, held by
+ * every device that loads the library until the process exits), so
+ * D*H*W*C above that limit is rejected with GFT_ERR_INVALID_ARGUMENT (order 1
+ * needs no scratch and has no limit).  The function calls no cudaMalloc /
+ * cudaFree and no allocating library routine.  Its first call on a device (the
+ * device current on the calling thread, which must own ``stream``) looks up
+ * the array's device address once; make that first call before any stream
+ * capture.  Every call shares the one array and each call overwrites it before
+ * reading it, so nothing needs clearing, but calls whose kernels overlap on the
+ * GPU (different streams without ordering) race on it. */
+size_t gft_advect_noalloc_max_elements(void);
+gft_status gft_advect_noalloc(
+    const void* density, int32_t density_dtype, const int64_t density_shape[5],
+    const float* vel_x, const float* vel_y, const float* vel_z, float dt,
+    int32_t order, int32_t clamp, int32_t boundary, float* output, void* stream);
 /* Gradient of gft_advect w.r.t. density and the staggered velocity components,
  * all overwritten.  In GFT_GRAD_REFERENCE mode each lookup's input gradient is
  * divided by its per-voxel sample count as the reference SampleGridLutGrad does. */
