@@ -96,6 +96,17 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
+def max_over_ranks(value, device):
+    """Max of a per-rank scalar over the process group (the slowest replica
+    defines the step time), followed by a barrier."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
 def _ddp():
     ws = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
@@ -151,10 +162,7 @@ def bench_ours(args):
         t_wall = time.perf_counter() - t_wall0
     ms = float(np.mean(times))
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+        ms = max_over_ranks(ms, dev)
     loss_val = float(step.g_loss.item())
 
     result = {}

@@ -1,0 +1,168 @@
+"""CPU-only checks of the host side: the C ABI library's exports and argument
+validation (no kernel launch), camera/transform matrices, the synthetic scene,
+and the multi-process (replica) timing reduction over gloo."""
+import ctypes
+import os
+import re
+import socket
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'gft.h')
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from gft import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        sys.path.insert(0, os.path.join(ROOT, 'global-flow-transport_gb300'))
+        import build
+        build.build()
+    return _lib
+
+
+def _declared():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(gft_\w+)\s*\(', text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    L = lib.load()
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(lib.exported_symbols())
+    assert b'sm_103a' in L.gft_version()
+
+
+def test_argument_errors_without_a_gpu(lib):
+    L = lib.load()
+    shape3 = lib.i64([1, 8, 8, 8, 3])
+    eye = np.eye(4, dtype=np.float32).reshape(-1)
+    fr = np.array([1, 3, -1, 1, 1, -1], dtype=np.float32)
+    p = eye.ctypes.data_as(ctypes.c_void_p)
+    f = fr.ctypes.data_as(ctypes.c_void_p)
+    out = lib.i32([4, 4, 4])
+    # three channels: Unimplemented, as resample_grid.cc:330-331
+    st = L.gft_raymarch_grid_transform(ctypes.c_void_p(1), 0, shape3, p, 1, p, p, f, 1, out, 1, 0, 0, 1,
+                                       ctypes.c_void_p(1), None)
+    assert st == lib.ERR_UNIMPLEMENTED
+    shape4 = lib.i64([1, 8, 8, 8, 4])
+    # invalid blend mode string value
+    st = L.gft_raymarch_grid_transform(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 9, 1,
+                                       ctypes.c_void_p(1), None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # model matrix batch mismatch
+    st = L.gft_raymarch_grid_transform(ctypes.c_void_p(1), 0, shape4, p, 2, p, p, f, 1, out, 1, 0, 0, 1,
+                                       ctypes.c_void_p(1), None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'model matrix' in L.gft_last_error()
+    # gradient needs LINEAR
+    st = L.gft_raymarch_grid_transform_grad(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                            p, 1, p, p, f, 1, out, 0, 0, 0, 1, 0, ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # reference-mode gradient without workspace
+    st = L.gft_raymarch_grid_transform_grad(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                            p, 1, p, p, f, 1, out, 1, 0, 0, 1, 0, ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_WORKSPACE
+    assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 0) >= 8 * 8 * 8 * 5 * 5 * 4
+    assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 1) == 0
+    # SampleGridTransform: cell centre offset must be 0.5 for transform modes
+    st = L.gft_sample_grid_transform(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 0, 0.0, 0,
+                                     0.25, 1, ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # mips without levels
+    st = L.gft_sample_grid_transform(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 2, 0, 0.0, 0,
+                                     0.5, 1, ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # blend gradient does not accept ALPHA_ADDITIVE (reduce_blend.cc:41)
+    st = L.gft_reduce_grid_blend_grad(ctypes.c_void_p(1), ctypes.c_void_p(1), ctypes.c_void_p(1), shape4, 3, 0, 0,
+                                      ctypes.c_void_p(1), None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # advection order
+    st = L.gft_advect(ctypes.c_void_p(1), 0, lib.i64([1, 8, 8, 8, 1]), ctypes.c_void_p(1), ctypes.c_void_p(1),
+                      ctypes.c_void_p(1), 1.0, 3, 0, 1, ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+
+
+def test_workspace_sizes(lib):
+    L = lib.load()
+    s = lib.i64([2, 16, 20, 12, 2])
+    # mips: levels 1..3 for both batch slices, 256 B aligned
+    n = L.gft_sample_grid_transform_workspace_size(s, 2, 3)
+    lv = [(16 >> m) * (20 >> m) * (12 >> m) * 2 for m in (1, 2, 3)]
+    assert n == 2 * 4 * sum((v + 63) // 64 * 64 for v in lv)
+    assert L.gft_sample_grid_transform_workspace_size(s, 0, 3) == 0
+    assert L.gft_advect_workspace_size(s, 1) == 0 and L.gft_advect_workspace_size(s, 2) >= 16 * 20 * 12 * 2 * 4
+
+
+def test_camera_matrices_follow_the_reference_conventions():
+    from phitest.render.camera import Camera
+    from phitest.render.transform import GridTransform, Transform
+    cam = Camera(GridTransform([16, 9, 11], translation=[0, 0, 2], parent=Transform(rotation_deg=[0, 30, 0])),
+                 nearFar=[1.0, 3.0], fov=40, aspect=11 / 9)
+    P = cam.projection_matrix()
+    n, f = 1.0, 3.0
+    assert np.isclose(P[2, 2], -(f + n) / (f - n)) and np.isclose(P[2, 3], -2 * f * n / (f - n))
+    assert np.isclose(P[3, 2], -1.0)
+    # camera sits at R_y(30) (0,0,2) and looks at the origin along its -z
+    pos = cam.transform.position_global()[:3]
+    assert np.allclose(pos, [2 * np.sin(np.radians(30)), 0, 2 * np.cos(np.radians(30))], atol=1e-6)
+    vs = cam.view_matrix() @ np.array([0, 0, 0, 1.0])
+    assert np.allclose(vs[:2], 0, atol=1e-6) and np.isclose(vs[2], -2.0)
+    assert np.allclose(cam.frustum(), [1, 3, cam.left, cam.right, cam.top, cam.bottom])
+    assert np.isclose(cam.depth_step, 2.0 / 16)
+    gt = GridTransform([8, 10, 6], center=True, normalize='MIN')
+    c = gt.get_transform_matrix() @ np.array([3, 5, 4, 1.0])
+    assert np.allclose(c[:3], 0, atol=1e-6)
+
+
+def test_synthetic_scene_is_seeded():
+    from gft import synthetic as syn
+    a = syn.plume_density((16, 20, 12), 5)
+    b = syn.plume_density((16, 20, 12), 5)
+    assert np.array_equal(a, b) and a.shape == (1, 16, 20, 12, 1) and a.max() > 0
+    vx, vy, vz = syn.curl_velocity((16, 20, 12), 6)
+    assert vx.shape == (1, 16, 20, 13, 1) and vy.shape == (1, 16, 21, 12, 1) and vz.shape == (1, 17, 20, 12, 1)
+    assert abs(float(np.mean(vy)) - 0.5) < 0.2
+
+
+_WORKER = r'''
+import os, sys
+sys.path[:0] = [%r, %r]
+import torch.distributed as dist
+import bench
+dist.init_process_group('gloo', rank=int(os.environ['RANK']), world_size=2)
+v = bench.max_over_ranks(1.5 + int(os.environ['RANK']), 'cpu')
+print('RESULT', v)
+dist.destroy_process_group()
+'''
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(('127.0.0.1', 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def test_replica_timing_reduction_gloo_two_ranks(tmp_path):
+    script = tmp_path / 'w.py'
+    script.write_text(_WORKER % (ROOT, os.path.join(ROOT, 'global-flow-transport_gb300')))
+    port = _free_port()
+    procs = []
+    for r in range(2):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE='2', MASTER_ADDR='127.0.0.1', MASTER_PORT=str(port),
+                   LOCAL_RANK=str(r))
+        procs.append(subprocess.Popen([sys.executable, str(script)], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.STDOUT, text=True))
+    outs = [p.communicate(timeout=120)[0] for p in procs]
+    for p, o in zip(procs, outs):
+        assert p.returncode == 0, o
+        assert 'RESULT 2.5' in o, o

@@ -1,0 +1,131 @@
+"""CPU checks of the FP64 oracle itself: exact adjoints against central finite
+differences, reference-mode gradient structure, and small known answers."""
+import numpy as np
+import pytest
+
+from scene_utils import scene, small_grid
+
+from oracle import advect as OA
+from oracle import blend as OB
+from oracle import raymarch as RM
+from oracle import resample as R
+from oracle import sampling as S
+from oracle import transforms as T
+
+EPS = 1e-6
+
+
+def _fd(f, x, d):
+    return (f(x + EPS * d) - f(x - EPS * d)) / (2 * EPS)
+
+
+@pytest.mark.parametrize('boundary', [S.BORDER, S.CLAMP, S.WRAP])
+@pytest.mark.parametrize('blend', [OB.BEER_LAMBERT, OB.ALPHA, OB.ALPHA_ADDITIVE, OB.ADDITIVE])
+def test_raymarch_exact_adjoint_fd(boundary, blend):
+    _, _, M, V, P, F = scene((8, 10, 9), 2, (9, 6, 7))
+    rng = np.random.default_rng(1)
+    x = small_grid((8, 10, 9), 4, 2) * 0.3
+    y = RM.raymarch_fwd(x, M, V, P, F, (9, 6, 7), boundary=boundary, blend_mode=blend)
+    dy = rng.standard_normal(y.shape)
+    g = RM.raymarch_bwd(x, y, dy, M, V, P, F, (9, 6, 7), boundary=boundary, blend_mode=blend, exact=True)
+    d = rng.standard_normal(x.shape)
+    fd = _fd(lambda z: np.sum(RM.raymarch_fwd(z, M, V, P, F, (9, 6, 7), boundary=boundary, blend_mode=blend) * dy), x, d)
+    assert abs(fd - np.sum(g * d)) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_raymarch_reference_normalisation_is_per_camera_weight_mean():
+    """With a constant cell gradient the reference-mode result per voxel is the
+    per-camera weighted mean, so for ADDITIVE blending and dy = 1 every reached
+    voxel gets exactly (number of cameras reaching it)."""
+    _, _, M, V, P, F = scene((8, 10, 9), 2, (9, 6, 7))
+    x = small_grid((8, 10, 9), 1, 3)
+    y = RM.raymarch_fwd(x, M, V, P, F, (9, 6, 7), boundary=S.CLAMP, blend_mode=OB.ADDITIVE)
+    g = RM.raymarch_bwd(x, y, np.ones_like(y), M, V, P, F, (9, 6, 7), boundary=S.CLAMP, blend_mode=OB.ADDITIVE)
+    vals = np.unique(np.round(g, 9))
+    assert set(vals.tolist()) <= {0.0, 1.0, 2.0}
+
+
+@pytest.mark.parametrize('boundary', [S.BORDER, S.CLAMP, S.WRAP])
+def test_lut_exact_adjoint_fd(boundary):
+    rng = np.random.default_rng(4)
+    x = small_grid((7, 8, 6), 2, 5)
+    lut = np.concatenate([rng.standard_normal((1, 7, 8, 6, 3)) * 1.4, np.zeros((1, 7, 8, 6, 1))], -1)
+    dy = rng.standard_normal((1, 1, 7, 8, 6, 2))
+    gx, gl = R.sample_grid_lut_grad(x, dy, lut, boundary=boundary, exact=True)
+    f = lambda xx, ll: np.sum(R.sample_grid_lut(xx, ll, boundary=boundary) * dy)
+    d = rng.standard_normal(x.shape)
+    assert np.isclose(_fd(lambda z: f(z, lut), x, d), np.sum(gx * d), rtol=1e-6, atol=1e-8)
+    dl = rng.standard_normal(lut.shape)
+    dl[..., 3] = 0
+    assert np.isclose(_fd(lambda z: f(x, z), lut, dl), np.sum(gl * dl), rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize('order,clamp', [(1, 'NONE'), (2, 'NONE'), (2, 'MC_SMOOTH'), (1, 'NEGATIVE')])
+def test_advect_exact_adjoint_fd(order, clamp):
+    rng = np.random.default_rng(6)
+    D, H, W = 7, 8, 6
+    d = small_grid((D, H, W), 1, 7)[0]
+    vx = rng.standard_normal((D, H, W + 1, 1)) * 0.7
+    vy = rng.standard_normal((D, H + 1, W, 1)) * 0.7
+    vz = rng.standard_normal((D + 1, H, W, 1)) * 0.7
+    go = rng.standard_normal(d.shape)
+    gd, gx, gy, gz = OA.warp_grad(d, vx, vy, vz, go, 1.1, order, clamp, S.CLAMP, exact=True)
+    f = lambda dd, a, b, c: np.sum(OA.warp(dd, a, b, c, 1.1, order, clamp, S.CLAMP) * go)
+    dd = rng.standard_normal(d.shape)
+    assert np.isclose(_fd(lambda z: f(z, vx, vy, vz), d, dd), np.sum(gd * dd), rtol=1e-6, atol=1e-8)
+    ex = rng.standard_normal(vx.shape)
+    assert np.isclose(_fd(lambda z: f(d, z, vy, vz), vx, ex), np.sum(gx * ex), rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize('blend', [OB.BEER_LAMBERT, OB.ALPHA, OB.ADDITIVE])
+@pytest.mark.parametrize('keep', [False, True])
+def test_blend_exact_adjoint_fd(blend, keep):
+    rng = np.random.default_rng(8)
+    x = rng.random((1, 9, 4, 3, 4)) * 0.3
+    y = OB.reduce_grid_blend(x, blend, keep)
+    dy = rng.standard_normal(y.shape)
+    g = OB.reduce_grid_blend_grad(dy, y, x, blend, keep, exact=True)
+    d = rng.standard_normal(x.shape)
+    fd = _fd(lambda z: np.sum(OB.reduce_grid_blend(z, blend, keep) * dy), x, d)
+    assert np.isclose(fd, np.sum(g * d), rtol=1e-6, atol=1e-9)
+
+
+def test_beer_lambert_matches_closed_form():
+    """renderer._blend_grid's closed form: L = sum l_i exp(-cumsum(s)_i), d = sum s."""
+    rng = np.random.default_rng(9)
+    x = rng.random((1, 12, 3, 2, 4)) * 0.2
+    y = OB.reduce_grid_blend(x, OB.BEER_LAMBERT, False)
+    cs = np.cumsum(x[..., 3:], axis=1)
+    L = np.sum(x[..., :3] * np.exp(-cs), axis=1)
+    assert np.allclose(y[..., :3], L) and np.allclose(y[..., 3:], cs[:, -1])
+
+
+def test_sampling_known_answers():
+    g = np.arange(2 * 3 * 4, dtype=np.float64).reshape(2, 3, 4, 1)  # value = 12 z + 4 y + x
+    p = np.array([[1.25, 0.5, 0.75]])
+    assert np.isclose(S.fetch_linear(g, p, S.CLAMP)[0, 0], 12 * 0.75 + 4 * 0.5 + 1.25)
+    # BORDER: half a cell outside -> 0, inside the half cell -> interpolated with a zero corner
+    assert S.fetch_linear(g, np.array([[-0.6, 0.0, 0.0]]), S.BORDER)[0, 0] == 0.0
+    assert np.isclose(S.fetch_linear(g, np.array([[-0.25, 0.0, 0.0]]), S.BORDER)[0, 0], 0.0)
+    assert np.isclose(S.fetch_linear(g, np.array([[3.25, 0.0, 0.0]]), S.BORDER)[0, 0], 3 * 0.75)
+    # NEAREST truncates pos + 0.5 toward zero
+    assert S.fetch_nearest(g, np.array([[-0.7, 0.0, 0.0]]), S.BORDER)[0, 0] == 0.0
+    assert S.fetch_nearest(g, np.array([[1.49, 1.6, 0.2]]), S.CLAMP)[0, 0] == 4 * 2 + 1
+    # WRAP
+    assert np.isclose(S.fetch_linear(g, np.array([[-1.0, 0.0, 0.0]]), S.WRAP)[0, 0], 3.0)
+    # mips: 2x2x2 means
+    m = S.build_mips(np.ones((4, 6, 8, 1)), 3)
+    assert [l.shape for l in m] == [(4, 6, 8, 1), (2, 3, 4, 1), (1, 1, 2, 1), (0, 0, 1, 1)]
+    assert S.usable_mip_levels((4, 6, 8), 3) == 2
+
+
+def test_lindepth_round_trip():
+    _, cams, M, V, P, F = scene((10, 12, 8), 1, (16, 9, 11))
+    cam = T.CameraXform(M[0], V[0], P[0], F[0])
+    rng = np.random.default_rng(10)
+    idx = rng.random((50, 3)) * [11, 9, 16]
+    os_ = T.idx_to_os_lindepth(cam, idx, np.array([11, 9, 16.0]))
+    back = T.os_to_idx_lindepth(cam, os_, np.array([11, 9, 16.0]))
+    assert np.allclose(back, idx, atol=1e-9)
+    back2 = T.os_to_idx(cam, T.idx_to_os(cam, idx, np.array([11, 9, 16.0])), np.array([11, 9, 16.0]))
+    assert np.allclose(back2, idx, atol=1e-9)
