@@ -256,9 +256,12 @@ __device__ __forceinline__ Vec<C> fetch_nearest(const S* __restrict__ g, Dims d,
 }
 
 // MIN/MAX over the 8 corners.  RAYMARCH=true: read3DInterpolatedWithExtrema
-// (sampling_v2.hpp:158-256), extrema of the valid corners from +-FLOAT_MAX and
-// the start value outside the BORDER domain.  RAYMARCH=false: read3DMin/Max
-// (sampling.hpp:372-491), 0 outside, and a start of 0 when any corner is invalid.
+// (sampling_v2.hpp:149-256): running extremum from +-FLOAT_MAX, updated per
+// valid corner (order fff, cff, fcf, ccf, ffc, cfc, fcc, ccc) as
+// m = m + t*(v - m) with t = (v < m) resp. (m < v); the first update cancels
+// against FLOAT_MAX to 0 exactly as in the reference; the start value outside
+// the BORDER domain.  RAYMARCH=false: read3DMin/Max (sampling.hpp:372-491),
+// 0 outside, and a start of 0 when any corner is invalid.
 template <int C, typename S, int BM, bool IS_MAX, bool RAYMARCH>
 __device__ __forceinline__ Vec<C> fetch_extremum(const S* __restrict__ g, Dims d, float px, float py, float pz) {
     const float start = IS_MAX ? -REF_FLOAT_MAX : REF_FLOAT_MAX;
@@ -280,7 +283,15 @@ __device__ __forceinline__ Vec<C> fetch_extremum(const S* __restrict__ g, Dims d
     for (int k = 0; k < 8; ++k) {
         if (ok[k]) {
             const Vec<C> v = Load<C, S>::at(g, flat3(xs[k], ys[k], zs[k], d));
-            acc = IS_MAX ? vmax(acc, v) : vmin(acc, v);
+            if constexpr (RAYMARCH) {
+#pragma unroll
+                for (int i = 0; i < C; ++i) {
+                    const float t = (IS_MAX ? (acc.v[i] < v.v[i]) : (v.v[i] < acc.v[i])) ? 1.f : 0.f;
+                    acc.v[i] = acc.v[i] + t * (v.v[i] - acc.v[i]);
+                }
+            } else {
+                acc = IS_MAX ? vmax(acc, v) : vmin(acc, v);
+            }
         }
     }
     return acc;

@@ -159,14 +159,21 @@ def fetch_extremum_lut(grid, pos, boundary, is_max):
 
 def fetch_extremum_raymarch(grid, pos, boundary, is_max):
     """MIN/MAX as used by the fused raymarch (read3DInterpolatedWithExtrema,
-    sampling_v2.hpp:158-256): extrema over the *valid* corners only, starting at
-    +-FLOAT_MAX; under BORDER a position outside returns the start value."""
+    sampling_v2.hpp:158-256).  The running extremum starts at +-FLOAT_MAX and
+    is updated per valid corner as m = m + t*(v - m), t = (v < m) resp. (m < v)
+    (read3DWithExtrema, sampling_v2.hpp:149-156), in the corner order fff, cff,
+    fcf, ccf, ffc, cfc, fcc, ccc (the argument evaluation order the reference
+    build uses; pinned by the golden vectors).  The first update cancels
+    against FLOAT_MAX to exactly 0, so the result is the extremum of 0 and the
+    corners after the first valid one.  Under BORDER a position outside returns
+    the start value."""
     dims = dims_xyz(grid)
     vals, valid, _ = _eight(grid, pos, boundary)
     shape = vals[0].shape
     acc = np.full(shape, -FLOAT_MAX if is_max else FLOAT_MAX)
     for v, ok in zip(vals, valid):
-        cand = np.maximum(acc, v) if is_max else np.minimum(acc, v)
+        t = (acc < v) if is_max else (v < acc)
+        cand = acc + t * (v - acc)
         acc = np.where(ok[..., None], cand, acc)
     if boundary == BORDER:
         acc = np.where(_border_inside(pos, dims)[..., None], acc,
