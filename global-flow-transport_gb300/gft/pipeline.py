@@ -43,6 +43,12 @@ CONFIGS = {
     # configs[0]-sized case for quick runs / CPU timing
     'cfg1': dict(grid=(64, 64, 64), views=1, image=(128, 128), samples=64, mips=3,
                  shadow=(64, 64, 64), seed=1000),
+    # stress grid (configs[4] sizes, one frame)
+    'cfg5': dict(grid=(256, 455, 256), views=5, image=(960, 540), samples=256, mips=4,
+                 shadow=(256, 196, 196), seed=5000),
+    # tiny case for tests
+    'tiny': dict(grid=(10, 12, 9), views=2, image=(9, 11), samples=12, mips=2,
+                 shadow=(8, 8, 8), seed=7),
 }
 
 

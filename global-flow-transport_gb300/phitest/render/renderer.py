@@ -325,6 +325,42 @@ class Renderer(object):
                 light_data = light_data + light_grid
         return light_data
 
+    def resample_grid3D_aligned(self, data, target_shape, align_x='BORDER', align_y='BORDER', align_z='BORDER'):
+        """Resize a grid with the TRANSFORM sampler (renderer.py:653-690).
+        align: BORDER, CENTER, STAGGER_INPUT or STAGGER_OUTPUT per axis."""
+        if data.dim() != 5 or len(target_shape) != 3:
+            raise ValueError('input must be NDHWC and target_shape DHW')
+        N, D, H, W, _ = data.shape
+        tz, ty, tx = target_shape
+
+        def get_scale(align, in_size, out_size):
+            a = align.upper()
+            if a == 'BORDER':
+                return 2. / in_size
+            if a == 'CENTER':
+                return 2. / out_size * (out_size - 1.) / (in_size - 1.)
+            if a == 'STAGGER_INPUT':
+                return 2. / (in_size - 1.)
+            if a == 'STAGGER_OUTPUT':
+                return 2. / (in_size + 1.)
+            raise ValueError('unknown alignment {}'.format(align))
+        in_scale = [get_scale(align_x, W, tx), get_scale(align_y, H, ty), get_scale(align_z, D, tz)]
+        in_transform = GridTransform([D, H, W], scale=in_scale, center=True)
+        target_transform = GridTransform(list(target_shape))
+        return self._sample_transform(data, [in_transform] * N, [target_transform]).squeeze(1)
+
+    def resample_grid3D_offset(self, data, offsets, target_shape):
+        """Shift-resample with constant per-batch offsets through the lookup
+        sampler (renderer.py:693-709).  offsets (K,3) -> [N, K, D, H, W, C]."""
+        offs = torch.as_tensor(np.asarray(offsets, dtype=np.float32), device=data.device)
+        if offs.dim() != 2 or offs.shape[1] != 3:
+            raise ValueError('Shape of offsets must be (N,3), is %s' % (tuple(offs.shape),))
+        if len(target_shape) != 3:
+            raise ValueError('target_shape must be (3,), is %s' % (target_shape,))
+        offs = torch.nn.functional.pad(offs, (0, 1)).view(offs.shape[0], 1, 1, 1, 4)
+        lut = offs.expand([offs.shape[0]] + list(target_shape) + [4]).contiguous()
+        return self._sample_LuT(data, lut, relative=True)
+
     def render_density(self, density_transform, light_list, camera_list, cut_alpha=True, background=None,
                        monochrome=False, split_cameras=False, custom_ops=None, tonemapping='NONE'):
         """Light grid + concat density + per-resolution camera batches + background

@@ -1,0 +1,89 @@
+"""The benchmark step and the checkpointed transport chain on a tiny config:
+graph replay equals eager execution, checkpointed gradients equal the plain
+ones, batched equals plain, and the step gradient matches the oracle chain."""
+import numpy as np
+import pytest
+import torch
+
+from scene_utils import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from gft import ops
+    ops.set_grad_mode('REFERENCE')
+    return torch.device('cuda', 0)
+
+
+def _np(t):
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+def test_graph_replay_equals_eager(gpu):
+    from gft.pipeline import RenderAdvectStep
+    s = RenderAdvectStep('tiny', gpu)
+    s.setup_static(s.make_inputs())
+    loss_e, grads_e = s.run_static()
+    loss_e, grads_e = float(loss_e), [_np(g) for g in grads_e]
+    s.capture(warmup=3)
+    loss_g, grads_g = s.replay()
+    torch.cuda.synchronize()
+    assert abs(float(loss_g) - loss_e) <= 1e-5 * abs(loss_e)
+    for a, b in zip(grads_g, grads_e):
+        assert rel_l2(_np(a), b) <= 1e-4
+
+
+def test_batched_equals_plain(gpu):
+    from gft.pipeline import RenderAdvectStep
+    a = RenderAdvectStep('tiny', gpu, mode='batched')
+    inp = a.make_inputs()
+    a.setup_static(inp)
+    b = RenderAdvectStep('tiny', gpu, mode='plain')
+    b.setup_static(inp)
+    la, ga = a.run_static()
+    lb, gb = b.run_static()
+    assert abs(float(la) - float(lb)) <= 1e-5 * abs(float(lb))
+    for x, y in zip(ga, gb):
+        assert rel_l2(_np(x), _np(y)) <= 1e-4
+
+
+def test_bf16_storage_step_close_to_fp32(gpu):
+    from gft.pipeline import RenderAdvectStep
+    a = RenderAdvectStep('tiny', gpu)
+    inp = a.make_inputs()
+    a.setup_static(inp)
+    b = RenderAdvectStep('tiny', gpu, storage_dtype=torch.bfloat16)
+    b.setup_static(inp)
+    la, ga = a.run_static()
+    lb, gb = b.run_static()
+    assert abs(float(la) - float(lb)) <= 1e-2 * abs(float(la))
+    assert rel_l2(_np(gb[0]), _np(ga[0])) <= 1e-2 * 5
+
+
+def test_checkpointed_chain_gradients(gpu):
+    from gft.chain import TransportChain
+    from gft.pipeline import RenderAdvectStep
+    from gft import synthetic as syn
+    s = RenderAdvectStep('tiny', gpu)
+    T = 5
+    d0 = torch.from_numpy(syn.plume_density(s.shape, 3)).to(gpu)
+    vels = []
+    for t in range(T - 1):
+        vx, vy, vz = syn.curl_velocity(s.shape, 10 + t)
+        vels.append(tuple(torch.from_numpy(v).to(gpu).requires_grad_(True) for v in (vx, vy, vz)))
+    with torch.no_grad():
+        targets = [s.render(torch.from_numpy(syn.plume_density(s.shape, 30 + t, t)).to(gpu))[..., :3] for t in range(T)]
+    res = []
+    for ck in (True, False):
+        d = d0.clone().requires_grad_(True)
+        chain = TransportChain(s, frames=T, checkpoint_every=2)
+        loss = chain.loss(d, vels, targets, use_checkpoints=ck)
+        g = torch.autograd.grad(loss, [d] + [v for tr in vels for v in tr])
+        res.append((float(loss), [_np(x) for x in g]))
+    assert abs(res[0][0] - res[1][0]) <= 1e-6 * abs(res[1][0])
+    for a, b in zip(res[0][1], res[1][1]):
+        assert rel_l2(a, b) <= 1e-4
