@@ -284,6 +284,11 @@ def kernel_roofline(step, dev, timed):
         bwd()
     tf = float(np.median(timed(fwd, 7)))
     tb = float(np.median(timed(bwd, 7)))
+    other = 'EXACT' if ops.get_grad_mode() == 'REFERENCE' else 'REFERENCE'
+    bwd_other = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                          ops.GRAD[other])
+    bwd_other()
+    tb_other = float(np.median(timed(bwd_other, 5)))
     nvox = int(np.prod(step.shape))
     s = 4
     pix = V * H * W
@@ -294,7 +299,9 @@ def kernel_roofline(step, dev, timed):
         'raymarch_fwd': {'ms': tf, 'alg_bytes': bytes_fwd, 'GBps': bytes_fwd / tf / 1e6,
                          'gather_GBps': samples * 8 * 16 / tf / 1e6, 'samples_per_s': samples / tf * 1e3},
         'raymarch_bwd': {'ms': tb, 'alg_bytes': bytes_bwd, 'GBps': bytes_bwd / tb / 1e6,
-                         'gather_GBps': samples * 8 * 16 / tb / 1e6, 'samples_per_s': samples / tb * 1e3},
+                         'gather_GBps': samples * 8 * 16 / tb / 1e6, 'samples_per_s': samples / tb * 1e3,
+                         'grad_mode': ops.get_grad_mode()},
+        'raymarch_bwd_' + other.lower(): {'ms': tb_other, 'samples_per_s': samples / tb_other * 1e3},
     }
     dom = 'raymarch_bwd' if tb >= tf else 'raymarch_fwd'
     k = kern[dom]

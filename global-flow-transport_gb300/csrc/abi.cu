@@ -232,10 +232,10 @@ gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, c
 size_t gft_raymarch_grid_transform_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
                                                        int32_t separate_camera_batch, int32_t grad_mode) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why) || grad_mode == GFT_GRAD_EXACT) return 0;
+    if (!grid_shape_ok(input_shape, why) || (grad_mode & ~GFT_GRAD_WEIGHTS_READY) == GFT_GRAD_EXACT) return 0;
     const size_t nvox = (size_t)input_shape[1] * input_shape[2] * input_shape[3];
     const size_t pairs = (size_t)input_shape[0] * (separate_camera_batch ? (size_t)std::max(num_cameras, 1) : 1);
-    return align256(sizeof(float) * nvox * input_shape[4] * pairs) + align256(sizeof(float) * nvox * pairs);
+    return align256(sizeof(float) * nvox * pairs);
 }
 
 gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dtype, const int64_t input_shape[5],
@@ -255,7 +255,11 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
     if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
     if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
+    const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
+    grad_mode &= ~GFT_GRAD_WEIGHTS_READY;
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
@@ -279,16 +283,44 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
     const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
                                   separate_camera_batch != 0);
     a.n_slots = (int)pairs.size();
-    float* buf = nullptr;
-    float* cnt = nullptr;
-    if (need > 0) {
-        const size_t nvox = (size_t)voxels(a.din);
-        buf = reinterpret_cast<float*>(workspace);
-        cnt = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) +
-                                       align256(sizeof(float) * nvox * a.C * pairs.size()));
-    }
-    if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, input_grad, buf, cnt,
-                             as_stream(stream)))
+    float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
+    if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
+                             cnt, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5], const float* matrix_m,
+                                                    int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                                    const float* frustum, int32_t num_cameras,
+                                                    const int32_t output_shape[3], int32_t boundary,
+                                                    int32_t separate_camera_batch, void* workspace,
+                                                    size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
+                                  separate_camera_batch);
+    if (st != GFT_OK) return st;
+    const size_t need = gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras,
+                                                                        separate_camera_batch, GFT_GRAD_REFERENCE);
+    if (workspace == nullptr || workspace_bytes < need)
+        return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    RaymarchArgs a{};
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.D = output_shape[0];
+    a.H = output_shape[1];
+    a.W = output_shape[2];
+    a.filter = GFT_FILTER_LINEAR;
+    a.boundary = boundary;
+    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                                  separate_camera_batch != 0);
+    a.n_slots = (int)pairs.size();
+    if (!launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }

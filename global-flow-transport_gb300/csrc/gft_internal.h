@@ -66,8 +66,11 @@ struct RaymarchArgs {
     int n_slots;  // output slots = N * (separate ? V : 1)
 };
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
+// Per-pair weight sums of the reference-normalised adjoint (pass 1).
+bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s);
+// weights_ready: ws_cnt already holds the pass-1 sums of the same geometry.
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
-                         const float* dout, bool exact, float* grad, float* ws_buf, float* ws_cnt,
+                         const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s);
 
 bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, float* ws, cudaStream_t s,

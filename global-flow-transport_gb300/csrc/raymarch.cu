@@ -11,6 +11,37 @@ namespace gft {
 
 constexpr int RM_BX = 8, RM_BY = 16;  // 128 threads, warp = 8x4 pixels
 
+// Ray clipping.  Under BORDER a LINEAR or NEAREST sample is 0 outside
+// (-1, dims + 0.5) in grid coordinates (the NEAREST domain int(p) in [0, dims)
+// reaches down to -1, the reference-normalised scatter window -1 < p - 0.5 <
+// dims up to dims + 0.5), and blending a zero sample leaves the accumulator
+// unchanged.  So a ray only needs the steps i whose position p0 + i*st can lie
+// in that box: [i_lo, i_hi] from a slab test, widened by a margin (0.05 voxels
+// and one step) far above the rounding of the iterated positions.  The steps
+// before i_lo are still iterated as additions, so the positions of the
+// processed samples are bit-identical to those of the full march.  Returns
+// false when no step can reach the box.
+__device__ __forceinline__ bool ray_clip(float3 p0, float3 st, int n, Dims d, int& i_lo, int& i_hi) {
+    float t0 = 0.f, t1 = (float)(n - 1);
+    const float lo = -1.05f;
+    auto axis = [&](float p, float s, float hi) {
+        if (fabsf(s) < 1e-20f) {
+            if (!(p >= lo && p <= hi)) t0 = 2.f * t1 + 2.f;  // never inside (NaN positions too)
+            return;
+        }
+        const float a = (lo - p) / s, b = (hi - p) / s;
+        t0 = fmaxf(t0, fminf(a, b));
+        t1 = fminf(t1, fmaxf(a, b));
+    };
+    axis(p0.x, st.x, (float)d.x + 0.55f);
+    axis(p0.y, st.y, (float)d.y + 0.55f);
+    axis(p0.z, st.z, (float)d.z + 0.55f);
+    if (!(t0 <= t1)) return false;
+    i_lo = max(0, (int)floorf(t0) - 1);
+    i_hi = min(n - 1, (int)ceilf(t1) + 1);
+    return true;
+}
+
 template <int C, typename S, int BM, bool LIN>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_fwd(const S* __restrict__ in, Dims din, int W, int H, int D, int filter, int blend_mode,
@@ -28,7 +59,22 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     const float3 step = make_float3((farp.x - nearp.x) / zmax, (farp.y - nearp.y) / zmax, (farp.z - nearp.z) / zmax);
     float3 pos = nearp;
     Vec<C> acc = vzero<C>();
-    for (int i = 0; i < D; ++i) {
+    int i0 = 0, i1 = D - 1;
+    // MIN/MAX samples outside are +-FLOAT_MAX, and BEER_LAMBERT_EXCLUSIVE
+    // multiplies a zero sample by exp(-density sum), which overflows for
+    // sums below -88: neither is clipped.
+    if (BM == BM_BORDER && (LIN || filter == F_NEAREST) && (C == 1 || blend_mode != BL_BEER_LAMBERT_EXCLUSIVE)) {
+        if (!ray_clip(nearp, step, D, din, i0, i1)) {
+            store<C>(out, ((int64_t)tab.out_slot[p] * H + y) * W + x, acc);
+            return;
+        }
+        for (int i = 0; i < i0; ++i) {
+            pos.x += step.x;
+            pos.y += step.y;
+            pos.z += step.z;
+        }
+    }
+    for (int i = i0; i <= i1; ++i) {
         Vec<C> smp;
         if constexpr (LIN) {
             smp = fetch_linear<C, S, BM>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
@@ -43,74 +89,139 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     store<C>(out, ((int64_t)tab.out_slot[p] * H + y) * W + x, acc);
 }
 
-// Adjoint: back to front from the far end point, re-sampling (LINEAR only as the
-// reference gradient op) and scattering each cell gradient trilinearly.
-// EXACT: scatter straight into the batch gradient.  Otherwise scatter into the
-// pair's buffer together with the trilinear weights, normalised afterwards.
-template <int C, typename S, int BM, bool EXACT>
-__global__ void __launch_bounds__(RM_BX* RM_BY)
-    k_raymarch_bwd(const S* __restrict__ in, Dims din, int W, int H, int D, int blend_mode,
-                   const float* __restrict__ out, const float* __restrict__ dout, float* __restrict__ grad,
-                   float* __restrict__ buf, float* __restrict__ cnt, const __grid_constant__ PairTable tab) {
-    const int p = blockIdx.z;
-    const int x = blockIdx.x * RM_BX + threadIdx.x;
-    const int y = blockIdx.y * RM_BY + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const CamX& cam = tab.cam[p];
-    const int64_t nvox = voxels(din);
-    const S* g = in + (size_t)tab.in_batch[p] * nvox * C;
-    float* dst;
-    float* count = nullptr;
-    if constexpr (EXACT) {
-        dst = grad + (size_t)tab.in_batch[p] * nvox * C;
-    } else {
-        dst = buf + (size_t)(tab.pair_base + p) * nvox * C;
-        count = cnt + (size_t)(tab.pair_base + p) * nvox;
-    }
+// Ray set-up shared by the adjoint kernels: far end point and step (the
+// reference's grad kernel walks from farPos by -step, raymarch_grid.cu.cc:354-370).
+__device__ __forceinline__ void ray_far_step(const CamX& cam, int x, int y, int W, int H, int D, float3& farp,
+                                             float3& step) {
     const float3 dinv = make_float3(1.f / (float)W, 1.f / (float)H, 1.f / (float)D);
     const float zmax = (float)max(D - 1, 1);
     const float3 nearp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, 0.5f), dinv);
-    const float3 farp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, zmax + 0.5f), dinv);
-    const float3 step = make_float3((farp.x - nearp.x) / zmax, (farp.y - nearp.y) / zmax, (farp.z - nearp.z) / zmax);
-    float3 pos = farp;
-    const int64_t pix = ((int64_t)tab.out_slot[p] * H + y) * W + x;
-    Vec<C> acc = loadf<C>(out, pix);
-    Vec<C> go = loadf<C>(dout, pix);
-    for (int i = D - 1; i >= 0; --i) {
-        const Vec<C> smp = fetch_linear<C, S, BM>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
-        const Vec<C> gc = blend_grad<C>(blend_mode, EXACT, go, smp, acc);
-        if constexpr (EXACT) {
-            scatter_linear<C, BM, 0>(dst, nullptr, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f, gc);
-        } else {
-            scatter_linear<C, BM, 2>(dst, count, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f, gc);
-        }
+    farp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, zmax + 0.5f), dinv);
+    step = make_float3((farp.x - nearp.x) / zmax, (farp.y - nearp.y) / zmax, (farp.z - nearp.z) / zmax);
+}
+
+// Clipped back-to-front march: the adjoint samples far - k*step, k in [0, D).
+// Returns false when no sample can reach the grid; otherwise advances pos over
+// the k < k_lo samples (by iterated subtraction, as the full march) and sets
+// the last sample k_hi that can.
+__device__ __forceinline__ bool clip_back_to_front(float3& pos, float3 step, int D, Dims d, int& k_lo, int& k_hi) {
+    if (!ray_clip(pos, make_float3(-step.x, -step.y, -step.z), D, d, k_lo, k_hi)) return false;
+    for (int k = 0; k < k_lo; ++k) {
         pos.x -= step.x;
         pos.y -= step.y;
         pos.z -= step.z;
     }
+    return true;
 }
 
-// grad[b] = sum over the pairs of batch b of buf / cnt where cnt > 0
-// (kNormalize3DGradients<T,true,AddGrad>, raymarch_grid.cu.cc:319-341).
-template <int C>
-__global__ void k_raymarch_normalize(const float* __restrict__ buf, const float* __restrict__ cnt, int64_t nvox,
-                                     const int* __restrict__ pair_batch_dummy, int npairs_per_batch, int N,
-                                     float* __restrict__ grad) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nvox * N) return;
-    const int b = (int)(t / nvox);
-    const int64_t v = t - (int64_t)b * nvox;
-    Vec<C> acc = vzero<C>();
-    for (int k = 0; k < npairs_per_batch; ++k) {
-        const int64_t pidx = (int64_t)b * npairs_per_batch + k;
-        const float n = cnt[pidx * nvox + v];
-        if (n > 0.f) {
-            const float w = 1.0f / n;
-            const Vec<C> gb = loadf<C>(buf, pidx * nvox + v);
-            acc = vadd(acc, vscale(gb, w));
+// --- adjoint scatters ----------------------------------------------------------
+// Each sample's cell gradient reaches its eight corners as vector reductions
+// (red.global.add.v4/v2.f32) in L2, whose sector throughput bounds these
+// kernels (a warp's 8x4 rays touch ~26 distinct 32-byte sectors per corner).
+// Measured alternatives that did not pay on GB300 at the 5-view 480x270x192
+// workload: summing the samples of 2x1, 1x2 or 2x2 neighbouring rays per
+// thread in registers (few share a footprint at 0.64 voxels per pixel;
+// 1.18-1.43 ms against 1.14 ms), and accumulating each block's samples of 2-8
+// steps in a shared-memory box flushed with coalesced reductions (2.3-3.6 ms:
+// the shared float atomics and the round barriers cost more than the L2
+// sectors they save).
+
+// One sample's trilinear scatter.  MODE 0 (exact adjoint): BORDER drops the
+// sample outside the forward's half-cell window.  MODE 1 (reference-normalised)
+// and MODE 2 (weight sums): BORDER drops it unless -1 < p < dims, the
+// reference's window; MODE 1 divides each corner's contribution by the
+// camera's weight sum there (the per-camera normalise-then-sum applied per
+// contribution, so all cameras accumulate into one gradient) and skips corners
+// with w == 0 or a zero sum.
+template <int C, int BM, int MODE>
+__device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
+                                               float px, float py, float pz, Vec<C> val) {
+    if constexpr (BM == BM_BORDER) {
+        if constexpr (MODE != 0) {
+            if (!(px > -1.f && px < (float)d.x && py > -1.f && py < (float)d.y && pz > -1.f && pz < (float)d.z))
+                return;
+        } else {
+            if (!border_inside(px, py, pz, d)) return;
         }
     }
-    store<C>(grad, t, acc);
+    const Corners c = corners<BM>(px, py, pz, d);
+    const float cw[3] = {c.wx, c.wy, c.wz};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
+        const bool ok = (sx ? c.vx1 : c.vx0) && (sy ? c.vy1 : c.vy0) && (sz ? c.vz1 : c.vz0);
+        if (BM != BM_BORDER || ok) {
+            const float w = (sx ? cw[0] : 1.f - cw[0]) * (sy ? cw[1] : 1.f - cw[1]) * (sz ? cw[2] : 1.f - cw[2]);
+            const int64_t f = flat3(sx ? c.x1 : c.x0, sy ? c.y1 : c.y0, sz ? c.z1 : c.z0, d);
+            if constexpr (MODE == 1) {
+                const float n = __ldg(cnt + f);
+                if (w != 0.f && n > 0.f) atomic_add<C>(grad, f, vscale(vscale(val, w), 1.0f / n));
+            } else {
+                atomic_add<C>(grad, f, vscale(val, w));
+            }
+        }
+    }
+}
+
+// Back to front from the far end point over the (clipped) samples of one ray.
+// MODE 2, the reference normalisation's first pass: per (batch, camera) pair
+// the per-voxel sum of the trilinear weights of all its samples (the float
+// sampleCounter of raymarch_grid.cu.cc:446-456); geometry only, C == 1, no
+// gathers.  MODE 0 / 1, the adjoint: re-sample (LINEAR only, as the reference
+// gradient op), step the blend adjoint and scatter the cell gradient into the
+// batch gradient; MODE 1 normalises by the pass-1 sums, which equals the
+// reference's per-camera normalise-then-sum (kNormalize3DGradients,
+// raymarch_grid.cu.cc:319-341 and :519-568) without per-camera buffers.
+//
+// Clipping (BORDER): a zero sample's adjoint step leaves the state unchanged
+// for ADDITIVE, ALPHA_ADDITIVE and C == 1, and for the two BEER_LAMBERT modes
+// when the density of the accumulated output is >= 0 (always the case for a
+// forward output; a negative one is first clamped by max(., 0), so such rays
+// march in full).  ALPHA changes its bookkeeping on every step and marches in
+// full.  (Non-finite adjoints are not propagated through skipped samples.)
+template <int C, typename S, int BM, int MODE>
+__global__ void __launch_bounds__(RM_BX* RM_BY)
+    k_raymarch_scatter(const S* __restrict__ in, Dims din, int W, int H, int D, int blend_mode,
+                       const float* __restrict__ out, const float* __restrict__ dout, float* __restrict__ grad,
+                       const float* __restrict__ cnt, const __grid_constant__ PairTable tab) {
+    const int p = blockIdx.z;
+    const int x = blockIdx.x * RM_BX + threadIdx.x;
+    const int y = blockIdx.y * RM_BY + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int64_t nvox = voxels(din);
+    float3 pos, step;
+    ray_far_step(tab.cam[p], x, y, W, H, D, pos, step);
+    const S* g = in + (size_t)tab.in_batch[p] * nvox * C;
+    float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * nvox : grad + (size_t)tab.in_batch[p] * nvox * C;
+    const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * nvox : nullptr;
+    Vec<C> acc = vzero<C>(), go = vzero<C>();
+    if constexpr (MODE != 2) {
+        const int64_t pix = ((int64_t)tab.out_slot[p] * H + y) * W + x;
+        acc = loadf<C>(out, pix);
+        go = loadf<C>(dout, pix);
+    }
+    int k_lo = 0, k_hi = D - 1;
+    if constexpr (BM == BM_BORDER) {
+        const bool clip = MODE == 2 || C == 1 || blend_mode == BL_ADDITIVE || blend_mode == BL_ALPHA_ADDITIVE ||
+                          ((blend_mode == BL_BEER_LAMBERT || blend_mode == BL_BEER_LAMBERT_EXCLUSIVE) &&
+                           acc.v[C - 1] >= 0.f);
+        if (clip && !clip_back_to_front(pos, step, D, din, k_lo, k_hi)) return;
+    }
+#pragma unroll 4
+    for (int k = k_lo; k <= k_hi; ++k) {
+        const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
+        Vec<C> val;
+        if constexpr (MODE == 2) {
+            val = vfill<C>(1.f);
+        } else {
+            const Vec<C> smp = fetch_linear<C, S, BM>(g, din, px, py, pz);
+            val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
+        }
+        scatter_sample<C, BM, MODE>(dst, count, din, px, py, pz, val);
+        pos.x -= step.x;
+        pos.y -= step.y;
+        pos.z -= step.z;
+    }
 }
 
 template <int C, typename S, int BM>
@@ -154,63 +265,70 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
 }
 
 template <int C, typename S, int BM>
-static void bwd_dispatch_exact(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a,
-                               const float* out, const float* dout, float* grad, float* buf, float* cnt,
-                               const PairTable& t) {
+static void bwd_dispatch(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
+                         const float* dout, float* grad, const float* cnt, const PairTable& t) {
     if (exact)
-        k_raymarch_bwd<C, S, BM, true><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend, out,
-                                                               dout, grad, buf, cnt, t);
+        k_raymarch_scatter<C, S, BM, 0><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend,
+                                                                  out, dout, grad, cnt, t);
     else
-        k_raymarch_bwd<C, S, BM, false><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend, out,
-                                                                dout, grad, buf, cnt, t);
+        k_raymarch_scatter<C, S, BM, 1><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend,
+                                                                  out, dout, grad, cnt, t);
 }
 
 template <int C, typename S>
 static void bwd_dispatch_bm(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a,
-                            const float* out, const float* dout, float* grad, float* buf, float* cnt,
-                            const PairTable& t) {
+                            const float* out, const float* dout, float* grad, const float* cnt, const PairTable& t) {
     switch (a.boundary) {
-        case BM_BORDER: bwd_dispatch_exact<C, S, BM_BORDER>(exact, grid, block, s, a, out, dout, grad, buf, cnt, t); break;
-        case BM_CLAMP: bwd_dispatch_exact<C, S, BM_CLAMP>(exact, grid, block, s, a, out, dout, grad, buf, cnt, t); break;
-        default: bwd_dispatch_exact<C, S, BM_WRAP>(exact, grid, block, s, a, out, dout, grad, buf, cnt, t); break;
+        case BM_BORDER: bwd_dispatch<C, S, BM_BORDER>(exact, grid, block, s, a, out, dout, grad, cnt, t); break;
+        case BM_CLAMP: bwd_dispatch<C, S, BM_CLAMP>(exact, grid, block, s, a, out, dout, grad, cnt, t); break;
+        default: bwd_dispatch<C, S, BM_WRAP>(exact, grid, block, s, a, out, dout, grad, cnt, t); break;
     }
 }
 
+template <int BM>
+static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
+                             const PairTable& t) {
+    k_raymarch_scatter<1, float, BM, 2><<<grid, block, 0, s>>>(nullptr, a.din, a.W, a.H, a.D, a.blend, nullptr,
+                                                                  nullptr, cnt, nullptr, t);
+}
+
+bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
+    const int64_t nvox = voxels(a.din);
+    if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * nvox * pairs.size(), s), "zero weights")) return false;
+    const dim3 block(RM_BX, RM_BY, 1);
+    const int gx = (a.W + RM_BX - 1) / RM_BX, gy = (a.H + RM_BY - 1) / RM_BY;
+    for (const PairTable& t : make_tables(pairs)) {
+        const dim3 grid(gx, gy, t.n);
+        switch (a.boundary) {
+            case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, t); break;
+            case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, t); break;
+            default: weights_dispatch<BM_WRAP>(grid, block, s, a, ws_cnt, t); break;
+        }
+        if (!launched(1, "raymarch weight launch")) return false;
+    }
+    return true;
+}
+
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
-                         const float* dout, bool exact, float* grad, float* ws_buf, float* ws_cnt,
+                         const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s) {
     const int64_t nvox = voxels(a.din);
-    if (exact) {
-        if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvox * a.C * a.N, s), "zero gradient")) return false;
-    } else {
-        const size_t np = pairs.size();
-        if (!cuda_ok(cudaMemsetAsync(ws_buf, 0, sizeof(float) * nvox * a.C * np, s), "zero buffer")) return false;
-        if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * nvox * np, s), "zero counter")) return false;
-    }
+    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvox * a.C * a.N, s), "zero gradient")) return false;
+    if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
     const dim3 block(RM_BX, RM_BY, 1);
+    const int gx = (a.W + RM_BX - 1) / RM_BX, gy = (a.H + RM_BY - 1) / RM_BY;
     for (const PairTable& t : make_tables(pairs)) {
-        const dim3 grid((a.W + RM_BX - 1) / RM_BX, (a.H + RM_BY - 1) / RM_BY, t.n);
+        const dim3 grid(gx, gy, t.n);
         if (a.dtype == 0) {
-            if (a.C == 4) bwd_dispatch_bm<4, float>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
-            else if (a.C == 2) bwd_dispatch_bm<2, float>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
-            else bwd_dispatch_bm<1, float>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
+            if (a.C == 4) bwd_dispatch_bm<4, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            else if (a.C == 2) bwd_dispatch_bm<2, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            else bwd_dispatch_bm<1, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
         } else {
-            if (a.C == 4) bwd_dispatch_bm<4, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
-            else if (a.C == 2) bwd_dispatch_bm<2, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
-            else bwd_dispatch_bm<1, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_buf, ws_cnt, t);
+            if (a.C == 4) bwd_dispatch_bm<4, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            else if (a.C == 2) bwd_dispatch_bm<2, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            else bwd_dispatch_bm<1, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
         }
         if (!launched(1, "raymarch backward launch")) return false;
-    }
-    if (!exact) {
-        // pairs are ordered batch-major with the same count per batch
-        const int per_batch = (int)(pairs.size() / a.N);
-        const int64_t total = nvox * a.N;
-        const int threads = 256;
-        const unsigned blocks = (unsigned)((total + threads - 1) / threads);
-        if (a.C == 4) k_raymarch_normalize<4><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
-        else if (a.C == 2) k_raymarch_normalize<2><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
-        else k_raymarch_normalize<1><<<blocks, threads, 0, s>>>(ws_buf, ws_cnt, nvox, nullptr, per_batch, a.N, grad);
-        if (!launched(1, "raymarch normalize launch")) return false;
     }
     return true;
 }

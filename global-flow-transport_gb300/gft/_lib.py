@@ -49,6 +49,8 @@ _SIGS = {
     'gft_raymarch_grid_transform_grad_workspace_size': (_SZ, [_I64P, _I32, _I32, _I32]),
     'gft_raymarch_grid_transform_grad': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                                 _I32, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_raymarch_grid_transform_grad_weights': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32, _I32,
+                                                        _P, _SZ, _P]),
     'gft_sample_grid_transform_workspace_size': (_SZ, [_I64P, _I32, _I32]),
     'gft_sample_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                          _I32, _I32, _I32, _I32, _F, _I32, _F, _I32, _P, _P, _SZ, _P]),

@@ -145,7 +145,55 @@ def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate):
     return out
 
 
-def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode):
+WEIGHTS_READY = 0x100  # GFT_GRAD_WEIGHTS_READY
+
+
+def _raymarch_weights(x, M, V, P, F, out_shape, boundary, separate):
+    """Pass 1 of the reference-normalised raymarch gradient (per-camera weight
+    sums) into a new workspace, on the current stream."""
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, _ = _mats(P)
+    Fh, _ = _frustum(F)
+    shape = _lib.i64(x.shape)
+    ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), GRAD['REFERENCE']),
+                    x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_grad_weights(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
+                                                          _lib.i32(out_shape), boundary, int(separate), _p(ws),
+                                                          ws.numel(), _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformGrad weights')
+    return ws
+
+
+_side_streams = {}
+
+
+def _side_stream(dev):
+    s = _side_streams.get(dev.index)
+    if s is None:
+        s = _side_streams[dev.index] = torch.cuda.Stream(dev)
+    return s
+
+
+def _raymarch_weights_async(x, M, V, P, F, out_shape, boundary, separate):
+    """Launches the geometry-only weight pass on a side stream forked from the
+    current one, so that it overlaps the rest of the forward pass (the pass is
+    bound by L2 reductions, the forward kernels by issue and L1); returns the
+    workspace and the event the backward waits on.  Fork and join are stream
+    waits, so a CUDA-graph capture records the two branches."""
+    cur = torch.cuda.current_stream(x.device)
+    side = _side_stream(x.device)
+    side.wait_stream(cur)
+    with torch.cuda.stream(side):
+        ws = _raymarch_weights(x, M, V, P, F, out_shape, boundary, separate)
+        ev = torch.cuda.Event()
+        ev.record(side)
+    return ws, ev
+
+
+def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None):
     lib = _lib.load()
     Mh, nm = _mats(M)
     Vh, nv = _mats(V)
@@ -153,8 +201,12 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
     Fh, _ = _frustum(F)
     shape = _lib.i64(x.shape)
     grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
-    ws_n = lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode)
-    ws = _workspace(ws_n, x.device)
+    if weights is not None and gmode == GRAD['REFERENCE']:
+        ws = weights
+        gmode = gmode | WEIGHTS_READY
+    else:
+        ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode),
+                        x.device)
     with torch.cuda.device(x.device):
         st = lib.gft_raymarch_grid_transform_grad(_p(x), _dtype_code(x), shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
                                                   _p(Ph), _p(Fh), nv, _lib.i32(out_shape), interp, boundary, blend,
@@ -168,6 +220,9 @@ class _Raymarch(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype):
         xs = _storage(x, storage_dtype)
+        ctx.weights = None
+        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+            ctx.weights = _raymarch_weights_async(xs, M, V, P, F, out_shape, boundary, separate)
         y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate)
         ctx.save_for_backward(xs, y)
         ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate)
@@ -178,8 +233,13 @@ class _Raymarch(torch.autograd.Function):
     def backward(ctx, dy):
         xs, y = ctx.saved_tensors
         M, V, P, F, out_shape, interp, boundary, blend, separate = ctx.args
+        ws = None
+        if ctx.weights is not None:
+            ws, ev = ctx.weights
+            torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                          GRAD[get_grad_mode()])
+                          GRAD[get_grad_mode()], weights=ws)
+        ctx.weights = None
         return (g.to(ctx.in_dtype),) + (None,) * 10
 
 

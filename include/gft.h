@@ -102,6 +102,21 @@ gft_status gft_raymarch_grid_transform_grad(
     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
     int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
     int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+/* The geometry-only first pass of the GFT_GRAD_REFERENCE raymarch gradient:
+ * per (batch, camera) pair the per-voxel sums of the trilinear weights of all
+ * ray samples (the reference's float sampleCounter, raymarch_grid.cu.cc:446-456),
+ * written into the workspace of gft_raymarch_grid_transform_grad.  It needs
+ * neither the forward output nor its gradient, so a caller can run it on
+ * another stream while the forward pass is still running; the gradient call
+ * then takes grad_mode GFT_GRAD_REFERENCE | GFT_GRAD_WEIGHTS_READY, the same
+ * geometry and workspace, and skips the pass.  No counterpart in the
+ * reference, whose gradient kernel accumulates the sums itself. */
+#define GFT_GRAD_WEIGHTS_READY 0x100
+gft_status gft_raymarch_grid_transform_grad_weights(
+    const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t boundary, int32_t separate_camera_batch, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- SampleGridTransform (resample_grid.cc:23-61, :268-447; launcher resample_grid.cu.cc:289-438) ----
  * output [N, separate_camera_batch ? num_cameras : 1, Do, Ho, Wo, C] fp32.

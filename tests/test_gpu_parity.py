@@ -85,6 +85,22 @@ def test_raymarch_backward(ops, C, blend, boundary, mode):
     assert rel_l2(np_(xt.grad), ref) <= GRAD_TOL
 
 
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+def test_raymarch_backward_weights_on_side_stream(ops, boundary):
+    """Autograd runs the reference-mode weight pass on a side stream during the
+    forward; the gradient op called alone runs it inline: same gradient."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 21) * 0.4
+    dy = cuda(np.random.default_rng(22).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+    xt = cuda(x).requires_grad_(True)
+    with ops.grad_mode('REFERENCE'):
+        y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11), 'LINEAR', boundary)
+        y.backward(dy)
+        g_inline = ops.raymarch_grid_transform_grad(cuda(x), y.detach(), dy, M, V, P, F, (13, 9, 11), 'LINEAR',
+                                                    boundary)
+    assert rel_l2(np_(xt.grad), np_(g_inline)) <= 1e-6
+
+
 def test_raymarch_not_separate_batch(ops):
     from oracle import raymarch as RM
     _, _, M, V, P, F = scene((8, 9, 7), 2, (9, 6, 5))

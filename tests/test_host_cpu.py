@@ -70,8 +70,22 @@ def test_argument_errors_without_a_gpu(lib):
     st = L.gft_raymarch_grid_transform_grad(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1), ctypes.c_void_p(1),
                                             p, 1, p, p, f, 1, out, 1, 0, 0, 1, 0, ctypes.c_void_p(1), None, 0, None)
     assert st == lib.ERR_WORKSPACE
-    assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 0) >= 8 * 8 * 8 * 5 * 5 * 4
+    assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 0) >= 8 * 8 * 8 * 5 * 4
     assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 1) == 0
+    # precomputed weight sums are a reference-mode workspace: not with EXACT
+    st = L.gft_raymarch_grid_transform_grad(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                            p, 1, p, p, f, 1, out, 1, 0, 0, 1, 1 | 0x100, ctypes.c_void_p(1), None,
+                                            0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    # the weight pass validates like the gradient: workspace, boundary, cameras
+    st = L.gft_raymarch_grid_transform_grad_weights(shape4, p, 1, p, p, f, 1, out, 0, 1, None, 0, None)
+    assert st == lib.ERR_WORKSPACE
+    st = L.gft_raymarch_grid_transform_grad_weights(shape4, p, 1, p, p, f, 1, out, 5, 1, ctypes.c_void_p(1),
+                                                    1 << 20, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
+    st = L.gft_raymarch_grid_transform_grad_weights(shape4, p, 2, p, p, f, 1, out, 0, 1, ctypes.c_void_p(1),
+                                                    1 << 20, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
     # SampleGridTransform: cell centre offset must be 0.5 for transform modes
     st = L.gft_sample_grid_transform(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 0, 0.0, 0,
                                      0.25, 1, ctypes.c_void_p(1), None, 0, None)
