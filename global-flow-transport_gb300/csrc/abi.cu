@@ -75,18 +75,24 @@ static Mat4 to_mat4(const double a[4][4]) {
 }
 
 static CamX make_cam(const float* M, const float* V, const float* P, const float* F) {
-    double m[4][4], v[4][4], p[4][4], mv[4][4], mvi[4][4], pi[4][4];
+    double m[4][4], v[4][4], p[4][4], mv[4][4], mvi[4][4], pi[4][4], q[4][4], r[4][4];
     mat_from_flat(M, m);
     mat_from_flat(V, v);
     mat_from_flat(P, p);
     matmul4(v, m, mv);
     inverse4(mv, mvi);
     inverse4(p, pi);
+    // q: rows 0-2 of MV^-1 P^-1 and row 3 of P^-1 (NDC -> OS, see CamX); r = P MV
+    matmul4(mvi, pi, q);
+    for (int j = 0; j < 4; ++j) q[3][j] = pi[3][j];
+    matmul4(p, mv, r);
     CamX c;
     c.mv = to_mat4(mv);
     c.mv_inv = to_mat4(mvi);
     c.p = to_mat4(p);
     c.p_inv = to_mat4(pi);
+    c.q = to_mat4(q);
+    c.r = to_mat4(r);
     c.near_ = F[0];
     c.far_ = F[1];
     c.p22 = (float)p[2][2];

@@ -380,10 +380,31 @@ __device__ __forceinline__ float4 mul(const Mat4& m, float4 v) {
                        m.r2.x * v.x + m.r2.y * v.y + m.r2.z * v.z + m.r2.w * v.w,
                        m.r3.x * v.x + m.r3.y * v.y + m.r3.z * v.z + m.r3.w * v.w);
 }
+// h + s * (column j of m)
+template <int J>
+__device__ __forceinline__ float4 add_col(float4 h, const Mat4& m, float s) {
+    const float a = J == 0 ? m.r0.x : J == 1 ? m.r0.y : m.r0.z;
+    const float b = J == 0 ? m.r1.x : J == 1 ? m.r1.y : m.r1.z;
+    const float c = J == 0 ? m.r2.x : J == 1 ? m.r2.y : m.r2.z;
+    const float d = J == 0 ? m.r3.x : J == 1 ? m.r3.y : m.r3.z;
+    return make_float4(fmaf(a, s, h.x), fmaf(b, s, h.y), fmaf(c, s, h.z), fmaf(d, s, h.w));
+}
+__device__ __forceinline__ float3 dehom(float4 h) {
+    const float iw = 1.f / h.w;
+    return make_float3(h.x * iw, h.y * iw, h.z * iw);
+}
 
-// Per (model, camera) constants: MV = V*M and the inverses of MV and P.
+// Per (model, camera) constants: MV = V*M, the inverses of MV and P, and two
+// products folded on the host in double precision:
+//   q (NDC -> OS): rows 0-2 are those of MV^-1 * P^-1, row 3 is row 3 of P^-1,
+//     so OS = (q ndc).xyz / (q ndc).w equals MV^-1 (P^-1 ndc / w) for any MV;
+//   r (OS -> clip) = P * MV.
+// Sample positions use the reference's operation sequence (two products, four
+// divisions) so that they round exactly as the reference's: its count
+// normalisation and NEAREST lookups jump where a position is integral.  The
+// folded forms serve the LOD's finite differences, which vary continuously.
 struct CamX {
-    Mat4 mv, mv_inv, p, p_inv;
+    Mat4 mv, mv_inv, p, p_inv, q, r;
     float near_, far_, p22, p23;  // frustum near/far, P[2][2], P[2][3]
 };
 
@@ -393,19 +414,26 @@ __device__ __forceinline__ float4 ndc_to_os(const CamX& c, float4 ndc) {
     vs = make_float4(vs.x / iw, vs.y / iw, vs.z / iw, vs.w / iw);
     return mul(c.mv_inv, vs);
 }
+__device__ __forceinline__ float4 idx_to_ndc(float3 idx, float3 dims_inv) {
+    return make_float4(idx.x * dims_inv.x * 2.f - 1.f, idx.y * dims_inv.y * 2.f - 1.f, idx.z * dims_inv.z * 2.f - 1.f,
+                       1.f);
+}
+// NDC depth of the linear-depth coordinate t = idx.z / dims.z (view depth
+// linear between near and far).
+__device__ __forceinline__ float lindepth_ndc_z(const CamX& c, float idx_z, float dinv_z) {
+    const float t = idx_z * dinv_z;
+    const float z = -(c.near_ + t * (c.far_ - c.near_));
+    return -c.p22 - c.p23 / z;
+}
 // IDXtoOS: idx -> NDC = idx*dims_inv*2-1 -> VS -> OS
 __device__ __forceinline__ float3 idx_to_os(const CamX& c, float3 idx, float3 dims_inv) {
-    const float4 ndc = make_float4(idx.x * dims_inv.x * 2.f - 1.f, idx.y * dims_inv.y * 2.f - 1.f,
-                                   idx.z * dims_inv.z * 2.f - 1.f, 1.f);
-    const float4 o = ndc_to_os(c, ndc);
+    const float4 o = ndc_to_os(c, idx_to_ndc(idx, dims_inv));
     return make_float3(o.x, o.y, o.z);
 }
-// IDXtoOSlinearDepth: view depth linear in idx.z/dims.z between near and far
+// IDXtoOSlinearDepth
 __device__ __forceinline__ float3 idx_to_os_lindepth(const CamX& c, float3 idx, float3 dims_inv) {
-    float4 ndc = make_float4(idx.x * dims_inv.x * 2.f - 1.f, idx.y * dims_inv.y * 2.f - 1.f, 0.f, 1.f);
-    const float t = idx.z * dims_inv.z;
-    const float z = -(c.near_ + t * (c.far_ - c.near_));
-    ndc.z = -c.p22 - c.p23 / z;
+    float4 ndc = idx_to_ndc(idx, dims_inv);
+    ndc.z = lindepth_ndc_z(c, idx.z, dims_inv.z);
     const float4 o = ndc_to_os(c, ndc);
     return make_float3(o.x, o.y, o.z);
 }
@@ -415,19 +443,26 @@ __device__ __forceinline__ float4 os_to_ndc(const CamX& c, float3 p) {
     const float iw = n.w;
     return make_float4(n.x / iw, n.y / iw, n.z / iw, n.w / iw);
 }
+// NDC -> idx of a frustum grid of the given dims; LIN: linear-depth z
+template <bool LIN>
+__device__ __forceinline__ float3 ndc_to_idx(const CamX& c, float3 n, float3 dims) {
+    float3 idx = make_float3((n.x * 0.5f + 0.5f) * dims.x, (n.y * 0.5f + 0.5f) * dims.y, (n.z * 0.5f + 0.5f) * dims.z);
+    if constexpr (LIN) {
+        const float z = -c.p23 / (n.z + c.p22);
+        const float t = -(z + c.near_) / (c.far_ - c.near_);
+        idx.z = t * dims.z;
+    }
+    return idx;
+}
 // OStoIDX
 __device__ __forceinline__ float3 os_to_idx(const CamX& c, float3 p, float3 dims) {
     const float4 n = os_to_ndc(c, p);
-    return make_float3((n.x * 0.5f + 0.5f) * dims.x, (n.y * 0.5f + 0.5f) * dims.y, (n.z * 0.5f + 0.5f) * dims.z);
+    return ndc_to_idx<false>(c, make_float3(n.x, n.y, n.z), dims);
 }
 // OStoIDXlinearDepth
 __device__ __forceinline__ float3 os_to_idx_lindepth(const CamX& c, float3 p, float3 dims) {
     const float4 n = os_to_ndc(c, p);
-    float3 idx = make_float3((n.x * 0.5f + 0.5f) * dims.x, (n.y * 0.5f + 0.5f) * dims.y, 0.f);
-    const float z = -c.p23 / (n.z + c.p22);
-    const float t = -(z + c.near_) / (c.far_ - c.near_);
-    idx.z = t * dims.z;
-    return idx;
+    return ndc_to_idx<true>(c, make_float3(n.x, n.y, n.z), dims);
 }
 
 // --- blend functors (blending.hpp:10-221) -------------------------------------

@@ -127,18 +127,40 @@ __device__ __forceinline__ float3 map_pos(const CamX& c, int cm, float3 idx, flo
 
 // samplePos3D<CM, MIP> (sampling.hpp:58-136): position and LOD from forward
 // differences; forward modes use Jacobian rows, reverse modes its columns.
-__device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv,
-                                             bool lod) {
-    const float3 p = map_pos(c, cm, idx, din, dout_inv);
-    if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
-    const float3 ex = map_pos(c, cm, make_float3(idx.x + 1.f, idx.y, idx.z), din, dout_inv);
-    const float3 ey = map_pos(c, cm, make_float3(idx.x, idx.y + 1.f, idx.z), din, dout_inv);
-    const float3 ez = map_pos(c, cm, make_float3(idx.x, idx.y, idx.z + 1.f), din, dout_inv);
-    const float3 dx = make_float3(p.x - ex.x, p.y - ex.y, p.z - ex.z);
-    const float3 dy = make_float3(p.x - ey.x, p.y - ey.y, p.z - ey.z);
-    const float3 dz = make_float3(p.x - ez.x, p.y - ez.y, p.z - ez.z);
+// The position follows the reference's operation sequence.  For the LOD the
+// neighbours idx + e_x, e_y, e_z differ from idx by a constant step in the
+// folded homogeneous coordinates (for the linear-depth z, by a step of NDC z
+// alone), so each costs a column add and a reciprocal instead of a transform;
+// the differences are taken between folded positions.
+template <int CM>
+__device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float3 din, float3 dout_inv, bool lod) {
+    float3 p, f, ex, ey, ez;
+    if constexpr (CM == CM_TRANSFORM || CM == CM_LINDEPTH) {
+        p = CM == CM_TRANSFORM ? idx_to_os(c, idx, dout_inv) : idx_to_os_lindepth(c, idx, dout_inv);
+        if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
+        float4 ndc = idx_to_ndc(idx, dout_inv);
+        if (CM == CM_LINDEPTH) ndc.z = lindepth_ndc_z(c, idx.z, dout_inv.z);
+        const float4 h = mul(c.q, ndc);
+        const float dz = CM == CM_TRANSFORM ? 2.f * dout_inv.z : lindepth_ndc_z(c, idx.z + 1.f, dout_inv.z) - ndc.z;
+        f = dehom(h);
+        ex = dehom(add_col<0>(h, c.q, 2.f * dout_inv.x));
+        ey = dehom(add_col<1>(h, c.q, 2.f * dout_inv.y));
+        ez = dehom(add_col<2>(h, c.q, dz));
+    } else {
+        constexpr bool LIN = CM == CM_LINDEPTH_REVERSE;
+        p = LIN ? os_to_idx_lindepth(c, idx, din) : os_to_idx(c, idx, din);
+        if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
+        const float4 h = mul(c.r, make_float4(idx.x, idx.y, idx.z, 1.f));
+        f = ndc_to_idx<LIN>(c, dehom(h), din);
+        ex = ndc_to_idx<LIN>(c, dehom(add_col<0>(h, c.r, 1.f)), din);
+        ey = ndc_to_idx<LIN>(c, dehom(add_col<1>(h, c.r, 1.f)), din);
+        ez = ndc_to_idx<LIN>(c, dehom(add_col<2>(h, c.r, 1.f)), din);
+    }
+    const float3 dx = make_float3(f.x - ex.x, f.y - ex.y, f.z - ex.z);
+    const float3 dy = make_float3(f.x - ey.x, f.y - ey.y, f.z - ey.z);
+    const float3 dz = make_float3(f.x - ez.x, f.y - ez.y, f.z - ez.z);
     float px, py, pz;
-    if (cm == CM_LINDEPTH || cm == CM_TRANSFORM) {
+    if constexpr (CM == CM_LINDEPTH || CM == CM_TRANSFORM) {
         px = sqrtf(dx.x * dx.x + dy.x * dy.x + dz.x * dz.x);
         py = sqrtf(dx.y * dx.y + dy.y * dy.y + dz.y * dz.y);
         pz = sqrtf(dx.z * dx.z + dy.z * dy.z + dz.z * dz.z);
@@ -149,6 +171,16 @@ __device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, 
     }
     const float dm = fmaxf(px, fmaxf(py, pz));
     return make_float4(p.x, p.y, p.z, fmaxf(0.f, log2f(dm)));
+}
+
+__device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv,
+                                             bool lod) {
+    switch (cm) {
+        case CM_LINDEPTH: return sample_pos_cm<CM_LINDEPTH>(c, idx, din, dout_inv, lod);
+        case CM_TRANSFORM: return sample_pos_cm<CM_TRANSFORM>(c, idx, din, dout_inv, lod);
+        case CM_LINDEPTH_REVERSE: return sample_pos_cm<CM_LINDEPTH_REVERSE>(c, idx, din, dout_inv, lod);
+        default: return sample_pos_cm<CM_TRANSFORM_REVERSE>(c, idx, din, dout_inv, lod);
+    }
 }
 
 template <int C, typename S, int BM>
