@@ -697,4 +697,85 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
     return GFT_OK;
 }
 
+// ---------------------------------------------------------------- pipeline fusions
+static bool single_channel_grid(const int64_t* shape, std::string& why) {
+    if (!grid_shape_ok(shape, why)) return false;
+    if (shape[4] != 1) {
+        why = "expected a single-channel grid [N, D, H, W, 1]";
+        return false;
+    }
+    return true;
+}
+
+gft_status gft_transmittance(const float* input, const int64_t shape[5], float* output, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_transmittance(input, (int)shape[0], dims_of(shape), output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_transmittance_grad(const float* output, const float* output_grad, const int64_t shape[5],
+                                  float* input_grad, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_transmittance_grad(output, output_grad, (int)shape[0], dims_of(shape), input_grad, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
+                             const int64_t shape[5], float ambient, float scale, float* output, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!density || !transmittance || !light_color || !output)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], voxels(dims_of(shape)), ambient,
+                              scale, output, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose_grad(const float* density, const float* transmittance, const float* light_color,
+                                  const int64_t shape[5], float ambient, float scale, const float* output_grad,
+                                  float* density_grad, float* transmittance_grad, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!density || !transmittance || !light_color || !output_grad || !density_grad || !transmittance_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (!launch_light_compose_grad(density, transmittance, light_color, output_grad, (int)shape[0],
+                                   voxels(dims_of(shape)), ambient, scale, density_grad, transmittance_grad,
+                                   as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_image_loss_workspace_size(int64_t pixels) {
+    if (pixels <= 0) return 0;
+    return align256(sizeof(float) * (size_t)image_loss_blocks(pixels));
+}
+
+gft_status gft_image_loss(const float* image, const float* target, const float background[3], int64_t pixels,
+                          float* loss, void* workspace, size_t workspace_bytes, void* stream) {
+    if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
+    if (!image || !target || !background || !loss) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    if (workspace == nullptr || workspace_bytes < gft_image_loss_workspace_size(pixels))
+        return fail(GFT_ERR_WORKSPACE, "image loss workspace too small");
+    if (!launch_image_loss(image, target, pixels, background, reinterpret_cast<float*>(workspace), loss,
+                           as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
+                               const float* loss_grad, float* image_grad, void* stream) {
+    if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
+    if (!image || !target || !background || !loss_grad || !image_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    if (!launch_image_loss_grad(image, target, pixels, background, loss_grad, image_grad, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
 }  // extern "C"

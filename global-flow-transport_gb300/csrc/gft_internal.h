@@ -66,9 +66,9 @@ struct RaymarchArgs {
     int n_slots;  // output slots = N * (separate ? V : 1)
 };
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
-// Per-pair weight sums of the reference-normalised adjoint (pass 1).
+// Per-pair reciprocal weight sums of the reference-normalised adjoint (pass 1).
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s);
-// weights_ready: ws_cnt already holds the pass-1 sums of the same geometry.
+// weights_ready: ws_cnt already holds the pass-1 reciprocals of the same geometry.
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
                          const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s);
@@ -123,5 +123,18 @@ struct AdvectArgs {
 bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s);
 bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
                        float* gvz, float* ws, cudaStream_t s);
+
+// pipeline fusions (compose.cu)
+bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st);
+bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st);
+bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, int64_t nvox, float ambient,
+                          float scale, float* out, cudaStream_t st);
+bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N,
+                               int64_t nvox, float ambient, float scale, float* gd, float* gt, cudaStream_t st);
+int image_loss_blocks(int64_t npix);
+bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], float* partial,
+                       float* loss, cudaStream_t st);
+bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], const float* gloss,
+                            float* gimg, cudaStream_t st);
 
 }  // namespace gft

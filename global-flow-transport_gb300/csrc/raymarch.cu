@@ -5,6 +5,8 @@
 // one launch (grid.z = pair), where the reference launches once per camera
 // with a host constant-buffer upload in between.  A warp covers an 8x4 pixel
 // tile so that the 32 rays of a warp gather from neighbouring voxels.
+#include <algorithm>
+
 #include "gft_internal.h"
 
 namespace gft {
@@ -129,10 +131,10 @@ __device__ __forceinline__ bool clip_back_to_front(float3& pos, float3 step, int
 // One sample's trilinear scatter.  MODE 0 (exact adjoint): BORDER drops the
 // sample outside the forward's half-cell window.  MODE 1 (reference-normalised)
 // and MODE 2 (weight sums): BORDER drops it unless -1 < p < dims, the
-// reference's window; MODE 1 divides each corner's contribution by the
-// camera's weight sum there (the per-camera normalise-then-sum applied per
-// contribution, so all cameras accumulate into one gradient) and skips corners
-// with w == 0 or a zero sum.
+// reference's window; MODE 1 scales each corner's contribution by the
+// reciprocal of the camera's weight sum there (the per-camera
+// normalise-then-sum applied per contribution, so all cameras accumulate into
+// one gradient) and skips corners with w == 0 or no weight.
 template <int C, int BM, int MODE>
 __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
                                                float px, float py, float pz, Vec<C> val) {
@@ -154,8 +156,8 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
             const float w = (sx ? cw[0] : 1.f - cw[0]) * (sy ? cw[1] : 1.f - cw[1]) * (sz ? cw[2] : 1.f - cw[2]);
             const int64_t f = flat3(sx ? c.x1 : c.x0, sy ? c.y1 : c.y0, sz ? c.z1 : c.z0, d);
             if constexpr (MODE == 1) {
-                const float n = __ldg(cnt + f);
-                if (w != 0.f && n > 0.f) atomic_add<C>(grad, f, vscale(vscale(val, w), 1.0f / n));
+                const float inv = __ldg(cnt + f);
+                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, f, vscale(vscale(val, w), inv));
             } else {
                 atomic_add<C>(grad, f, vscale(val, w));
             }
@@ -292,6 +294,14 @@ static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const Raymar
                                                                   nullptr, cnt, nullptr, t);
 }
 
+// Weight sums -> their reciprocals (0 where no sample reached the voxel).
+__global__ void k_invert_weights(float* __restrict__ w, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = w[i];
+        w[i] = v > 0.f ? 1.f / v : 0.f;
+    }
+}
+
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
     const int64_t nvox = voxels(a.din);
     if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * nvox * pairs.size(), s), "zero weights")) return false;
@@ -306,7 +316,13 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
         }
         if (!launched(1, "raymarch weight launch")) return false;
     }
-    return true;
+    const int64_t n = nvox * (int64_t)pairs.size();
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (n + 255) / 256, cap = (int64_t)std::max(sms, 1) * 8;
+    k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), 256, 0, s>>>(ws_cnt, n);
+    return launched(1, "raymarch weight inversion launch");
 }
 
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,

@@ -51,6 +51,13 @@ _SIGS = {
                                                 _I32, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
     'gft_raymarch_grid_transform_grad_weights': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32, _I32,
                                                         _P, _SZ, _P]),
+    'gft_transmittance': (_I32, [_P, _I64P, _P, _P]),
+    'gft_transmittance_grad': (_I32, [_P, _P, _I64P, _P, _P]),
+    'gft_light_compose': (_I32, [_P, _P, _P, _I64P, _F, _F, _P, _P]),
+    'gft_light_compose_grad': (_I32, [_P, _P, _P, _I64P, _F, _F, _P, _P, _P, _P]),
+    'gft_image_loss_workspace_size': (_SZ, [ctypes.c_int64]),
+    'gft_image_loss': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _SZ, _P]),
+    'gft_image_loss_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),
     'gft_sample_grid_transform_workspace_size': (_SZ, [_I64P, _I32, _I32]),
     'gft_sample_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                          _I32, _I32, _I32, _I32, _F, _I32, _F, _I32, _P, _P, _SZ, _P]),

@@ -1,0 +1,128 @@
+"""Fused kernels for the glue of the render + advect step (libgft.so
+gft_transmittance / gft_light_compose / gft_image_loss and their gradients).
+
+Each function is an autograd op equal to a composition of tensor ops of the
+reference's renderer; ``gft.pipeline`` uses them in its batched mode and keeps
+the plain tensor composition in its plain mode.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from .ops import _cuda, _p, _stream, _workspace
+
+
+def _shape(t):
+    return _lib.i64(t.shape)
+
+
+class _Transmittance(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x):
+        lib = _lib.load()
+        out = torch.empty_like(x)
+        with torch.cuda.device(x.device):
+            _lib.check(lib.gft_transmittance(_p(x), _shape(x), _p(out), _stream(x.device)), 'Transmittance')
+        ctx.save_for_backward(out)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (out,) = ctx.saved_tensors
+        lib = _lib.load()
+        g = g.contiguous()
+        gx = torch.empty_like(out)
+        with torch.cuda.device(out.device):
+            _lib.check(lib.gft_transmittance_grad(_p(out), _p(g), _shape(out), _p(gx), _stream(out.device)),
+                       'TransmittanceGrad')
+        return gx
+
+
+def transmittance(x):
+    """exp(-exclusive depth sum) of a [N, D, H, W, 1] grid: equals
+    exp(-cat([0, reduce_grid_blend(x, 'BEER_LAMBERT', keep_dims=True)[:, :-1]], 1))."""
+    x = _cuda(x, 'input')
+    if x.dim() != 5 or x.shape[4] != 1:
+        raise _lib.GftInvalidArgument('expected [N, D, H, W, 1], got %s' % (tuple(x.shape),))
+    return _Transmittance.apply(x)
+
+
+class _LightCompose(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, d, tr, color, ambient, scale):
+        lib = _lib.load()
+        out = torch.empty(tuple(d.shape[:4]) + (4,), dtype=torch.float32, device=d.device)
+        with torch.cuda.device(d.device):
+            _lib.check(lib.gft_light_compose(_p(d), _p(tr), _p(color), _shape(d), float(ambient), float(scale),
+                                             _p(out), _stream(d.device)), 'LightCompose')
+        ctx.save_for_backward(d, tr, color)
+        ctx.k = (float(ambient), float(scale))
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        d, tr, color = ctx.saved_tensors
+        ambient, scale = ctx.k
+        lib = _lib.load()
+        g = g.contiguous()
+        gd = torch.empty_like(d)
+        gt = torch.empty_like(tr)
+        with torch.cuda.device(d.device):
+            _lib.check(lib.gft_light_compose_grad(_p(d), _p(tr), _p(color), _shape(d), ambient, scale, _p(g),
+                                                  _p(gd), _p(gt), _stream(d.device)), 'LightComposeGrad')
+        return gd, gt, None, None, None
+
+
+def light_compose(density, transmittance, light_color, ambient, scale):
+    """cat([density * (transmittance * light_color + ambient), density], -1) * scale
+    for density, transmittance [N, D, H, W, 1] and light_color [D, H, W, 3] or
+    [1, D, H, W, 3] (constant: no gradient)."""
+    d = _cuda(density, 'density')
+    tr = _cuda(transmittance, 'transmittance')
+    color = _cuda(light_color, 'light_color')
+    if d.dim() != 5 or d.shape[4] != 1 or tuple(tr.shape) != tuple(d.shape):
+        raise _lib.GftInvalidArgument('density and transmittance must both be [N, D, H, W, 1]')
+    if color.numel() != int(np.prod(d.shape[1:4])) * 3 or color.shape[-1] != 3:
+        raise _lib.GftInvalidArgument('light_color must be [D, H, W, 3]')
+    return _LightCompose.apply(d, tr, color.detach(), ambient, scale)
+
+
+class _ImageLoss(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, img, target, bkg):
+        lib = _lib.load()
+        npix = img.numel() // 4
+        loss = torch.empty((), dtype=torch.float32, device=img.device)
+        ws = _workspace(lib.gft_image_loss_workspace_size(npix), img.device)
+        with torch.cuda.device(img.device):
+            _lib.check(lib.gft_image_loss(_p(img), _p(target), _p(bkg), npix, _p(loss), _p(ws), ws.numel(),
+                                          _stream(img.device)), 'ImageLoss')
+        ctx.save_for_backward(img, target)
+        ctx.bkg = bkg
+        return loss
+
+    @staticmethod
+    def backward(ctx, g):
+        img, target = ctx.saved_tensors
+        lib = _lib.load()
+        gi = torch.empty_like(img)
+        g = g.contiguous()
+        with torch.cuda.device(img.device):
+            _lib.check(lib.gft_image_loss_grad(_p(img), _p(target), _p(ctx.bkg), img.numel() // 4, _p(g), _p(gi),
+                                               _stream(img.device)), 'ImageLossGrad')
+        return gi, None, None
+
+
+def image_loss(image, target, background):
+    """mean((image[..., :3] + background * exp(-image[..., 3:]) - target) ** 2)
+    for image [..., 4], target [..., 3] and a background colour of 3 floats
+    (host values; a CUDA tensor is copied to the host, which a CUDA-graph
+    capture does not allow)."""
+    img = _cuda(image, 'image')
+    tgt = _cuda(target, 'target')
+    if img.shape[-1] != 4 or tuple(tgt.shape) != tuple(img.shape[:-1]) + (3,):
+        raise _lib.GftInvalidArgument('image must be [..., 4] and target [..., 3] of the same pixels')
+    if isinstance(background, torch.Tensor):
+        background = background.detach().cpu().numpy()
+    bkg = np.ascontiguousarray(np.asarray(background, dtype=np.float32).reshape(3))
+    return _ImageLoss.apply(img, tgt, bkg)

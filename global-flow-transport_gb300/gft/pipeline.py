@@ -8,15 +8,18 @@ SpotLight.grid_lighting and VelocityGrid.warp of the reference).
     img    = raymarch(concat(light, d) * depth_step, cameras)   BEER_LAMBERT
     loss   = mean((img.rgb + bkg * exp(-img.a) - target)^2)
 
-``batched``: all cameras in one raymarch launch, fused advection, and the
-whole forward + backward captured in one CUDA graph.  ``plain``: the
-reference's launch structure -- one raymarch launch per camera, advection
-composed from four SampleGridLut calls plus elementwise ops, no graph.
+``batched``: all cameras in one raymarch launch, fused advection, the
+transmittance, light composition and image loss as single kernels
+(gft.fused), and the whole forward + backward captured in one CUDA graph.
+``plain``: the reference's launch structure -- one raymarch launch per camera,
+advection composed from four SampleGridLut calls plus elementwise ops, the
+shadow, lighting and loss composed from tensor ops, no graph.
 All constants are device tensors created up front so the step is capturable.
 """
 import numpy as np
 import torch
 
+from . import fused
 from . import ops
 from . import synthetic as syn
 from phitest.render.lighting import SpotLight
@@ -80,7 +83,8 @@ class RenderAdvectStep:
         fall = self.spot.falloff(_Holder(self.gt), self.dev)  # [D,H,W,1]
         col = torch.tensor(self.spot.c * np.float32(self.spot.i), dtype=torch.float32, device=self.dev)
         self.falloff_col = (fall * col)[None].contiguous()  # [1,D,H,W,3]
-        self.bkg = torch.tensor([0.0, 0.5, 1.0], dtype=torch.float32, device=self.dev)
+        self.bkg_host = np.array([0.0, 0.5, 1.0], dtype=np.float32)
+        self.bkg = torch.from_numpy(self.bkg_host).to(self.dev)
         self.graph = None
 
     # --------------------------------------------------------------- inputs
@@ -106,16 +110,22 @@ class RenderAdvectStep:
         from phitest.render.renderer import _InverseSampleGrad
         sh = _InverseSampleGrad.apply(d * self.shadow_step, self.M, self.Vs, self.Ps, self.Fs, self.shadow_res,
                                       'TRANSFORM_LINDEPTH', 'TRANSFORM_LINDEPTH_REVERSE', self.rs, None)
-        sh = ops.reduce_grid_blend(sh[0], 'BEER_LAMBERT', keep_dims=True)
-        sh = torch.cat([torch.zeros_like(sh[:, :1]), sh[:, :-1]], dim=1)  # BORDER shift
-        tr = torch.exp(-sh)
+        if self.mode == 'plain':
+            sh = ops.reduce_grid_blend(sh[0], 'BEER_LAMBERT', keep_dims=True)
+            sh = torch.cat([torch.zeros_like(sh[:, :1]), sh[:, :-1]], dim=1)  # BORDER shift
+            tr = torch.exp(-sh)
+        else:
+            tr = fused.transmittance(sh[0])
         trv = _InverseSampleGrad.apply(tr, self.M, self.Vs, self.Ps, self.Fs, self.shape,
                                        'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_LINDEPTH', self.rs, None)
         return trv[0]  # [1,D,H,W,1]
 
     def render(self, d):
-        light = d * (self.shadow(d) * self.falloff_col + self.ambient)
-        data = torch.cat([light, d], dim=-1) * self.depth_step
+        if self.mode == 'plain':
+            light = d * (self.shadow(d) * self.falloff_col + self.ambient)
+            data = torch.cat([light, d], dim=-1) * self.depth_step
+        else:
+            data = fused.light_compose(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step)
         if self.mode == 'plain':
             imgs = [ops.raymarch_grid_transform(data, self.M, self.V[i:i + 1], self.P[i:i + 1], self.F[i:i + 1],
                                                 self.res) for i in range(len(self.V))]
@@ -128,6 +138,8 @@ class RenderAdvectStep:
     def loss(self, d_prev, vx, vy, vz, target):
         d = self.advect(d_prev, vx, vy, vz)
         img = self.render(d)
+        if self.mode != 'plain':
+            return fused.image_loss(img, target, self.bkg_host)
         rgb = img[..., :3] + self.bkg * torch.exp(-img[..., 3:])
         return torch.mean((rgb - target) ** 2)
 

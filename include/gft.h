@@ -103,9 +103,10 @@ gft_status gft_raymarch_grid_transform_grad(
     int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
     int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
 /* The geometry-only first pass of the GFT_GRAD_REFERENCE raymarch gradient:
- * per (batch, camera) pair the per-voxel sums of the trilinear weights of all
- * ray samples (the reference's float sampleCounter, raymarch_grid.cu.cc:446-456),
- * written into the workspace of gft_raymarch_grid_transform_grad.  It needs
+ * per (batch, camera) pair the reciprocals of the per-voxel sums of the
+ * trilinear weights of all ray samples (the reference's float sampleCounter,
+ * raymarch_grid.cu.cc:446-456; 0 where no sample reaches a voxel), written
+ * into the workspace of gft_raymarch_grid_transform_grad.  It needs
  * neither the forward output nor its gradient, so a caller can run it on
  * another stream while the forward pass is still running; the gradient call
  * then takes grad_mode GFT_GRAD_REFERENCE | GFT_GRAD_WEIGHTS_READY, the same
@@ -221,6 +222,36 @@ gft_status gft_advect_grad(
     const float* output_grad,
     float* density_grad, float* vel_x_grad, float* vel_y_grad, float* vel_z_grad,
     void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- Pipeline fusions (no counterpart op in the reference) ----
+ * Each replaces a chain of tensor ops with which the reference's renderer
+ * composes the shadow pass, the lighting and the image loss
+ * (phitest/render/lighting.py:106-121 and :236-262, renderer.py:1012-1052);
+ * elementwise products and sums round like those separate ops.
+ *
+ * gft_transmittance: input [N, D, H, W, 1] (light-frustum density x depth step),
+ * output[z] = exp(-sum_{z' < z} input[z']) along D: ReduceGridBlend
+ * BEER_LAMBERT keep_dims, the one-cell shift in depth and exp. */
+gft_status gft_transmittance(const float* input, const int64_t shape[5], float* output, void* stream);
+gft_status gft_transmittance_grad(const float* output, const float* output_grad, const int64_t shape[5],
+                                  float* input_grad, void* stream);
+/* gft_light_compose: density, transmittance [N, D, H, W, 1] (shape), light_color
+ * [D, H, W, 3] shared by the batch; output [N, D, H, W, 4] =
+ * concat(density * (transmittance * light_color + ambient), density) * scale. */
+gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
+                             const int64_t shape[5], float ambient, float scale, float* output, void* stream);
+gft_status gft_light_compose_grad(const float* density, const float* transmittance, const float* light_color,
+                                  const int64_t shape[5], float ambient, float scale, const float* output_grad,
+                                  float* density_grad, float* transmittance_grad, void* stream);
+/* gft_image_loss: image [pixels, 4] (rgb + density), target [pixels, 3],
+ * background = 3 host floats; *loss (device) = mean over pixels and rgb of
+ * (rgb + background * exp(-density) - target)^2, summed in a fixed order.
+ * gft_image_loss_grad: image_grad [pixels, 4] for the device scalar loss_grad. */
+size_t gft_image_loss_workspace_size(int64_t pixels);
+gft_status gft_image_loss(const float* image, const float* target, const float background[3], int64_t pixels,
+                          float* loss, void* workspace, size_t workspace_bytes, void* stream);
+gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
+                               const float* loss_grad, float* image_grad, void* stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

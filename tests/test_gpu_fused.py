@@ -1,0 +1,85 @@
+"""The fused pipeline kernels (gft.fused) against the tensor-op compositions
+they replace: forward and gradients on seeded inputs."""
+import numpy as np
+import pytest
+import torch
+
+from scene_utils import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def fused():
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from gft import fused as _f
+    return _f
+
+
+def _np(t):
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize('shape', [(1, 7, 5, 9, 1), (2, 16, 12, 33, 1)])
+def test_transmittance(fused, shape):
+    from gft import ops
+    g = torch.Generator().manual_seed(3)
+    x = (torch.rand(shape, generator=g) * 0.3).cuda()
+    gy = torch.randn(shape, generator=g).cuda()
+    a = x.clone().requires_grad_(True)
+    y = fused.transmittance(a)
+    y.backward(gy)
+    b = x.clone().requires_grad_(True)
+    sh = ops.reduce_grid_blend(b, 'BEER_LAMBERT', keep_dims=True)
+    ref = torch.exp(-torch.cat([torch.zeros_like(sh[:, :1]), sh[:, :-1]], dim=1))
+    ref.backward(gy)
+    assert rel_l2(_np(y), _np(ref)) <= 1e-7
+    assert rel_l2(_np(a.grad), _np(b.grad)) <= 1e-6
+
+
+@pytest.mark.parametrize('N', [1, 2])
+def test_light_compose(fused, N):
+    g = torch.Generator().manual_seed(4)
+    D, H, W = 6, 10, 7
+    d0 = torch.rand((N, D, H, W, 1), generator=g).cuda()
+    t0 = torch.rand((N, D, H, W, 1), generator=g).cuda()
+    col = torch.rand((1, D, H, W, 3), generator=g).cuda()
+    gy = torch.randn((N, D, H, W, 4), generator=g).cuda()
+    d1, t1 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    y = fused.light_compose(d1, t1, col, 0.64, 0.37)
+    y.backward(gy)
+    d2, t2 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    ref = torch.cat([d2 * (t2 * col + 0.64), d2], dim=-1) * 0.37
+    ref.backward(gy)
+    assert rel_l2(_np(y), _np(ref)) <= 1e-7
+    assert rel_l2(_np(d1.grad), _np(d2.grad)) <= 1e-6
+    assert rel_l2(_np(t1.grad), _np(t2.grad)) <= 1e-6
+
+
+def test_image_loss(fused):
+    g = torch.Generator().manual_seed(5)
+    img0 = torch.rand((5, 27, 48, 4), generator=g).cuda()
+    tgt = torch.rand((5, 27, 48, 3), generator=g).cuda()
+    bkg = torch.tensor([0.0, 0.5, 1.0]).cuda()
+    a = img0.clone().requires_grad_(True)
+    loss = fused.image_loss(a, tgt, bkg)
+    (loss * 3.0).backward()
+    b = img0.clone().requires_grad_(True)
+    ref = torch.mean((b[..., :3] + bkg * torch.exp(-b[..., 3:]) - tgt) ** 2)
+    (ref * 3.0).backward()
+    assert abs(float(loss) - float(ref)) <= 1e-6 * abs(float(ref))
+    assert rel_l2(_np(a.grad), _np(b.grad)) <= 1e-6
+    # repeated calls are deterministic (fixed-order reduction)
+    assert float(fused.image_loss(a, tgt, bkg)) == float(loss)
+
+
+def test_fused_argument_errors(fused):
+    from gft import _lib
+    with pytest.raises(_lib.GftInvalidArgument):
+        fused.transmittance(torch.zeros((1, 4, 4, 4, 2), device='cuda'))
+    with pytest.raises(_lib.GftInvalidArgument):
+        fused.light_compose(torch.zeros((1, 4, 4, 4, 1), device='cuda'), torch.zeros((1, 4, 4, 3, 1), device='cuda'),
+                            torch.zeros((4, 4, 4, 3), device='cuda'), 0.5, 1.0)
+    with pytest.raises(_lib.GftInvalidArgument):
+        fused.image_loss(torch.zeros((2, 3, 4), device='cuda'), torch.zeros((2, 3, 4), device='cuda'), [0, 0, 0])
