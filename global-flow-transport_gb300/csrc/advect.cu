@@ -30,10 +30,9 @@ __device__ __forceinline__ float3 lut_at(const float* __restrict__ vx, const flo
     return make_float3(cx * (-dt), cy * (-dt), cz * (-dt));
 }
 
+// Slices below 2^32 cells (checked by the launchers): 32-bit division.
 __device__ __forceinline__ void unflat(int64_t v, Dims d, int& x, int& y, int& z) {
-    x = (int)(v % d.x);
-    y = (int)((v / d.x) % d.y);
-    z = (int)(v / ((int64_t)d.x * d.y));
+    unflat32((uint32_t)v, d, x, y, z);
 }
 
 // Trilinear value plus the MIN/MAX of the lookup op (read3DMin/Max) from one
@@ -158,7 +157,18 @@ static bool adv_fwd_c(const AdvectArgs& a, float* out, float* ws, cudaStream_t s
     return true;
 }
 
+// The advection kernels index a grid slice (and the three staggered
+// components together) with 32-bit arithmetic.
+static bool advect_size_ok(Dims d) {
+    const int64_t n = voxels(d);
+    const int64_t stag = n * 3 + (int64_t)d.y * d.z + (int64_t)d.x * d.z + (int64_t)d.x * d.y;
+    if (stag < MAX_SLICE_CELLS) return true;
+    set_error("advection grid too large for 32-bit cell indexing");
+    return false;
+}
+
 bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s) {
+    if (!advect_size_ok(a.d)) return false;
     if (a.dtype == 0) {
         if (a.C == 4) return adv_fwd_c<4, float>(a, out, ws, s);
         if (a.C == 2) return adv_fwd_c<2, float>(a, out, ws, s);
@@ -286,25 +296,25 @@ __global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restric
 // average (each face receives half of both adjacent cells).
 __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, float dt, float* __restrict__ gvx,
                                    float* __restrict__ gvy, float* __restrict__ gvz) {
-    const int64_t nx = (int64_t)(dm.x + 1) * dm.y * dm.z;
-    const int64_t ny = (int64_t)dm.x * (dm.y + 1) * dm.z;
-    const int64_t nz = (int64_t)dm.x * dm.y * (dm.z + 1);
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // nx + ny + nz < 2^32 (checked by the launcher): 32-bit index arithmetic
+    const uint32_t nx = (uint32_t)(dm.x + 1) * dm.y * dm.z;
+    const uint32_t ny = (uint32_t)dm.x * (dm.y + 1) * dm.z;
+    const uint32_t nz = (uint32_t)dm.x * dm.y * (dm.z + 1);
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const float h = -0.5f * dt;
     if (t < nx) {
-        const int i = (int)(t % (dm.x + 1));
-        const int64_t r = t / (dm.x + 1);  // z*H + y
+        const uint32_t r = t / (uint32_t)(dm.x + 1);  // z*H + y
+        const int i = (int)(t - r * (uint32_t)(dm.x + 1));
         float a = 0.f;
-        if (i > 0) a += glut[(r * dm.x + i - 1) * 3 + 0];
-        if (i < dm.x) a += glut[(r * dm.x + i) * 3 + 0];
+        if (i > 0) a += glut[((int64_t)r * dm.x + i - 1) * 3 + 0];
+        if (i < dm.x) a += glut[((int64_t)r * dm.x + i) * 3 + 0];
         gvx[t] = h * a;
         return;
     }
     t -= nx;
     if (t < ny) {
-        const int x = (int)(t % dm.x);
-        const int j = (int)((t / dm.x) % (dm.y + 1));
-        const int z = (int)(t / ((int64_t)dm.x * (dm.y + 1)));
+        int x, j, z;
+        unflat32(t, Dims{dm.x, dm.y + 1, dm.z}, x, j, z);
         float a = 0.f;
         if (j > 0) a += glut[((((int64_t)z * dm.y) + j - 1) * dm.x + x) * 3 + 1];
         if (j < dm.y) a += glut[((((int64_t)z * dm.y) + j) * dm.x + x) * 3 + 1];
@@ -313,9 +323,9 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
     }
     t -= ny;
     if (t < nz) {
-        const int64_t plane = (int64_t)dm.x * dm.y;
+        const uint32_t plane = (uint32_t)dm.x * dm.y;
         const int64_t k = t / plane;
-        const int64_t xy = t - k * plane;
+        const int64_t xy = t - (uint32_t)k * plane;
         float a = 0.f;
         if (k > 0) a += glut[((k - 1) * plane + xy) * 3 + 2];
         if (k < dm.z) a += glut[(k * plane + xy) * 3 + 2];
@@ -386,6 +396,7 @@ static bool adv_bwd_c(const AdvectArgs& a, bool exact, const float* dy, float* g
 
 bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
                        float* gvz, float* ws, cudaStream_t s) {
+    if (!advect_size_ok(a.d)) return false;
     if (a.C == 4) return adv_bwd_c<4>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
     if (a.C == 2) return adv_bwd_c<2>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
     return adv_bwd_c<1>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);

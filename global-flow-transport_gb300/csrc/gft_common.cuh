@@ -27,6 +27,18 @@ __device__ __forceinline__ int64_t flat3(int x, int y, int z, Dims d) {
     return ((int64_t)z * d.y + y) * d.x + x;
 }
 
+// Cell (x, y, z) of a flat index v < 2^32 of a grid of dims d: two 32-bit
+// divisions (the per-cell kernels run one grid slice per blockIdx.y).
+__device__ __forceinline__ void unflat32(uint32_t v, Dims d, int& x, int& y, int& z) {
+    const uint32_t q = v / (uint32_t)d.x;
+    x = (int)(v - q * (uint32_t)d.x);
+    const uint32_t zz = q / (uint32_t)d.y;
+    y = (int)(q - zz * (uint32_t)d.y);
+    z = (int)zz;
+}
+// Grid slices up to this many cells run as one launch dimension.
+constexpr int64_t MAX_SLICE_CELLS = int64_t(1) << 32;
+
 // --- small fixed-size channel vectors ----------------------------------------
 template <int C>
 struct Vec {

@@ -17,11 +17,10 @@ constexpr int RS_THREADS = 256;
 // x as kGenerateMip3D does.
 template <int C, typename S>
 __global__ void k_mip_level(const S* __restrict__ src, Dims ds, float* __restrict__ dst, Dims dd) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= voxels(dd)) return;
-    const int x = (int)(t % dd.x);
-    const int y = (int)((t / dd.x) % dd.y);
-    const int z = (int)(t / ((int64_t)dd.x * dd.y));
+    int x, y, z;
+    unflat32(t, dd, x, y, z);
     Vec<C> c[2];
 #pragma unroll
     for (int dx = 0; dx < 2; ++dx) {
@@ -63,8 +62,16 @@ static void mip_launch(const void* src, int dtype, Dims ds, float* dst, Dims dd,
         k_mip_level<C, __nv_bfloat16><<<blocks, RS_THREADS, 0, s>>>((const __nv_bfloat16*)src, ds, dst, dd);
 }
 
+// The per-cell kernels index one grid slice with 32-bit arithmetic.
+static bool slice_ok(int64_t cells) {
+    if (cells < MAX_SLICE_CELLS) return true;
+    set_error("a grid slice has 2^32 or more cells");
+    return false;
+}
+
 bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, float* ws, cudaStream_t s,
                        MipSet* set) {
+    if (!slice_ok(voxels(d))) return false;
     set->levels = levels;
     set->lvl[0] = (const float*)input;  // reinterpreted by the sampler according to dtype
     set->dims[0] = d;
@@ -91,8 +98,8 @@ bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, 
 // Level 0 is read with the storage type S, coarser levels are fp32.
 template <int C, typename S, int BM>
 __device__ __forceinline__ Vec<C> read_level(int filter, const MipSet& ms, int m, float3 p, float cco) {
-    const float sc = (float)(1 << m);
-    const float px = p.x / sc - cco, py = p.y / sc - cco, pz = p.z / sc - cco;
+    const float inv = __int_as_float((127 - m) << 23);  // 2^-m: the product rounds exactly as p / 2^m
+    const float px = p.x * inv - cco, py = p.y * inv - cco, pz = p.z * inv - cco;
     if (m == 0) return fetch<C, S, BM, false>(filter, reinterpret_cast<const S*>(ms.lvl[0]), ms.dims[0], px, py, pz);
     return fetch<C, float, BM, false>(filter, ms.lvl[m], ms.dims[m], px, py, pz);
 }
@@ -188,11 +195,11 @@ __global__ void __launch_bounds__(RS_THREADS)
     k_sample_transform(Dims dout, int filter, int mip_mode, float bias, float cco, int cm, const MipSet ms,
                        float* __restrict__ out, const __grid_constant__ PairTable tab) {
     const int64_t nv = voxels(dout);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nv * tab.n) return;
-    const int p = (int)(t / nv);
-    const int64_t v = t - (int64_t)p * nv;
-    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int p = blockIdx.y;
+    int x, y, z;
+    unflat32(v, dout, x, y, z);
     const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
     const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
     const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
@@ -206,7 +213,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 }
 
 template <int C, typename S>
-static void st_fwd(int bm, unsigned blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
+static void st_fwd(int bm, dim3 blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
                    const PairTable& t) {
     switch (bm) {
         case BM_BORDER:
@@ -227,12 +234,13 @@ static void st_fwd(int bm, unsigned blocks, cudaStream_t s, const SampleArgs& a,
 bool launch_sample_transform_fwd(const SampleArgs& a, const std::vector<Pair>& pairs, const MipSet* mips,
                                  float* out, cudaStream_t s) {
     const int64_t nv = voxels(a.dout);
+    if (!slice_ok(nv)) return false;
     for (int b = 0; b < a.N; ++b) {
         std::vector<Pair> pb;
         for (const Pair& p : pairs)
             if (p.in_batch == b) pb.push_back(p);
         for (const PairTable& t : make_tables(pb)) {
-            const unsigned blocks = (unsigned)((nv * t.n + RS_THREADS - 1) / RS_THREADS);
+            const dim3 blocks((unsigned)((nv + RS_THREADS - 1) / RS_THREADS), t.n);
             if (a.dtype == 0) {
                 if (a.C == 4) st_fwd<4, float>(a.boundary, blocks, s, a, mips[b], out, t);
                 else if (a.C == 2) st_fwd<2, float>(a.boundary, blocks, s, a, mips[b], out, t);
@@ -256,11 +264,11 @@ __global__ void __launch_bounds__(RS_THREADS)
                            float* __restrict__ grad, unsigned int* __restrict__ count,
                            const __grid_constant__ PairTable tab) {
     const int64_t nv = voxels(dout);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nv * tab.n) return;
-    const int p = (int)(t / nv);
-    const int64_t v = t - (int64_t)p * nv;
-    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int p = blockIdx.y;
+    int x, y, z;
+    unflat32(v, dout, x, y, z);
     const float3 dinf = make_float3((float)din.x, (float)din.y, (float)din.z);
     const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
     const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), dinf, dinv, false);
@@ -292,7 +300,7 @@ static void normalize_any(int C, float* grad, unsigned int* count, int64_t nv, c
 }
 
 template <int C, int COUNT>
-static void stb_launch(int bm, unsigned blocks, cudaStream_t s, Dims din, Dims dout, int cm, float cco,
+static void stb_launch(int bm, dim3 blocks, cudaStream_t s, Dims din, Dims dout, int cm, float cco,
                        const float* dy, float* grad, unsigned int* count, const PairTable& t) {
     switch (bm) {
         case BM_BORDER:
@@ -311,6 +319,7 @@ bool launch_sample_transform_bwd(int N, int C, Dims din, Dims dout, int boundary
                                  const std::vector<Pair>& pairs, const float* dy, bool exact, float* grad,
                                  unsigned int* count, cudaStream_t s) {
     const int64_t nvi = voxels(din), nvo = voxels(dout);
+    if (!slice_ok(nvo)) return false;
     if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvi * C * N, s), "zero gradient")) return false;
     if (!exact && !cuda_ok(cudaMemsetAsync(count, 0, sizeof(unsigned int) * nvi, s), "zero counter")) return false;
     for (int b = 0; b < N; ++b) {
@@ -319,7 +328,7 @@ bool launch_sample_transform_bwd(int N, int C, Dims din, Dims dout, int boundary
             if (p.in_batch == b) pb.push_back(p);
         float* gb = grad + (size_t)b * nvi * C;
         for (const PairTable& t : make_tables(pb)) {
-            const unsigned blocks = (unsigned)((nvo * t.n + RS_THREADS - 1) / RS_THREADS);
+            const dim3 blocks((unsigned)((nvo + RS_THREADS - 1) / RS_THREADS), t.n);
             if (exact) {
                 if (C == 4) stb_launch<4, 0>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
                 else if (C == 2) stb_launch<2, 0>(boundary, blocks, s, din, dout, coord_mode, cco, dy, gb, count, t);
@@ -370,18 +379,18 @@ template <int C, typename S, int BM>
 __global__ void __launch_bounds__(RS_THREADS)
     k_lut_fwd(const float* __restrict__ lut, const LutK k, const MipSet ms, float* __restrict__ out) {
     const int64_t nv = voxels(k.dout);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nv * k.n_cam) return;
-    const int c = (int)(t / nv);
-    const int64_t v = t - (int64_t)c * nv;
-    const int x = (int)(v % k.dout.x), y = (int)((v / k.dout.x) % k.dout.y), z = (int)(v / ((int64_t)k.dout.x * k.dout.y));
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int c = blockIdx.y;
+    int x, y, z;
+    unflat32(v, k.dout, x, y, z);
     const float4 pos = lut_pos(lut, k.cam0 + c, v, x, y, z, k);
     const Vec<C> r = sample_mip<C, S, BM>(k.filter, k.mip_mode, ms, pos, k.bias, k.cco);
     store<C>(out, (int64_t)(k.slot0 + c) * nv + v, r);
 }
 
 template <int C, typename S>
-static void lut_fwd_launch(int bm, unsigned blocks, cudaStream_t s, const float* lut, const LutK& k,
+static void lut_fwd_launch(int bm, dim3 blocks, cudaStream_t s, const float* lut, const LutK& k,
                            const MipSet& ms, float* out) {
     switch (bm) {
         case BM_BORDER: k_lut_fwd<C, S, BM_BORDER><<<blocks, RS_THREADS, 0, s>>>(lut, k, ms, out); break;
@@ -407,9 +416,10 @@ static LutK make_lutk(const LutArgs& a, int b) {
 
 bool launch_lut_fwd(const LutArgs& a, const float* lut, const MipSet* mips, float* out, cudaStream_t s) {
     const int64_t nv = voxels(a.dout);
+    if (!slice_ok(nv)) return false;
     for (int b = 0; b < a.N; ++b) {
         const LutK k = make_lutk(a, b);
-        const unsigned blocks = (unsigned)((nv * k.n_cam + RS_THREADS - 1) / RS_THREADS);
+        const dim3 blocks((unsigned)((nv + RS_THREADS - 1) / RS_THREADS), k.n_cam);
         if (a.dtype == 0) {
             if (a.C == 4) lut_fwd_launch<4, float>(a.boundary, blocks, s, lut, k, mips[b], out);
             else if (a.C == 2) lut_fwd_launch<2, float>(a.boundary, blocks, s, lut, k, mips[b], out);
@@ -432,11 +442,11 @@ __global__ void __launch_bounds__(RS_THREADS)
               const float* __restrict__ dy, float* __restrict__ grad, float* __restrict__ lut_grad,
               unsigned int* __restrict__ count) {
     const int64_t nv = voxels(k.dout);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nv * k.n_cam) return;
-    const int c = (int)(t / nv);
-    const int64_t v = t - (int64_t)c * nv;
-    const int x = (int)(v % k.dout.x), y = (int)((v / k.dout.x) % k.dout.y), z = (int)(v / ((int64_t)k.dout.x * k.dout.y));
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int c = blockIdx.y;
+    int x, y, z;
+    unflat32(v, k.dout, x, y, z);
     const float4 pos = lut_pos(lut, k.cam0 + c, v, x, y, z, k);
     const float px = pos.x - k.cco, py = pos.y - k.cco, pz = pos.z - k.cco;
     const Vec<C> g = loadf<C>(dy, (int64_t)(k.slot0 + c) * nv + v);
@@ -456,7 +466,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 }
 
 template <int C, int COUNT>
-static void lut_bwd_launch(int bm, unsigned blocks, cudaStream_t s, const float* in, Dims din, const float* lut,
+static void lut_bwd_launch(int bm, dim3 blocks, cudaStream_t s, const float* in, Dims din, const float* lut,
                            const LutK& k, const float* dy, float* grad, float* lut_grad, unsigned int* count) {
     switch (bm) {
         case BM_BORDER:
@@ -474,6 +484,7 @@ static void lut_bwd_launch(int bm, unsigned blocks, cudaStream_t s, const float*
 bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, const float* dy, bool exact,
                     float* grad, float* lut_grad, unsigned int* count, cudaStream_t s) {
     const int64_t nvi = voxels(a.din), nvo = voxels(a.dout);
+    if (!slice_ok(nvo)) return false;
     if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvi * a.C * a.N, s), "zero gradient")) return false;
     if (!cuda_ok(cudaMemsetAsync(lut_grad, 0, sizeof(float) * 4 * nvo * a.n_lut, s), "zero lookup gradient"))
         return false;
@@ -482,7 +493,7 @@ bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, cons
         const LutK k = make_lutk(a, b);
         const float* inb = input + (size_t)b * nvi * a.C;
         float* gb = grad + (size_t)b * nvi * a.C;
-        const unsigned blocks = (unsigned)((nvo * k.n_cam + RS_THREADS - 1) / RS_THREADS);
+        const dim3 blocks((unsigned)((nvo + RS_THREADS - 1) / RS_THREADS), k.n_cam);
         if (exact) {
             if (a.C == 4) lut_bwd_launch<4, 0>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
             else if (a.C == 2) lut_bwd_launch<2, 0>(a.boundary, blocks, s, inb, a.din, lut, k, dy, gb, lut_grad, count);
@@ -506,11 +517,11 @@ bool launch_lut_bwd(const LutArgs& a, const float* input, const float* lut, cons
 __global__ void __launch_bounds__(RS_THREADS)
     k_lod_transform(Dims din, Dims dout, int cm, float* __restrict__ out, const __grid_constant__ PairTable tab) {
     const int64_t nv = voxels(dout);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nv * tab.n) return;
-    const int p = (int)(t / nv);
-    const int64_t v = t - (int64_t)p * nv;
-    const int x = (int)(v % dout.x), y = (int)((v / dout.x) % dout.y), z = (int)(v / ((int64_t)dout.x * dout.y));
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int p = blockIdx.y;
+    int x, y, z;
+    unflat32(v, dout, x, y, z);
     const float3 dinf = make_float3((float)din.x, (float)din.y, (float)din.z);
     const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
     const CamX& c = tab.cam[p];
@@ -534,8 +545,9 @@ __global__ void __launch_bounds__(RS_THREADS)
 bool launch_lod_transform(Dims din, Dims dout, const std::vector<Pair>& pairs, bool inverse, float* out,
                           cudaStream_t s) {
     const int64_t nv = voxels(dout);
+    if (!slice_ok(nv)) return false;
     for (const PairTable& t : make_tables(pairs)) {
-        const unsigned blocks = (unsigned)((nv * t.n + RS_THREADS - 1) / RS_THREADS);
+        const dim3 blocks((unsigned)((nv + RS_THREADS - 1) / RS_THREADS), t.n);
         k_lod_transform<<<blocks, RS_THREADS, 0, s>>>(din, dout, inverse ? CM_LINDEPTH_REVERSE : CM_LINDEPTH, out, t);
         if (!launched(1, "lod transform launch")) return false;
     }
