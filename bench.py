@@ -43,7 +43,10 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """nvidia-smi clocks/throttle sampling (every 50 ms) around the timed
+    region.  A reader thread stamps each sample on arrival; the summary keeps
+    the samples inside [start, stop] of the region (mark()/__exit__), widened
+    to the nearest three samples when the region is shorter than that."""
     Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
          'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
          'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
@@ -52,29 +55,50 @@ class ClockSampler:
         self.idx = gpu_index
         self.out_path = out_path
         self.proc = None
+        self.samples = []  # (arrival time, line)
+        self.t0 = self.t1 = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            if line.strip():
+                self.samples.append((time.perf_counter(), line.strip()))
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.idx), '--query-gpu=' + self.Q,
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                          '--format=csv,noheader,nounits', '-lms', '50'],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            t_end = time.perf_counter() + 3.0
+            while not self.samples and time.perf_counter() < t_end:  # sampler running before the region
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
+    def mark(self):
+        self.t0 = time.perf_counter()
+
     def __exit__(self, *a):
-        self.lines = []
+        self.t1 = time.perf_counter()
         if self.proc is not None:
+            time.sleep(0.06)  # one more sample after the region
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
-            if self.out_path:
-                with open(self.out_path, 'w') as f:
-                    f.write('\n'.join(self.lines) + '\n')
+            self.thread.join(timeout=2)
+        t0 = self.t0 if self.t0 is not None else self.t1
+        inside = [l for t, l in self.samples if t0 <= t <= self.t1 + 0.055]
+        if len(inside) < 3 and self.samples:
+            mid = 0.5 * (t0 + self.t1)
+            inside = [l for _, l in sorted(self.samples, key=lambda s: abs(s[0] - mid))[:3]]
+        self.lines = inside
+        if self.out_path:
+            with open(self.out_path, 'w') as f:
+                f.write('\n'.join(l for _, l in self.samples) + '\n')
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -157,6 +181,7 @@ def bench_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local, os.path.join(ROOT, 'gpurun_out', 'bench_clocks.csv') if args.save_clocks else None) as cs:
+        cs.mark()
         t_wall0 = time.perf_counter()
         times = timed(step.replay, args.steps)
         t_wall = time.perf_counter() - t_wall0
@@ -221,7 +246,7 @@ def extras(args, step, dev, timed, storage, inputs, ms):
         loss, _ = step.replay()
         loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
 
-    k = max(3, args.steps // 2)
+    k = min(max(3, args.steps // 2), 50)
     for _ in range(2):
         e2e_step()
     torch.cuda.synchronize()
@@ -240,7 +265,7 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     for _ in range(2):
         plain.run_static()
     torch.cuda.synchronize()
-    pt = timed(plain.run_static, max(3, args.steps // 3))
+    pt = timed(plain.run_static, min(max(3, args.steps // 3), 30))
     out['plain'] = {'value': 1000.0 / float(np.mean(pt)), 'unit': 'iters/s', 'ms_per_step': float(np.mean(pt)),
                     'what': 'same step, one raymarch launch per camera, advection from 4 SampleGridLut calls + '
                             'elementwise ops, no CUDA graph'}
@@ -260,10 +285,29 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     return out
 
 
+SCATTER_PROFILE = os.path.join(ROOT, 'profiles', 'raymarch_scatter_cfg2.md')
+
+
+def _profiled_traffic():
+    """DRAM bytes per launch of the raymarch adjoint scatter pass from the
+    committed ncu summary (its ``dram_bytes_per_launch:`` line), else None."""
+    try:
+        with open(SCATTER_PROFILE) as f:
+            for line in f:
+                if line.strip().startswith('dram_bytes_per_launch:'):
+                    return int(line.split(':', 1)[1].strip().split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def kernel_roofline(step, dev, timed):
-    """Times the raymarch forward and backward launches (the dominant kernels)
-    alone with CUDA events on their stream and converts the algorithmic bytes
-    per launch into GB/s against the measured HBM peak."""
+    """Times the render kernels alone with CUDA events on their stream (L2
+    flushed before each launch) and converts the algorithmic bytes per launch
+    into GB/s against the measured HBM peak.  The dominant kernel is the
+    raymarch adjoint's scatter pass (k_raymarch_scatter, one launch for the 5
+    views), timed with its per-camera weight sums precomputed
+    (GFT_GRAD_WEIGHTS_READY: a gradient memset plus the scatter launch)."""
     import numpy as np
     import torch
     from gft import ops
@@ -274,41 +318,56 @@ def kernel_roofline(step, dev, timed):
         data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
     D, H, W = step.res
     V = len(step.cams)
+    mode = ops.get_grad_mode()
     fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True)
     y = fwd()
+    torch.manual_seed(0)
     dy = torch.randn_like(y) * 1e-3
-    bwd = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                    ops.GRAD[ops.get_grad_mode()])
+    bwd = lambda m: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                      ops.GRAD[m])
+    weights = lambda: ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True)
+    ws = weights()
+    scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                        ops.GRAD['REFERENCE'], weights=ws)
     for _ in range(2):
-        fwd()
-        bwd()
+        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter()
     tf = float(np.median(timed(fwd, 7)))
-    tb = float(np.median(timed(bwd, 7)))
-    other = 'EXACT' if ops.get_grad_mode() == 'REFERENCE' else 'REFERENCE'
-    bwd_other = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                          ops.GRAD[other])
-    bwd_other()
-    tb_other = float(np.median(timed(bwd_other, 5)))
+    tb_ref = float(np.median(timed(lambda: bwd('REFERENCE'), 7)))
+    tb_ex = float(np.median(timed(lambda: bwd('EXACT'), 7)))
+    tw = float(np.median(timed(weights, 7)))
+    ts = float(np.median(timed(scatter, 7)))
     nvox = int(np.prod(step.shape))
-    s = 4
+    s, C = 4, 4
     pix = V * H * W
-    bytes_fwd = nvox * 4 * s + pix * 4 * 4
-    bytes_bwd = nvox * 4 * s + 2 * pix * 4 * 4 + 2 * nvox * 4 * 4
     samples = pix * D
+    bytes_fwd = nvox * C * s + pix * C * 4
+    # scatter pass: grid read, image + adjoint read, per-camera reciprocal
+    # weights read, gradient read-modify-write
+    bytes_scatter = nvox * C * s + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
+    bytes_exact = nvox * C * s + 2 * pix * C * 4 + 2 * nvox * C * 4
+    bytes_weights = 2 * V * nvox * 4
     kern = {
         'raymarch_fwd': {'ms': tf, 'alg_bytes': bytes_fwd, 'GBps': bytes_fwd / tf / 1e6,
-                         'gather_GBps': samples * 8 * 16 / tf / 1e6, 'samples_per_s': samples / tf * 1e3},
-        'raymarch_bwd': {'ms': tb, 'alg_bytes': bytes_bwd, 'GBps': bytes_bwd / tb / 1e6,
-                         'gather_GBps': samples * 8 * 16 / tb / 1e6, 'samples_per_s': samples / tb * 1e3,
-                         'grad_mode': ops.get_grad_mode()},
-        'raymarch_bwd_' + other.lower(): {'ms': tb_other, 'samples_per_s': samples / tb_other * 1e3},
+                         'samples_per_s': samples / tf * 1e3},
+        'raymarch_bwd_scatter': {'ms': ts, 'alg_bytes': bytes_scatter, 'GBps': bytes_scatter / ts / 1e6,
+                                 'samples_per_s': samples / ts * 1e3, 'what': 'reference normalisation, weights ready'},
+        'raymarch_bwd_weights': {'ms': tw, 'alg_bytes': bytes_weights, 'GBps': bytes_weights / tw / 1e6,
+                                 'samples_per_s': samples / tw * 1e3},
+        'raymarch_bwd_reference': {'ms': tb_ref, 'what': 'whole op: weights + inversion + scatter'},
+        'raymarch_bwd_exact': {'ms': tb_ex, 'alg_bytes': bytes_exact, 'GBps': bytes_exact / tb_ex / 1e6,
+                               'samples_per_s': samples / tb_ex * 1e3},
+        'grad_mode': mode,
     }
-    dom = 'raymarch_bwd' if tb >= tf else 'raymarch_fwd'
-    k = kern[dom]
-    return {'roofline': {'kernel': dom, 'bound': 'hbm', 'achieved': k['GBps'], 'peak': peak, 'unit': 'GB/s',
-                         'frac': k['GBps'] / peak, 'peak_source': src, 'traffic': None,
-                         'note': 'algorithmic bytes = compulsory unique traffic; the grid is L2-resident, so the '
-                                 'binding resource is L1/L2 gather throughput (gather_GBps)'},
+    traffic = _profiled_traffic()
+    return {'roofline': {'kernel': 'k_raymarch_scatter (raymarch adjoint scatter pass, 5 views)', 'bound': 'hbm',
+                         'achieved': kern['raymarch_bwd_scatter']['GBps'], 'peak': peak, 'unit': 'GB/s',
+                         'frac': kern['raymarch_bwd_scatter']['GBps'] / peak, 'peak_source': src,
+                         'traffic': traffic, 'alg_bytes': bytes_scatter,
+                         'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, '
+                                           'profiles/raymarch_scatter_cfg2.md' if traffic else None,
+                         'note': 'algorithmic bytes = compulsory unique traffic; the 60 MB grid stays in the '
+                                 '129 MB L2, and the pass is bound by the L2 sector throughput of its trilinear '
+                                 'gradient reductions (8 per sample), not by HBM'},
             'kernels': kern}
 
 
@@ -339,7 +398,12 @@ def kernel_only(args):
         'advect_bwd': lambda: ops._advect_bwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
                                               step.s_vz.detach(), torch.ones_like(d), 1.0, 2, 1, 1, gm),
         'shadow_fwd': lambda: step.shadow(d),
+        'raymarch_weights': lambda: ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True),
     }
+    if args.kernel_only == 'raymarch_scatter':
+        ws = ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True)
+        fns['raymarch_scatter'] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
+                                                            0, 0, True, ops.GRAD['REFERENCE'], weights=ws)
     fn = fns[args.kernel_only]
     for _ in range(args.repeat):
         fn()
@@ -370,7 +434,7 @@ def bench_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--config', default='cfg2')
@@ -381,7 +445,8 @@ def main():
     ap.add_argument('--cpu-budget', type=float, default=20.0)
     ap.add_argument('--save-clocks', action='store_true')
     ap.add_argument('--kernel-only', default=None,
-                    choices=['raymarch_fwd', 'raymarch_bwd', 'advect_fwd', 'advect_bwd', 'shadow_fwd'],
+                    choices=['raymarch_fwd', 'raymarch_bwd', 'raymarch_weights', 'raymarch_scatter', 'advect_fwd',
+                             'advect_bwd', 'shadow_fwd'],
                     help='run one op of the workload --repeat times (profiling)')
     ap.add_argument('--repeat', type=int, default=3)
     args = ap.parse_args()
