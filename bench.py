@@ -180,7 +180,7 @@ def bench_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local, os.path.join(ROOT, 'gpurun_out', 'bench_clocks.csv') if args.save_clocks else None) as cs:
+    with ClockSampler(local, args.save_clocks) as cs:
         cs.mark()
         t_wall0 = time.perf_counter()
         times = timed(step.replay, args.steps)
@@ -443,7 +443,7 @@ def main():
     ap.add_argument('--quick', action='store_true', help='only the timed graph replays')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-budget', type=float, default=20.0)
-    ap.add_argument('--save-clocks', action='store_true')
+    ap.add_argument('--save-clocks', default=None, metavar='CSV', help='write every clock sample to this file')
     ap.add_argument('--kernel-only', default=None,
                     choices=['raymarch_fwd', 'raymarch_bwd', 'raymarch_weights', 'raymarch_scatter', 'advect_fwd',
                              'advect_bwd', 'shadow_fwd'],

@@ -40,13 +40,13 @@ class RenderSettings:
 
 
 CONFIGS = {
-    # configs[1]: multi-view frame, 5 views 480x270, 192 samples, 3 mips, spot light + shadow volume
+    # multi-view frame: 5 views 480x270, 192 samples, 3 mips, spot light + shadow volume
     'cfg2': dict(grid=(128, 227, 128), views=5, image=(480, 270), samples=192, mips=3,
                  shadow=(256, 196, 196), seed=2000),
-    # configs[0]-sized case for quick runs / CPU timing
+    # 64^3 single-view case for quick runs / CPU timing
     'cfg1': dict(grid=(64, 64, 64), views=1, image=(128, 128), samples=64, mips=3,
                  shadow=(64, 64, 64), seed=1000),
-    # stress grid (configs[4] sizes, one frame)
+    # stress grid 256x455x256, 5 views 960x540, 256 samples (one frame)
     'cfg5': dict(grid=(256, 455, 256), views=5, image=(960, 540), samples=256, mips=4,
                  shadow=(256, 196, 196), seed=5000),
     # tiny case for tests
@@ -115,10 +115,10 @@ class RenderAdvectStep:
             sh = torch.cat([torch.zeros_like(sh[:, :1]), sh[:, :-1]], dim=1)  # BORDER shift
             tr = torch.exp(-sh)
         else:
-            tr = fused.transmittance(sh[0])
+            tr = fused.transmittance(sh.squeeze(0))  # a view: no zero-fill in the backward
         trv = _InverseSampleGrad.apply(tr, self.M, self.Vs, self.Ps, self.Fs, self.shape,
                                        'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_LINDEPTH', self.rs, None)
-        return trv[0]  # [1,D,H,W,1]
+        return trv.squeeze(0)  # [1,D,H,W,1]
 
     def render(self, d):
         if self.mode == 'plain':
@@ -133,7 +133,7 @@ class RenderAdvectStep:
         else:
             img = ops.raymarch_grid_transform(data, self.M, self.V, self.P, self.F, self.res,
                                               storage_dtype=self.storage_dtype)
-        return img[0]  # [V,H,W,4]
+        return img.squeeze(0)  # [V,H,W,4]
 
     def loss(self, d_prev, vx, vy, vz, target):
         d = self.advect(d_prev, vx, vy, vz)

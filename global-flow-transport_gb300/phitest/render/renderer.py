@@ -50,7 +50,7 @@ class _InverseSampleGrad(torch.autograd.Function):
                                               boundary=r.boundary_mode, mipmapping=r.mip_mode,
                                               num_mipmaps=r.num_mips, mip_bias=r.mip_bias + r.gradient_mip_bias_add,
                                               coordinate_mode=inv_cm, separate_camera_batch=False)  # V1DHWC
-            dx.append(torch.sum(dxv, dim=0))  # 1DHWC
+            dx.append(torch.sum(dxv, dim=0) if views > 1 else dxv[0])  # 1DHWC (one view: the slice itself)
         dx = torch.cat(dx, dim=0) if batch > 1 else dx[0]
         return (dx,) + (None,) * 9
 

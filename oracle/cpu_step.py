@@ -1,7 +1,7 @@
 """CPU baseline: the FP64 oracle port of one render + advect step, timed on a
 bounded sample of the workload and extrapolated to a full step.
 
-TEST / BASELINE INFRASTRUCTURE ONLY (imported by bench.py's CPU legs).
+TEST / CPU-BASELINE INFRASTRUCTURE ONLY (imported by bench.py's CPU legs).
 
 The step is the one of gft.pipeline (cfg2): MacCormack advection fwd+bwd, the
 spot-light shadow pass (light-frustum resample with mips, cumulative sum,
