@@ -325,7 +325,8 @@ def kernel_roofline(step, dev, timed):
     dy = torch.randn_like(y) * 1e-3
     bwd = lambda m: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
                                       ops.GRAD[m])
-    weights = lambda: ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True)
+    weights = lambda: ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P, step.F,
+                                            step.res, 0, True)
     ws = weights()
     scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
                                         ops.GRAD['REFERENCE'], weights=ws)
@@ -398,10 +399,12 @@ def kernel_only(args):
         'advect_bwd': lambda: ops._advect_bwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
                                               step.s_vz.detach(), torch.ones_like(d), 1.0, 2, 1, 1, gm),
         'shadow_fwd': lambda: step.shadow(d),
-        'raymarch_weights': lambda: ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True),
+        'raymarch_weights': lambda: ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P,
+                                                          step.F, step.res, 0, True),
     }
     if args.kernel_only == 'raymarch_scatter':
-        ws = ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True)
+        ws = ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P, step.F, step.res, 0,
+                                   True)
         fns['raymarch_scatter'] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
                                                             0, 0, True, ops.GRAD['REFERENCE'], weights=ws)
     fn = fns[args.kernel_only]

@@ -148,21 +148,22 @@ def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate):
 WEIGHTS_READY = 0x100  # GFT_GRAD_WEIGHTS_READY
 
 
-def _raymarch_weights(x, M, V, P, F, out_shape, boundary, separate):
-    """Pass 1 of the reference-normalised raymarch gradient (per-camera weight
-    sums) into a new workspace, on the current stream."""
+def _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate):
+    """Pass 1 of the reference-normalised raymarch gradient (per-camera
+    reciprocal weight sums) for an input of ``x_shape`` into a new workspace,
+    on the current stream."""
     lib = _lib.load()
     Mh, nm = _mats(M)
     Vh, nv = _mats(V)
     Ph, _ = _mats(P)
     Fh, _ = _frustum(F)
-    shape = _lib.i64(x.shape)
+    shape = _lib.i64(x_shape)
     ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), GRAD['REFERENCE']),
-                    x.device)
-    with torch.cuda.device(x.device):
+                    device)
+    with torch.cuda.device(device):
         st = lib.gft_raymarch_grid_transform_grad_weights(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
                                                           _lib.i32(out_shape), boundary, int(separate), _p(ws),
-                                                          ws.numel(), _stream(x.device))
+                                                          ws.numel(), _stream(device))
     _lib.check(st, 'RaymarchGridTransformGrad weights')
     return ws
 
@@ -177,20 +178,53 @@ def _side_stream(dev):
     return s
 
 
-def _raymarch_weights_async(x, M, V, P, F, out_shape, boundary, separate):
+def _raymarch_weights_async(x_shape, device, M, V, P, F, out_shape, boundary, separate):
     """Launches the geometry-only weight pass on a side stream forked from the
     current one, so that it overlaps the rest of the forward pass (the pass is
     bound by L2 reductions, the forward kernels by issue and L1); returns the
     workspace and the event the backward waits on.  Fork and join are stream
     waits, so a CUDA-graph capture records the two branches."""
-    cur = torch.cuda.current_stream(x.device)
-    side = _side_stream(x.device)
+    cur = torch.cuda.current_stream(device)
+    side = _side_stream(device)
     side.wait_stream(cur)
     with torch.cuda.stream(side):
-        ws = _raymarch_weights(x, M, V, P, F, out_shape, boundary, separate)
+        ws = _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate)
         ev = torch.cuda.Event()
         ev.record(side)
     return ws, ev
+
+
+_prefetched = {}
+
+
+def _weights_key(x_shape, M, V, P, F, out_shape, boundary, separate, device):
+    return (tuple(int(v) for v in x_shape), _mats(M)[0].tobytes(), _mats(V)[0].tobytes(), _mats(P)[0].tobytes(),
+            _frustum(F)[0].tobytes(), tuple(int(v) for v in out_shape), int(boundary), bool(separate),
+            _cuda_device(device).index)
+
+
+def _cuda_device(device):
+    """torch.device with an explicit index (``'cuda'`` means the current device)."""
+    dev = torch.device('cuda') if device is None else torch.device(device)
+    return dev if dev.index is not None else torch.device('cuda', torch.cuda.current_device())
+
+
+def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
+                              boundary='BORDER', separate_camera_batch=True, device=None):
+    """Starts the first, geometry-only pass of the reference-normalised
+    raymarch gradient (the per-camera weight sums) on a side stream now, so
+    that it overlaps whatever the caller runs before the raymarch.  The next
+    differentiable raymarch_grid_transform with the same input shape, device
+    and geometry takes it over; until then it holds one float per voxel and
+    camera.  Under CUDA-graph capture that raymarch and its backward must be
+    captured too (they join the side stream)."""
+    dev = _cuda_device(device)
+    out_shape = _shape3(output_shape)
+    b = _enum(BOUNDARY, boundary, 'boundary')
+    key = _weights_key(input_shape, matrix_m, matrix_v, matrix_p, frustum_params, out_shape, b,
+                       separate_camera_batch, dev)
+    _prefetched[key] = _raymarch_weights_async(tuple(input_shape), dev, matrix_m, matrix_v, matrix_p, frustum_params,
+                                               out_shape, b, bool(separate_camera_batch))
 
 
 def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None):
@@ -222,7 +256,9 @@ class _Raymarch(torch.autograd.Function):
         xs = _storage(x, storage_dtype)
         ctx.weights = None
         if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
-            ctx.weights = _raymarch_weights_async(xs, M, V, P, F, out_shape, boundary, separate)
+            key = _weights_key(xs.shape, M, V, P, F, out_shape, boundary, separate, xs.device)
+            ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(tuple(xs.shape), xs.device, M, V, P,
+                                                                                F, out_shape, boundary, separate)
         y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate)
         ctx.save_for_backward(xs, y)
         ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate)

@@ -119,7 +119,7 @@ def main():
     # and G/W amplifies any difference of the sample positions (the reference
     # inverts MV and P in fp32, this repository in fp64).  Compare where every
     # camera that reaches a voxel has W >= thr.
-    inv = ops._raymarch_weights(data, step.M, step.V, step.P, step.F, step.res, 0, True)
+    inv = ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P, step.F, step.res, 0, True)
     inv = inv[:nv * data[0, ..., 0].numel() * 4].view(torch.float32).view(nv, -1)
     wmin = torch.where(inv > 0, 1.0 / inv, torch.full_like(inv, float('inf'))).min(0).values
     masked = {}

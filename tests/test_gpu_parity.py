@@ -101,6 +101,31 @@ def test_raymarch_backward_weights_on_side_stream(ops, boundary):
     assert rel_l2(np_(xt.grad), np_(g_inline)) <= 1e-6
 
 
+def test_raymarch_backward_prefetched_weights(ops):
+    """A weight pass prefetched for the same geometry is taken over by the next
+    differentiable raymarch; a different geometry does not take it."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 23) * 0.4
+    dy = cuda(np.random.default_rng(24).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+    grads = []
+    for prefetch in (False, True):
+        xt = cuda(x).requires_grad_(True)
+        with ops.grad_mode('REFERENCE'):
+            if prefetch:
+                ops.prefetch_raymarch_weights(x.shape, M, V, P, F, (13, 9, 11), device='cuda')
+                assert len(ops._prefetched) == 1
+            y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11))
+            assert len(ops._prefetched) == 0
+            y.backward(dy)
+        grads.append(np_(xt.grad))
+    assert rel_l2(grads[1], grads[0]) <= 1e-6
+    ops.prefetch_raymarch_weights(x.shape, M, V, P, F, (13, 9, 12), device='cuda')
+    with ops.grad_mode('REFERENCE'):
+        ops.raymarch_grid_transform(cuda(x).requires_grad_(True), M, V, P, F, (13, 9, 11))
+    assert len(ops._prefetched) == 1
+    ops._prefetched.clear()
+
+
 def test_raymarch_not_separate_batch(ops):
     from oracle import raymarch as RM
     _, _, M, V, P, F = scene((8, 9, 7), 2, (9, 6, 5))
