@@ -5,7 +5,7 @@
 //   transmittance    tr[z] = exp(-sum_{z' < z} s[z'])  -- ReduceGridBlend
 //                    BEER_LAMBERT (C == 1, inclusive depth sum), the one-cell
 //                    BORDER shift and exp of the shadow pass
-//                    (lighting.py:236-262), one thread per depth column;
+//                    (lighting.py:236-262), a segmented depth scan;
 //   light compose    out = concat(d * (tr * color + ambient), d) * scale
 //                    (lighting.py:106-121, renderer.py:1012-1030);
 //   image loss       mean((img.rgb + bkg * exp(-img.a) - target)^2) with its
@@ -30,50 +30,74 @@ static unsigned grid_for(int64_t n, int threads) {
 }
 
 // --- transmittance -------------------------------------------------------------
-__global__ void __launch_bounds__(CP_THREADS)
-    k_transmittance(const float* __restrict__ s, int N, Dims d, float* __restrict__ out) {
-    const int64_t plane = (int64_t)d.x * d.y;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= plane * N) return;
-    const int b = (int)(t / plane);
-    const int64_t base = (int64_t)b * plane * d.z + (t - (int64_t)b * plane);
-    float acc = 0.f;
-#pragma unroll 4
-    for (int z = 0; z < d.z; ++z) {
-        const int64_t i = base + (int64_t)z * plane;
-        out[i] = expf(-acc);
-        acc = __fadd_rn(acc, s[i]);
-    }
-}
+// Forward: tr[z] = exp(-sum_{z' < z} s[z']).  Adjoint (REVERSE): d tr[z] /
+// d s[z'] = -tr[z] for z' < z, so gs[z] = sum_{z'' > z} -tr[z''] g[z''].
+// Both scans run segmented: a block of 32 consecutive columns x 8 depth
+// segments; each thread scans its segment, the segment totals are exchanged
+// through shared memory, and each thread starts from the total of the
+// segments before (REVERSE: after) its own.  (The 196x196 columns of the
+// shadow frustum alone would give one thread per column too few threads to
+// hide the latency of 256 dependent steps.)  The sums associate differently
+// from a sequential scan: rounding only.
+constexpr int TS_COLS = 32, TS_SEGS = 8;
 
-// d tr[z] / d s[z'] = -tr[z] for z' < z: gs[z] = sum_{z'' > z} -tr[z''] g[z''],
-// accumulated from the far end as the blend adjoint does.
-__global__ void __launch_bounds__(CP_THREADS)
-    k_transmittance_grad(const float* __restrict__ tr, const float* __restrict__ g, int N, Dims d,
-                         float* __restrict__ gs) {
+template <bool REVERSE>
+__global__ void __launch_bounds__(TS_COLS* TS_SEGS)
+    k_transmittance_seg(const float* __restrict__ a, const float* __restrict__ b, int N, Dims d,
+                        float* __restrict__ out) {
+    __shared__ float tot[TS_SEGS][TS_COLS];
     const int64_t plane = (int64_t)d.x * d.y;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= plane * N) return;
-    const int b = (int)(t / plane);
-    const int64_t base = (int64_t)b * plane * d.z + (t - (int64_t)b * plane);
-    float acc = 0.f;
-#pragma unroll 4
-    for (int z = d.z - 1; z >= 0; --z) {
+    const int64_t col = (int64_t)blockIdx.x * TS_COLS + threadIdx.x;
+    const int seg = threadIdx.y;
+    const bool ok = col < plane * N;
+    const int bb = ok ? (int)(col / plane) : 0;
+    const int64_t base = (int64_t)bb * plane * d.z + (col - (int64_t)bb * plane);
+    const int len = (d.z + TS_SEGS - 1) / TS_SEGS;
+    const int z0 = seg * len, z1 = min(z0 + len, d.z);
+    // value of one depth step: the density (forward) or -tr * g (adjoint)
+    auto val = [&](int z) {
         const int64_t i = base + (int64_t)z * plane;
-        gs[i] = acc;
-        acc = __fadd_rn(acc, -__fmul_rn(g[i], tr[i]));
+        return REVERSE ? -__fmul_rn(b[i], a[i]) : a[i];
+    };
+    float s = 0.f;
+    if (ok) {
+        for (int z = z0; z < z1; ++z) s = __fadd_rn(s, val(z));
+    }
+    tot[seg][threadIdx.x] = s;
+    __syncthreads();
+    if (!ok) return;
+    float off = 0.f;
+    if (!REVERSE) {
+        for (int k = 0; k < seg; ++k) off = __fadd_rn(off, tot[k][threadIdx.x]);
+        float acc = off;
+        for (int z = z0; z < z1; ++z) {
+            const int64_t i = base + (int64_t)z * plane;
+            out[i] = expf(-acc);
+            acc = __fadd_rn(acc, a[i]);
+        }
+    } else {
+        for (int k = TS_SEGS - 1; k > seg; --k) off = __fadd_rn(off, tot[k][threadIdx.x]);
+        float acc = off;
+        for (int z = z1 - 1; z >= z0; --z) {
+            const int64_t i = base + (int64_t)z * plane;
+            out[i] = acc;
+            acc = __fadd_rn(acc, val(z));
+        }
     }
 }
 
 bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st) {
     const int64_t cols = (int64_t)d.x * d.y * N;
-    k_transmittance<<<(unsigned)((cols + CP_THREADS - 1) / CP_THREADS), CP_THREADS, 0, st>>>(s, N, d, out);
+    k_transmittance_seg<false><<<(unsigned)((cols + TS_COLS - 1) / TS_COLS), dim3(TS_COLS, TS_SEGS), 0, st>>>(
+        s, nullptr, N, d, out);
     return launched(1, "transmittance launch");
 }
 
+// tr, g: the forward output and its adjoint
 bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st) {
     const int64_t cols = (int64_t)d.x * d.y * N;
-    k_transmittance_grad<<<(unsigned)((cols + CP_THREADS - 1) / CP_THREADS), CP_THREADS, 0, st>>>(tr, g, N, d, gs);
+    k_transmittance_seg<true><<<(unsigned)((cols + TS_COLS - 1) / TS_COLS), dim3(TS_COLS, TS_SEGS), 0, st>>>(
+        tr, g, N, d, gs);
     return launched(1, "transmittance gradient launch");
 }
 
