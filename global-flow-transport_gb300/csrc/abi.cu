@@ -131,6 +131,10 @@ std::vector<PairTable> make_tables(const std::vector<Pair>& pairs) {
             t.cam[k] = pairs[i + k].cam;
             t.in_batch[k] = pairs[i + k].in_batch;
             t.out_slot[k] = pairs[i + k].out_slot;
+            t.rw[k] = pairs[i + k].W;
+            t.rh[k] = pairs[i + k].H;
+            t.rd[k] = pairs[i + k].D;
+            t.pix0[k] = pairs[i + k].pix0;
         }
         out.push_back(t);
     }
@@ -185,6 +189,16 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// Raymarch pairs of one image size: pair k writes output slot out_slot.
+void set_uniform_images(std::vector<Pair>& pairs, int D, int H, int W) {
+    for (Pair& p : pairs) {
+        p.W = W;
+        p.H = H;
+        p.D = D;
+        p.pix0 = (int64_t)p.out_slot * H * W;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -228,8 +242,9 @@ gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, c
     a.filter = interpolation;
     a.boundary = boundary;
     a.blend = blending_mode;
-    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
-                                  separate_camera_batch != 0);
+    auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                            separate_camera_batch != 0);
+    set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
     if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
     return GFT_OK;
@@ -286,8 +301,9 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
     a.filter = interpolation;
     a.boundary = boundary;
     a.blend = blending_mode;
-    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
-                                  separate_camera_batch != 0);
+    auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                            separate_camera_batch != 0);
+    set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
     if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
@@ -323,8 +339,150 @@ gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5]
     a.W = output_shape[2];
     a.filter = GFT_FILTER_LINEAR;
     a.boundary = boundary;
-    const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
-                                  separate_camera_batch != 0);
+    auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N,
+                            separate_camera_batch != 0);
+    set_uniform_images(pairs, a.D, a.H, a.W);
+    a.n_slots = (int)pairs.size();
+    if (!launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+// ---------------------------------------------------------------- raymarch, cameras of different image sizes
+static bool multi_shapes_ok(const int32_t* shapes, int32_t num_cameras, std::string& why) {
+    if (shapes == nullptr || num_cameras <= 0) {
+        why = "output_shapes must hold num_cameras x 3 positive sizes";
+        return false;
+    }
+    for (int c = 0; c < 3 * num_cameras; ++c)
+        if (shapes[c] < 1) {
+            why = "All shape dimensions must be positive (output_shapes)";
+            return false;
+        }
+    return true;
+}
+
+// Every (batch, camera) pair with its own image; the output of batch slice n
+// holds the cameras' images one after another.
+static std::vector<Pair> multi_pairs(const float* M, int num_m, const float* V, const float* P, const float* F,
+                                     int num_cameras, int batch, const int32_t* shapes) {
+    auto pairs = make_pairs(M, num_m, V, P, F, num_cameras, batch, true);
+    int64_t per_batch = 0;
+    for (int c = 0; c < num_cameras; ++c) per_batch += (int64_t)shapes[3 * c + 1] * shapes[3 * c + 2];
+    for (Pair& p : pairs) {
+        int64_t off = 0;
+        for (int c = 0; c < p.camera; ++c) off += (int64_t)shapes[3 * c + 1] * shapes[3 * c + 2];
+        p.D = shapes[3 * p.camera];
+        p.H = shapes[3 * p.camera + 1];
+        p.W = shapes[3 * p.camera + 2];
+        p.pix0 = (int64_t)p.in_batch * per_batch + off;
+    }
+    return pairs;
+}
+
+gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                             const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                             const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                             const int32_t* output_shapes, int32_t interpolation, int32_t boundary,
+                                             int32_t blending_mode, float* output, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(blending_mode, 0, 4) ||
+        !enum_in(input_dtype, 0, 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
+    if (st != GFT_OK) return st;
+    if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    RaymarchArgs a{};
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.blend = blending_mode;
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
+    a.n_slots = (int)pairs.size();
+    if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+size_t gft_raymarch_grid_transform_multi_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
+                                                             int32_t grad_mode) {
+    return gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras, 1, grad_mode);
+}
+
+gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t input_dtype,
+                                                  const int64_t input_shape[5], const float* output,
+                                                  const float* output_grad, const float* matrix_m, int32_t num_m,
+                                                  const float* matrix_v, const float* matrix_p, const float* frustum,
+                                                  int32_t num_cameras, const int32_t* output_shapes,
+                                                  int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                                  int32_t grad_mode, float* input_grad, void* workspace,
+                                                  size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (interpolation != GFT_FILTER_LINEAR)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "gradient supports LINEAR interpolation only");
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
+    const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
+    grad_mode &= ~GFT_GRAD_WEIGHTS_READY;
+    if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
+    if (st != GFT_OK) return st;
+    if (!input || !output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    const size_t need = gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, grad_mode);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    RaymarchArgs a{};
+    a.input = input;
+    a.dtype = input_dtype;
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.filter = interpolation;
+    a.boundary = boundary;
+    a.blend = blending_mode;
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
+    a.n_slots = (int)pairs.size();
+    float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
+    if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
+                             cnt, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_shape[5], const float* matrix_m,
+                                                          int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                                          const float* frustum, int32_t num_cameras,
+                                                          const int32_t* output_shapes, int32_t boundary,
+                                                          void* workspace, size_t workspace_bytes, void* stream) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
+    if (st != GFT_OK) return st;
+    const size_t need = gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras,
+                                                                              GFT_GRAD_REFERENCE);
+    if (workspace == nullptr || workspace_bytes < need)
+        return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    RaymarchArgs a{};
+    a.N = (int)input_shape[0];
+    a.C = (int)input_shape[4];
+    a.din = dims_of(input_shape);
+    a.filter = GFT_FILTER_LINEAR;
+    a.boundary = boundary;
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
     a.n_slots = (int)pairs.size();
     if (!launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream)))
         return GFT_ERR_CUDA;

@@ -19,6 +19,13 @@ struct PairTable {
     CamX cam[MAX_PAIRS];
     int in_batch[MAX_PAIRS];  // batch slice of the input grid
     int out_slot[MAX_PAIRS];  // slot in the output's [N * V] leading dims
+    // raymarch only: each pair's image (width, height, depth samples), its first
+    // output pixel, and the first block of its pixel tiles in this launch
+    // (tile0[n] = blocks of the launch), so that cameras of different image
+    // sizes share one launch
+    int rw[MAX_PAIRS], rh[MAX_PAIRS], rd[MAX_PAIRS];
+    int64_t pix0[MAX_PAIRS];
+    int tile0[MAX_PAIRS + 1];
     int pair_base;            // global index of pair 0 of this launch
     int n;                    // pairs in this launch
 };
@@ -29,6 +36,8 @@ struct Pair {
     int in_batch;
     int out_slot;
     int camera;
+    int W = 0, H = 0, D = 0;  // raymarch image of the pair
+    int64_t pix0 = 0;         // raymarch: first output pixel of the pair
 };
 
 // Builds the (batch, camera) pairs with MV = V*M and the inverses computed in

@@ -44,14 +44,47 @@ __device__ __forceinline__ bool ray_clip(float3 p0, float3 st, int n, Dims d, in
     return true;
 }
 
+// The blocks of one launch tile the images of all its pairs (8x16 pixels per
+// block, row-major per pair, pairs one after another, tab.tile0): pairs may
+// differ in image size and sample count.  Sets this thread's pair, pixel and
+// the pair's geometry; false for pixels outside the pair's image.
+struct RayPix {
+    int p, x, y, W, H, D;
+};
+__device__ __forceinline__ bool ray_pixel(const PairTable& tab, RayPix& r) {
+    const int b = blockIdx.x;
+    int p = 0;
+    while (p + 1 < tab.n && b >= tab.tile0[p + 1]) ++p;
+    r.p = p;
+    r.W = tab.rw[p];
+    r.H = tab.rh[p];
+    r.D = tab.rd[p];
+    const int tiles_x = (r.W + RM_BX - 1) / RM_BX;
+    const int t = b - tab.tile0[p];
+    const int ty = t / tiles_x;
+    r.x = (t - ty * tiles_x) * RM_BX + threadIdx.x;
+    r.y = ty * RM_BY + threadIdx.y;
+    return r.x < r.W && r.y < r.H;
+}
+
+// Fills tab.tile0 (host side) and returns the blocks of the launch.
+static unsigned set_ray_tiles(PairTable& t) {
+    int b = 0;
+    for (int k = 0; k < t.n; ++k) {
+        t.tile0[k] = b;
+        b += ((t.rw[k] + RM_BX - 1) / RM_BX) * ((t.rh[k] + RM_BY - 1) / RM_BY);
+    }
+    t.tile0[t.n] = b;
+    return (unsigned)b;
+}
+
 template <int C, typename S, int BM, bool LIN>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
-    k_raymarch_fwd(const S* __restrict__ in, Dims din, int W, int H, int D, int filter, int blend_mode,
-                   float* __restrict__ out, const __grid_constant__ PairTable tab) {
-    const int p = blockIdx.z;
-    const int x = blockIdx.x * RM_BX + threadIdx.x;
-    const int y = blockIdx.y * RM_BY + threadIdx.y;
-    if (x >= W || y >= H) return;
+    k_raymarch_fwd(const S* __restrict__ in, Dims din, int filter, int blend_mode, float* __restrict__ out,
+                   const __grid_constant__ PairTable tab) {
+    RayPix r;
+    if (!ray_pixel(tab, r)) return;
+    const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     const CamX& cam = tab.cam[p];
     const S* g = in + (size_t)tab.in_batch[p] * voxels(din) * C;
     const float3 dinv = make_float3(1.f / (float)W, 1.f / (float)H, 1.f / (float)D);
@@ -67,7 +100,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     // sums below -88: neither is clipped.
     if (BM == BM_BORDER && (LIN || filter == F_NEAREST) && (C == 1 || blend_mode != BL_BEER_LAMBERT_EXCLUSIVE)) {
         if (!ray_clip(nearp, step, D, din, i0, i1)) {
-            store<C>(out, ((int64_t)tab.out_slot[p] * H + y) * W + x, acc);
+            store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
             return;
         }
         for (int i = 0; i < i0; ++i) {
@@ -88,7 +121,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         pos.y += step.y;
         pos.z += step.z;
     }
-    store<C>(out, ((int64_t)tab.out_slot[p] * H + y) * W + x, acc);
+    store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
 }
 
 // Ray set-up shared by the adjoint kernels: far end point and step (the
@@ -183,13 +216,12 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
 // full.  (Non-finite adjoints are not propagated through skipped samples.)
 template <int C, typename S, int BM, int MODE>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
-    k_raymarch_scatter(const S* __restrict__ in, Dims din, int W, int H, int D, int blend_mode,
-                       const float* __restrict__ out, const float* __restrict__ dout, float* __restrict__ grad,
-                       const float* __restrict__ cnt, const __grid_constant__ PairTable tab) {
-    const int p = blockIdx.z;
-    const int x = blockIdx.x * RM_BX + threadIdx.x;
-    const int y = blockIdx.y * RM_BY + threadIdx.y;
-    if (x >= W || y >= H) return;
+    k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
+                       const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
+                       const __grid_constant__ PairTable tab) {
+    RayPix r;
+    if (!ray_pixel(tab, r)) return;
+    const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     const int64_t nvox = voxels(din);
     float3 pos, step;
     ray_far_step(tab.cam[p], x, y, W, H, D, pos, step);
@@ -198,7 +230,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * nvox : nullptr;
     Vec<C> acc = vzero<C>(), go = vzero<C>();
     if constexpr (MODE != 2) {
-        const int64_t pix = ((int64_t)tab.out_slot[p] * H + y) * W + x;
+        const int64_t pix = tab.pix0[p] + (int64_t)y * W + x;
         acc = loadf<C>(out, pix);
         go = loadf<C>(dout, pix);
     }
@@ -230,11 +262,9 @@ template <int C, typename S, int BM>
 static void fwd_dispatch_lin(bool lin, dim3 grid, dim3 block, cudaStream_t s, const void* in, const RaymarchArgs& a,
                              float* out, const PairTable& t) {
     if (lin)
-        k_raymarch_fwd<C, S, BM, true><<<grid, block, 0, s>>>((const S*)in, a.din, a.W, a.H, a.D, a.filter, a.blend,
-                                                               out, t);
+        k_raymarch_fwd<C, S, BM, true><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend, out, t);
     else
-        k_raymarch_fwd<C, S, BM, false><<<grid, block, 0, s>>>((const S*)in, a.din, a.W, a.H, a.D, a.filter, a.blend,
-                                                                out, t);
+        k_raymarch_fwd<C, S, BM, false><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend, out, t);
 }
 
 template <int C, typename S>
@@ -250,8 +280,8 @@ static void fwd_dispatch_bm(dim3 grid, dim3 block, cudaStream_t s, const Raymarc
 
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s) {
     const dim3 block(RM_BX, RM_BY, 1);
-    for (const PairTable& t : make_tables(pairs)) {
-        const dim3 grid((a.W + RM_BX - 1) / RM_BX, (a.H + RM_BY - 1) / RM_BY, t.n);
+    for (PairTable& t : make_tables(pairs)) {
+        const dim3 grid(set_ray_tiles(t));
         if (a.dtype == 0) {
             if (a.C == 4) fwd_dispatch_bm<4, float>(grid, block, s, a, out, t);
             else if (a.C == 2) fwd_dispatch_bm<2, float>(grid, block, s, a, out, t);
@@ -270,11 +300,11 @@ template <int C, typename S, int BM>
 static void bwd_dispatch(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
                          const float* dout, float* grad, const float* cnt, const PairTable& t) {
     if (exact)
-        k_raymarch_scatter<C, S, BM, 0><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend,
-                                                                  out, dout, grad, cnt, t);
+        k_raymarch_scatter<C, S, BM, 0><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
+                                                                  cnt, t);
     else
-        k_raymarch_scatter<C, S, BM, 1><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.W, a.H, a.D, a.blend,
-                                                                  out, dout, grad, cnt, t);
+        k_raymarch_scatter<C, S, BM, 1><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
+                                                                  cnt, t);
 }
 
 template <int C, typename S>
@@ -290,8 +320,8 @@ static void bwd_dispatch_bm(bool exact, dim3 grid, dim3 block, cudaStream_t s, c
 template <int BM>
 static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
                              const PairTable& t) {
-    k_raymarch_scatter<1, float, BM, 2><<<grid, block, 0, s>>>(nullptr, a.din, a.W, a.H, a.D, a.blend, nullptr,
-                                                                  nullptr, cnt, nullptr, t);
+    k_raymarch_scatter<1, float, BM, 2><<<grid, block, 0, s>>>(nullptr, a.din, a.blend, nullptr, nullptr, cnt,
+                                                                  nullptr, t);
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel).
@@ -306,9 +336,8 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
     const int64_t nvox = voxels(a.din);
     if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * nvox * pairs.size(), s), "zero weights")) return false;
     const dim3 block(RM_BX, RM_BY, 1);
-    const int gx = (a.W + RM_BX - 1) / RM_BX, gy = (a.H + RM_BY - 1) / RM_BY;
-    for (const PairTable& t : make_tables(pairs)) {
-        const dim3 grid(gx, gy, t.n);
+    for (PairTable& t : make_tables(pairs)) {
+        const dim3 grid(set_ray_tiles(t));
         switch (a.boundary) {
             case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, t); break;
             case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, t); break;
@@ -332,9 +361,8 @@ bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
     if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvox * a.C * a.N, s), "zero gradient")) return false;
     if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
     const dim3 block(RM_BX, RM_BY, 1);
-    const int gx = (a.W + RM_BX - 1) / RM_BX, gy = (a.H + RM_BY - 1) / RM_BY;
-    for (const PairTable& t : make_tables(pairs)) {
-        const dim3 grid(gx, gy, t.n);
+    for (PairTable& t : make_tables(pairs)) {
+        const dim3 grid(set_ray_tiles(t));
         if (a.dtype == 0) {
             if (a.C == 4) bwd_dispatch_bm<4, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
             else if (a.C == 2) bwd_dispatch_bm<2, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);

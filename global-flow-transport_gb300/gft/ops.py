@@ -311,6 +311,125 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
                          bool(separate_camera_batch), GRAD[get_grad_mode()])
 
 
+# ------------------------------------------------------------------ raymarch, uneven camera batches
+def _shapes3(shapes, nv):
+    s = [[int(v) for v in (sh.tolist() if isinstance(sh, (np.ndarray, torch.Tensor)) else sh)] for sh in shapes]
+    if len(s) != nv or any(len(v) != 3 or min(v) < 1 for v in s):
+        raise _lib.GftInvalidArgument('output_shapes must hold one positive (depth, height, width) per camera')
+    return s
+
+
+def _raymarch_multi_weights(x_shape, device, M, V, P, F, shapes, boundary):
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, _ = _mats(P)
+    Fh, _ = _frustum(F)
+    shape = _lib.i64(x_shape)
+    ws = _workspace(lib.gft_raymarch_grid_transform_multi_grad_workspace_size(shape, nv, GRAD['REFERENCE']), device)
+    with torch.cuda.device(device):
+        st = lib.gft_raymarch_grid_transform_multi_grad_weights(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
+                                                                _lib.i32(sum(shapes, [])), boundary, _p(ws),
+                                                                ws.numel(), _stream(device))
+    _lib.check(st, 'RaymarchGridTransformMulti weights')
+    return ws
+
+
+def _raymarch_multi_fwd(x, M, V, P, F, shapes, interp, boundary, blend):
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, npj = _mats(P)
+    Fh, nf = _frustum(F)
+    if not (nv == npj == nf):
+        raise _lib.GftInvalidArgument('camera batch size mismatch')
+    N, C = x.shape[0], x.shape[4]
+    npix = sum(h * w for _, h, w in shapes)
+    out = torch.empty((N, npix, C), dtype=torch.float32, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_multi(_p(x), _dtype_code(x), _lib.i64(x.shape), _p(Mh), nm, _p(Vh),
+                                                   _p(Ph), _p(Fh), nv, _lib.i32(sum(shapes, [])), interp, boundary,
+                                                   blend, _p(out), _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformMulti')
+    return out
+
+
+def _raymarch_multi_bwd(x, y, dy, M, V, P, F, shapes, interp, boundary, blend, gmode, weights=None):
+    lib = _lib.load()
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, _ = _mats(P)
+    Fh, _ = _frustum(F)
+    shape = _lib.i64(x.shape)
+    grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    if weights is not None and gmode == GRAD['REFERENCE']:
+        ws = weights
+        gmode = gmode | WEIGHTS_READY
+    else:
+        ws = _workspace(lib.gft_raymarch_grid_transform_multi_grad_workspace_size(shape, nv, gmode), x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_multi_grad(_p(x), _dtype_code(x), shape, _p(y), _p(dy), _p(Mh), nm,
+                                                        _p(Vh), _p(Ph), _p(Fh), nv, _lib.i32(sum(shapes, [])),
+                                                        interp, boundary, blend, gmode, _p(grad), _p(ws),
+                                                        ws.numel(), _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformMultiGrad')
+    return grad
+
+
+class _RaymarchMulti(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, M, V, P, F, shapes, interp, boundary, blend, storage_dtype):
+        xs = _storage(x, storage_dtype)
+        ctx.weights = None
+        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+            cur = torch.cuda.current_stream(xs.device)
+            side = _side_stream(xs.device)
+            side.wait_stream(cur)
+            with torch.cuda.stream(side):
+                ws = _raymarch_multi_weights(tuple(xs.shape), xs.device, M, V, P, F, shapes, boundary)
+                ev = torch.cuda.Event()
+                ev.record(side)
+            ctx.weights = (ws, ev)
+        y = _raymarch_multi_fwd(xs, M, V, P, F, shapes, interp, boundary, blend)
+        ctx.save_for_backward(xs, y)
+        ctx.args = (M, V, P, F, shapes, interp, boundary, blend)
+        ctx.in_dtype = x.dtype
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        xs, y = ctx.saved_tensors
+        M, V, P, F, shapes, interp, boundary, blend = ctx.args
+        ws = None
+        if ctx.weights is not None:
+            ws, ev = ctx.weights
+            torch.cuda.current_stream(xs.device).wait_event(ev)
+        g = _raymarch_multi_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, shapes, interp, boundary, blend,
+                                GRAD[get_grad_mode()], weights=ws)
+        ctx.weights = None
+        return (g.to(ctx.in_dtype),) + (None,) * 9
+
+
+def raymarch_grid_transform_multi(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shapes,
+                                  interpolation='LINEAR', boundary='BORDER', blending_mode='BEER_LAMBERT',
+                                  storage_dtype=None):
+    """RaymarchGridTransform for cameras of different image sizes in one launch
+    (global sampling): camera c renders output_shapes[c] = (depth samples,
+    height, width).  Returns one [N, H_c, W_c, C] image per camera, views of one
+    [N, sum_c H_c W_c, C] buffer; each equals
+    raymarch_grid_transform(input, ..., camera c alone, output_shapes[c])[:, 0]."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    if x.dim() != 5 or x.shape[4] > 4:
+        raise _lib.GftInvalidArgument('Invalid input shape (NDHWC): %s' % (tuple(x.shape),))
+    nv = _mats(matrix_v)[1]
+    shapes = _shapes3(output_shapes, nv)
+    y = _RaymarchMulti.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, shapes,
+                             _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                             _enum(BLEND, blending_mode, 'blending_mode'), storage_dtype)
+    sizes = [h * w for _, h, w in shapes]
+    return [part.view(x.shape[0], h, w, x.shape[4]) for part, (_, h, w) in zip(torch.split(y, sizes, dim=1), shapes)]
+
+
 # ------------------------------------------------------------------ SampleGridTransform
 def _sample_transform_fwd(x, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco, separate):
     lib = _lib.load()

@@ -119,6 +119,36 @@ gft_status gft_raymarch_grid_transform_grad_weights(
     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
     int32_t boundary, int32_t separate_camera_batch, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- RaymarchGridTransform over cameras of different image sizes ----
+ * No counterpart op in the reference, which takes one output_shape per call
+ * (raymarch_grid.cc:28-52): the reference renders uneven camera batches with
+ * one call per image size.  Global sampling (every batch slice with every
+ * camera).  output_shapes = num_cameras x (depth samples, height, width);
+ * output (and output_grad) hold, for each batch slice n and camera c, an
+ * H_c x W_c x C image, the cameras one after another: camera c of slice n
+ * starts at pixel n * P + P_c, with P = sum of all H_c W_c and P_c the sum over
+ * the cameras before c.  All cameras run in one launch (up to 16 per launch).
+ * Semantics per camera are those of gft_raymarch_grid_transform(_grad). */
+gft_status gft_raymarch_grid_transform_multi(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* output_shapes,
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, float* output, void* stream);
+size_t gft_raymarch_grid_transform_multi_grad_workspace_size(
+    const int64_t input_shape[5], int32_t num_cameras, int32_t grad_mode);
+gft_status gft_raymarch_grid_transform_multi_grad(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* output, const float* output_grad,
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* output_shapes,
+    int32_t interpolation, int32_t boundary, int32_t blending_mode,
+    int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+gft_status gft_raymarch_grid_transform_multi_grad_weights(
+    const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* output_shapes,
+    int32_t boundary, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- SampleGridTransform (resample_grid.cc:23-61, :268-447; launcher resample_grid.cu.cc:289-438) ----
  * output [N, separate_camera_batch ? num_cameras : 1, Do, Ho, Wo, C] fp32.
  * The workspace holds the mip pyramid (empty without mips). */

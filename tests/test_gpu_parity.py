@@ -315,3 +315,62 @@ def test_advect(ops, order, clamp, boundary, mode):
     assert rel_l2(np_(dtn.grad)[0], gd) <= GRAD_TOL
     for got, want in zip(vs, (gvx, gvy, gvz)):
         assert rel_l2(np_(got.grad)[0], want) <= GRAD_TOL
+
+
+# ------------------------------------------------------------------ raymarch, uneven camera batches
+UNEVEN = [(13, 9, 11), (7, 6, 5), (11, 12, 16)]  # (depth samples, height, width) per camera
+
+
+def _uneven_scene(C, seed, batch=1):
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = np.concatenate([small_grid((10, 14, 12), C, seed + b) for b in range(batch)], 0) * 0.4
+    return x, np.concatenate([M] * batch, 0), V, P, F
+
+
+@pytest.mark.parametrize('C', [1, 2, 4])
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+@pytest.mark.parametrize('batch', [1, 2])
+def test_raymarch_multi_forward_equals_per_camera(ops, C, boundary, batch):
+    x, M, V, P, F = _uneven_scene(C, 31, batch)
+    imgs = ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, UNEVEN, 'LINEAR', boundary)
+    for c, shp in enumerate(UNEVEN):
+        one = ops.raymarch_grid_transform(cuda(x), M, V[c:c + 1], P[c:c + 1], F[c:c + 1], shp, 'LINEAR', boundary)
+        assert imgs[c].shape == (batch, shp[1], shp[2], C)
+        assert torch.equal(imgs[c], one[:, 0])
+
+
+def test_raymarch_multi_forward_oracle(ops):
+    from oracle import raymarch as RM
+    x, M, V, P, F = _uneven_scene(4, 35)
+    imgs = ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, UNEVEN)
+    for c, shp in enumerate(UNEVEN):
+        ref = RM.raymarch_fwd(x, M, V[c:c + 1], P[c:c + 1], F[c:c + 1], shp)
+        assert rel_l2(np_(imgs[c]), ref[:, 0]) <= FWD_TOL
+
+
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+@pytest.mark.parametrize('C', [1, 4])
+def test_raymarch_multi_backward_equals_sum_over_cameras(ops, mode, C):
+    x, M, V, P, F = _uneven_scene(C, 41)
+    rng = np.random.default_rng(42)
+    dys = [cuda(rng.standard_normal((1, h, w, C)).astype(np.float32)) for _, h, w in UNEVEN]
+    with ops.grad_mode(mode):
+        xt = cuda(x).requires_grad_(True)
+        imgs = ops.raymarch_grid_transform_multi(xt, M, V, P, F, UNEVEN)
+        sum((im * dy).sum() for im, dy in zip(imgs, dys)).backward()
+        g_sum = torch.zeros_like(xt)
+        for c, shp in enumerate(UNEVEN):
+            xc = cuda(x).requires_grad_(True)
+            one = ops.raymarch_grid_transform(xc, M, V[c:c + 1], P[c:c + 1], F[c:c + 1], shp)
+            one.backward(dys[c][:, None])
+            g_sum += xc.grad
+    assert rel_l2(np_(xt.grad), np_(g_sum)) <= 1e-5
+
+
+def test_raymarch_multi_argument_errors(ops):
+    from gft import _lib
+    x, M, V, P, F = _uneven_scene(4, 43)
+    with pytest.raises(_lib.GftInvalidArgument):
+        ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, UNEVEN[:2])
+    with pytest.raises(_lib.GftInvalidArgument):
+        ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, [(13, 9, 11), (7, 0, 5), (11, 12, 16)])
