@@ -274,6 +274,7 @@ def extras(args, step, dev, timed, storage, inputs, ms):
 
     # ---- per-kernel timing of the dominant ops (roofline) -------------------
     out.update(kernel_roofline(step, dev, timed))
+    out['uneven_views'] = uneven_views(dev, timed)
 
     # ---- CPU baseline ------------------------------------------------------------
     if not args.no_cpu:
@@ -283,6 +284,53 @@ def extras(args, step, dev, timed, storage, inputs, ms):
         except Exception as e:  # the baseline is reported, not required
             out['cpu_baseline'] = {'error': repr(e)}
     return out
+
+
+def uneven_views(dev, timed):
+    """One frame of the uneven-view batch workload: density 96x170x96 (C = 4
+    light + density), one fixed 256x256 view plus 8 seeded upper-hemisphere
+    views of 64-256 pixels square, 128 samples, reference-normalised gradient.
+    Raymarch forward + adjoint of all 9 views in one launch each
+    (raymarch_grid_transform_multi) against one launch per view (the
+    reference's structure: one call per image size)."""
+    import numpy as np
+    import torch
+    from gft import ops
+    from gft import synthetic as syn
+    from phitest.render.transform import GridTransform
+    shape = (96, 170, 96)
+    gt = GridTransform(list(shape), center=True, normalize='MIN')
+    M = syn.model_matrix(gt)
+    cams, shapes = syn.hemisphere_cameras(8, 128, seed=4000)
+    V, P, F = syn.camera_params(cams)
+    d = torch.from_numpy(syn.plume_density(shape, 4000)).to(dev)
+    x = (torch.cat([d * 0.7, d * 0.5, d * 0.3, d], -1) * 0.02).contiguous()
+    ref = ops.GRAD['REFERENCE']
+    y = ops._raymarch_multi_fwd(x, M, V, P, F, [list(s) for s in shapes], 1, 0, 0)
+    torch.manual_seed(0)
+    dy = torch.randn_like(y) * 1e-3
+    sl = [list(s) for s in shapes]
+
+    def multi():
+        yy = ops._raymarch_multi_fwd(x, M, V, P, F, sl, 1, 0, 0)
+        ops._raymarch_multi_bwd(x, yy, dy, M, V, P, F, sl, 1, 0, 0, ref)
+
+    offs = np.cumsum([0] + [h * w for _, h, w in shapes])
+    dys = [dy[:, offs[c]:offs[c + 1]].reshape(1, 1, shapes[c][1], shapes[c][2], 4).contiguous()
+           for c in range(len(shapes))]
+
+    def per_view():
+        for c, s in enumerate(shapes):
+            yc = ops._raymarch_fwd(x, M, V[c:c + 1], P[c:c + 1], F[c:c + 1], s, 1, 0, 0, True)
+            ops._raymarch_bwd(x, yc, dys[c], M, V[c:c + 1], P[c:c + 1], F[c:c + 1], s, 1, 0, 0, True, ref)
+
+    for _ in range(2):
+        multi(), per_view()
+    tm = float(np.median(timed(multi, 7)))
+    tp = float(np.median(timed(per_view, 7)))
+    return {'workload': 'density 96x170x96, views 256^2 + 8 x (64-256)^2 upper hemisphere, 128 samples, '
+                        'raymarch fwd + reference-normalised adjoint',
+            'sizes': [s[1] for s in shapes], 'one_launch_ms': tm, 'per_view_ms': tp, 'speedup': tp / tm}
 
 
 SCATTER_PROFILE = os.path.join(ROOT, 'profiles', 'raymarch_scatter_cfg2.md')

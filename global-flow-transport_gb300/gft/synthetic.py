@@ -92,3 +92,24 @@ def camera_params(cams):
 
 def model_matrix(gt):
     return gt.get_transform_matrix().transpose().astype(np.float32)[None]
+
+
+def hemisphere_cameras(n_random, samples, sizes=(64, 256), radius=2.5, fov=30.0, seed=0, fixed_size=256):
+    """One fixed camera (on the +z axis, ``fixed_size`` square) plus
+    ``n_random`` cameras at seeded uniform directions on the upper hemisphere
+    with square resolutions drawn uniformly from ``sizes``; all look at the
+    origin.  Returns (cameras, [(samples, h, w)] per camera)."""
+    rng = np.random.default_rng(seed)
+    near, far = radius - 1.2, radius + 1.2
+    cams, shapes = [], []
+    dirs = [(0.0, 0.0)]
+    for _ in range(n_random):
+        u = rng.random()
+        dirs.append((float(np.degrees(np.arcsin(u))), float(rng.uniform(-180.0, 180.0))))  # elevation, azimuth
+    for k, (elev, azim) in enumerate(dirs):
+        s = fixed_size if k == 0 else int(rng.integers(sizes[0], sizes[1] + 1))
+        t = GridTransform([samples, s, s], translation=[0, 0, radius],
+                          parent=Transform(rotation_deg=[-elev, azim, 0]))
+        cams.append(Camera(t, nearFar=[near, far], fov=fov, aspect=1.0))
+        shapes.append((samples, s, s))
+    return cams, shapes
