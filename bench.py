@@ -275,6 +275,7 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     # ---- per-kernel timing of the dominant ops (roofline) -------------------
     out.update(kernel_roofline(step, dev, timed))
     out['uneven_views'] = uneven_views(dev, timed)
+    out['transport_chain'] = transport_chain(step, dev, timed)
 
     # ---- CPU baseline ------------------------------------------------------------
     if not args.no_cpu:
@@ -284,6 +285,59 @@ def extras(args, step, dev, timed, storage, inputs, ms):
         except Exception as e:  # the baseline is reported, not required
             out['cpu_baseline'] = {'error': repr(e)}
     return out
+
+
+def transport_chain(step, dev, timed, frames=16, every=4):
+    """The global-transport chain on the step's workload: an initial density
+    and 15 seeded staggered velocity fields, MacCormack advection through 16
+    frames, every frame rendered by the 5 views and compared with its target,
+    gradients to the initial density and all velocities, the adjoint
+    recomputing each 4-frame segment from its stored first density
+    (gft.chain.TransportChain).  One CUDA graph per iteration when capture
+    succeeds, else eager."""
+    import numpy as np
+    import torch
+    from gft import synthetic as syn
+    from gft.chain import TransportChain
+    shape = step.shape
+    d0 = torch.from_numpy(syn.plume_density(shape, 3000)).to(dev).requires_grad_(True)
+    vels = []
+    for t in range(frames - 1):
+        vx, vy, vz = syn.curl_velocity(shape, 3100 + t)
+        vels.append(tuple(torch.from_numpy(v).to(dev).requires_grad_(True) for v in (vx, vy, vz)))
+    with torch.no_grad():
+        targets = [step.render(torch.from_numpy(syn.plume_density(shape, 3200 + t, t)).to(dev))[..., :3].contiguous()
+                   for t in range(frames)]
+    chain = TransportChain(step, frames=frames, checkpoint_every=every)
+    params = [d0] + [v for tr in vels for v in tr]
+
+    def it():
+        loss = chain.loss(d0, vels, targets)
+        return loss, torch.autograd.grad(loss, params)
+
+    graph, why = None, None
+    try:
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                it()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            out = it()
+        run = graph.replay
+    except Exception as e:
+        graph, why = None, repr(e)[:200]
+        torch.cuda.synchronize(dev)
+        run = it
+    run()
+    ms = float(np.median(timed(run, 5, flush_l2=False)))
+    return {'workload': '%d frames, density %s, 5 views, MacCormack chain, fwd+bwd to the initial density and all '
+                        'velocities, checkpoint every %d frames' % (frames, 'x'.join(map(str, shape)), every),
+            'ms_per_iteration': ms, 'iters_per_s': 1000.0 / ms, 'cuda_graph': graph is not None,
+            'frames_per_s': frames * 1000.0 / ms, **({'capture_error': why} if why else {})}
 
 
 def uneven_views(dev, timed):

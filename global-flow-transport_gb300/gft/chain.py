@@ -11,6 +11,7 @@ O(T/k + k) grids instead of O(T).
 import torch
 from torch.utils.checkpoint import checkpoint
 
+from . import fused, ops
 from .pipeline import RenderAdvectStep
 
 
@@ -27,8 +28,11 @@ class TransportChain:
         loss = d.new_zeros(())
         for t in range(t0, t1):
             img = s.render(d)
-            rgb = img[..., :3] + s.bkg * torch.exp(-img[..., 3:])
-            loss = loss + torch.mean((rgb - targets[t]) ** 2)
+            if s.mode == 'plain':
+                rgb = img[..., :3] + s.bkg * torch.exp(-img[..., 3:])
+                loss = loss + torch.mean((rgb - targets[t]) ** 2)
+            else:
+                loss = loss + fused.image_loss(img, targets[t], s.bkg_host)
             if t + 1 < self.T:
                 vx, vy, vz = vels[t]
                 d = s.advect(d, vx, vy, vz)
@@ -40,8 +44,18 @@ class TransportChain:
         for t0 in range(0, self.T, self.k):
             t1 = min(self.T, t0 + self.k)
             if use_checkpoints:
-                d, l = checkpoint(self._segment, d, vels, targets, t0, t1, use_reentrant=False)
+                d, l = checkpoint(self._checkpointed, d, vels, targets, t0, t1, use_reentrant=False,
+                                  preserve_rng_state=False)  # no randomness; capturable
             else:
                 d, l = self._segment(d, vels, targets, t0, t1)
             total = total + l
         return total
+
+    def _checkpointed(self, d, vels, targets, t0, t1):
+        # A checkpointed segment's backward runs on the nodes of its first
+        # forward and only regenerates their saved tensors by running the
+        # segment again; the contexts of that second run are dropped.  So
+        # neither run may start a raymarch gradient's weight pass ahead on a
+        # side stream: the passes run in the backward.
+        with ops.side_stream_weights(False):
+            return self._segment(d, vels, targets, t0, t1)

@@ -22,7 +22,7 @@ COORD = {'TRANSFORM_LINDEPTH': 0, 'TRANSFORM_LINDEPTH_REVERSE': 1, 'TRANSFORM': 
 GRAD = {'REFERENCE': 0, 'EXACT': 1}
 CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
 
-_state = {'grad_mode': 'REFERENCE'}
+_state = {'grad_mode': 'REFERENCE', 'side_weights': True}
 
 
 def set_grad_mode(mode):
@@ -36,6 +36,23 @@ def set_grad_mode(mode):
 
 def get_grad_mode():
     return _state['grad_mode']
+
+
+class side_stream_weights:
+    """Context manager: whether a differentiable raymarch forward starts its
+    gradient's weight pass on a side stream (default) or leaves it to the
+    backward.  Disable it where a forward's backward may never run, e.g. the
+    first forward of a checkpointed segment (which the backward recomputes)."""
+
+    def __init__(self, enabled):
+        self.enabled = bool(enabled)
+
+    def __enter__(self):
+        self.prev = _state['side_weights']
+        _state['side_weights'] = self.enabled
+
+    def __exit__(self, *a):
+        _state['side_weights'] = self.prev
 
 
 class grad_mode:
@@ -255,7 +272,8 @@ class _Raymarch(torch.autograd.Function):
     def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype):
         xs = _storage(x, storage_dtype)
         ctx.weights = None
-        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+        if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
+                and interp == FILTER['LINEAR']):
             key = _weights_key(xs.shape, M, V, P, F, out_shape, boundary, separate, xs.device)
             ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(tuple(xs.shape), xs.device, M, V, P,
                                                                                 F, out_shape, boundary, separate)
@@ -381,7 +399,8 @@ class _RaymarchMulti(torch.autograd.Function):
     def forward(ctx, x, M, V, P, F, shapes, interp, boundary, blend, storage_dtype):
         xs = _storage(x, storage_dtype)
         ctx.weights = None
-        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+        if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
+                and interp == FILTER['LINEAR']):
             cur = torch.cuda.current_stream(xs.device)
             side = _side_stream(xs.device)
             side.wait_stream(cur)
