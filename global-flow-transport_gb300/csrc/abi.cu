@@ -254,9 +254,9 @@ size_t gft_raymarch_grid_transform_grad_workspace_size(const int64_t input_shape
                                                        int32_t separate_camera_batch, int32_t grad_mode) {
     std::string why;
     if (!grid_shape_ok(input_shape, why) || (grad_mode & ~GFT_GRAD_WEIGHTS_READY) == GFT_GRAD_EXACT) return 0;
-    const size_t nvox = (size_t)input_shape[1] * input_shape[2] * input_shape[3];
+    const size_t cells = (size_t)brick_cells(dims_of(input_shape));
     const size_t pairs = (size_t)input_shape[0] * (separate_camera_batch ? (size_t)std::max(num_cameras, 1) : 1);
-    return align256(sizeof(float) * nvox * pairs);
+    return align256(sizeof(float) * cells * pairs);
 }
 
 gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dtype, const int64_t input_shape[5],

@@ -36,6 +36,18 @@ __device__ __forceinline__ void unflat32(uint32_t v, Dims d, int& x, int& y, int
     y = (int)(q - zz * (uint32_t)d.y);
     z = (int)zz;
 }
+// Brick layout of the per-camera weight sums of the reference-normalised
+// raymarch gradient: 2x2x2 voxels per 32-byte sector, bricks in x, y, z order.
+// A warp's reduction to one corner of 32 neighbouring rays' samples then
+// touches about half as many sectors as with rows of voxels.
+__host__ __device__ inline int64_t brick_cells(Dims d) {
+    return (int64_t)((d.x + 1) / 2) * ((d.y + 1) / 2) * ((d.z + 1) / 2) * 8;
+}
+__device__ __forceinline__ int64_t brick_index(int x, int y, int z, Dims d) {
+    const int64_t b = ((int64_t)(z >> 1) * ((d.y + 1) / 2) + (y >> 1)) * ((d.x + 1) / 2) + (x >> 1);
+    return b * 8 + ((z & 1) << 2 | (y & 1) << 1 | (x & 1));
+}
+
 // Grid slices up to this many cells run as one launch dimension.
 constexpr int64_t MAX_SLICE_CELLS = int64_t(1) << 32;
 

@@ -187,12 +187,14 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
         const bool ok = (sx ? c.vx1 : c.vx0) && (sy ? c.vy1 : c.vy0) && (sz ? c.vz1 : c.vz0);
         if (BM != BM_BORDER || ok) {
             const float w = (sx ? cw[0] : 1.f - cw[0]) * (sy ? cw[1] : 1.f - cw[1]) * (sz ? cw[2] : 1.f - cw[2]);
-            const int64_t f = flat3(sx ? c.x1 : c.x0, sy ? c.y1 : c.y0, sz ? c.z1 : c.z0, d);
+            const int x = sx ? c.x1 : c.x0, y = sy ? c.y1 : c.y0, z = sz ? c.z1 : c.z0;
             if constexpr (MODE == 1) {
-                const float inv = __ldg(cnt + f);
-                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, f, vscale(vscale(val, w), inv));
+                const float inv = __ldg(cnt + brick_index(x, y, z, d));
+                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, flat3(x, y, z, d), vscale(vscale(val, w), inv));
+            } else if constexpr (MODE == 2) {
+                atomic_add<C>(grad, brick_index(x, y, z, d), vscale(val, w));
             } else {
-                atomic_add<C>(grad, f, vscale(val, w));
+                atomic_add<C>(grad, flat3(x, y, z, d), vscale(val, w));
             }
         }
     }
@@ -201,8 +203,8 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
 // Back to front from the far end point over the (clipped) samples of one ray.
 // MODE 2, the reference normalisation's first pass: per (batch, camera) pair
 // the per-voxel sum of the trilinear weights of all its samples (the float
-// sampleCounter of raymarch_grid.cu.cc:446-456); geometry only, C == 1, no
-// gathers.  MODE 0 / 1, the adjoint: re-sample (LINEAR only, as the reference
+// sampleCounter of raymarch_grid.cu.cc:446-456) in the brick layout
+// (brick_index); geometry only, C == 1, no gathers.  MODE 0 / 1, the adjoint: re-sample (LINEAR only, as the reference
 // gradient op), step the blend adjoint and scatter the cell gradient into the
 // batch gradient; MODE 1 normalises by the pass-1 sums, which equals the
 // reference's per-camera normalise-then-sum (kNormalize3DGradients,
@@ -226,8 +228,9 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     float3 pos, step;
     ray_far_step(tab.cam[p], x, y, W, H, D, pos, step);
     const S* g = in + (size_t)tab.in_batch[p] * nvox * C;
-    float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * nvox : grad + (size_t)tab.in_batch[p] * nvox * C;
-    const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * nvox : nullptr;
+    float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * brick_cells(din)
+                           : grad + (size_t)tab.in_batch[p] * nvox * C;
+    const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * brick_cells(din) : nullptr;
     Vec<C> acc = vzero<C>(), go = vzero<C>();
     if constexpr (MODE != 2) {
         const int64_t pix = tab.pix0[p] + (int64_t)y * W + x;
@@ -333,8 +336,8 @@ __global__ void k_invert_weights(float* __restrict__ w, int64_t n) {
 }
 
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
-    const int64_t nvox = voxels(a.din);
-    if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * nvox * pairs.size(), s), "zero weights")) return false;
+    const int64_t cells = brick_cells(a.din);
+    if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * cells * pairs.size(), s), "zero weights")) return false;
     const dim3 block(RM_BX, RM_BY, 1);
     for (PairTable& t : make_tables(pairs)) {
         const dim3 grid(set_ray_tiles(t));
@@ -345,7 +348,7 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
         }
         if (!launched(1, "raymarch weight launch")) return false;
     }
-    const int64_t n = nvox * (int64_t)pairs.size();
+    const int64_t n = cells * (int64_t)pairs.size();
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

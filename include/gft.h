@@ -106,9 +106,10 @@ gft_status gft_raymarch_grid_transform_grad(
  * per (batch, camera) pair the reciprocals of the per-voxel sums of the
  * trilinear weights of all ray samples (the reference's float sampleCounter,
  * raymarch_grid.cu.cc:446-456; 0 where no sample reaches a voxel), written
- * into the workspace of gft_raymarch_grid_transform_grad.  It needs
- * neither the forward output nor its gradient, so a caller can run it on
- * another stream while the forward pass is still running; the gradient call
+ * into the workspace of gft_raymarch_grid_transform_grad in an internal
+ * layout (2x2x2-voxel bricks).  It needs neither the forward output nor its
+ * gradient, so a caller can run it on another stream while the forward pass
+ * is still running; the gradient call
  * then takes grad_mode GFT_GRAD_REFERENCE | GFT_GRAD_WEIGHTS_READY, the same
  * geometry and workspace, and skips the pass.  No counterpart in the
  * reference, whose gradient kernel accumulates the sums itself. */
