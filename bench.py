@@ -417,21 +417,23 @@ def kernel_roofline(step, dev, timed):
     with torch.no_grad():
         d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
         light = d * (step.shadow(d) * step.falloff_col + step.ambient)
-        data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
+        # the raymarch input in the brick layout the step uses
+        data = ops.to_bricks((torch.cat([light, d], dim=-1) * step.depth_step).contiguous())
+    grid = step.shape
     D, H, W = step.res
     V = len(step.cams)
     mode = ops.get_grad_mode()
-    fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True)
+    fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid)
     y = fwd()
     torch.manual_seed(0)
     dy = torch.randn_like(y) * 1e-3
     bwd = lambda m: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                      ops.GRAD[m])
-    weights = lambda: ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P, step.F,
-                                            step.res, 0, True)
+                                      ops.GRAD[m], grid=grid)
+    shape5 = (data.shape[0],) + tuple(grid) + (data.shape[-1],)
+    weights = lambda: ops._raymarch_weights(shape5, data.device, step.M, step.V, step.P, step.F, step.res, 0, True)
     ws = weights()
     scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                        ops.GRAD['REFERENCE'], weights=ws)
+                                        ops.GRAD['REFERENCE'], weights=ws, grid=grid)
     for _ in range(2):
         fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter()
     tf = float(np.median(timed(fwd, 7)))
@@ -488,27 +490,30 @@ def kernel_only(args):
     with torch.no_grad():
         d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
         light = d * (step.shadow(d) * step.falloff_col + step.ambient)
-        data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
-        y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True)
+        data = ops.to_bricks((torch.cat([light, d], dim=-1) * step.depth_step).contiguous())
+        grid = step.shape
+        y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid)
         dy = torch.randn_like(y) * 1e-3
     gm = ops.GRAD[ops.get_grad_mode()]
     fns = {
-        'raymarch_fwd': lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True),
+        'raymarch_fwd': lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                                  grid=grid),
         'raymarch_bwd': lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0,
-                                                  True, gm),
+                                                  True, gm, grid=grid),
         'advect_fwd': lambda: ops._advect_fwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
                                               step.s_vz.detach(), 1.0, 2, 1, 1),
         'advect_bwd': lambda: ops._advect_bwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
                                               step.s_vz.detach(), torch.ones_like(d), 1.0, 2, 1, 1, gm),
         'shadow_fwd': lambda: step.shadow(d),
-        'raymarch_weights': lambda: ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P,
-                                                          step.F, step.res, 0, True),
+        'raymarch_weights': lambda: ops._raymarch_weights((1,) + tuple(grid) + (4,), data.device, step.M, step.V,
+                                                          step.P, step.F, step.res, 0, True),
     }
     if args.kernel_only == 'raymarch_scatter':
-        ws = ops._raymarch_weights(tuple(data.shape), data.device, step.M, step.V, step.P, step.F, step.res, 0,
-                                   True)
+        ws = ops._raymarch_weights((1,) + tuple(grid) + (4,), data.device, step.M, step.V, step.P, step.F, step.res,
+                                   0, True)
         fns['raymarch_scatter'] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
-                                                            0, 0, True, ops.GRAD['REFERENCE'], weights=ws)
+                                                            0, 0, True, ops.GRAD['REFERENCE'], weights=ws,
+                                                            grid=grid)
     fn = fns[args.kernel_only]
     for _ in range(args.repeat):
         fn()

@@ -225,7 +225,11 @@ gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, c
     if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
     if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
+    const int layout = (input_dtype & GFT_LAYOUT_BRICK) ? LAYOUT_BRICK : LAYOUT_FLAT;
+    input_dtype &= ~GFT_LAYOUT_BRICK;
     if (!enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid input dtype");
+    if (layout == LAYOUT_BRICK && interpolation != GFT_FILTER_LINEAR)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "the brick layout supports LINEAR interpolation only");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
@@ -233,6 +237,7 @@ gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, c
     RaymarchArgs a;
     a.input = input;
     a.dtype = input_dtype;
+    a.layout = layout;
     a.N = (int)input_shape[0];
     a.C = (int)input_shape[4];
     a.din = dims_of(input_shape);
@@ -278,6 +283,8 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
     const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
     grad_mode &= ~GFT_GRAD_WEIGHTS_READY;
+    const int layout = (input_dtype & GFT_LAYOUT_BRICK) ? LAYOUT_BRICK : LAYOUT_FLAT;
+    input_dtype &= ~GFT_LAYOUT_BRICK;
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
@@ -292,6 +299,7 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
     RaymarchArgs a;
     a.input = input;
     a.dtype = input_dtype;
+    a.layout = layout;
     a.N = (int)input_shape[0];
     a.C = (int)input_shape[4];
     a.din = dims_of(input_shape);
@@ -883,28 +891,36 @@ gft_status gft_transmittance_grad(const float* output, const float* output_grad,
     return GFT_OK;
 }
 
+static bool layout_ok(int32_t layout) { return layout == 0 || layout == GFT_LAYOUT_BRICK; }
+
 gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
-                             const int64_t shape[5], float ambient, float scale, float* output, void* stream) {
+                             const int64_t shape[5], float ambient, float scale, int32_t output_layout, float* output,
+                             void* stream) {
     std::string why;
     if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!layout_ok(output_layout)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid layout");
+    if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
     if (!density || !transmittance || !light_color || !output)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
-    if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], voxels(dims_of(shape)), ambient,
-                              scale, output, as_stream(stream)))
+    if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], dims_of(shape), ambient, scale,
+                              output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, output, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }
 
 gft_status gft_light_compose_grad(const float* density, const float* transmittance, const float* light_color,
-                                  const int64_t shape[5], float ambient, float scale, const float* output_grad,
-                                  float* density_grad, float* transmittance_grad, void* stream) {
+                                  const int64_t shape[5], float ambient, float scale, int32_t output_layout,
+                                  const float* output_grad, float* density_grad, float* transmittance_grad,
+                                  void* stream) {
     std::string why;
     if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!layout_ok(output_layout)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid layout");
+    if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
     if (!density || !transmittance || !light_color || !output_grad || !density_grad || !transmittance_grad)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
-    if (!launch_light_compose_grad(density, transmittance, light_color, output_grad, (int)shape[0],
-                                   voxels(dims_of(shape)), ambient, scale, density_grad, transmittance_grad,
-                                   as_stream(stream)))
+    if (!launch_light_compose_grad(density, transmittance, light_color, output_grad, (int)shape[0], dims_of(shape),
+                                   ambient, scale, output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, density_grad,
+                                   transmittance_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }

@@ -102,13 +102,16 @@ bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, f
 }
 
 // --- light compose ---------------------------------------------------------------
-// density, tr [N, V] (V voxels per batch slice), color [V, 3] shared by all
-// slices, out [N, V, 4].
+// density, tr [N, V] (V voxels per batch slice, rows), color [V, 3] shared by
+// all slices; out [N, cells, 4] in layout L (rows, or the raymarch's bricks).
+// One batch slice per blockIdx.y.
+template <int L>
 __global__ void __launch_bounds__(CP_THREADS)
     k_light_compose(const float* __restrict__ dens, const float* __restrict__ tr, const float* __restrict__ color,
-                    int64_t nvox, int64_t n, float ambient, float scale, float* __restrict__ out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t v = i % nvox;
+                    Dims d, float ambient, float scale, float* __restrict__ out) {
+    const int64_t nvox = voxels(d), b = blockIdx.y;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b * nvox + v;
         const float dv = dens[i], t = tr[i];
         float r[3];
 #pragma unroll
@@ -116,20 +119,34 @@ __global__ void __launch_bounds__(CP_THREADS)
             const float lc = __fmul_rn(dv, __fadd_rn(__fmul_rn(t, color[v * 3 + c]), ambient));
             r[c] = __fmul_rn(lc, scale);
         }
-        reinterpret_cast<float4*>(out)[i] = make_float4(r[0], r[1], r[2], __fmul_rn(dv, scale));
+        int64_t o = i;
+        if constexpr (L == LAYOUT_BRICK) {
+            int x, y, z;
+            unflat32((uint32_t)v, d, x, y, z);
+            o = b * brick_cells(d) + brick_index(x, y, z, d);
+        }
+        reinterpret_cast<float4*>(out)[o] = make_float4(r[0], r[1], r[2], __fmul_rn(dv, scale));
     }
 }
 
 // g_d = g3 * s + sum_c (g_c * s) * (t * color_c + ambient);
-// g_t = sum_c (g_c * s) * d * color_c.
+// g_t = sum_c (g_c * s) * d * color_c.  g in layout L.
+template <int L>
 __global__ void __launch_bounds__(CP_THREADS)
     k_light_compose_grad(const float* __restrict__ dens, const float* __restrict__ tr,
-                         const float* __restrict__ color, const float* __restrict__ g, int64_t nvox, int64_t n,
-                         float ambient, float scale, float* __restrict__ gd, float* __restrict__ gt) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t v = i % nvox;
+                         const float* __restrict__ color, const float* __restrict__ g, Dims d, float ambient,
+                         float scale, float* __restrict__ gd, float* __restrict__ gt) {
+    const int64_t nvox = voxels(d), b = blockIdx.y;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b * nvox + v;
+        int64_t o = i;
+        if constexpr (L == LAYOUT_BRICK) {
+            int x, y, z;
+            unflat32((uint32_t)v, d, x, y, z);
+            o = b * brick_cells(d) + brick_index(x, y, z, d);
+        }
         const float dv = dens[i], t = tr[i];
-        const float4 gi = reinterpret_cast<const float4*>(g)[i];
+        const float4 gi = reinterpret_cast<const float4*>(g)[o];
         const float gl[3] = {__fmul_rn(gi.x, scale), __fmul_rn(gi.y, scale), __fmul_rn(gi.z, scale)};
         float sd = 0.f, st = 0.f;
 #pragma unroll
@@ -143,18 +160,23 @@ __global__ void __launch_bounds__(CP_THREADS)
     }
 }
 
-bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, int64_t nvox, float ambient,
-                          float scale, float* out, cudaStream_t st) {
-    const int64_t n = nvox * N;
-    k_light_compose<<<grid_for(n, CP_THREADS), CP_THREADS, 0, st>>>(dens, tr, color, nvox, n, ambient, scale, out);
+bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
+                          float scale, int layout, float* out, cudaStream_t st) {
+    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
+    if (layout == LAYOUT_BRICK)
+        k_light_compose<LAYOUT_BRICK><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, out);
+    else
+        k_light_compose<LAYOUT_FLAT><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, out);
     return launched(1, "light compose launch");
 }
 
-bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N,
-                               int64_t nvox, float ambient, float scale, float* gd, float* gt, cudaStream_t st) {
-    const int64_t n = nvox * N;
-    k_light_compose_grad<<<grid_for(n, CP_THREADS), CP_THREADS, 0, st>>>(dens, tr, color, g, nvox, n, ambient,
-                                                                          scale, gd, gt);
+bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
+                               float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st) {
+    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
+    if (layout == LAYOUT_BRICK)
+        k_light_compose_grad<LAYOUT_BRICK><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, g, d, ambient, scale, gd, gt);
+    else
+        k_light_compose_grad<LAYOUT_FLAT><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, g, d, ambient, scale, gd, gt);
     return launched(1, "light compose gradient launch");
 }
 

@@ -48,6 +48,20 @@ __device__ __forceinline__ int64_t brick_index(int x, int y, int z, Dims d) {
     return b * 8 + ((z & 1) << 2 | (y & 1) << 1 | (x & 1));
 }
 
+// Cell layouts of a grid slice: rows (NDHWC) or 2x2x2-voxel bricks
+// (brick_index; one 128-byte line per brick for C == 4 fp32).
+constexpr int LAYOUT_FLAT = 0, LAYOUT_BRICK = 1;
+template <int L>
+__device__ __forceinline__ int64_t cell_index(int x, int y, int z, Dims d) {
+    if constexpr (L == LAYOUT_BRICK) return brick_index(x, y, z, d);
+    return flat3(x, y, z, d);
+}
+template <int L>
+__host__ __device__ inline int64_t slice_cells(Dims d) {
+    if constexpr (L == LAYOUT_BRICK) return brick_cells(d);
+    return voxels(d);
+}
+
 // Grid slices up to this many cells run as one launch dimension.
 constexpr int64_t MAX_SLICE_CELLS = int64_t(1) << 32;
 
@@ -237,16 +251,17 @@ __device__ __forceinline__ bool border_inside(float px, float py, float pz, Dims
     return ax >= 0.f && ax < (float)d.x && ay >= 0.f && ay < (float)d.y && az >= 0.f && az < (float)d.z;
 }
 
-template <int C, typename S, int BM>
+template <int C, typename S, int BM, int L = LAYOUT_FLAT>
 __device__ __forceinline__ Vec<C> read_corner(const S* g, Dims d, int x, int y, int z, bool ok) {
     if constexpr (BM == BM_BORDER) {
         if (!ok) return vzero<C>();
     }
-    return Load<C, S>::at(g, flat3(x, y, z, d));
+    return Load<C, S>::at(g, cell_index<L>(x, y, z, d));
 }
 
-// Trilinear fetch (read3DInterpolated): p has cell centres at integers.
-template <int C, typename S, int BM>
+// Trilinear fetch (read3DInterpolated): p has cell centres at integers; L is
+// the cell layout of g.
+template <int C, typename S, int BM, int L = LAYOUT_FLAT>
 __device__ __forceinline__ Vec<C> fetch_linear(const S* __restrict__ g, Dims d, float px, float py, float pz) {
     if constexpr (BM == BM_BORDER) {
         if (!border_inside(px, py, pz, d)) return vzero<C>();
@@ -262,26 +277,53 @@ __device__ __forceinline__ Vec<C> fetch_linear(const S* __restrict__ g, Dims d, 
         if ((unsigned)x0 < (unsigned)(d.x - 1) && (unsigned)y0 < (unsigned)(d.y - 1) &&
             (unsigned)z0 < (unsigned)(d.z - 1)) {
             const float wx = px - fx, wy = py - fy, wz = pz - fz;
-            const int64_t sy = d.x, sz = (int64_t)d.x * d.y;
-            const int64_t b = ((int64_t)z0 * d.y + y0) * d.x + x0;
-            const Vec<C> fff = Load<C, S>::at(g, b), cff = Load<C, S>::at(g, b + 1);
-            const Vec<C> fcf = Load<C, S>::at(g, b + sy), ccf = Load<C, S>::at(g, b + sy + 1);
-            const Vec<C> ffc = Load<C, S>::at(g, b + sz), cfc = Load<C, S>::at(g, b + sz + 1);
-            const Vec<C> fcc = Load<C, S>::at(g, b + sz + sy), ccc = Load<C, S>::at(g, b + sz + sy + 1);
+            int64_t i000, i100, i010, i110, i001, i101, i011, i111;
+            if constexpr (L == LAYOUT_BRICK) {
+                // brick index = x term + y term + z term (brick_index)
+                const int64_t bx = (d.x + 1) / 2, bxy = bx * ((d.y + 1) / 2);
+                const int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+                const int64_t tx0 = (int64_t)(x0 >> 1) * 8 + (x0 & 1), tx1 = (int64_t)(x1 >> 1) * 8 + (x1 & 1);
+                const int64_t ty0 = (int64_t)(y0 >> 1) * bx * 8 + ((y0 & 1) << 1);
+                const int64_t ty1 = (int64_t)(y1 >> 1) * bx * 8 + ((y1 & 1) << 1);
+                const int64_t tz0 = (int64_t)(z0 >> 1) * bxy * 8 + ((z0 & 1) << 2);
+                const int64_t tz1 = (int64_t)(z1 >> 1) * bxy * 8 + ((z1 & 1) << 2);
+                i000 = tz0 + ty0 + tx0;
+                i100 = tz0 + ty0 + tx1;
+                i010 = tz0 + ty1 + tx0;
+                i110 = tz0 + ty1 + tx1;
+                i001 = tz1 + ty0 + tx0;
+                i101 = tz1 + ty0 + tx1;
+                i011 = tz1 + ty1 + tx0;
+                i111 = tz1 + ty1 + tx1;
+            } else {
+                const int64_t sy = d.x, sz = (int64_t)d.x * d.y;
+                i000 = ((int64_t)z0 * d.y + y0) * d.x + x0;
+                i100 = i000 + 1;
+                i010 = i000 + sy;
+                i110 = i000 + sy + 1;
+                i001 = i000 + sz;
+                i101 = i000 + sz + 1;
+                i011 = i000 + sz + sy;
+                i111 = i000 + sz + sy + 1;
+            }
+            const Vec<C> fff = Load<C, S>::at(g, i000), cff = Load<C, S>::at(g, i100);
+            const Vec<C> fcf = Load<C, S>::at(g, i010), ccf = Load<C, S>::at(g, i110);
+            const Vec<C> ffc = Load<C, S>::at(g, i001), cfc = Load<C, S>::at(g, i101);
+            const Vec<C> fcc = Load<C, S>::at(g, i011), ccc = Load<C, S>::at(g, i111);
             const Vec<C> v0 = vlerp(vlerp(fff, cff, wx), vlerp(fcf, ccf, wx), wy);
             const Vec<C> v1 = vlerp(vlerp(ffc, cfc, wx), vlerp(fcc, ccc, wx), wy);
             return vlerp(v0, v1, wz);
         }
     }
     const Corners c = corners<BM>(px, py, pz, d);
-    const Vec<C> fff = read_corner<C, S, BM>(g, d, c.x0, c.y0, c.z0, c.vx0 && c.vy0 && c.vz0);
-    const Vec<C> cff = read_corner<C, S, BM>(g, d, c.x1, c.y0, c.z0, c.vx1 && c.vy0 && c.vz0);
-    const Vec<C> fcf = read_corner<C, S, BM>(g, d, c.x0, c.y1, c.z0, c.vx0 && c.vy1 && c.vz0);
-    const Vec<C> ccf = read_corner<C, S, BM>(g, d, c.x1, c.y1, c.z0, c.vx1 && c.vy1 && c.vz0);
-    const Vec<C> ffc = read_corner<C, S, BM>(g, d, c.x0, c.y0, c.z1, c.vx0 && c.vy0 && c.vz1);
-    const Vec<C> cfc = read_corner<C, S, BM>(g, d, c.x1, c.y0, c.z1, c.vx1 && c.vy0 && c.vz1);
-    const Vec<C> fcc = read_corner<C, S, BM>(g, d, c.x0, c.y1, c.z1, c.vx0 && c.vy1 && c.vz1);
-    const Vec<C> ccc = read_corner<C, S, BM>(g, d, c.x1, c.y1, c.z1, c.vx1 && c.vy1 && c.vz1);
+    const Vec<C> fff = read_corner<C, S, BM, L>(g, d, c.x0, c.y0, c.z0, c.vx0 && c.vy0 && c.vz0);
+    const Vec<C> cff = read_corner<C, S, BM, L>(g, d, c.x1, c.y0, c.z0, c.vx1 && c.vy0 && c.vz0);
+    const Vec<C> fcf = read_corner<C, S, BM, L>(g, d, c.x0, c.y1, c.z0, c.vx0 && c.vy1 && c.vz0);
+    const Vec<C> ccf = read_corner<C, S, BM, L>(g, d, c.x1, c.y1, c.z0, c.vx1 && c.vy1 && c.vz0);
+    const Vec<C> ffc = read_corner<C, S, BM, L>(g, d, c.x0, c.y0, c.z1, c.vx0 && c.vy0 && c.vz1);
+    const Vec<C> cfc = read_corner<C, S, BM, L>(g, d, c.x1, c.y0, c.z1, c.vx1 && c.vy0 && c.vz1);
+    const Vec<C> fcc = read_corner<C, S, BM, L>(g, d, c.x0, c.y1, c.z1, c.vx0 && c.vy1 && c.vz1);
+    const Vec<C> ccc = read_corner<C, S, BM, L>(g, d, c.x1, c.y1, c.z1, c.vx1 && c.vy1 && c.vz1);
     const Vec<C> v0 = vlerp(vlerp(fff, cff, c.wx), vlerp(fcf, ccf, c.wx), c.wy);
     const Vec<C> v1 = vlerp(vlerp(ffc, cfc, c.wx), vlerp(fcc, ccc, c.wx), c.wy);
     return vlerp(v0, v1, c.wz);

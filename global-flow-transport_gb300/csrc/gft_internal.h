@@ -72,6 +72,7 @@ struct RaymarchArgs {
     Dims din;
     int D, H, W;
     int filter, boundary, blend;
+    int layout = LAYOUT_FLAT;  // cell layout of the input and its gradient
     int n_slots;  // output slots = N * (separate ? V : 1)
 };
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
@@ -136,10 +137,10 @@ bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* 
 // pipeline fusions (compose.cu)
 bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st);
 bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st);
-bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, int64_t nvox, float ambient,
-                          float scale, float* out, cudaStream_t st);
-bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N,
-                               int64_t nvox, float ambient, float scale, float* gd, float* gt, cudaStream_t st);
+bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
+                          float scale, int layout, float* out, cudaStream_t st);
+bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
+                               float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st);
 int image_loss_blocks(int64_t npix);
 bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], float* partial,
                        float* loss, cudaStream_t st);

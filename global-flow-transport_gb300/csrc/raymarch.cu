@@ -78,7 +78,7 @@ static unsigned set_ray_tiles(PairTable& t) {
     return (unsigned)b;
 }
 
-template <int C, typename S, int BM, bool LIN>
+template <int C, typename S, int BM, bool LIN, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_fwd(const S* __restrict__ in, Dims din, int filter, int blend_mode, float* __restrict__ out,
                    const __grid_constant__ PairTable tab) {
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     if (!ray_pixel(tab, r)) return;
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     const CamX& cam = tab.cam[p];
-    const S* g = in + (size_t)tab.in_batch[p] * voxels(din) * C;
+    const S* g = in + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     const float3 dinv = make_float3(1.f / (float)W, 1.f / (float)H, 1.f / (float)D);
     const float zmax = (float)max(D - 1, 1);
     const float3 nearp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, 0.5f), dinv);
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     for (int i = i0; i <= i1; ++i) {
         Vec<C> smp;
         if constexpr (LIN) {
-            smp = fetch_linear<C, S, BM>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
+            smp = fetch_linear<C, S, BM, L>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
         } else {
             smp = fetch<C, S, BM, true>(filter, g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
         }
@@ -168,7 +168,7 @@ __device__ __forceinline__ bool clip_back_to_front(float3& pos, float3 step, int
 // reciprocal of the camera's weight sum there (the per-camera
 // normalise-then-sum applied per contribution, so all cameras accumulate into
 // one gradient) and skips corners with w == 0 or no weight.
-template <int C, int BM, int MODE>
+template <int C, int BM, int MODE, int L>
 __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
                                                float px, float py, float pz, Vec<C> val) {
     if constexpr (BM == BM_BORDER) {
@@ -190,11 +190,11 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
             const int x = sx ? c.x1 : c.x0, y = sy ? c.y1 : c.y0, z = sz ? c.z1 : c.z0;
             if constexpr (MODE == 1) {
                 const float inv = __ldg(cnt + brick_index(x, y, z, d));
-                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, flat3(x, y, z, d), vscale(vscale(val, w), inv));
+                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(vscale(val, w), inv));
             } else if constexpr (MODE == 2) {
                 atomic_add<C>(grad, brick_index(x, y, z, d), vscale(val, w));
             } else {
-                atomic_add<C>(grad, flat3(x, y, z, d), vscale(val, w));
+                atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(val, w));
             }
         }
     }
@@ -216,7 +216,7 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
 // forward output; a negative one is first clamped by max(., 0), so such rays
 // march in full).  ALPHA changes its bookkeeping on every step and marches in
 // full.  (Non-finite adjoints are not propagated through skipped samples.)
-template <int C, typename S, int BM, int MODE>
+template <int C, typename S, int BM, int MODE, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
@@ -227,9 +227,9 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     const int64_t nvox = voxels(din);
     float3 pos, step;
     ray_far_step(tab.cam[p], x, y, W, H, D, pos, step);
-    const S* g = in + (size_t)tab.in_batch[p] * nvox * C;
+    const S* g = in + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * brick_cells(din)
-                           : grad + (size_t)tab.in_batch[p] * nvox * C;
+                           : grad + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * brick_cells(din) : nullptr;
     Vec<C> acc = vzero<C>(), go = vzero<C>();
     if constexpr (MODE != 2) {
@@ -251,10 +251,10 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         if constexpr (MODE == 2) {
             val = vfill<C>(1.f);
         } else {
-            const Vec<C> smp = fetch_linear<C, S, BM>(g, din, px, py, pz);
+            const Vec<C> smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
-        scatter_sample<C, BM, MODE>(dst, count, din, px, py, pz, val);
+        scatter_sample<C, BM, MODE, L>(dst, count, din, px, py, pz, val);
         pos.x -= step.x;
         pos.y -= step.y;
         pos.z -= step.z;
@@ -264,10 +264,16 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
 template <int C, typename S, int BM>
 static void fwd_dispatch_lin(bool lin, dim3 grid, dim3 block, cudaStream_t s, const void* in, const RaymarchArgs& a,
                              float* out, const PairTable& t) {
-    if (lin)
-        k_raymarch_fwd<C, S, BM, true><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend, out, t);
+    // the brick layout is produced for the LINEAR render path only
+    if (a.layout == LAYOUT_BRICK)
+        k_raymarch_fwd<C, S, BM, true, LAYOUT_BRICK><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
+                                                                           out, t);
+    else if (lin)
+        k_raymarch_fwd<C, S, BM, true, LAYOUT_FLAT><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
+                                                                          out, t);
     else
-        k_raymarch_fwd<C, S, BM, false><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend, out, t);
+        k_raymarch_fwd<C, S, BM, false, LAYOUT_FLAT><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
+                                                                           out, t);
 }
 
 template <int C, typename S>
@@ -299,15 +305,24 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
     return true;
 }
 
+template <int C, typename S, int BM, int L>
+static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
+                           const float* dout, float* grad, const float* cnt, const PairTable& t) {
+    if (exact)
+        k_raymarch_scatter<C, S, BM, 0, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
+                                                                     cnt, t);
+    else
+        k_raymarch_scatter<C, S, BM, 1, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
+                                                                     cnt, t);
+}
+
 template <int C, typename S, int BM>
 static void bwd_dispatch(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
                          const float* dout, float* grad, const float* cnt, const PairTable& t) {
-    if (exact)
-        k_raymarch_scatter<C, S, BM, 0><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                  cnt, t);
+    if (a.layout == LAYOUT_BRICK)
+        bwd_dispatch_l<C, S, BM, LAYOUT_BRICK>(exact, grid, block, s, a, out, dout, grad, cnt, t);
     else
-        k_raymarch_scatter<C, S, BM, 1><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                  cnt, t);
+        bwd_dispatch_l<C, S, BM, LAYOUT_FLAT>(exact, grid, block, s, a, out, dout, grad, cnt, t);
 }
 
 template <int C, typename S>
@@ -323,8 +338,8 @@ static void bwd_dispatch_bm(bool exact, dim3 grid, dim3 block, cudaStream_t s, c
 template <int BM>
 static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
                              const PairTable& t) {
-    k_raymarch_scatter<1, float, BM, 2><<<grid, block, 0, s>>>(nullptr, a.din, a.blend, nullptr, nullptr, cnt,
-                                                                  nullptr, t);
+    k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(nullptr, a.din, a.blend, nullptr, nullptr,
+                                                                               cnt, nullptr, t);
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel).
@@ -360,8 +375,8 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
                          const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s) {
-    const int64_t nvox = voxels(a.din);
-    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * nvox * a.C * a.N, s), "zero gradient")) return false;
+    const int64_t cells = a.layout == LAYOUT_BRICK ? brick_cells(a.din) : voxels(a.din);
+    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * cells * a.C * a.N, s), "zero gradient")) return false;
     if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
     const dim3 block(RM_BX, RM_BY, 1);
     for (PairTable& t : make_tables(pairs)) {

@@ -53,8 +53,8 @@ _SIGS = {
                                                         _P, _SZ, _P]),
     'gft_transmittance': (_I32, [_P, _I64P, _P, _P]),
     'gft_transmittance_grad': (_I32, [_P, _P, _I64P, _P, _P]),
-    'gft_light_compose': (_I32, [_P, _P, _P, _I64P, _F, _F, _P, _P]),
-    'gft_light_compose_grad': (_I32, [_P, _P, _P, _I64P, _F, _F, _P, _P, _P, _P]),
+    'gft_light_compose': (_I32, [_P, _P, _P, _I64P, _F, _F, _I32, _P, _P]),
+    'gft_light_compose_grad': (_I32, [_P, _P, _P, _I64P, _F, _F, _I32, _P, _P, _P, _P]),
     'gft_image_loss_workspace_size': (_SZ, [ctypes.c_int64]),
     'gft_image_loss': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _SZ, _P]),
     'gft_image_loss_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),

@@ -9,6 +9,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import ops
 from .ops import _cuda, _p, _stream, _workspace
 
 
@@ -49,34 +50,40 @@ def transmittance(x):
 
 class _LightCompose(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, d, tr, color, ambient, scale):
+    def forward(ctx, d, tr, color, ambient, scale, brick):
         lib = _lib.load()
-        out = torch.empty(tuple(d.shape[:4]) + (4,), dtype=torch.float32, device=d.device)
+        if brick:
+            out = torch.empty((d.shape[0], ops.brick_cells(d.shape[1:4]), 4), dtype=torch.float32, device=d.device)
+        else:
+            out = torch.empty(tuple(d.shape[:4]) + (4,), dtype=torch.float32, device=d.device)
+        layout = ops.LAYOUT_BRICK if brick else 0
         with torch.cuda.device(d.device):
             _lib.check(lib.gft_light_compose(_p(d), _p(tr), _p(color), _shape(d), float(ambient), float(scale),
-                                             _p(out), _stream(d.device)), 'LightCompose')
+                                             layout, _p(out), _stream(d.device)), 'LightCompose')
         ctx.save_for_backward(d, tr, color)
-        ctx.k = (float(ambient), float(scale))
+        ctx.k = (float(ambient), float(scale), layout)
         return out
 
     @staticmethod
     def backward(ctx, g):
         d, tr, color = ctx.saved_tensors
-        ambient, scale = ctx.k
+        ambient, scale, layout = ctx.k
         lib = _lib.load()
         g = g.contiguous()
         gd = torch.empty_like(d)
         gt = torch.empty_like(tr)
         with torch.cuda.device(d.device):
-            _lib.check(lib.gft_light_compose_grad(_p(d), _p(tr), _p(color), _shape(d), ambient, scale, _p(g),
-                                                  _p(gd), _p(gt), _stream(d.device)), 'LightComposeGrad')
-        return gd, gt, None, None, None
+            _lib.check(lib.gft_light_compose_grad(_p(d), _p(tr), _p(color), _shape(d), ambient, scale, layout,
+                                                  _p(g), _p(gd), _p(gt), _stream(d.device)), 'LightComposeGrad')
+        return gd, gt, None, None, None, None
 
 
-def light_compose(density, transmittance, light_color, ambient, scale):
+def light_compose(density, transmittance, light_color, ambient, scale, brick=False):
     """cat([density * (transmittance * light_color + ambient), density], -1) * scale
     for density, transmittance [N, D, H, W, 1] and light_color [D, H, W, 3] or
-    [1, D, H, W, 3] (constant: no gradient)."""
+    [1, D, H, W, 3] (constant: no gradient).  ``brick``: the result in the
+    raymarch's 2x2x2 brick layout, [N, brick_cells(D, H, W), 4], for
+    ops.raymarch_grid_transform_bricked."""
     d = _cuda(density, 'density')
     tr = _cuda(transmittance, 'transmittance')
     color = _cuda(light_color, 'light_color')
@@ -84,7 +91,7 @@ def light_compose(density, transmittance, light_color, ambient, scale):
         raise _lib.GftInvalidArgument('density and transmittance must both be [N, D, H, W, 1]')
     if color.numel() != int(np.prod(d.shape[1:4])) * 3 or color.shape[-1] != 3:
         raise _lib.GftInvalidArgument('light_color must be [D, H, W, 3]')
-    return _LightCompose.apply(d, tr, color.detach(), ambient, scale)
+    return _LightCompose.apply(d, tr, color.detach(), ambient, scale, bool(brick))
 
 
 class _ImageLoss(torch.autograd.Function):

@@ -143,7 +143,44 @@ def _storage(x, storage_dtype):
 
 
 # ------------------------------------------------------------------ raymarch
-def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate):
+LAYOUT_BRICK = 0x10  # GFT_LAYOUT_BRICK
+
+
+def brick_cells(dhw):
+    """Cells of one batch slice of a D x H x W grid in the raymarch's 2x2x2
+    brick layout (GFT_LAYOUT_BRICK)."""
+    D, H, W = (int(v) for v in dhw)
+    return ((D + 1) // 2) * ((H + 1) // 2) * ((W + 1) // 2) * 8
+
+
+def to_bricks(x):
+    """[N, D, H, W, C] rows -> [N, brick_cells((D, H, W)), C] 2x2x2 bricks (the
+    cells outside the grid are 0)."""
+    N, D, H, W, C = x.shape
+    xp = torch.nn.functional.pad(x, (0, 0, 0, W % 2, 0, H % 2, 0, D % 2))
+    Dp, Hp, Wp = xp.shape[1:4]
+    xb = xp.reshape(N, Dp // 2, 2, Hp // 2, 2, Wp // 2, 2, C).permute(0, 1, 3, 5, 2, 4, 6, 7)
+    return xb.reshape(N, -1, C).contiguous()
+
+
+def from_bricks(xb, grid_shape):
+    """Inverse of to_bricks for a grid of shape (D, H, W)."""
+    D, H, W = (int(v) for v in grid_shape)
+    N, C = xb.shape[0], xb.shape[-1]
+    Bz, By, Bx = (D + 1) // 2, (H + 1) // 2, (W + 1) // 2
+    x = xb.reshape(N, Bz, By, Bx, 2, 2, 2, C).permute(0, 1, 4, 2, 5, 3, 6, 7).reshape(N, 2 * Bz, 2 * By, 2 * Bx, C)
+    return x[:, :D, :H, :W].contiguous()
+
+
+def _grid5(x, grid):
+    """The logical [N, D, H, W, C] shape and the dtype code of a raymarch input:
+    NDHWC rows (grid None) or bricks of a D x H x W grid ([N, cells, C])."""
+    if grid is None:
+        return tuple(x.shape), _dtype_code(x)
+    return (x.shape[0],) + tuple(int(v) for v in grid) + (x.shape[-1],), _dtype_code(x) | LAYOUT_BRICK
+
+
+def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=None):
     lib = _lib.load()
     D, H, W = out_shape
     Mh, nm = _mats(M)
@@ -152,10 +189,11 @@ def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate):
     Fh, nf = _frustum(F)
     if not (nv == npj == nf):
         raise _lib.GftInvalidArgument('camera batch size mismatch')
-    N, C = x.shape[0], x.shape[4]
+    shape5, code = _grid5(x, grid)
+    N, C = shape5[0], shape5[4]
     out = torch.empty((N, nv if separate else 1, H, W, C), dtype=torch.float32, device=x.device)
     with torch.cuda.device(x.device):
-        st = lib.gft_raymarch_grid_transform(_p(x), _dtype_code(x), _lib.i64(x.shape), _p(Mh), nm, _p(Vh), _p(Ph),
+        st = lib.gft_raymarch_grid_transform(_p(x), code, _lib.i64(shape5), _p(Mh), nm, _p(Vh), _p(Ph),
                                              _p(Fh), nv, _lib.i32(out_shape), interp, boundary, blend, int(separate),
                                              _p(out), _stream(x.device))
     _lib.check(st, 'RaymarchGridTransform')
@@ -244,13 +282,15 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
                                                out_shape, b, bool(separate_camera_batch))
 
 
-def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None):
+def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None,
+                  grid=None):
     lib = _lib.load()
     Mh, nm = _mats(M)
     Vh, nv = _mats(V)
     Ph, _ = _mats(P)
     Fh, _ = _frustum(F)
-    shape = _lib.i64(x.shape)
+    shape5, code = _grid5(x, grid)
+    shape = _lib.i64(shape5)
     grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
     if weights is not None and gmode == GRAD['REFERENCE']:
         ws = weights
@@ -259,7 +299,7 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
         ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode),
                         x.device)
     with torch.cuda.device(x.device):
-        st = lib.gft_raymarch_grid_transform_grad(_p(x), _dtype_code(x), shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
+        st = lib.gft_raymarch_grid_transform_grad(_p(x), code, shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
                                                   _p(Ph), _p(Fh), nv, _lib.i32(out_shape), interp, boundary, blend,
                                                   int(separate), gmode, _p(grad), _p(ws), ws.numel(),
                                                   _stream(x.device))
@@ -269,32 +309,33 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
 
 class _Raymarch(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype):
+    def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype, grid=None):
         xs = _storage(x, storage_dtype)
+        shape5 = _grid5(xs, grid)[0]
         ctx.weights = None
         if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
                 and interp == FILTER['LINEAR']):
-            key = _weights_key(xs.shape, M, V, P, F, out_shape, boundary, separate, xs.device)
-            ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(tuple(xs.shape), xs.device, M, V, P,
-                                                                                F, out_shape, boundary, separate)
-        y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate)
+            key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
+            ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
+                                                                                out_shape, boundary, separate)
+        y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=grid)
         ctx.save_for_backward(xs, y)
-        ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate)
+        ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate, grid)
         ctx.in_dtype = x.dtype
         return y
 
     @staticmethod
     def backward(ctx, dy):
         xs, y = ctx.saved_tensors
-        M, V, P, F, out_shape, interp, boundary, blend, separate = ctx.args
+        M, V, P, F, out_shape, interp, boundary, blend, separate, grid = ctx.args
         ws = None
         if ctx.weights is not None:
             ws, ev = ctx.weights
             torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                          GRAD[get_grad_mode()], weights=ws)
+                          GRAD[get_grad_mode()], weights=ws, grid=grid)
         ctx.weights = None
-        return (g.to(ctx.in_dtype),) + (None,) * 10
+        return (g.to(ctx.in_dtype),) + (None,) * 11
 
 
 def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
@@ -309,6 +350,26 @@ def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params,
     y = _Raymarch.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, out_shape,
                         _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
                         _enum(BLEND, blending_mode, 'blending_mode'), bool(separate_camera_batch), storage_dtype)
+    return y.unsqueeze(2) if keep_dims else y
+
+
+def raymarch_grid_transform_bricked(input, grid_shape, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
+                                    boundary='BORDER', blending_mode='BEER_LAMBERT', keep_dims=False,
+                                    separate_camera_batch=True, storage_dtype=None):
+    """raymarch_grid_transform (LINEAR) of a grid of logical shape
+    [N, *grid_shape, C] stored in the 2x2x2 brick layout, input
+    [N, brick_cells(grid_shape), C] (e.g. gft.fused.light_compose(brick=True));
+    its gradient comes back in the same layout.  The bricks put the corner
+    gathers of a warp's neighbouring rays into fewer cache lines."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    grid = _shape3(grid_shape)
+    if x.dim() != 3 or x.shape[1] != brick_cells(grid) or x.shape[2] > 4:
+        raise _lib.GftInvalidArgument('bricked input must be [N, brick_cells(grid_shape), C], got %s'
+                                      % (tuple(x.shape),))
+    out_shape = _shape3(output_shape)
+    y = _Raymarch.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, out_shape, FILTER['LINEAR'],
+                        _enum(BOUNDARY, boundary, 'boundary'), _enum(BLEND, blending_mode, 'blending_mode'),
+                        bool(separate_camera_batch), storage_dtype, tuple(grid))
     return y.unsqueeze(2) if keep_dims else y
 
 

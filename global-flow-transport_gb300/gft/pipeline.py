@@ -125,14 +125,16 @@ class RenderAdvectStep:
             light = d * (self.shadow(d) * self.falloff_col + self.ambient)
             data = torch.cat([light, d], dim=-1) * self.depth_step
         else:
-            data = fused.light_compose(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step)
+            # the raymarch input in the brick layout (written directly by the light composition)
+            data = fused.light_compose(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step,
+                                       brick=True)
         if self.mode == 'plain':
             imgs = [ops.raymarch_grid_transform(data, self.M, self.V[i:i + 1], self.P[i:i + 1], self.F[i:i + 1],
                                                 self.res) for i in range(len(self.V))]
             img = torch.cat(imgs, dim=1)
         else:
-            img = ops.raymarch_grid_transform(data, self.M, self.V, self.P, self.F, self.res,
-                                              storage_dtype=self.storage_dtype)
+            img = ops.raymarch_grid_transform_bricked(data, self.shape, self.M, self.V, self.P, self.F, self.res,
+                                                      storage_dtype=self.storage_dtype)
         return img.squeeze(0)  # [V,H,W,4]
 
     def loss(self, d_prev, vx, vy, vz, target):

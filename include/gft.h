@@ -64,6 +64,16 @@ typedef enum {
 } gft_coord;
 /* Storage type of density-like inputs; all arithmetic is fp32. */
 typedef enum { GFT_DTYPE_F32 = 0, GFT_DTYPE_BF16 = 1 } gft_dtype;
+/* OR-ed into the input_dtype of gft_raymarch_grid_transform(_grad): the input
+ * grid, and the input gradient the adjoint writes, are stored per batch slice
+ * in 2x2x2-voxel bricks instead of NDHWC rows: voxel (x, y, z) of a D x H x W
+ * slice is cell ((z/2 * ceil(H/2) + y/2) * ceil(W/2) + x/2) * 8 +
+ * (z%2)*4 + (y%2)*2 + x%2 of ceil(D/2)*ceil(H/2)*ceil(W/2)*8 cells (each C
+ * values); cells outside the grid are never read.  A warp's corner gathers
+ * then touch fewer cache lines.  LINEAR interpolation only.  No counterpart in
+ * the reference (which reads NDHWC rows); gft_light_compose writes this
+ * layout directly. */
+#define GFT_LAYOUT_BRICK 0x10
 /* GFT_GRAD_REFERENCE reproduces the reference's gradient normalisations
  * (per-voxel sample count for resample/lookup, resample_grid.cu.cc:814-832;
  * per-camera sum of trilinear weights for raymarch, raymarch_grid.cu.cc:519-568).
@@ -268,12 +278,17 @@ gft_status gft_transmittance_grad(const float* output, const float* output_grad,
                                   float* input_grad, void* stream);
 /* gft_light_compose: density, transmittance [N, D, H, W, 1] (shape), light_color
  * [D, H, W, 3] shared by the batch; output [N, D, H, W, 4] =
- * concat(density * (transmittance * light_color + ambient), density) * scale. */
+ * concat(density * (transmittance * light_color + ambient), density) * scale,
+ * in NDHWC rows (output_layout 0) or in the raymarch's brick layout
+ * (output_layout GFT_LAYOUT_BRICK); the gradient reads output_grad in that
+ * layout. */
 gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
-                             const int64_t shape[5], float ambient, float scale, float* output, void* stream);
+                             const int64_t shape[5], float ambient, float scale, int32_t output_layout,
+                             float* output, void* stream);
 gft_status gft_light_compose_grad(const float* density, const float* transmittance, const float* light_color,
-                                  const int64_t shape[5], float ambient, float scale, const float* output_grad,
-                                  float* density_grad, float* transmittance_grad, void* stream);
+                                  const int64_t shape[5], float ambient, float scale, int32_t output_layout,
+                                  const float* output_grad, float* density_grad, float* transmittance_grad,
+                                  void* stream);
 /* gft_image_loss: image [pixels, 4] (rgb + density), target [pixels, 3],
  * background = 3 host floats; *loss (device) = mean over pixels and rgb of
  * (rgb + background * exp(-density) - target)^2, summed in a fixed order.

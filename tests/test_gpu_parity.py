@@ -374,3 +374,43 @@ def test_raymarch_multi_argument_errors(ops):
         ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, UNEVEN[:2])
     with pytest.raises(_lib.GftInvalidArgument):
         ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, [(13, 9, 11), (7, 0, 5), (11, 12, 16)])
+
+
+# ------------------------------------------------------------------ raymarch, brick layout
+@pytest.mark.parametrize('C', [1, 2, 4])
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP', 'WRAP'])
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_bricked_equals_rows(ops, C, boundary, mode):
+    """Odd grid sizes (padded bricks), forward bit-identical, gradient in the
+    brick layout equal to the row gradient."""
+    _, _, M, V, P, F = scene((9, 13, 11), 3, (13, 9, 11))
+    x = small_grid((9, 13, 11), C, 51) * 0.4
+    dy = cuda(np.random.default_rng(52).standard_normal((1, 3, 9, 11, C)).astype(np.float32))
+    xr = cuda(x).requires_grad_(True)
+    xb = ops.to_bricks(cuda(x)).requires_grad_(True)
+    assert torch.equal(ops.from_bricks(xb.detach(), (9, 13, 11)), xr.detach())
+    with ops.grad_mode(mode):
+        yr = ops.raymarch_grid_transform(xr, M, V, P, F, (13, 9, 11), 'LINEAR', boundary)
+        yb = ops.raymarch_grid_transform_bricked(xb, (9, 13, 11), M, V, P, F, (13, 9, 11), boundary)
+        assert torch.equal(yr, yb)
+        yr.backward(dy)
+        yb.backward(dy)
+    assert rel_l2(np_(ops.from_bricks(xb.grad, (9, 13, 11))), np_(xr.grad)) <= 1e-6
+
+
+def test_light_compose_bricked(ops):
+    from gft import fused
+    g = torch.Generator().manual_seed(6)
+    D, H, W = 7, 10, 5
+    d0 = torch.rand((1, D, H, W, 1), generator=g).cuda()
+    t0 = torch.rand((1, D, H, W, 1), generator=g).cuda()
+    col = torch.rand((1, D, H, W, 3), generator=g).cuda()
+    gb = torch.randn((1, ops.brick_cells((D, H, W)), 4), generator=g).cuda()
+    d1, t1 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    yb = fused.light_compose(d1, t1, col, 0.64, 0.37, brick=True)
+    d2, t2 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    yr = fused.light_compose(d2, t2, col, 0.64, 0.37)
+    assert torch.equal(ops.from_bricks(yb.detach(), (D, H, W)), yr.detach())
+    yb.backward(gb)
+    yr.backward(ops.from_bricks(gb, (D, H, W)))
+    assert torch.equal(d1.grad, d2.grad) and torch.equal(t1.grad, t2.grad)

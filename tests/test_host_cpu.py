@@ -180,3 +180,22 @@ def test_replica_timing_reduction_gloo_two_ranks(tmp_path):
     for p, o in zip(procs, outs):
         assert p.returncode == 0, o
         assert 'RESULT 2.5' in o, o
+
+
+def test_brick_layout_conversion():
+    """to_bricks / from_bricks follow the documented GFT_LAYOUT_BRICK cell order."""
+    import torch
+    from gft import ops
+    D, H, W, C = 5, 4, 7, 2
+    x = torch.arange(D * H * W * C, dtype=torch.float32).reshape(1, D, H, W, C)
+    xb = ops.to_bricks(x)
+    assert xb.shape == (1, ops.brick_cells((D, H, W)), C)
+
+    def cell(xx, yy, zz):
+        b = ((zz >> 1) * ((H + 1) // 2) + (yy >> 1)) * ((W + 1) // 2) + (xx >> 1)
+        return b * 8 + ((zz & 1) << 2 | (yy & 1) << 1 | (xx & 1))
+    for zz in range(D):
+        for yy in range(H):
+            for xx in range(W):
+                assert torch.equal(xb[0, cell(xx, yy, zz)], x[0, zz, yy, xx])
+    assert torch.equal(ops.from_bricks(xb, (D, H, W)), x)
