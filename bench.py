@@ -274,6 +274,7 @@ def extras(args, step, dev, timed, storage, inputs, ms):
 
     # ---- per-kernel timing of the dominant ops (roofline) -------------------
     out.update(kernel_roofline(step, dev, timed))
+    out['static_cameras'] = static_cameras(args, dev, timed, storage, inputs)
     out['uneven_views'] = uneven_views(dev, timed)
     out['transport_chain'] = transport_chain(step, dev, timed)
 
@@ -285,6 +286,30 @@ def extras(args, step, dev, timed, storage, inputs, ms):
         except Exception as e:  # the baseline is reported, not required
             out['cpu_baseline'] = {'error': repr(e)}
     return out
+
+
+def static_cameras(args, dev, timed, storage, inputs):
+    """The same graph step with ops.set_raymarch_weight_cache(True): for a
+    fixed camera rig the reference-normalised gradient's weight sums depend on
+    the geometry alone, so they are computed once and reused instead of in
+    every step (opt-in; the headline number recomputes them every step)."""
+    import numpy as np
+    from gft import ops
+    from gft.pipeline import RenderAdvectStep
+    if args.grad_mode != 'REFERENCE':
+        return None
+    ops.set_raymarch_weight_cache(True)
+    try:
+        st = RenderAdvectStep(args.config, dev, storage_dtype=storage, mode='batched')
+        st.setup_static(inputs)
+        st.capture(warmup=args.warmup)
+        for _ in range(3):
+            st.replay()
+        t = timed(st.replay, min(max(10, args.steps // 2), 100))
+        return {'ms_per_step': float(np.mean(t)), 'value': 1000.0 / float(np.mean(t)), 'unit': 'iters/s',
+                'what': 'cached raymarch weight sums (fixed cameras), otherwise the timed step'}
+    finally:
+        ops.set_raymarch_weight_cache(False)
 
 
 def transport_chain(step, dev, timed, frames=16, every=4):

@@ -250,6 +250,42 @@ def _raymarch_weights_async(x_shape, device, M, V, P, F, out_shape, boundary, se
 
 
 _prefetched = {}
+_weight_cache = {'enabled': False, 'max': 4, 'entries': {}}
+
+
+def set_raymarch_weight_cache(enabled, max_entries=4):
+    """Static camera rigs: keep the reference-normalised raymarch gradient's
+    per-camera weight sums (a function of the cameras, the grid shape, the
+    image size and the boundary mode only) across calls and reuse them when
+    exactly the same geometry comes back, instead of recomputing them in every
+    backward.  Off by default.  Entries are keyed by the matrix and frustum
+    values, so changed cameras are recomputed; each entry holds one float per
+    voxel and camera (75 MB at 128x227x128 and 5 views), at most
+    ``max_entries`` are kept.  An entry is filled on the current stream outside
+    CUDA-graph capture and the stream is synchronised once then."""
+    _weight_cache['enabled'] = bool(enabled)
+    _weight_cache['max'] = max(1, int(max_entries))
+    if not enabled:
+        _weight_cache['entries'].clear()
+
+
+def _cached_weights(shape5, device, M, V, P, F, out_shape, boundary, separate):
+    """The cached weight workspace for this geometry, filling it if allowed;
+    None when the cache is off or a capture is running and the entry is new."""
+    if not _weight_cache['enabled']:
+        return None
+    key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, device)
+    ent = _weight_cache['entries']
+    if key in ent:
+        return ent[key]
+    if torch.cuda.is_current_stream_capturing():
+        return None
+    ws = _raymarch_weights(shape5, device, M, V, P, F, out_shape, boundary, separate)
+    torch.cuda.current_stream(device).synchronize()
+    if len(ent) >= _weight_cache['max']:
+        ent.pop(next(iter(ent)))
+    ent[key] = ws
+    return ws
 
 
 def _weights_key(x_shape, M, V, P, F, out_shape, boundary, separate, device):
@@ -278,6 +314,8 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
     b = _enum(BOUNDARY, boundary, 'boundary')
     key = _weights_key(input_shape, matrix_m, matrix_v, matrix_p, frustum_params, out_shape, b,
                        separate_camera_batch, dev)
+    if _weight_cache['enabled'] and key in _weight_cache['entries']:
+        return
     _prefetched[key] = _raymarch_weights_async(tuple(input_shape), dev, matrix_m, matrix_v, matrix_p, frustum_params,
                                                out_shape, b, bool(separate_camera_batch))
 
@@ -313,11 +351,14 @@ class _Raymarch(torch.autograd.Function):
         xs = _storage(x, storage_dtype)
         shape5 = _grid5(xs, grid)[0]
         ctx.weights = None
-        if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
-                and interp == FILTER['LINEAR']):
-            key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
-            ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
-                                                                                out_shape, boundary, separate)
+        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+            cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
+            if cached is not None:
+                ctx.weights = (cached, None)
+            elif _state['side_weights']:
+                key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
+                ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
+                                                                                    out_shape, boundary, separate)
         y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=grid)
         ctx.save_for_backward(xs, y)
         ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate, grid)
@@ -331,7 +372,8 @@ class _Raymarch(torch.autograd.Function):
         ws = None
         if ctx.weights is not None:
             ws, ev = ctx.weights
-            torch.cuda.current_stream(xs.device).wait_event(ev)
+            if ev is not None:
+                torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
                           GRAD[get_grad_mode()], weights=ws, grid=grid)
         ctx.weights = None

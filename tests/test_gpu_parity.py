@@ -126,6 +126,50 @@ def test_raymarch_backward_prefetched_weights(ops):
     ops._prefetched.clear()
 
 
+def test_raymarch_weight_cache_static_cameras(ops):
+    """With the weight cache on, a repeated geometry reuses its weight sums (no
+    new entry), changed cameras get their own entry, and every gradient matches
+    the uncached one (float atomics: summation order only); a step captured in
+    a CUDA graph after the entry exists replays to the same gradient."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    _, _, M2, V2, P2, F2 = scene((10, 14, 12), 3, (13, 9, 11), arc=120.0, tilt=20.0)
+    x = small_grid((10, 14, 12), 4, 25) * 0.4
+    dy = cuda(np.random.default_rng(26).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+
+    def grad(m, v, p, f):
+        xt = cuda(x).requires_grad_(True)
+        with ops.grad_mode('REFERENCE'):
+            ops.raymarch_grid_transform(xt, m, v, p, f, (13, 9, 11)).backward(dy)
+        return xt.grad.clone()
+
+    base, base2 = grad(M, V, P, F), grad(M2, V2, P2, F2)
+    ops.set_raymarch_weight_cache(True, max_entries=2)
+    try:
+        g1 = grad(M, V, P, F)
+        assert len(ops._weight_cache['entries']) == 1
+        g2 = grad(M, V, P, F)
+        assert len(ops._weight_cache['entries']) == 1
+        assert rel_l2(np_(g1), np_(base)) <= 1e-6 and rel_l2(np_(g2), np_(base)) <= 1e-6
+        g3 = grad(M2, V2, P2, F2)
+        assert len(ops._weight_cache['entries']) == 2 and rel_l2(np_(g3), np_(base2)) <= 1e-6
+        xt = cuda(x).requires_grad_(True)
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s), ops.grad_mode('REFERENCE'):
+            ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11)).backward(dy)
+        torch.cuda.current_stream().wait_stream(s)
+        xt.grad = None
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph), ops.grad_mode('REFERENCE'):
+            ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11)).backward(dy)
+        graph.replay()
+        torch.cuda.synchronize()
+        assert len(ops._weight_cache['entries']) == 2 and rel_l2(np_(xt.grad), np_(base)) <= 1e-6
+    finally:
+        ops.set_raymarch_weight_cache(False)
+    assert len(ops._weight_cache['entries']) == 0
+
+
 def test_raymarch_not_separate_batch(ops):
     from oracle import raymarch as RM
     _, _, M, V, P, F = scene((8, 9, 7), 2, (9, 6, 5))
