@@ -163,51 +163,134 @@ __device__ __forceinline__ void ray_far_step(const CamX& cam, int x, int y, int 
 
 // --- adjoint scatters ----------------------------------------------------------
 // Each sample's cell gradient reaches its eight corners as vector reductions
-// (red.global.add.v4/v2.f32) in L2, whose sector throughput bounds these
-// kernels (a warp's 8x4 rays touch ~26 distinct 32-byte sectors per corner).
-// Measured alternatives that did not pay on GB300 at the 5-view 480x270x192
-// workload: summing the samples of 2x1, 1x2 or 2x2 neighbouring rays per
-// thread in registers (few share a footprint at 0.64 voxels per pixel;
-// 1.18-1.43 ms against 1.14 ms), and accumulating each block's samples of 2-8
-// steps in a shared-memory box flushed with coalesced reductions (2.3-3.6 ms:
-// the shared float atomics and the round barriers cost more than the L2
-// sectors they save).
+// (red.global.add.v4/v2.f32) in L2.  The lanes of a warp sample one depth per
+// step (warp_clip_range), so neighbouring lanes often share a cell, and samples
+// with the same base cell floor(p) share all eight corners: along each 8-lane
+// pixel row, a run of lanes with the same base cell hands its members'
+// fractions and values to the run's first lane (one shuffle round per member),
+// which sums the eight corner contributions and issues one reduction per
+// corner -- about half the reductions of one per lane and corner at the
+// 5-view 480x270x192 workload (rows of 0.36-0.53 voxels per pixel).  Measured
+// on GB300 there: weight pass 0.66 -> 0.59 ms, exact adjoint 1.17 -> 1.04 ms,
+// normalised adjoint 1.29 -> 1.27 ms (its 32 accumulators, 8 corners x 4
+// channels, take 80 registers; capping them at 64 or 72 spills and is slower,
+// as is loading the reciprocal weights before the shuffle rounds).  Alternatives measured earlier that did
+// not pay: summing 2x1 / 1x2 / 2x2 neighbouring rays per thread in registers,
+// and per-block shared-memory accumulation boxes flushed with coalesced
+// reductions (the shared float atomics and round barriers cost more than the
+// L2 sectors they save).
+//
+// Trilinear corner weights, corner k = (k & 1, k >> 1 & 1, k >> 2 & 1).
+__device__ __forceinline__ void corner_weights(float fx, float fy, float fz, float w[8]) {
+    const float ax[2] = {1.f - fx, fx}, ay[2] = {1.f - fy, fy};
+    float wxy[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) wxy[j] = ax[j & 1] * ay[j >> 1];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] = wxy[k & 3] * ((k & 4) ? fz : 1.f - fz);
+}
 
-// One sample's trilinear scatter.  MODE 0 (exact adjoint): BORDER drops the
-// sample outside the forward's half-cell window.  MODE 1 (reference-normalised)
-// and MODE 2 (weight sums): BORDER drops it unless -1 < p < dims, the
-// reference's window; MODE 1 scales each corner's contribution by the
-// reciprocal of the camera's weight sum there (the per-camera
-// normalise-then-sum applied per contribution, so all cameras accumulate into
-// one gradient) and skips corners with w == 0 or no weight.
+// Bit k set where corner k's weight is non-zero, for fractions in [0, 1).
+__device__ __forceinline__ unsigned zero_weight_mask(float fx, float fy, float fz) {
+    return 0xffu & (fx != 0.f ? 0xffu : 0x55u) & (fy != 0.f ? 0xffu : 0x33u) & (fz != 0.f ? 0xffu : 0x0fu);
+}
+
+// One step of the warp's samples.  All 32 lanes call it; act = this lane has a
+// sample.  MODE 0 (exact adjoint): BORDER drops the sample outside the
+// forward's half-cell window.  MODE 1 (reference-normalised) and MODE 2 (weight
+// sums): BORDER drops it unless -1 < p < dims, the reference's window; MODE 1
+// scales each corner's sum by the reciprocal of the camera's weight sum there
+// (the per-camera normalise-then-sum applied per contribution, so all cameras
+// accumulate into one gradient) and skips corners with no weight.  Zero-weight
+// contributions are skipped; the ceil corner is floor + 1 (the reference's
+// ceil(p) equals floor(p) only where the ceil weight is 0).
 template <int C, int BM, int MODE, int L>
-__device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
-                                               float px, float py, float pz, Vec<C> val) {
+__device__ __forceinline__ void scatter_step(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
+                                             bool act, float px, float py, float pz, Vec<C> val) {
+    const unsigned lane = (threadIdx.y & 3u) * RM_BX + threadIdx.x;  // blockDim.x == RM_BX
     if constexpr (BM == BM_BORDER) {
-        if constexpr (MODE != 0) {
-            if (!(px > -1.f && px < (float)d.x && py > -1.f && py < (float)d.y && pz > -1.f && pz < (float)d.z))
-                return;
-        } else {
-            if (!border_inside(px, py, pz, d)) return;
+        if constexpr (MODE != 0)
+            act = act && px > -1.f && px < (float)d.x && py > -1.f && py < (float)d.y && pz > -1.f && pz < (float)d.z;
+        else
+            act = act && border_inside(px, py, pz, d);
+    }
+    const float flx = floorf(px), fly = floorf(py), flz = floorf(pz);
+    const int x0 = (int)flx, y0 = (int)fly, z0 = (int)flz;
+    const float wx = px - flx, wy = py - fly, wz = pz - flz;
+    const int ux = __shfl_up_sync(0xffffffffu, x0, 1), uy = __shfl_up_sync(0xffffffffu, y0, 1),
+              uz = __shfl_up_sync(0xffffffffu, z0, 1);
+    const unsigned acts = __ballot_sync(0xffffffffu, act);
+    const bool same = act && (lane & (RM_BX - 1)) != 0 && ((acts >> ((lane - 1) & 31u)) & 1u) && ux == x0 &&
+                      uy == y0 && uz == z0;
+    const unsigned follow = __ballot_sync(0xffffffffu, same);
+    const bool head = act && !same;
+    // members after the head: the 'same' lanes directly following it (a run
+    // never crosses a row, whose first lane is never 'same'), at most 7
+    const int n = head ? __ffs(~(unsigned)((unsigned long long)follow >> (lane + 1))) - 1 : 0;
+    const int rounds = __reduce_max_sync(0xffffffffu, n);
+    // Corner weights as products of per-axis factors (1 - f, f); f lies in
+    // [0, 1), so a weight is zero exactly where it takes an f that is 0: those
+    // corners get no contribution (masked below, nz), as in a per-corner skip.
+    float acc[8][C];
+    unsigned nz = zero_weight_mask(wx, wy, wz);
+    {
+        float w[8];
+        corner_weights(wx, wy, wz, w);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[k][c] = w[k] * val.v[c];
+    }
+    for (int r = 1; r <= rounds; ++r) {
+        const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
+                    mz = __shfl_down_sync(0xffffffffu, wz, r);
+        float mv[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) mv[c] = __shfl_down_sync(0xffffffffu, val.v[c], r);
+        if (r <= n) {
+            const unsigned m = zero_weight_mask(mx, my, mz);
+            nz |= m;
+            float w[8];
+            corner_weights(mx, my, mz, w);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if ((m >> k) & 1u) {
+#pragma unroll
+                    for (int c = 0; c < C; ++c) acc[k][c] = fmaf(w[k], mv[c], acc[k][c]);
+                }
+            }
         }
     }
-    const Corners c = corners<BM>(px, py, pz, d);
-    const float cw[3] = {c.wx, c.wy, c.wz};
+    if (!head) return;
+    int xs[2] = {x0, x0 + 1}, ys[2] = {y0, y0 + 1}, zs[2] = {z0, z0 + 1};
+    bool vx[2] = {true, true}, vy[2] = {true, true}, vz[2] = {true, true};
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        if constexpr (BM == BM_BORDER) {
+            vx[i] = xs[i] > -1 && xs[i] < d.x;
+            vy[i] = ys[i] > -1 && ys[i] < d.y;
+            vz[i] = zs[i] > -1 && zs[i] < d.z;
+        } else {
+            xs[i] = remap<BM>(xs[i], d.x);
+            ys[i] = remap<BM>(ys[i], d.y);
+            zs[i] = remap<BM>(zs[i], d.z);
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
-        const bool ok = (sx ? c.vx1 : c.vx0) && (sy ? c.vy1 : c.vy0) && (sz ? c.vz1 : c.vz0);
-        if (BM != BM_BORDER || ok) {
-            const float w = (sx ? cw[0] : 1.f - cw[0]) * (sy ? cw[1] : 1.f - cw[1]) * (sz ? cw[2] : 1.f - cw[2]);
-            const int x = sx ? c.x1 : c.x0, y = sy ? c.y1 : c.y0, z = sz ? c.z1 : c.z0;
-            if constexpr (MODE == 1) {
-                const float inv = __ldg(cnt + brick_index(x, y, z, d));
-                if (w != 0.f && inv > 0.f) atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(vscale(val, w), inv));
-            } else if constexpr (MODE == 2) {
-                atomic_add<C>(grad, brick_index(x, y, z, d), vscale(val, w));
-            } else {
-                atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(val, w));
-            }
+        if (!((nz >> k) & 1u) || !(vx[sx] && vy[sy] && vz[sz])) continue;
+        const int x = xs[sx], y = ys[sy], z = zs[sz];
+        Vec<C> a;
+#pragma unroll
+        for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];
+        if constexpr (MODE == 1) {
+            const float inv = __ldg(cnt + brick_index(x, y, z, d));
+            if (inv > 0.f) atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(a, inv));
+        } else if constexpr (MODE == 2) {
+            atomic_add<C>(grad, brick_index(x, y, z, d), a);
+        } else {
+            atomic_add<C>(grad, cell_index<L>(x, y, z, d), a);
         }
     }
 }
@@ -216,11 +299,12 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
 // MODE 2, the reference normalisation's first pass: per (batch, camera) pair
 // the per-voxel sum of the trilinear weights of all its samples (the float
 // sampleCounter of raymarch_grid.cu.cc:446-456) in the brick layout
-// (brick_index); geometry only, C == 1, no gathers.  MODE 0 / 1, the adjoint: re-sample (LINEAR only, as the reference
-// gradient op), step the blend adjoint and scatter the cell gradient into the
-// batch gradient; MODE 1 normalises by the pass-1 sums, which equals the
-// reference's per-camera normalise-then-sum (kNormalize3DGradients,
-// raymarch_grid.cu.cc:319-341 and :519-568) without per-camera buffers.
+// (brick_index); geometry only, C == 1, no gathers.  MODE 0 / 1, the adjoint:
+// re-sample (LINEAR only, as the reference gradient op), step the blend
+// adjoint and scatter the cell gradient into the batch gradient; MODE 1
+// normalises by the pass-1 sums, which equals the reference's per-camera
+// normalise-then-sum (kNormalize3DGradients, raymarch_grid.cu.cc:319-341 and
+// :519-568) without per-camera buffers.
 //
 // Clipping (BORDER): a zero sample's adjoint step leaves the state unchanged
 // for ADDITIVE, ALPHA_ADDITIVE and C == 1, and for the two BEER_LAMBERT modes
@@ -228,13 +312,15 @@ __device__ __forceinline__ void scatter_sample(float* __restrict__ grad, const f
 // forward output; a negative one is first clamped by max(., 0), so such rays
 // march in full).  ALPHA changes its bookkeeping on every step and marches in
 // full.  (Non-finite adjoints are not propagated through skipped samples.)
+// Every lane stays in the loop to its warp's last step (scatter_step is
+// warp-collective); lanes without a sample at a step pass act = false.
 template <int C, typename S, int BM, int MODE, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
                        const __grid_constant__ PairTable tab) {
     RayPix r;
-    const bool live = ray_pixel(tab, r);  // every lane stays to the warp's clip reduction
+    const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     float3 pos, step;
     ray_far_step(tab.cam[p], x, y, W, H, D, pos, step);
@@ -256,28 +342,25 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
                            acc.v[C - 1] >= 0.f);
         const bool hit = live && (!clip || ray_clip(pos, make_float3(-step.x, -step.y, -step.z), D, din, k_lo, k_hi));
         warp_clip_range(hit, D, k_lo, k_hi, w_lo, w_hi);
-        if (!hit) return;
         for (int k = 0; k < w_lo; ++k) {  // iterated subtraction, as the full march
             pos.x -= step.x;
             pos.y -= step.y;
             pos.z -= step.z;
         }
     } else if (!live) {
-        return;
+        k_lo = D;
+        k_hi = -1;
     }
-#pragma unroll 4
+#pragma unroll 2
     for (int k = w_lo; k <= w_hi; ++k) {
-        if (k >= k_lo && k <= k_hi) {
-            const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
-            Vec<C> val;
-            if constexpr (MODE == 2) {
-                val = vfill<C>(1.f);
-            } else {
-                const Vec<C> smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
-                val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
-            }
-            scatter_sample<C, BM, MODE, L>(dst, count, din, px, py, pz, val);
+        const bool on = k >= k_lo && k <= k_hi;
+        const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
+        Vec<C> val = vfill<C>(1.f);
+        if (MODE != 2 && on) {
+            const Vec<C> smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
+            val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
+        scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val);
         pos.x -= step.x;
         pos.y -= step.y;
         pos.z -= step.z;
