@@ -139,24 +139,43 @@ __device__ __forceinline__ float3 map_pos(const CamX& c, int cm, float3 idx, flo
 // folded homogeneous coordinates (for the linear-depth z, by a step of NDC z
 // alone), so each costs a column add and a reciprocal instead of a transform;
 // the differences are taken between folded positions.
+//
+// outside_zero: the caller's samples are zero at every mip level outside
+// 0 <= p < din (LINEAR under BORDER with a half-cell centre offset: level m
+// reads p * 2^-m, exactly, inside [0, (din >> m) * 2^m)), so there the LOD,
+// which cannot change the result, is not computed.
 template <int CM>
-__device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float3 din, float3 dout_inv, bool lod) {
+__device__ __forceinline__ bool skip_lod(float3 p, float3 din, bool outside_zero) {
+    return outside_zero && !(p.x >= 0.f && p.x < din.x && p.y >= 0.f && p.y < din.y && p.z >= 0.f && p.z < din.z);
+}
+
+template <int CM>
+__device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float3 din, float3 dout_inv, bool lod,
+                                                bool outside_zero = false) {
     float3 p, f, ex, ey, ez;
     if constexpr (CM == CM_TRANSFORM || CM == CM_LINDEPTH) {
-        p = CM == CM_TRANSFORM ? idx_to_os(c, idx, dout_inv) : idx_to_os_lindepth(c, idx, dout_inv);
-        if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
         float4 ndc = idx_to_ndc(idx, dout_inv);
         if (CM == CM_LINDEPTH) ndc.z = lindepth_ndc_z(c, idx.z, dout_inv.z);
         const float4 h = mul(c.q, ndc);
-        const float dz = CM == CM_TRANSFORM ? 2.f * dout_inv.z : lindepth_ndc_z(c, idx.z + 1.f, dout_inv.z) - ndc.z;
         f = dehom(h);
+        if (outside_zero) {
+            // The folded position differs from the exact one by rounding only:
+            // half a cell (plus 1e-3 relative) outside the domain, the exact one
+            // is outside too and every level samples zero, so it is not needed.
+            const float m = 0.5f + 1e-3f * fmaxf(fabsf(f.x), fmaxf(fabsf(f.y), fabsf(f.z)));
+            if (f.x <= -m || f.x >= din.x + m || f.y <= -m || f.y >= din.y + m || f.z <= -m || f.z >= din.z + m)
+                return make_float4(f.x, f.y, f.z, 0.f);
+        }
+        p = CM == CM_TRANSFORM ? idx_to_os(c, idx, dout_inv) : idx_to_os_lindepth(c, idx, dout_inv);
+        if (!lod || skip_lod<CM>(p, din, outside_zero)) return make_float4(p.x, p.y, p.z, 0.f);
+        const float dz = CM == CM_TRANSFORM ? 2.f * dout_inv.z : lindepth_ndc_z(c, idx.z + 1.f, dout_inv.z) - ndc.z;
         ex = dehom(add_col<0>(h, c.q, 2.f * dout_inv.x));
         ey = dehom(add_col<1>(h, c.q, 2.f * dout_inv.y));
         ez = dehom(add_col<2>(h, c.q, dz));
     } else {
         constexpr bool LIN = CM == CM_LINDEPTH_REVERSE;
         p = LIN ? os_to_idx_lindepth(c, idx, din) : os_to_idx(c, idx, din);
-        if (!lod) return make_float4(p.x, p.y, p.z, 0.f);
+        if (!lod || skip_lod<CM>(p, din, outside_zero)) return make_float4(p.x, p.y, p.z, 0.f);
         const float4 h = mul(c.r, make_float4(idx.x, idx.y, idx.z, 1.f));
         f = ndc_to_idx<LIN>(c, dehom(h), din);
         ex = ndc_to_idx<LIN>(c, dehom(add_col<0>(h, c.r, 1.f)), din);
@@ -181,12 +200,12 @@ __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float
 }
 
 __device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv,
-                                             bool lod) {
+                                             bool lod, bool outside_zero = false) {
     switch (cm) {
-        case CM_LINDEPTH: return sample_pos_cm<CM_LINDEPTH>(c, idx, din, dout_inv, lod);
-        case CM_TRANSFORM: return sample_pos_cm<CM_TRANSFORM>(c, idx, din, dout_inv, lod);
-        case CM_LINDEPTH_REVERSE: return sample_pos_cm<CM_LINDEPTH_REVERSE>(c, idx, din, dout_inv, lod);
-        default: return sample_pos_cm<CM_TRANSFORM_REVERSE>(c, idx, din, dout_inv, lod);
+        case CM_LINDEPTH: return sample_pos_cm<CM_LINDEPTH>(c, idx, din, dout_inv, lod, outside_zero);
+        case CM_TRANSFORM: return sample_pos_cm<CM_TRANSFORM>(c, idx, din, dout_inv, lod, outside_zero);
+        case CM_LINDEPTH_REVERSE: return sample_pos_cm<CM_LINDEPTH_REVERSE>(c, idx, din, dout_inv, lod, outside_zero);
+        default: return sample_pos_cm<CM_TRANSFORM_REVERSE>(c, idx, din, dout_inv, lod, outside_zero);
     }
 }
 
@@ -203,7 +222,7 @@ __global__ void __launch_bounds__(RS_THREADS)
     const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
     const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
     const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
-                                  mip_mode != MIP_NONE);
+                                  mip_mode != MIP_NONE, BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f);
     Vec<C> r;
     if ((filter == F_LINEAR || filter == F_NEAREST) && (BM == BM_BORDER || BM == BM_CLAMP))
         r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
