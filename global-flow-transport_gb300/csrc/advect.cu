@@ -199,7 +199,8 @@ __global__ void __launch_bounds__(AD_THREADS)
     Vec<C> f, mn, mx;
     fetch_linear_minmax<C, float, BM>(d, dm, l.x + (float)x, l.y + (float)y, l.z + (float)z, f, mn, mx);
     const float bx = -l.x + (float)x, by = -l.y + (float)y, bz = -l.z + (float)z;
-    const Vec<C> back = fetch_linear<C, float, BM>(fwd, dm, bx, by, bz);
+    Vec<C> back, ddx, ddy, ddz;  // back lookup value and its spatial derivative, one corner set
+    fetch_linear_grad<C, BM>(fwd, dm, bx, by, bz, back, ddx, ddy, ddz);
     const Vec<C> dv = loadf<C>(d, t);
     Vec<C> g = loadf<C>(dy, t);
     Vec<C> gcorr, gback;
@@ -215,8 +216,6 @@ __global__ void __launch_bounds__(AD_THREADS)
     store<C>(gd, t, vscale(gcorr, 0.5f));
     store<C>(gdir, t, g);
     scatter_linear<C, BM, COUNT>(gfwd_sc, cnt2, dm, bx, by, bz, gback);
-    Vec<C> ddx, ddy, ddz;
-    fetch_grad<C, BM>(fwd, dm, bx, by, bz, ddx, ddy, ddz);
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
     for (int i = 0; i < C; ++i) {
@@ -247,14 +246,17 @@ __global__ void __launch_bounds__(AD_THREADS)
     const float3 l = lut_at(vx, vy, vz, dm, x, y, z, dt);
     const float px = l.x + (float)x, py = l.y + (float)y, pz = l.z + (float)z;
     Vec<C> gf = loadf<C>(gdir, t);
-    if (first_order) {
-        if (negative) {
-            const Vec<C> f = fetch_linear<C, float, BM>(d, dm, px, py, pz);
+    Vec<C> ddx, ddy, ddz;
+    if (first_order && negative) {
+        Vec<C> f;
+        fetch_linear_grad<C, BM>(d, dm, px, py, pz, f, ddx, ddy, ddz);
 #pragma unroll
-            for (int i = 0; i < C; ++i)
-                if (!(f.v[i] >= 0.f)) gf.v[i] = 0.f;
-        }
+        for (int i = 0; i < C; ++i)
+            if (!(f.v[i] >= 0.f)) gf.v[i] = 0.f;
     } else {
+        fetch_grad<C, BM>(d, dm, px, py, pz, ddx, ddy, ddz);
+    }
+    if (!first_order) {
         Vec<C> sc = loadf<C>(gfwd_sc, t);
         if (COUNT) {
             const unsigned int n = cnt2[t];
@@ -263,8 +265,6 @@ __global__ void __launch_bounds__(AD_THREADS)
         gf = vadd(gf, sc);
     }
     scatter_linear<C, BM, COUNT>(gd_sc, cnt3, dm, px, py, pz, gf);
-    Vec<C> ddx, ddy, ddz;
-    fetch_grad<C, BM>(d, dm, px, py, pz, ddx, ddy, ddz);
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
     for (int i = 0; i < C; ++i) {

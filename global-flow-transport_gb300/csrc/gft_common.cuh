@@ -424,6 +424,39 @@ __device__ __forceinline__ void fetch_grad(const float* __restrict__ g, Dims d, 
     }
 }
 
+// Trilinear value and its spatial derivative from one set of corner reads:
+// the value of fetch_linear and the derivative of fetch_grad (ceil corners, as
+// read3DGrad; the value is the same, a zero fraction giving a zero weight).
+template <int C, int BM>
+__device__ __forceinline__ void fetch_linear_grad(const float* __restrict__ g, Dims d, float px, float py, float pz,
+                                                  Vec<C>& val, Vec<C>& dx, Vec<C>& dy, Vec<C>& dz) {
+    if constexpr (BM == BM_BORDER) {
+        if (!border_inside(px, py, pz, d)) {
+            val = dx = dy = dz = vzero<C>();
+            return;
+        }
+    }
+    const Corners c = corners<BM>(px, py, pz, d);
+    const Vec<C> fff = read_corner<C, float, BM>(g, d, c.x0, c.y0, c.z0, c.vx0 && c.vy0 && c.vz0);
+    const Vec<C> cff = read_corner<C, float, BM>(g, d, c.x1, c.y0, c.z0, c.vx1 && c.vy0 && c.vz0);
+    const Vec<C> fcf = read_corner<C, float, BM>(g, d, c.x0, c.y1, c.z0, c.vx0 && c.vy1 && c.vz0);
+    const Vec<C> ccf = read_corner<C, float, BM>(g, d, c.x1, c.y1, c.z0, c.vx1 && c.vy1 && c.vz0);
+    const Vec<C> ffc = read_corner<C, float, BM>(g, d, c.x0, c.y0, c.z1, c.vx0 && c.vy0 && c.vz1);
+    const Vec<C> cfc = read_corner<C, float, BM>(g, d, c.x1, c.y0, c.z1, c.vx1 && c.vy0 && c.vz1);
+    const Vec<C> fcc = read_corner<C, float, BM>(g, d, c.x0, c.y1, c.z1, c.vx0 && c.vy1 && c.vz1);
+    const Vec<C> ccc = read_corner<C, float, BM>(g, d, c.x1, c.y1, c.z1, c.vx1 && c.vy1 && c.vz1);
+    const Vec<C> v0 = vlerp(vlerp(fff, cff, c.wx), vlerp(fcf, ccf, c.wx), c.wy);
+    const Vec<C> v1 = vlerp(vlerp(ffc, cfc, c.wx), vlerp(fcc, ccc, c.wx), c.wy);
+    val = vlerp(v0, v1, c.wz);
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        auto L = [](float a, float b, float t) { return a + t * (b - a); };
+        dx.v[i] = L(L(cff.v[i] - fff.v[i], ccf.v[i] - fcf.v[i], c.wy), L(cfc.v[i] - ffc.v[i], ccc.v[i] - fcc.v[i], c.wy), c.wz);
+        dy.v[i] = L(L(fcf.v[i] - fff.v[i], ccf.v[i] - cff.v[i], c.wx), L(fcc.v[i] - ffc.v[i], ccc.v[i] - cfc.v[i], c.wx), c.wz);
+        dz.v[i] = L(L(ffc.v[i] - fff.v[i], cfc.v[i] - cff.v[i], c.wx), L(fcc.v[i] - fcf.v[i], ccc.v[i] - ccf.v[i], c.wx), c.wy);
+    }
+}
+
 // Trilinear scatter (scatterGradInterpolated, resample_grid.cu.cc:760-812 and
 // sampling_v2.hpp:458-484).  COUNT: 0 none, 1 +1 per reached corner (uint32
 // counter), 2 +w per reached corner (float counter).  With a counter (the
