@@ -231,8 +231,9 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
     const int n = head ? __ffs(~(unsigned)((unsigned long long)follow >> (lane + 1))) - 1 : 0;
     const int rounds = __reduce_max_sync(0xffffffffu, n);
     // Corner weights as products of per-axis factors (1 - f, f); f lies in
-    // [0, 1), so a weight is zero exactly where it takes an f that is 0: those
-    // corners get no contribution (masked below, nz), as in a per-corner skip.
+    // [0, 1), so a weight is zero exactly where it takes an f that is 0.  A
+    // zero weight adds +0 to a finite sum; corners that no member reaches with
+    // a non-zero weight are not reduced (nz).  (MODE 2: the value is 1.)
     float acc[8][C];
     unsigned nz = zero_weight_mask(wx, wy, wz);
     {
@@ -241,26 +242,24 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 #pragma unroll
         for (int k = 0; k < 8; ++k)
 #pragma unroll
-            for (int c = 0; c < C; ++c) acc[k][c] = w[k] * val.v[c];
+            for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? w[k] : w[k] * val.v[c];
     }
     for (int r = 1; r <= rounds; ++r) {
         const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
                     mz = __shfl_down_sync(0xffffffffu, wz, r);
         float mv[C];
+        if constexpr (MODE != 2) {
 #pragma unroll
-        for (int c = 0; c < C; ++c) mv[c] = __shfl_down_sync(0xffffffffu, val.v[c], r);
+            for (int c = 0; c < C; ++c) mv[c] = __shfl_down_sync(0xffffffffu, val.v[c], r);
+        }
         if (r <= n) {
-            const unsigned m = zero_weight_mask(mx, my, mz);
-            nz |= m;
+            nz |= zero_weight_mask(mx, my, mz);
             float w[8];
             corner_weights(mx, my, mz, w);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                if ((m >> k) & 1u) {
+            for (int k = 0; k < 8; ++k)
 #pragma unroll
-                    for (int c = 0; c < C; ++c) acc[k][c] = fmaf(w[k], mv[c], acc[k][c]);
-                }
-            }
+                for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? acc[k][c] + w[k] : fmaf(w[k], mv[c], acc[k][c]);
         }
     }
     if (!head) return;
@@ -278,21 +277,36 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
             zs[i] = remap<BM>(zs[i], d.z);
         }
     }
+    // cell indices as sums of per-axis terms (brick_index, flat3)
+    const int64_t bx = (d.x + 1) / 2, bxy = bx * ((d.y + 1) / 2);
+    int64_t bt[3][2], ct[3][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        bt[0][i] = (int64_t)(xs[i] >> 1) * 8 + (xs[i] & 1);
+        bt[1][i] = (int64_t)(ys[i] >> 1) * bx * 8 + ((ys[i] & 1) << 1);
+        bt[2][i] = (int64_t)(zs[i] >> 1) * bxy * 8 + ((zs[i] & 1) << 2);
+        if constexpr (L == LAYOUT_FLAT) {
+            ct[0][i] = xs[i];
+            ct[1][i] = (int64_t)ys[i] * d.x;
+            ct[2][i] = (int64_t)zs[i] * d.x * d.y;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
         if (!((nz >> k) & 1u) || !(vx[sx] && vy[sy] && vz[sz])) continue;
-        const int x = xs[sx], y = ys[sy], z = zs[sz];
+        const int64_t bi = bt[0][sx] + bt[1][sy] + bt[2][sz];
+        const int64_t ci = L == LAYOUT_FLAT ? ct[0][sx] + ct[1][sy] + ct[2][sz] : bi;
         Vec<C> a;
 #pragma unroll
         for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];
         if constexpr (MODE == 1) {
-            const float inv = __ldg(cnt + brick_index(x, y, z, d));
-            if (inv > 0.f) atomic_add<C>(grad, cell_index<L>(x, y, z, d), vscale(a, inv));
+            const float inv = __ldg(cnt + bi);
+            if (inv > 0.f) atomic_add<C>(grad, ci, vscale(a, inv));
         } else if constexpr (MODE == 2) {
-            atomic_add<C>(grad, brick_index(x, y, z, d), a);
+            atomic_add<C>(grad, bi, a);
         } else {
-            atomic_add<C>(grad, cell_index<L>(x, y, z, d), a);
+            atomic_add<C>(grad, ci, a);
         }
     }
 }
