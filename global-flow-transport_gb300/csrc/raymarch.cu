@@ -175,8 +175,8 @@ __device__ __forceinline__ void ray_far_step(const CamX& cam, int x, int y, int 
 // 5-view 480x270x192 workload (rows of 0.36-0.53 voxels per pixel).  Measured
 // on GB300 there: weight pass 0.66 -> 0.59 ms, exact adjoint 1.17 -> 1.04 ms,
 // normalised adjoint 1.29 -> 1.27 ms (its 32 accumulators, 8 corners x 4
-// channels, take 80 registers; capping them at 64 or 72 spills and is slower,
-// as is loading the reciprocal weights before the shuffle rounds).  Alternatives measured earlier that did
+// channels, take 80 registers; loading the reciprocal weights before the
+// shuffle rounds was slower).  Alternatives measured earlier that did
 // not pay: summing 2x1 / 1x2 / 2x2 neighbouring rays per thread in registers,
 // and per-block shared-memory accumulation boxes flushed with coalesced
 // reductions (the shared float atomics and round barriers cost more than the
@@ -367,7 +367,10 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         k_lo = D;
         k_hi = -1;
     }
-#pragma unroll 2
+    // Not unrolled: the step body is large, and unrolled copies stalled on
+    // instruction fetch (unroll 2 / 4: 13 % / 36 % slower normalised pass at
+    // 480x270x192; capping registers at 64 or 72 spilled and was slower too).
+#pragma unroll 1
     for (int k = w_lo; k <= w_hi; ++k) {
         const bool on = k >= k_lo && k <= k_hi;
         const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
