@@ -149,6 +149,14 @@ __device__ __forceinline__ bool skip_lod(float3 p, float3 din, bool outside_zero
     return outside_zero && !(p.x >= 0.f && p.x < din.x && p.y >= 0.f && p.y < din.y && p.z >= 0.f && p.z < din.z);
 }
 
+// Homogeneous divide for the LOD's finite differences (and the folded
+// position of the outside test): the fast reciprocal intrinsic, whose error of
+// a few ulp is far below the differences taken.
+__device__ __forceinline__ float3 dehom_lod(float4 h) {
+    const float iw = __fdividef(1.f, h.w);
+    return make_float3(h.x * iw, h.y * iw, h.z * iw);
+}
+
 template <int CM>
 __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float3 din, float3 dout_inv, bool lod,
                                                 bool outside_zero = false) {
@@ -157,7 +165,7 @@ __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float
         float4 ndc = idx_to_ndc(idx, dout_inv);
         if (CM == CM_LINDEPTH) ndc.z = lindepth_ndc_z(c, idx.z, dout_inv.z);
         const float4 h = mul(c.q, ndc);
-        f = dehom(h);
+        f = dehom_lod(h);
         if (outside_zero) {
             // The folded position differs from the exact one by rounding only:
             // half a cell (plus 1e-3 relative) outside the domain, the exact one
@@ -169,34 +177,36 @@ __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float
         p = CM == CM_TRANSFORM ? idx_to_os(c, idx, dout_inv) : idx_to_os_lindepth(c, idx, dout_inv);
         if (!lod || skip_lod<CM>(p, din, outside_zero)) return make_float4(p.x, p.y, p.z, 0.f);
         const float dz = CM == CM_TRANSFORM ? 2.f * dout_inv.z : lindepth_ndc_z(c, idx.z + 1.f, dout_inv.z) - ndc.z;
-        ex = dehom(add_col<0>(h, c.q, 2.f * dout_inv.x));
-        ey = dehom(add_col<1>(h, c.q, 2.f * dout_inv.y));
-        ez = dehom(add_col<2>(h, c.q, dz));
+        ex = dehom_lod(add_col<0>(h, c.q, 2.f * dout_inv.x));
+        ey = dehom_lod(add_col<1>(h, c.q, 2.f * dout_inv.y));
+        ez = dehom_lod(add_col<2>(h, c.q, dz));
     } else {
         constexpr bool LIN = CM == CM_LINDEPTH_REVERSE;
         p = LIN ? os_to_idx_lindepth(c, idx, din) : os_to_idx(c, idx, din);
         if (!lod || skip_lod<CM>(p, din, outside_zero)) return make_float4(p.x, p.y, p.z, 0.f);
         const float4 h = mul(c.r, make_float4(idx.x, idx.y, idx.z, 1.f));
-        f = ndc_to_idx<LIN>(c, dehom(h), din);
-        ex = ndc_to_idx<LIN>(c, dehom(add_col<0>(h, c.r, 1.f)), din);
-        ey = ndc_to_idx<LIN>(c, dehom(add_col<1>(h, c.r, 1.f)), din);
-        ez = ndc_to_idx<LIN>(c, dehom(add_col<2>(h, c.r, 1.f)), din);
+        f = ndc_to_idx<LIN>(c, dehom_lod(h), din);
+        ex = ndc_to_idx<LIN>(c, dehom_lod(add_col<0>(h, c.r, 1.f)), din);
+        ey = ndc_to_idx<LIN>(c, dehom_lod(add_col<1>(h, c.r, 1.f)), din);
+        ez = ndc_to_idx<LIN>(c, dehom_lod(add_col<2>(h, c.r, 1.f)), din);
     }
     const float3 dx = make_float3(f.x - ex.x, f.y - ex.y, f.z - ex.z);
     const float3 dy = make_float3(f.x - ey.x, f.y - ey.y, f.z - ey.z);
     const float3 dz = make_float3(f.x - ez.x, f.y - ez.y, f.z - ez.z);
-    float px, py, pz;
+    // lod = log2 of the largest per-axis step length = half the log2 of the
+    // largest squared length (no square roots); the fast log2 intrinsic
+    float qx, qy, qz;
     if constexpr (CM == CM_LINDEPTH || CM == CM_TRANSFORM) {
-        px = sqrtf(dx.x * dx.x + dy.x * dy.x + dz.x * dz.x);
-        py = sqrtf(dx.y * dx.y + dy.y * dy.y + dz.y * dz.y);
-        pz = sqrtf(dx.z * dx.z + dy.z * dy.z + dz.z * dz.z);
+        qx = dx.x * dx.x + dy.x * dy.x + dz.x * dz.x;
+        qy = dx.y * dx.y + dy.y * dy.y + dz.y * dz.y;
+        qz = dx.z * dx.z + dy.z * dy.z + dz.z * dz.z;
     } else {
-        px = sqrtf(dx.x * dx.x + dx.y * dx.y + dx.z * dx.z);
-        py = sqrtf(dy.x * dy.x + dy.y * dy.y + dy.z * dy.z);
-        pz = sqrtf(dz.x * dz.x + dz.y * dz.y + dz.z * dz.z);
+        qx = dx.x * dx.x + dx.y * dx.y + dx.z * dx.z;
+        qy = dy.x * dy.x + dy.y * dy.y + dy.z * dy.z;
+        qz = dz.x * dz.x + dz.y * dz.y + dz.z * dz.z;
     }
-    const float dm = fmaxf(px, fmaxf(py, pz));
-    return make_float4(p.x, p.y, p.z, fmaxf(0.f, log2f(dm)));
+    const float qm = fmaxf(qx, fmaxf(qy, qz));
+    return make_float4(p.x, p.y, p.z, fmaxf(0.f, 0.5f * __log2f(qm)));
 }
 
 __device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, float3 din, float3 dout_inv,
