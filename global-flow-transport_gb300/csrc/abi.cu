@@ -839,7 +839,11 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
                            size_t workspace_bytes, void* stream) {
     gft_status st = check_advect(density_shape, vel_x, vel_y, vel_z, order, clamp, boundary);
     if (st != GFT_OK) return st;
+    const bool forward_ready = (grad_mode & GFT_GRAD_FORWARD_READY) != 0;
+    grad_mode &= ~GFT_GRAD_FORWARD_READY;
     if (!enum_in(grad_mode, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (forward_ready && (order != 2 || density_shape[0] != 1))
+        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_FORWARD_READY needs order 2 and one batch slice");
     if (!density || !output_grad || !density_grad || !vel_x_grad || !vel_y_grad || !vel_z_grad)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     const size_t need = gft_advect_grad_workspace_size(density_shape, order);
@@ -857,8 +861,8 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
     a.order = order;
     a.clamp = clamp;
     a.boundary = boundary;
-    if (!launch_advect_bwd(a, grad_mode == GFT_GRAD_EXACT, output_grad, density_grad, vel_x_grad, vel_y_grad,
-                           vel_z_grad, reinterpret_cast<float*>(workspace), as_stream(stream)))
+    if (!launch_advect_bwd(a, grad_mode == GFT_GRAD_EXACT, forward_ready, output_grad, density_grad, vel_x_grad,
+                           vel_y_grad, vel_z_grad, reinterpret_cast<float*>(workspace), as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }

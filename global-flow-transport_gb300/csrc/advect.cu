@@ -334,8 +334,8 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
 }
 
 template <int C, int BM, int COUNT>
-static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float* gvx, float* gvy, float* gvz,
-                         float* ws, cudaStream_t s) {
+static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* dy, float* gd, float* gvx, float* gvy,
+                         float* gvz, float* ws, cudaStream_t s) {
     const int64_t nv = voxels(a.d);
     const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
     const size_t vc = (size_t)nv * C;
@@ -357,7 +357,8 @@ static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float*
         if (a.order == 2) {
             if (!cuda_ok(cudaMemsetAsync(gfwd_sc, 0, sizeof(float) * vc, s), "zero scatter")) return false;
             if (COUNT && !cuda_ok(cudaMemsetAsync(cnt2, 0, sizeof(unsigned int) * nv, s), "zero counter")) return false;
-            k_adv_sl<C, float, BM><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
+            if (!forward_ready)  // else fwd holds this slice's semi-Lagrangian grid already
+                k_adv_sl<C, float, BM><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
             k_adv_bwd_back<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
                                                                       dyb, gdb, gfwd_sc, cnt2, gdir, glut);
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
@@ -369,7 +370,7 @@ static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float*
                                                                      nullptr, gd_sc, cnt3, glut);
         }
         k_adv_bwd_density<C, COUNT != 0><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
-        if (!launched(a.order == 2 ? 4 : 2, "advect gradient launch")) return false;
+        if (!launched(a.order == 2 ? (forward_ready ? 3 : 4) : 2, "advect gradient launch")) return false;
     }
     const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
                           (int64_t)a.d.x * a.d.y * (a.d.z + 1);
@@ -379,27 +380,27 @@ static bool adv_bwd_impl(const AdvectArgs& a, const float* dy, float* gd, float*
 }
 
 template <int C>
-static bool adv_bwd_c(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy, float* gvz,
-                      float* ws, cudaStream_t s) {
+static bool adv_bwd_c(const AdvectArgs& a, bool exact, bool fr, const float* dy, float* gd, float* gvx, float* gvy,
+                      float* gvz, float* ws, cudaStream_t s) {
     switch (a.boundary) {
         case BM_BORDER:
-            return exact ? adv_bwd_impl<C, BM_BORDER, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_BORDER, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+            return exact ? adv_bwd_impl<C, BM_BORDER, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_BORDER, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
         case BM_CLAMP:
-            return exact ? adv_bwd_impl<C, BM_CLAMP, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_CLAMP, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+            return exact ? adv_bwd_impl<C, BM_CLAMP, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_CLAMP, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
         default:
-            return exact ? adv_bwd_impl<C, BM_WRAP, 0>(a, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_WRAP, 1>(a, dy, gd, gvx, gvy, gvz, ws, s);
+            return exact ? adv_bwd_impl<C, BM_WRAP, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
+                         : adv_bwd_impl<C, BM_WRAP, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
     }
 }
 
-bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
-                       float* gvz, float* ws, cudaStream_t s) {
+bool launch_advect_bwd(const AdvectArgs& a, bool exact, bool forward_ready, const float* dy, float* gd, float* gvx,
+                       float* gvy, float* gvz, float* ws, cudaStream_t s) {
     if (!advect_size_ok(a.d)) return false;
-    if (a.C == 4) return adv_bwd_c<4>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
-    if (a.C == 2) return adv_bwd_c<2>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
-    return adv_bwd_c<1>(a, exact, dy, gd, gvx, gvy, gvz, ws, s);
+    if (a.C == 4) return adv_bwd_c<4>(a, exact, forward_ready, dy, gd, gvx, gvy, gvz, ws, s);
+    if (a.C == 2) return adv_bwd_c<2>(a, exact, forward_ready, dy, gd, gvx, gvy, gvz, ws, s);
+    return adv_bwd_c<1>(a, exact, forward_ready, dy, gd, gvx, gvy, gvz, ws, s);
 }
 
 // ---- allocation-free advection ---------------------------------------------------

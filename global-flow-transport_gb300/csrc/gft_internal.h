@@ -131,8 +131,10 @@ struct AdvectArgs {
     int order, clamp, boundary;
 };
 bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s);
-bool launch_advect_bwd(const AdvectArgs& a, bool exact, const float* dy, float* gd, float* gvx, float* gvy,
-                       float* gvz, float* ws, cudaStream_t s);
+// forward_ready: ws starts with the semi-Lagrangian grid of launch_advect_fwd
+// (order 2, N == 1), which is then not recomputed.
+bool launch_advect_bwd(const AdvectArgs& a, bool exact, bool forward_ready, const float* dy, float* gd, float* gvx,
+                       float* gvy, float* gvz, float* ws, cudaStream_t s);
 
 // pipeline fusions (compose.cu)
 bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st);

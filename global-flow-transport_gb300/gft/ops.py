@@ -800,11 +800,15 @@ def reduce_grid_blend_grad(output_grad, output, input, blending_mode='BEER_LAMBE
 
 
 # ------------------------------------------------------------------ advection
-def _advect_fwd(d, vx, vy, vz, dt, order, clamp, boundary):
+FORWARD_READY = 0x200  # GFT_GRAD_FORWARD_READY
+
+
+def _advect_fwd(d, vx, vy, vz, dt, order, clamp, boundary, ws=None):
     lib = _lib.load()
     shape = _lib.i64(d.shape)
     out = torch.empty(d.shape, dtype=torch.float32, device=d.device)
-    ws = _workspace(lib.gft_advect_workspace_size(shape, order), d.device)
+    if ws is None:
+        ws = _workspace(lib.gft_advect_workspace_size(shape, order), d.device)
     with torch.cuda.device(d.device):
         st = lib.gft_advect(_p(d), _dtype_code(d), shape, _p(vx), _p(vy), _p(vz), float(dt), order, clamp, boundary,
                             _p(out), _p(ws), ws.numel(), _stream(d.device))
@@ -812,12 +816,19 @@ def _advect_fwd(d, vx, vy, vz, dt, order, clamp, boundary):
     return out
 
 
-def _advect_bwd(d, vx, vy, vz, dy, dt, order, clamp, boundary, gmode):
+def _advect_grad_workspace(shape, order, device):
+    return _workspace(_lib.load().gft_advect_grad_workspace_size(_lib.i64(shape), order), device)
+
+
+def _advect_bwd(d, vx, vy, vz, dy, dt, order, clamp, boundary, gmode, ws=None):
+    """ws: the workspace the forward ran in (gmode then carries FORWARD_READY),
+    else a new one."""
     lib = _lib.load()
     shape = _lib.i64(d.shape)
     gd = torch.empty(d.shape, dtype=torch.float32, device=d.device)
     gvx, gvy, gvz = (torch.empty(v.shape, dtype=torch.float32, device=d.device) for v in (vx, vy, vz))
-    ws = _workspace(lib.gft_advect_grad_workspace_size(shape, order), d.device)
+    if ws is None:
+        ws = _advect_grad_workspace(d.shape, order, d.device)
     with torch.cuda.device(d.device):
         st = lib.gft_advect_grad(_p(d), shape, _p(vx), _p(vy), _p(vz), float(dt), order, clamp, boundary, gmode,
                                  _p(dy), _p(gd), _p(gvx), _p(gvy), _p(gvz), _p(ws), ws.numel(), _stream(d.device))
@@ -837,7 +848,13 @@ class _Advect(torch.autograd.Function):
     @staticmethod
     def forward(ctx, d, vx, vy, vz, dt, order, clamp, boundary, storage_dtype):
         ds = _storage(d, storage_dtype)
-        y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary)
+        # MacCormack on one fp32 slice: run the forward in the gradient's
+        # workspace and keep it, so that the backward reads the intermediate
+        # semi-Lagrangian grid instead of recomputing it
+        ctx.ws = None
+        if any(ctx.needs_input_grad[:4]) and order == 2 and ds.shape[0] == 1 and ds is d and d.dtype == torch.float32:
+            ctx.ws = _advect_grad_workspace(d.shape, order, d.device)
+        y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary, ws=ctx.ws)
         ctx.save_for_backward(d, vx, vy, vz)
         ctx.args = (dt, order, clamp, boundary)
         return y
@@ -846,8 +863,10 @@ class _Advect(torch.autograd.Function):
     def backward(ctx, dy):
         d, vx, vy, vz = ctx.saved_tensors
         dt, order, clamp, boundary = ctx.args
+        gmode = GRAD[get_grad_mode()]
+        ws, ctx.ws = ctx.ws, None
         gd, gvx, gvy, gvz = _advect_bwd(d.float().contiguous(), vx, vy, vz, _cuda(dy, 'output_grad'), dt, order,
-                                        clamp, boundary, GRAD[get_grad_mode()])
+                                        clamp, boundary, gmode | (FORWARD_READY if ws is not None else 0), ws=ws)
         return gd.to(d.dtype), gvx.view_as(vx), gvy.view_as(vy), gvz.view_as(vz), None, None, None, None, None
 
 

@@ -254,7 +254,14 @@ gft_status gft_advect_noalloc(
     int32_t order, int32_t clamp, int32_t boundary, float* output, void* stream);
 /* Gradient of gft_advect w.r.t. density and the staggered velocity components,
  * all overwritten.  In GFT_GRAD_REFERENCE mode each lookup's input gradient is
- * divided by its per-voxel sample count as the reference SampleGridLutGrad does. */
+ * divided by its per-voxel sample count as the reference SampleGridLutGrad does.
+ * grad_mode | GFT_GRAD_FORWARD_READY (order 2, N == 1 only): the workspace is
+ * the one gft_advect was given for the same fp32 density, velocity, dt and
+ * boundary, and still holds the MacCormack intermediate (the semi-Lagrangian
+ * grid) that gft_advect left at its start; the gradient reads it instead of
+ * recomputing it.  No counterpart in the reference, whose gradient re-runs its
+ * lookups. */
+#define GFT_GRAD_FORWARD_READY 0x200
 size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t order);
 gft_status gft_advect_grad(
     const float* density, const int64_t density_shape[5],

@@ -365,6 +365,27 @@ def test_advect(ops, order, clamp, boundary, mode):
 UNEVEN = [(13, 9, 11), (7, 6, 5), (11, 12, 16)]  # (depth samples, height, width) per camera
 
 
+def test_advect_backward_reuses_forward_intermediate(ops):
+    """MacCormack on one fp32 slice: autograd runs the forward in the gradient
+    workspace and the backward reads its semi-Lagrangian grid
+    (GFT_GRAD_FORWARD_READY); the gradients equal those of a backward that
+    recomputes it (float atomics: summation order only)."""
+    from gft import synthetic as syn
+    shape = (10, 12, 9)
+    d = cuda(syn.plume_density(shape, 31))
+    vx, vy, vz = (cuda(v) for v in syn.curl_velocity(shape, 32))
+    dy = cuda(np.random.default_rng(33).standard_normal((1,) + shape + (1,)).astype(np.float32))
+    for mode in ('REFERENCE', 'EXACT'):
+        ts = [t.clone().requires_grad_(True) for t in (d, vx, vy, vz)]
+        with ops.grad_mode(mode):
+            y = ops.advect(*ts, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP')
+            y.backward(dy)
+            ref = ops._advect_bwd(d, vx, vy, vz, dy, 1.0, 2, ops.CLAMP['MC_SMOOTH'], ops.BOUNDARY['CLAMP'],
+                                  ops.GRAD[mode])
+        for t, r in zip(ts, ref):
+            assert rel_l2(np_(t.grad).reshape(-1), np_(r).reshape(-1)) <= 1e-6
+
+
 def _uneven_scene(C, seed, batch=1):
     _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
     x = np.concatenate([small_grid((10, 14, 12), C, seed + b) for b in range(batch)], 0) * 0.4

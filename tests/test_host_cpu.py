@@ -102,6 +102,12 @@ def test_argument_errors_without_a_gpu(lib):
     st = L.gft_advect(ctypes.c_void_p(1), 0, lib.i64([1, 8, 8, 8, 1]), ctypes.c_void_p(1), ctypes.c_void_p(1),
                       ctypes.c_void_p(1), 1.0, 3, 0, 1, ctypes.c_void_p(1), None, 0, None)
     assert st == lib.ERR_INVALID_ARGUMENT
+    # the forward's intermediate is reused only for MacCormack on one batch slice
+    one = ctypes.c_void_p(1)
+    for shape, order in (([1, 8, 8, 8, 1], 1), ([2, 8, 8, 8, 1], 2)):
+        st = L.gft_advect_grad(one, lib.i64(shape), one, one, one, 1.0, order, 0, 1, 1 | 0x200, one, one, one, one,
+                               one, one, 1 << 30, None)
+        assert st == lib.ERR_INVALID_ARGUMENT and b'FORWARD_READY' in L.gft_last_error()
 
 
 def test_workspace_sizes(lib):
