@@ -829,7 +829,8 @@ size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t or
     if (!grid_shape_ok(density_shape, why)) return 0;
     const size_t nv = (size_t)density_shape[1] * density_shape[2] * density_shape[3];
     const size_t C = (size_t)density_shape[4];
-    return align256(sizeof(float) * (nv * (4 * C + 3)) + sizeof(unsigned int) * 2 * nv);
+    // + 16 bytes: the single-channel layout pads two regions to even offsets
+    return align256(sizeof(float) * (nv * (4 * C + 3)) + sizeof(unsigned int) * 2 * nv + 16);
 }
 
 gft_status gft_advect_grad(const float* density, const int64_t density_shape[5], const float* vel_x,

@@ -180,6 +180,43 @@ bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t 
 }
 
 // ---- adjoint ---------------------------------------------------------------------
+// Single-channel reference-mode scatters keep each voxel's gradient sum and
+// its sample count side by side (float2: sum, count) and add both with one
+// vector reduction per corner instead of a float and an integer reduction;
+// counts stay far below 2^24, where float counting is exact.
+// COUNT: 0 exact (no counts), 1 uint counters, 2 packed (C == 1 only)
+template <int C, int COUNT>
+constexpr bool packed_count() {
+    return C == 1 && COUNT == 2;
+}
+
+// scatter_linear<1, BM, 1> into interleaved (sum, count) pairs
+template <int BM>
+__device__ __forceinline__ void scatter_linear_packed(float* __restrict__ buf, Dims d, float px, float py, float pz,
+                                                      float val) {
+    if constexpr (BM == BM_BORDER) {
+        if (!(px > -1.f && px < (float)d.x && py > -1.f && py < (float)d.y && pz > -1.f && pz < (float)d.z)) return;
+    }
+    const Corners c = corners<BM>(px, py, pz, d);
+    const float cw[3] = {c.wx, c.wy, c.wz};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
+        const bool ok = (sx ? c.vx1 : c.vx0) && (sy ? c.vy1 : c.vy0) && (sz ? c.vz1 : c.vz0);
+        if (BM != BM_BORDER || ok) {
+            const float w = (sx ? cw[0] : 1.f - cw[0]) * (sy ? cw[1] : 1.f - cw[1]) * (sz ? cw[2] : 1.f - cw[2]);
+            const int64_t f = flat3(sx ? c.x1 : c.x0, sy ? c.y1 : c.y0, sz ? c.z1 : c.z0, d);
+            atomicAdd(reinterpret_cast<float2*>(buf) + f, make_float2(val * w, 1.f));
+        }
+    }
+}
+
+// (sum / count where count > 0) of a packed pair, as the uint-counter form
+__device__ __forceinline__ float packed_normalised(const float* __restrict__ buf, int64_t t) {
+    const float2 v = reinterpret_cast<const float2*>(buf)[t];
+    return v.y > 0.f ? v.x * (1.0f / v.y) : v.x;
+}
+
 // Stage B (MacCormack only): route the output gradient through the MC_SMOOTH
 // `where` (TF semantics: each branch gets the gradient where selected, none to
 // min/max), store the direct density term 0.5*g_corr, scatter the back-lookup
@@ -215,7 +252,10 @@ __global__ void __launch_bounds__(AD_THREADS)
     }
     store<C>(gd, t, vscale(gcorr, 0.5f));
     store<C>(gdir, t, g);
-    scatter_linear<C, BM, COUNT>(gfwd_sc, cnt2, dm, bx, by, bz, gback);
+    if constexpr (packed_count<C, COUNT>())
+        scatter_linear_packed<BM>(gfwd_sc, dm, bx, by, bz, gback.v[0]);
+    else
+        scatter_linear<C, BM, COUNT>(gfwd_sc, cnt2, dm, bx, by, bz, gback);
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
     for (int i = 0; i < C; ++i) {
@@ -257,14 +297,22 @@ __global__ void __launch_bounds__(AD_THREADS)
         fetch_grad<C, BM>(d, dm, px, py, pz, ddx, ddy, ddz);
     }
     if (!first_order) {
-        Vec<C> sc = loadf<C>(gfwd_sc, t);
-        if (COUNT) {
-            const unsigned int n = cnt2[t];
-            if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+        Vec<C> sc;
+        if constexpr (packed_count<C, COUNT>()) {
+            sc.v[0] = packed_normalised(gfwd_sc, t);
+        } else {
+            sc = loadf<C>(gfwd_sc, t);
+            if (COUNT) {
+                const unsigned int n = cnt2[t];
+                if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+            }
         }
         gf = vadd(gf, sc);
     }
-    scatter_linear<C, BM, COUNT>(gd_sc, cnt3, dm, px, py, pz, gf);
+    if constexpr (packed_count<C, COUNT>())
+        scatter_linear_packed<BM>(gd_sc, dm, px, py, pz, gf.v[0]);
+    else
+        scatter_linear<C, BM, COUNT>(gd_sc, cnt3, dm, px, py, pz, gf);
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
     for (int i = 0; i < C; ++i) {
@@ -279,15 +327,21 @@ __global__ void __launch_bounds__(AD_THREADS)
 }
 
 // Stage D: density gradient = direct term + (normalised) forward-lookup scatter.
-template <int C, bool NORM>
+template <int C, int COUNT>
 __global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restrict__ gd_sc,
                                   const unsigned int* __restrict__ cnt3, int64_t nv) {
+    constexpr bool NORM = COUNT != 0;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nv) return;
-    Vec<C> sc = loadf<C>(gd_sc, t);
-    if (NORM) {
-        const unsigned int n = cnt3[t];
-        if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+    Vec<C> sc;
+    if constexpr (packed_count<C, COUNT>()) {
+        sc.v[0] = packed_normalised(gd_sc, t);
+    } else {
+        sc = loadf<C>(gd_sc, t);
+        if (NORM) {
+            const unsigned int n = cnt3[t];
+            if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+        }
     }
     store<C>(gd, t, vadd(loadf<C>(gd, t), sc));
 }
@@ -339,24 +393,30 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
     const int64_t nv = voxels(a.d);
     const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
     const size_t vc = (size_t)nv * C;
+    // packed: the two scatter targets hold (sum, count) pairs at even offsets
+    // (8-byte aligned with ws), no counters
+    constexpr bool PACK = packed_count<C, COUNT>();
+    const size_t sc_floats = PACK ? 2 * vc : vc, vc_pad = PACK ? (vc + 1) & ~size_t(1) : vc;
     float* fwd = ws;
-    float* gfwd_sc = fwd + vc;
-    float* gdir = gfwd_sc + vc;
-    float* gd_sc = gdir + vc;
-    float* glut = gd_sc + vc;
-    unsigned int* cnt2 = reinterpret_cast<unsigned int*>(glut + (size_t)nv * 3);
-    unsigned int* cnt3 = cnt2 + nv;
+    float* gfwd_sc = fwd + vc_pad;
+    float* gdir = gfwd_sc + sc_floats;
+    float* gd_sc = gdir + vc_pad;
+    float* glut = gd_sc + sc_floats;
+    unsigned int* cnt2 = PACK ? nullptr : reinterpret_cast<unsigned int*>(glut + (size_t)nv * 3);
+    unsigned int* cnt3 = PACK ? nullptr : cnt2 + nv;
     if (!cuda_ok(cudaMemsetAsync(glut, 0, sizeof(float) * nv * 3, s), "zero lookup gradient")) return false;
     const float* dens = reinterpret_cast<const float*>(a.density);
     for (int b = 0; b < a.N; ++b) {
         const float* db = dens + (size_t)b * vc;
         const float* dyb = dy + (size_t)b * vc;
         float* gdb = gd + (size_t)b * vc;
-        if (!cuda_ok(cudaMemsetAsync(gd_sc, 0, sizeof(float) * vc, s), "zero scatter")) return false;
-        if (COUNT && !cuda_ok(cudaMemsetAsync(cnt3, 0, sizeof(unsigned int) * nv, s), "zero counter")) return false;
+        if (!cuda_ok(cudaMemsetAsync(gd_sc, 0, sizeof(float) * sc_floats, s), "zero scatter")) return false;
+        if (COUNT && !PACK && !cuda_ok(cudaMemsetAsync(cnt3, 0, sizeof(unsigned int) * nv, s), "zero counter"))
+            return false;
         if (a.order == 2) {
-            if (!cuda_ok(cudaMemsetAsync(gfwd_sc, 0, sizeof(float) * vc, s), "zero scatter")) return false;
-            if (COUNT && !cuda_ok(cudaMemsetAsync(cnt2, 0, sizeof(unsigned int) * nv, s), "zero counter")) return false;
+            if (!cuda_ok(cudaMemsetAsync(gfwd_sc, 0, sizeof(float) * sc_floats, s), "zero scatter")) return false;
+            if (COUNT && !PACK && !cuda_ok(cudaMemsetAsync(cnt2, 0, sizeof(unsigned int) * nv, s), "zero counter"))
+                return false;
             if (!forward_ready)  // else fwd holds this slice's semi-Lagrangian grid already
                 k_adv_sl<C, float, BM><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
             k_adv_bwd_back<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
@@ -369,7 +429,7 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
                                                                      a.clamp == CLAMP_NEGATIVE, dyb, nullptr,
                                                                      nullptr, gd_sc, cnt3, glut);
         }
-        k_adv_bwd_density<C, COUNT != 0><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
+        k_adv_bwd_density<C, COUNT><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
         if (!launched(a.order == 2 ? (forward_ready ? 3 : 4) : 2, "advect gradient launch")) return false;
     }
     const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
@@ -379,19 +439,23 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
     return launched(1, "velocity gradient launch");
 }
 
+template <int C, int BM>
+static bool adv_bwd_bm(const AdvectArgs& a, bool exact, bool fr, const float* dy, float* gd, float* gvx, float* gvy,
+                       float* gvz, float* ws, cudaStream_t s) {
+    if (exact) return adv_bwd_impl<C, BM, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+    if constexpr (C == 1) {
+        if ((reinterpret_cast<uintptr_t>(ws) & 7u) == 0) return adv_bwd_impl<C, BM, 2>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+    }
+    return adv_bwd_impl<C, BM, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+}
+
 template <int C>
 static bool adv_bwd_c(const AdvectArgs& a, bool exact, bool fr, const float* dy, float* gd, float* gvx, float* gvy,
                       float* gvz, float* ws, cudaStream_t s) {
     switch (a.boundary) {
-        case BM_BORDER:
-            return exact ? adv_bwd_impl<C, BM_BORDER, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_BORDER, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
-        case BM_CLAMP:
-            return exact ? adv_bwd_impl<C, BM_CLAMP, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_CLAMP, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
-        default:
-            return exact ? adv_bwd_impl<C, BM_WRAP, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s)
-                         : adv_bwd_impl<C, BM_WRAP, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+        case BM_BORDER: return adv_bwd_bm<C, BM_BORDER>(a, exact, fr, dy, gd, gvx, gvy, gvz, ws, s);
+        case BM_CLAMP: return adv_bwd_bm<C, BM_CLAMP>(a, exact, fr, dy, gd, gvx, gvy, gvz, ws, s);
+        default: return adv_bwd_bm<C, BM_WRAP>(a, exact, fr, dy, gd, gvx, gvy, gvz, ws, s);
     }
 }
 

@@ -337,10 +337,10 @@ def test_blend(ops, C, blend, keep):
 @pytest.mark.parametrize('order,clamp', [(1, 'NONE'), (2, 'NONE'), (2, 'MC_SMOOTH'), (1, 'NEGATIVE'), (2, 'NEGATIVE')])
 @pytest.mark.parametrize('boundary', BOUNDS)
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
-def test_advect(ops, order, clamp, boundary, mode):
+def test_advect(ops, order, clamp, boundary, mode, shape=(9, 10, 8)):
     from oracle import advect as OA
     rng = np.random.default_rng(50)
-    D, H, W = 9, 10, 8
+    D, H, W = shape
     d = small_grid((D, H, W), 1, 51, positive=(clamp != 'NEGATIVE'))
     vx = (rng.standard_normal((1, D, H, W + 1, 1)) * 0.8).astype(np.float32)
     vy = (rng.standard_normal((1, D, H + 1, W, 1)) * 0.8).astype(np.float32)
@@ -359,6 +359,14 @@ def test_advect(ops, order, clamp, boundary, mode):
     assert rel_l2(np_(dtn.grad)[0], gd) <= GRAD_TOL
     for got, want in zip(vs, (gvx, gvy, gvz)):
         assert rel_l2(np_(got.grad)[0], want) <= GRAD_TOL
+
+
+@pytest.mark.parametrize('order', [1, 2])
+@pytest.mark.parametrize('boundary', BOUNDS)
+def test_advect_odd_voxel_count(ops, order, boundary):
+    """An odd number of voxels: the single-channel reference-mode adjoint pads
+    its packed (sum, count) regions to even offsets."""
+    test_advect(ops, order, 'MC_SMOOTH' if order == 2 else 'NONE', boundary, 'REFERENCE', shape=(9, 11, 7))
 
 
 # ------------------------------------------------------------------ raymarch, uneven camera batches
