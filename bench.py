@@ -428,13 +428,44 @@ def _profiled_traffic():
     return None
 
 
+def _clipped_samples(step):
+    """Ray samples inside the raymarch's clipped step ranges at this workload
+    (the kernels' BORDER slab test, in float64): the samples the forward
+    stores and the adjoint reads back."""
+    import numpy as np
+    D, H, W = step.res
+    gz, gy, gx = step.shape
+    m = np.asarray(step.M, np.float64)[0].T
+    ys, xs = np.meshgrid(np.arange(H) + 0.5, np.arange(W) + 0.5, indexing='ij')
+    zmax = max(D - 1, 1)
+    hi = np.array([gx, gy, gz], np.float64) + 0.55
+    total = 0
+    for c in range(len(step.cams)):
+        inv = np.linalg.inv(np.asarray(step.V, np.float64)[c].T @ m) @ np.linalg.inv(np.asarray(step.P, np.float64)[c].T)
+
+        def os_at(zi):
+            ndc = np.stack([xs / W * 2 - 1, ys / H * 2 - 1, np.full_like(xs, zi / D * 2 - 1), np.ones_like(xs)], -1)
+            h = ndc @ inv.T
+            return h[..., :3] / h[..., 3:4]
+        near = os_at(0.5)
+        st = (os_at(zmax + 0.5) - near) / zmax
+        with np.errstate(divide='ignore', invalid='ignore'):
+            a, b = (-1.05 - near) / st, (hi - near) / st
+        t0 = np.maximum(0.0, np.max(np.minimum(a, b), -1))
+        t1 = np.minimum(D - 1.0, np.min(np.maximum(a, b), -1))
+        i0, i1 = np.maximum(0, np.floor(t0) - 1), np.minimum(D - 1, np.ceil(t1) + 1)
+        total += int(np.sum(np.where(t0 <= t1, i1 - i0 + 1, 0)))
+    return total
+
+
 def kernel_roofline(step, dev, timed):
     """Times the render kernels alone with CUDA events on their stream (L2
     flushed before each launch) and converts the algorithmic bytes per launch
     into GB/s against the measured HBM peak.  The dominant kernel is the
     raymarch adjoint's scatter pass (k_raymarch_scatter, one launch for the 5
-    views), timed with its per-camera weight sums precomputed
-    (GFT_GRAD_WEIGHTS_READY: a gradient memset plus the scatter launch)."""
+    views) as the step runs it: reading the samples the forward stored, with
+    its per-camera weight sums precomputed (GFT_GRAD_WEIGHTS_READY: a gradient
+    memset plus the scatter launch)."""
     import numpy as np
     import torch
     from gft import ops
@@ -448,39 +479,50 @@ def kernel_roofline(step, dev, timed):
     D, H, W = step.res
     V = len(step.cams)
     mode = ops.get_grad_mode()
-    fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid)
+    shape5 = (data.shape[0],) + tuple(grid) + (data.shape[-1],)
+    smp = ops._samples_buffer(shape5, V, step.res, True, dev)
+    fwd = lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid,
+                                    samples=smp)
     y = fwd()
     torch.manual_seed(0)
     dy = torch.randn_like(y) * 1e-3
     bwd = lambda m: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                      ops.GRAD[m], grid=grid)
-    shape5 = (data.shape[0],) + tuple(grid) + (data.shape[-1],)
+                                      ops.GRAD[m], grid=grid, samples=smp)
     weights = lambda: ops._raymarch_weights(shape5, data.device, step.M, step.V, step.P, step.F, step.res, 0, True)
     ws = weights()
     scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                        ops.GRAD['REFERENCE'], weights=ws, grid=grid)
+                                        ops.GRAD['REFERENCE'], weights=ws, grid=grid, samples=smp)
+    resample = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                         ops.GRAD['REFERENCE'], weights=ws, grid=grid)
     for _ in range(2):
-        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter()
+        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter(), resample()
     tf = float(np.median(timed(fwd, 7)))
     tb_ref = float(np.median(timed(lambda: bwd('REFERENCE'), 7)))
     tb_ex = float(np.median(timed(lambda: bwd('EXACT'), 7)))
     tw = float(np.median(timed(weights, 7)))
     ts = float(np.median(timed(scatter, 7)))
+    tr = float(np.median(timed(resample, 7)))
     nvox = int(np.prod(step.shape))
     s, C = 4, 4
     pix = V * H * W
     samples = pix * D
-    bytes_fwd = nvox * C * s + pix * C * 4
-    # scatter pass: grid read, image + adjoint read, per-camera reciprocal
-    # weights read, gradient read-modify-write
-    bytes_scatter = nvox * C * s + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
-    bytes_exact = nvox * C * s + 2 * pix * C * 4 + 2 * nvox * C * 4
+    stored = _clipped_samples(step) * C * 4  # bytes of the sample store written / read
+    bytes_fwd = nvox * C * s + pix * C * 4 + stored
+    # scatter pass: stored samples read, image + adjoint read, per-camera
+    # reciprocal weights read, gradient read-modify-write
+    bytes_scatter = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
+    bytes_resample = nvox * C * s + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
+    bytes_exact = stored + 2 * pix * C * 4 + 2 * nvox * C * 4
     bytes_weights = 2 * V * nvox * 4
     kern = {
         'raymarch_fwd': {'ms': tf, 'alg_bytes': bytes_fwd, 'GBps': bytes_fwd / tf / 1e6,
                          'samples_per_s': samples / tf * 1e3},
         'raymarch_bwd_scatter': {'ms': ts, 'alg_bytes': bytes_scatter, 'GBps': bytes_scatter / ts / 1e6,
-                                 'samples_per_s': samples / ts * 1e3, 'what': 'reference normalisation, weights ready'},
+                                 'samples_per_s': samples / ts * 1e3,
+                                 'what': 'reference normalisation, weights ready, stored samples'},
+        'raymarch_bwd_scatter_resampling': {'ms': tr, 'alg_bytes': bytes_resample, 'GBps': bytes_resample / tr / 1e6,
+                                            'what': 'the same pass re-sampling the grid (no sample store)'},
+        'raymarch_samples_stored_bytes': stored,
         'raymarch_bwd_weights': {'ms': tw, 'alg_bytes': bytes_weights, 'GBps': bytes_weights / tw / 1e6,
                                  'samples_per_s': samples / tw * 1e3},
         'raymarch_bwd_reference': {'ms': tb_ref, 'what': 'whole op: weights + inversion + scatter'},
@@ -495,9 +537,10 @@ def kernel_roofline(step, dev, timed):
                          'traffic': traffic, 'alg_bytes': bytes_scatter,
                          'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, '
                                            'profiles/raymarch_scatter_cfg2.md' if traffic else None,
-                         'note': 'algorithmic bytes = compulsory unique traffic; the 60 MB grid stays in the '
-                                 '129 MB L2, and the pass is bound by the L2 sector throughput of its trilinear '
-                                 'gradient reductions (8 per sample), not by HBM'},
+                         'note': 'algorithmic bytes = compulsory unique traffic (the stored samples the pass '
+                                 'reads, image and adjoint, reciprocal weights, gradient read-modify-write); the '
+                                 'pass is bound by the L1/L2 path of its merged trilinear gradient reductions and '
+                                 'by latency, not by HBM'},
             'kernels': kern}
 
 
@@ -517,14 +560,15 @@ def kernel_only(args):
         light = d * (step.shadow(d) * step.falloff_col + step.ambient)
         data = ops.to_bricks((torch.cat([light, d], dim=-1) * step.depth_step).contiguous())
         grid = step.shape
-        y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid)
+        smp = ops._samples_buffer((1,) + tuple(grid) + (4,), len(step.cams), step.res, True, dev)
+        y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid, samples=smp)
         dy = torch.randn_like(y) * 1e-3
     gm = ops.GRAD[ops.get_grad_mode()]
     fns = {
         'raymarch_fwd': lambda: ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                                  grid=grid),
+                                                  grid=grid, samples=smp),
         'raymarch_bwd': lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0,
-                                                  True, gm, grid=grid),
+                                                  True, gm, grid=grid, samples=smp),
         'advect_fwd': lambda: ops._advect_fwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
                                               step.s_vz.detach(), 1.0, 2, 1, 1),
         'advect_bwd': lambda: ops._advect_bwd(step.s_d.detach(), step.s_vx.detach(), step.s_vy.detach(),
@@ -538,7 +582,7 @@ def kernel_only(args):
                                    0, True)
         fns['raymarch_scatter'] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
                                                             0, 0, True, ops.GRAD['REFERENCE'], weights=ws,
-                                                            grid=grid)
+                                                            grid=grid, samples=smp)
     fn = fns[args.kernel_only]
     for _ in range(args.repeat):
         fn()

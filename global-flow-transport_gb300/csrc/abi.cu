@@ -210,12 +210,55 @@ const char* gft_version(void) { return "gft-gb300 0.1 (sm_103a)"; }
 unsigned long long gft_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------- raymarch
+static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                    const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                    const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                    const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
+                                    int32_t blending_mode, int32_t separate_camera_batch, float* output,
+                                    float* samples, size_t samples_bytes, void* stream);
+
 gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, const int64_t input_shape[5],
                                        const float* matrix_m, int32_t num_m, const float* matrix_v,
                                        const float* matrix_p, const float* frustum, int32_t num_cameras,
                                        const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
                                        int32_t blending_mode, int32_t separate_camera_batch, float* output,
                                        void* stream) {
+    return raymarch_fwd_impl(input, input_dtype, input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum,
+                             num_cameras, output_shape, interpolation, boundary, blending_mode,
+                             separate_camera_batch, output, nullptr, 0, stream);
+}
+
+gft_status gft_raymarch_grid_transform_store(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                             const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                             const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                             const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
+                                             int32_t blending_mode, int32_t separate_camera_batch, float* output,
+                                             float* samples, size_t samples_bytes, void* stream) {
+    if (interpolation != GFT_FILTER_LINEAR)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "the sample store supports LINEAR interpolation only");
+    if (samples == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    return raymarch_fwd_impl(input, input_dtype, input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum,
+                             num_cameras, output_shape, interpolation, boundary, blending_mode,
+                             separate_camera_batch, output, samples, samples_bytes, stream);
+}
+
+size_t gft_raymarch_grid_transform_samples_size(const int64_t input_shape[5], int32_t num_cameras,
+                                                const int32_t output_shape[3], int32_t separate_camera_batch) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why) || !channels_ok(input_shape[4]) || output_shape == nullptr ||
+        output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1 || num_cameras < 1)
+        return 0;
+    std::vector<Pair> pairs((size_t)input_shape[0] * (separate_camera_batch ? (size_t)num_cameras : 1));
+    set_uniform_images(pairs, output_shape[0], output_shape[1], output_shape[2]);
+    return align256(sizeof(float) * (size_t)raymarch_samples_floats(pairs, (int)input_shape[4]));
+}
+
+static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                    const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                    const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                    const int32_t output_shape[3], int32_t interpolation, int32_t boundary,
+                                    int32_t blending_mode, int32_t separate_camera_batch, float* output,
+                                    float* samples, size_t samples_bytes, void* stream) {
     std::string why;
     if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
@@ -251,6 +294,11 @@ gft_status gft_raymarch_grid_transform(const void* input, int32_t input_dtype, c
                             separate_camera_batch != 0);
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
+    if (samples != nullptr) {
+        if (samples_bytes < sizeof(float) * (size_t)raymarch_samples_floats(pairs, a.C))
+            return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
+        a.samples_out = samples;
+    }
     if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
     return GFT_OK;
 }
@@ -264,6 +312,15 @@ size_t gft_raymarch_grid_transform_grad_workspace_size(const int64_t input_shape
     return align256(sizeof(float) * cells * pairs);
 }
 
+static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                     const float* output, const float* output_grad, const float* matrix_m,
+                                     int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+                                     int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                     int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
+                                     size_t samples_bytes, float* input_grad, void* workspace,
+                                     size_t workspace_bytes, void* stream);
+
 gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dtype, const int64_t input_shape[5],
                                             const float* output, const float* output_grad, const float* matrix_m,
                                             int32_t num_m, const float* matrix_v, const float* matrix_p,
@@ -271,6 +328,33 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
                                             int32_t interpolation, int32_t boundary, int32_t blending_mode,
                                             int32_t separate_camera_batch, int32_t grad_mode, float* input_grad,
                                             void* workspace, size_t workspace_bytes, void* stream) {
+    return raymarch_grad_impl(input, input_dtype, input_shape, output, output_grad, matrix_m, num_m, matrix_v,
+                              matrix_p, frustum, num_cameras, output_shape, interpolation, boundary, blending_mode,
+                              separate_camera_batch, grad_mode, nullptr, 0, input_grad, workspace, workspace_bytes,
+                              stream);
+}
+
+gft_status gft_raymarch_grid_transform_grad_stored(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5], const float* output,
+    const float* output_grad, const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3], int32_t interpolation,
+    int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
+    size_t samples_bytes, float* input_grad, void* workspace, size_t workspace_bytes, void* stream) {
+    if (samples == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    return raymarch_grad_impl(input, input_dtype, input_shape, output, output_grad, matrix_m, num_m, matrix_v,
+                              matrix_p, frustum, num_cameras, output_shape, interpolation, boundary, blending_mode,
+                              separate_camera_batch, grad_mode, samples, samples_bytes, input_grad, workspace,
+                              workspace_bytes, stream);
+}
+
+static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                     const float* output, const float* output_grad, const float* matrix_m,
+                                     int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+                                     int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                     int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
+                                     size_t samples_bytes, float* input_grad, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
     std::string why;
     if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
@@ -313,6 +397,11 @@ gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dty
                             separate_camera_batch != 0);
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
+    if (samples != nullptr) {
+        if (samples_bytes < sizeof(float) * (size_t)raymarch_samples_floats(pairs, a.C))
+            return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
+        a.samples_in = samples;
+    }
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
     if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
                              cnt, as_stream(stream)))

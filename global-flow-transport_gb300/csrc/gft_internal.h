@@ -25,6 +25,7 @@ struct PairTable {
     // sizes share one launch
     int rw[MAX_PAIRS], rh[MAX_PAIRS], rd[MAX_PAIRS];
     int64_t pix0[MAX_PAIRS];
+    int64_t smp0[MAX_PAIRS];  // raymarch sample store: first float of each pair
     int tile0[MAX_PAIRS + 1];
     int pair_base;            // global index of pair 0 of this launch
     int n;                    // pairs in this launch
@@ -74,7 +75,13 @@ struct RaymarchArgs {
     int filter, boundary, blend;
     int layout = LAYOUT_FLAT;  // cell layout of the input and its gradient
     int n_slots;  // output slots = N * (separate ? V : 1)
+    // Sample store (LINEAR only): the forward writes each clipped-range sample,
+    // the adjoint reads it instead of re-sampling (raymarch_samples_floats).
+    float* samples_out = nullptr;
+    const float* samples_in = nullptr;
 };
+// Floats of the sample store of these pairs (uniform or per-pair images).
+int64_t raymarch_samples_floats(const std::vector<Pair>& pairs, int C);
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
 // Per-pair reciprocal weight sums of the reference-normalised adjoint (pass 1).
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s);

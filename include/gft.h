@@ -112,6 +112,34 @@ gft_status gft_raymarch_grid_transform_grad(
     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
     int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
     int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+/* Sample store (no counterpart in the reference, whose gradient re-samples the
+ * grid): gft_raymarch_grid_transform_store is gft_raymarch_grid_transform
+ * (LINEAR interpolation) that also writes every ray sample it blends, within
+ * each ray's clipped step range, into `samples` (an internal layout of
+ * gft_raymarch_grid_transform_samples_size bytes: per camera, per 8x16-pixel
+ * tile, per depth sample, 128 x C floats).  gft_raymarch_grid_transform_grad_stored
+ * is gft_raymarch_grid_transform_grad reading those samples instead of
+ * re-sampling the input; input, geometry and output_shape must be those of
+ * the store call, with the input unchanged in between.  The adjoint then uses
+ * the samples at the forward's positions (marched front to back), which
+ * differ from the re-sampled back-to-front positions by float rounding only. */
+size_t gft_raymarch_grid_transform_samples_size(
+    const int64_t input_shape[5], int32_t num_cameras, const int32_t output_shape[3],
+    int32_t separate_camera_batch);
+gft_status gft_raymarch_grid_transform_store(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
+    float* output, float* samples, size_t samples_bytes, void* stream);
+gft_status gft_raymarch_grid_transform_grad_stored(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* output, const float* output_grad,
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
+    int32_t grad_mode, const float* samples, size_t samples_bytes, float* input_grad,
+    void* workspace, size_t workspace_bytes, void* stream);
 /* The geometry-only first pass of the GFT_GRAD_REFERENCE raymarch gradient:
  * per (batch, camera) pair the reciprocals of the per-voxel sums of the
  * trilinear weights of all ray samples (the reference's float sampleCounter,

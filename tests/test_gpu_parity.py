@@ -170,6 +170,54 @@ def test_raymarch_weight_cache_static_cameras(ops):
     assert len(ops._weight_cache['entries']) == 0
 
 
+@pytest.mark.parametrize('C', [1, 4])
+@pytest.mark.parametrize('blend', BLENDS)
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_sample_store(ops, C, blend, boundary, mode):
+    """The backward reading the samples the forward stored equals the backward
+    re-sampling the grid, up to the rounding of the sample positions (forward
+    front to back, adjoint back to front); the forward output is unchanged."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), C, 27) * 0.4
+    dy = cuda(np.random.default_rng(28).standard_normal((1, 3, 9, 11, C)).astype(np.float32))
+    grads, outs = [], []
+    for store in (False, True):
+        ops.set_raymarch_sample_store(store)
+        try:
+            xt = cuda(x).requires_grad_(True)
+            with ops.grad_mode(mode):
+                y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11), 'LINEAR', boundary, blend)
+                y.backward(dy)
+        finally:
+            ops.set_raymarch_sample_store(True)
+        grads.append(np_(xt.grad))
+        outs.append(np_(y))
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(grads[1], grads[0]) <= 1e-5
+
+
+def test_raymarch_sample_store_many_pairs(ops):
+    """More (batch, camera) pairs than one launch table holds (2 x 9 = 18):
+    the store offsets continue across the tables."""
+    _, _, M, V, P, F = scene((10, 14, 12), 9, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 29) * 0.4
+    x = np.concatenate([x, x[:, ::-1].copy()], axis=0)
+    M2 = np.stack([M[0], M[0]]) if np.asarray(M).ndim == 3 else M
+    dy = cuda(np.random.default_rng(30).standard_normal((2, 9, 9, 11, 4)).astype(np.float32))
+    grads = []
+    for store in (False, True):
+        ops.set_raymarch_sample_store(store)
+        try:
+            xt = cuda(x).requires_grad_(True)
+            with ops.grad_mode('REFERENCE'):
+                ops.raymarch_grid_transform(xt, M2, V, P, F, (13, 9, 11)).backward(dy)
+        finally:
+            ops.set_raymarch_sample_store(True)
+        grads.append(np_(xt.grad))
+    assert rel_l2(grads[1], grads[0]) <= 1e-5
+
+
 def test_raymarch_not_separate_batch(ops):
     from oracle import raymarch as RM
     _, _, M, V, P, F = scene((8, 9, 7), 2, (9, 6, 5))

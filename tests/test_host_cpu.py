@@ -72,6 +72,19 @@ def test_argument_errors_without_a_gpu(lib):
     assert st == lib.ERR_WORKSPACE
     assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 0) >= 8 * 8 * 8 * 5 * 4
     assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 1) == 0
+    # sample store: LINEAR only, a large enough store, a store pointer
+    assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == ((8 + 7) // 8) * ((4 + 15) // 16) * 4 \
+        * 128 * 4 * 4
+    st = L.gft_raymarch_grid_transform_store(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 0, 0, 0, 1,
+                                             ctypes.c_void_p(1), ctypes.c_void_p(1), 1 << 20, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'LINEAR' in L.gft_last_error()
+    st = L.gft_raymarch_grid_transform_store(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 1,
+                                             ctypes.c_void_p(1), ctypes.c_void_p(1), 64, None)
+    assert st == lib.ERR_WORKSPACE
+    st = L.gft_raymarch_grid_transform_grad_stored(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1),
+                                                   ctypes.c_void_p(1), p, 1, p, p, f, 1, out, 1, 0, 0, 1, 1, None, 0,
+                                                   ctypes.c_void_p(1), None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT
     # precomputed weight sums are a reference-mode workspace: not with EXACT
     st = L.gft_raymarch_grid_transform_grad(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1), ctypes.c_void_p(1),
                                             p, 1, p, p, f, 1, out, 1, 0, 0, 1, 1 | 0x100, ctypes.c_void_p(1), None,
