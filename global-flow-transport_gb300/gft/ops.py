@@ -388,26 +388,26 @@ class _Raymarch(torch.autograd.Function):
                 key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
                 ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
                                                                                     out_shape, boundary, separate)
-        ctx.samples = None
+        samples = None
         if ctx.needs_input_grad[0] and interp == FILTER['LINEAR'] and _state['sample_store']:
-            ctx.samples = _samples_buffer(shape5, _mats(V)[1], out_shape, separate, xs.device)
+            samples = _samples_buffer(shape5, _mats(V)[1], out_shape, separate, xs.device)
         y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=grid,
-                          samples=ctx.samples)
-        ctx.save_for_backward(xs, y)
+                          samples=samples)
+        # a saved tensor, so that checkpointing drops and recomputes it
+        ctx.save_for_backward(xs, y, samples)
         ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate, grid)
         ctx.in_dtype = x.dtype
         return y
 
     @staticmethod
     def backward(ctx, dy):
-        xs, y = ctx.saved_tensors
+        xs, y, samples = ctx.saved_tensors
         M, V, P, F, out_shape, interp, boundary, blend, separate, grid = ctx.args
         ws = None
         if ctx.weights is not None:
             ws, ev = ctx.weights
             if ev is not None:
                 torch.cuda.current_stream(xs.device).wait_event(ev)
-        samples, ctx.samples = ctx.samples, None
         g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
                           GRAD[get_grad_mode()], weights=ws, grid=grid, samples=samples)
         ctx.weights = None
@@ -885,20 +885,20 @@ class _Advect(torch.autograd.Function):
         # MacCormack on one fp32 slice: run the forward in the gradient's
         # workspace and keep it, so that the backward reads the intermediate
         # semi-Lagrangian grid instead of recomputing it
-        ctx.ws = None
+        ws = None
         if any(ctx.needs_input_grad[:4]) and order == 2 and ds.shape[0] == 1 and ds is d and d.dtype == torch.float32:
-            ctx.ws = _advect_grad_workspace(d.shape, order, d.device)
-        y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary, ws=ctx.ws)
-        ctx.save_for_backward(d, vx, vy, vz)
+            ws = _advect_grad_workspace(d.shape, order, d.device)
+        y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary, ws=ws)
+        # the workspace is a saved tensor, so that checkpointing drops and recomputes it
+        ctx.save_for_backward(d, vx, vy, vz, ws)
         ctx.args = (dt, order, clamp, boundary)
         return y
 
     @staticmethod
     def backward(ctx, dy):
-        d, vx, vy, vz = ctx.saved_tensors
+        d, vx, vy, vz, ws = ctx.saved_tensors
         dt, order, clamp, boundary = ctx.args
         gmode = GRAD[get_grad_mode()]
-        ws, ctx.ws = ctx.ws, None
         gd, gvx, gvy, gvz = _advect_bwd(d.float().contiguous(), vx, vy, vz, _cuda(dy, 'output_grad'), dt, order,
                                         clamp, boundary, gmode | (FORWARD_READY if ws is not None else 0), ws=ws)
         return gd.to(d.dtype), gvx.view_as(vx), gvy.view_as(vy), gvz.view_as(vz), None, None, None, None, None
