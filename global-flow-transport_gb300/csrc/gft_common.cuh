@@ -178,6 +178,30 @@ template <int C>
 __device__ __forceinline__ Vec<C> loadf(const float* p, int64_t i) {
     return Load<C, float>::at(p, i);
 }
+// Streaming (evict-first) store and load of data written once and read once
+// (st.global.cs / ld.global.cs), so that it does not push reused data out of L2.
+template <int C>
+__device__ __forceinline__ void store_stream(float* p, int64_t i, Vec<C> a) {
+    if constexpr (C == 4) {
+        __stcs(reinterpret_cast<float4*>(p) + i, make_float4(a.v[0], a.v[1], a.v[2], a.v[3]));
+    } else if constexpr (C == 2) {
+        __stcs(reinterpret_cast<float2*>(p) + i, make_float2(a.v[0], a.v[1]));
+    } else {
+        __stcs(p + i, a.v[0]);
+    }
+}
+template <int C>
+__device__ __forceinline__ Vec<C> load_stream(const float* p, int64_t i) {
+    if constexpr (C == 4) {
+        const float4 f = __ldcs(reinterpret_cast<const float4*>(p) + i);
+        return Vec<4>{{f.x, f.y, f.z, f.w}};
+    } else if constexpr (C == 2) {
+        const float2 f = __ldcs(reinterpret_cast<const float2*>(p) + i);
+        return Vec<2>{{f.x, f.y}};
+    } else {
+        return Vec<1>{{__ldcs(p + i)}};
+    }
+}
 
 // Atomic add of a channel vector; C == 4 and C == 2 use the sm_90+ vector
 // reductions (one red.global.v4/v2.f32 per voxel instead of C scalar ones).

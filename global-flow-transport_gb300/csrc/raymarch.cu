@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             Vec<C> smp;
             if constexpr (LIN) {
                 smp = fetch_linear<C, S, BM, L>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
-                if (samples) store<C>(samples, sample_index(tab, p, D, i), smp);
+                if (samples) store_stream<C>(samples, sample_index(tab, p, D, i), smp);
             } else {
                 smp = fetch<C, S, BM, true>(filter, g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
             }
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             Vec<C> smp;
             if (use_store) {
                 const int i = D - 1 - k;
-                smp = i >= s_lo && i <= s_hi ? loadf<C>(samples, sample_index(tab, p, D, i)) : vzero<C>();
+                smp = i >= s_lo && i <= s_hi ? load_stream<C>(samples, sample_index(tab, p, D, i)) : vzero<C>();
             } else {
                 smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             }
