@@ -6,6 +6,8 @@
 // kScatterLuT3DGradients :1051-1081, kComputeLoD3D :1288-1300) and the
 // sampler of sampling.hpp.  All cameras of a batch slice run in one launch;
 // per-camera transforms travel in the launch parameters.
+#include <algorithm>
+
 #include "gft_internal.h"
 
 namespace gft {
@@ -32,6 +34,79 @@ __global__ void k_mip_level(const S* __restrict__ src, Dims ds, float* __restric
         c[dx] = vscale(vadd(a, b), 0.5f);
     }
     store<C>(dst, t, vscale(vadd(c[0], c[1]), 0.5f));
+}
+
+// The 2x2x2 mean of kGenerateMip3D in its operation order (z pairs, then y,
+// then x); at(dx, dy, dz) reads a child.
+template <int C, typename F>
+__device__ __forceinline__ Vec<C> mip_mean(F at) {
+    Vec<C> c[2];
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx) {
+        const Vec<C> a = vscale(vadd(at(dx, 0, 0), at(dx, 0, 1)), 0.5f);
+        const Vec<C> b = vscale(vadd(at(dx, 1, 0), at(dx, 1, 1)), 0.5f);
+        c[dx] = vscale(vadd(a, b), 0.5f);
+    }
+    return vscale(vadd(c[0], c[1]), 0.5f);
+}
+
+// Levels 1 to `levels` (<= 3) in one launch: a block of 64 threads computes a
+// 4x4x4 tile of level 1 (from an 8x8x8 region of level 0), then from that tile
+// in shared memory the 2x2x2 level-2 cells and the level-3 cell above it; a
+// parent exists exactly where its children do (dims >> 1 per level).
+template <int C, typename S>
+__global__ void __launch_bounds__(64)
+    k_mip_pyramid(const S* __restrict__ src, Dims d0, float* __restrict__ l1, Dims d1, float* __restrict__ l2, Dims d2,
+                  float* __restrict__ l3, Dims d3, int levels) {
+    __shared__ float s1[64 * C];
+    __shared__ float s2[8 * C];
+    const unsigned tx = (d1.x + 3) / 4, ty = (d1.y + 3) / 4;
+    unsigned b = blockIdx.x;
+    const int bx = (int)(b % tx);
+    b /= tx;
+    const int by = (int)(b % ty), bz = (int)(b / ty);
+    const int t = threadIdx.x, lx = t & 3, ly = (t >> 2) & 3, lz = t >> 4;
+    const int x = bx * 4 + lx, y = by * 4 + ly, z = bz * 4 + lz;
+    Vec<C> v = vzero<C>();
+    if (x < d1.x && y < d1.y && z < d1.z) {
+        v = mip_mean<C>([&](int dx, int dy, int dz) {
+            return Load<C, S>::at(src, flat3(2 * x + dx, 2 * y + dy, 2 * z + dz, d0));
+        });
+        store<C>(l1, flat3(x, y, z, d1), v);
+    }
+    if (levels < 2) return;  // uniform over the launch
+#pragma unroll
+    for (int c = 0; c < C; ++c) s1[t * C + c] = v.v[c];
+    __syncthreads();
+    if (t < 8) {
+        const int cx = t & 1, cy = (t >> 1) & 1, cz = t >> 2;
+        const int x2 = bx * 2 + cx, y2 = by * 2 + cy, z2 = bz * 2 + cz;
+        Vec<C> v2 = vzero<C>();
+        if (x2 < d2.x && y2 < d2.y && z2 < d2.z) {
+            v2 = mip_mean<C>([&](int dx, int dy, int dz) {
+                Vec<C> r;
+                const int k = ((2 * cz + dz) * 4 + 2 * cy + dy) * 4 + 2 * cx + dx;
+#pragma unroll
+                for (int c = 0; c < C; ++c) r.v[c] = s1[k * C + c];
+                return r;
+            });
+            store<C>(l2, flat3(x2, y2, z2, d2), v2);
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) s2[t * C + c] = v2.v[c];
+    }
+    if (levels < 3) return;
+    __syncthreads();
+    if (t == 0 && bx < d3.x && by < d3.y && bz < d3.z) {
+        const Vec<C> v3 = mip_mean<C>([&](int dx, int dy, int dz) {
+            Vec<C> r;
+            const int k = (dz * 2 + dy) * 2 + dx;
+#pragma unroll
+            for (int c = 0; c < C; ++c) r.v[c] = s2[k * C + c];
+            return r;
+        });
+        store<C>(l3, flat3(bx, by, bz, d3), v3);
+    }
 }
 
 int usable_mip_levels(Dims d, int num_mips) {
@@ -76,20 +151,40 @@ bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, 
     set->lvl[0] = (const float*)input;  // reinterpreted by the sampler according to dtype
     set->dims[0] = d;
     float* p = ws;
-    const void* src = input;
-    int src_dtype = dtype;
-    for (int m = 1; m <= levels; ++m) {
+    for (int m = 1; m <= levels; ++m) {  // level pointers and dims
         const Dims dm{d.x >> m, d.y >> m, d.z >> m};
-        if (C == 4) mip_launch<4>(src, src_dtype, set->dims[m - 1], p, dm, s);
-        else if (C == 2) mip_launch<2>(src, src_dtype, set->dims[m - 1], p, dm, s);
-        else mip_launch<1>(src, src_dtype, set->dims[m - 1], p, dm, s);
-        if (!launched(1, "mip generation launch")) return false;
         set->lvl[m] = p;
         set->dims[m] = dm;
-        src = p;
-        src_dtype = 0;
         const size_t v = (size_t)voxels(dm) * C;
         p += (v + 63) & ~size_t(63);
+    }
+    // levels 1-3 in one launch, further levels one launch each
+    const int first = std::min(levels, 3);
+    if (first > 0) {
+        const Dims d1 = set->dims[1], d2 = set->dims[std::min(first, 2)], d3 = set->dims[first];
+        const int64_t blocks = (int64_t)((d1.x + 3) / 4) * ((d1.y + 3) / 4) * ((d1.z + 3) / 4);
+        float* l1 = const_cast<float*>(set->lvl[1]);
+        float* l2 = const_cast<float*>(set->lvl[std::min(first, 2)]);
+        float* l3 = const_cast<float*>(set->lvl[first]);
+        if (dtype == 0) {
+            if (C == 4) k_mip_pyramid<4, float><<<(unsigned)blocks, 64, 0, s>>>((const float*)input, d, l1, d1, l2, d2, l3, d3, first);
+            else if (C == 2) k_mip_pyramid<2, float><<<(unsigned)blocks, 64, 0, s>>>((const float*)input, d, l1, d1, l2, d2, l3, d3, first);
+            else k_mip_pyramid<1, float><<<(unsigned)blocks, 64, 0, s>>>((const float*)input, d, l1, d1, l2, d2, l3, d3, first);
+        } else {
+            const __nv_bfloat16* in = (const __nv_bfloat16*)input;
+            if (C == 4) k_mip_pyramid<4, __nv_bfloat16><<<(unsigned)blocks, 64, 0, s>>>(in, d, l1, d1, l2, d2, l3, d3, first);
+            else if (C == 2) k_mip_pyramid<2, __nv_bfloat16><<<(unsigned)blocks, 64, 0, s>>>(in, d, l1, d1, l2, d2, l3, d3, first);
+            else k_mip_pyramid<1, __nv_bfloat16><<<(unsigned)blocks, 64, 0, s>>>(in, d, l1, d1, l2, d2, l3, d3, first);
+        }
+        if (!launched(1, "mip pyramid launch")) return false;
+    }
+    for (int m = 4; m <= levels; ++m) {
+        const Dims dm{d.x >> m, d.y >> m, d.z >> m};
+        float* dst = const_cast<float*>(set->lvl[m]);
+        if (C == 4) mip_launch<4>(set->lvl[m - 1], 0, set->dims[m - 1], dst, dm, s);
+        else if (C == 2) mip_launch<2>(set->lvl[m - 1], 0, set->dims[m - 1], dst, dm, s);
+        else mip_launch<1>(set->lvl[m - 1], 0, set->dims[m - 1], dst, dm, s);
+        if (!launched(1, "mip generation launch")) return false;
     }
     return true;
 }
