@@ -171,6 +171,17 @@ bool grid_shape_ok(const int64_t* s, std::string& why) {
 
 bool channels_ok(int64_t c) { return c == 1 || c == 2 || c == 4; }
 
+// The raymarch kernels index a grid slice (rows or bricks) with 32-bit cell
+// arithmetic, as the resampling and advection kernels do.
+bool raymarch_grid_ok(const int64_t* s, std::string& why) {
+    if (!grid_shape_ok(s, why)) return false;
+    if (brick_cells(Dims{(int)s[3], (int)s[2], (int)s[1]}) >= MAX_SLICE_CELLS) {
+        why = "a grid slice has 2^32 or more cells";
+        return false;
+    }
+    return true;
+}
+
 Dims dims_of(const int64_t* s) { return Dims{(int)s[3], (int)s[2], (int)s[1]}; }
 
 gft_status check_cameras(const float* M, int num_m, int64_t batch, const float* V, const float* P, const float* F,
@@ -260,7 +271,7 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
                                     int32_t blending_mode, int32_t separate_camera_batch, float* output,
                                     float* samples, size_t samples_bytes, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
     if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
         return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
@@ -356,7 +367,7 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
                                      size_t samples_bytes, float* input_grad, void* workspace,
                                      size_t workspace_bytes, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
     if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
         return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
@@ -416,7 +427,7 @@ gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5]
                                                     int32_t separate_camera_batch, void* workspace,
                                                     size_t workspace_bytes, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
         return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive (output_shape)");
     if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
@@ -483,7 +494,7 @@ gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dt
                                              const int32_t* output_shapes, int32_t interpolation, int32_t boundary,
                                              int32_t blending_mode, float* output, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
     if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!enum_in(interpolation, 0, 3) || !enum_in(boundary, 0, 2) || !enum_in(blending_mode, 0, 4) ||
@@ -521,7 +532,7 @@ gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t inp
                                                   int32_t grad_mode, float* input_grad, void* workspace,
                                                   size_t workspace_bytes, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
     if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (interpolation != GFT_FILTER_LINEAR)
@@ -564,7 +575,7 @@ gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_sh
                                                           const int32_t* output_shapes, int32_t boundary,
                                                           void* workspace, size_t workspace_bytes, void* stream) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);

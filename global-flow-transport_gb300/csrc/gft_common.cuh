@@ -301,16 +301,17 @@ __device__ __forceinline__ Vec<C> fetch_linear(const S* __restrict__ g, Dims d, 
         if ((unsigned)x0 < (unsigned)(d.x - 1) && (unsigned)y0 < (unsigned)(d.y - 1) &&
             (unsigned)z0 < (unsigned)(d.z - 1)) {
             const float wx = px - fx, wy = py - fy, wz = pz - fz;
-            int64_t i000, i100, i010, i110, i001, i101, i011, i111;
+            // 32-bit cell indices: every caller limits a grid slice to 2^32 cells
+            uint32_t i000, i100, i010, i110, i001, i101, i011, i111;
             if constexpr (L == LAYOUT_BRICK) {
                 // brick index = x term + y term + z term (brick_index)
-                const int64_t bx = (d.x + 1) / 2, bxy = bx * ((d.y + 1) / 2);
-                const int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
-                const int64_t tx0 = (int64_t)(x0 >> 1) * 8 + (x0 & 1), tx1 = (int64_t)(x1 >> 1) * 8 + (x1 & 1);
-                const int64_t ty0 = (int64_t)(y0 >> 1) * bx * 8 + ((y0 & 1) << 1);
-                const int64_t ty1 = (int64_t)(y1 >> 1) * bx * 8 + ((y1 & 1) << 1);
-                const int64_t tz0 = (int64_t)(z0 >> 1) * bxy * 8 + ((z0 & 1) << 2);
-                const int64_t tz1 = (int64_t)(z1 >> 1) * bxy * 8 + ((z1 & 1) << 2);
+                const uint32_t bx = (uint32_t)(d.x + 1) / 2, bxy = bx * ((uint32_t)(d.y + 1) / 2);
+                const uint32_t x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+                const uint32_t tx0 = (uint32_t)(x0 >> 1) * 8u + (x0 & 1), tx1 = (x1 >> 1) * 8u + (x1 & 1);
+                const uint32_t ty0 = (uint32_t)(y0 >> 1) * bx * 8u + ((y0 & 1) << 1);
+                const uint32_t ty1 = (y1 >> 1) * bx * 8u + ((y1 & 1) << 1);
+                const uint32_t tz0 = (uint32_t)(z0 >> 1) * bxy * 8u + ((z0 & 1) << 2);
+                const uint32_t tz1 = (z1 >> 1) * bxy * 8u + ((z1 & 1) << 2);
                 i000 = tz0 + ty0 + tx0;
                 i100 = tz0 + ty0 + tx1;
                 i010 = tz0 + ty1 + tx0;
@@ -320,8 +321,8 @@ __device__ __forceinline__ Vec<C> fetch_linear(const S* __restrict__ g, Dims d, 
                 i011 = tz1 + ty1 + tx0;
                 i111 = tz1 + ty1 + tx1;
             } else {
-                const int64_t sy = d.x, sz = (int64_t)d.x * d.y;
-                i000 = ((int64_t)z0 * d.y + y0) * d.x + x0;
+                const uint32_t sy = d.x, sz = (uint32_t)d.x * d.y;
+                i000 = ((uint32_t)z0 * d.y + y0) * d.x + x0;
                 i100 = i000 + 1;
                 i010 = i000 + sy;
                 i110 = i000 + sy + 1;

@@ -303,26 +303,28 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
             zs[i] = remap<BM>(zs[i], d.z);
         }
     }
-    // cell indices as sums of per-axis terms (brick_index, flat3)
-    const int64_t bx = (d.x + 1) / 2, bxy = bx * ((d.y + 1) / 2);
-    int64_t bt[3][2], ct[3][2];
+    // cell indices as sums of per-axis terms (brick_index, flat3), in 32 bits:
+    // the callers limit a grid slice to 2^32 cells (terms of invalid corners
+    // wrap but are not used)
+    const uint32_t bx = (uint32_t)(d.x + 1) / 2, bxy = bx * ((uint32_t)(d.y + 1) / 2);
+    uint32_t bt[3][2], ct[3][2];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-        bt[0][i] = (int64_t)(xs[i] >> 1) * 8 + (xs[i] & 1);
-        bt[1][i] = (int64_t)(ys[i] >> 1) * bx * 8 + ((ys[i] & 1) << 1);
-        bt[2][i] = (int64_t)(zs[i] >> 1) * bxy * 8 + ((zs[i] & 1) << 2);
+        bt[0][i] = (uint32_t)(xs[i] >> 1) * 8u + (uint32_t)(xs[i] & 1);
+        bt[1][i] = (uint32_t)(ys[i] >> 1) * bx * 8u + ((uint32_t)(ys[i] & 1) << 1);
+        bt[2][i] = (uint32_t)(zs[i] >> 1) * bxy * 8u + ((uint32_t)(zs[i] & 1) << 2);
         if constexpr (L == LAYOUT_FLAT) {
-            ct[0][i] = xs[i];
-            ct[1][i] = (int64_t)ys[i] * d.x;
-            ct[2][i] = (int64_t)zs[i] * d.x * d.y;
+            ct[0][i] = (uint32_t)xs[i];
+            ct[1][i] = (uint32_t)ys[i] * (uint32_t)d.x;
+            ct[2][i] = (uint32_t)zs[i] * (uint32_t)d.x * (uint32_t)d.y;
         }
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
         if (!((nz >> k) & 1u) || !(vx[sx] && vy[sy] && vz[sz])) continue;
-        const int64_t bi = bt[0][sx] + bt[1][sy] + bt[2][sz];
-        const int64_t ci = L == LAYOUT_FLAT ? ct[0][sx] + ct[1][sy] + ct[2][sz] : bi;
+        const uint32_t bi = bt[0][sx] + bt[1][sy] + bt[2][sz];
+        const uint32_t ci = L == LAYOUT_FLAT ? ct[0][sx] + ct[1][sy] + ct[2][sz] : bi;
         Vec<C> a;
 #pragma unroll
         for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];

@@ -72,6 +72,11 @@ def test_argument_errors_without_a_gpu(lib):
     assert st == lib.ERR_WORKSPACE
     assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 0) >= 8 * 8 * 8 * 5 * 4
     assert L.gft_raymarch_grid_transform_grad_workspace_size(shape4, 5, 1, 1) == 0
+    # the raymarch kernels index a grid slice with 32-bit cell arithmetic
+    huge = lib.i64([1, 2048, 2048, 1025, 4])
+    st = L.gft_raymarch_grid_transform(ctypes.c_void_p(1), 0, huge, p, 1, p, p, f, 1, out, 1, 0, 0, 1,
+                                       ctypes.c_void_p(1), None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'2^32' in L.gft_last_error()
     # sample store: LINEAR only, a large enough store, a store pointer
     assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == ((8 + 7) // 8) * ((4 + 15) // 16) * 4 \
         * 128 * 4 * 4
