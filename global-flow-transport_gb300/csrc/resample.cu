@@ -314,43 +314,55 @@ __device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, 
     }
 }
 
-template <int C, typename S, int BM>
+// One kernel per coordinate mode (the transform and its LOD are inlined for
+// that mode only).  The transform sampler reads nothing under WRAP, as the
+// reference's (zeros for any coordinate mode).
+template <int C, typename S, int BM, int CM>
 __global__ void __launch_bounds__(RS_THREADS)
-    k_sample_transform(Dims dout, int filter, int mip_mode, float bias, float cco, int cm, const MipSet ms,
+    k_sample_transform(Dims dout, int filter, int mip_mode, float bias, float cco, const MipSet ms,
                        float* __restrict__ out, const __grid_constant__ PairTable tab) {
     const int64_t nv = voxels(dout);
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
     const int p = blockIdx.y;
-    int x, y, z;
-    unflat32(v, dout, x, y, z);
-    const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
-    const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
-    const float4 pos = sample_pos(tab.cam[p], cm, make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
-                                  mip_mode != MIP_NONE, BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f);
-    Vec<C> r;
-    if ((filter == F_LINEAR || filter == F_NEAREST) && (BM == BM_BORDER || BM == BM_CLAMP))
-        r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
-    else
-        r = vzero<C>();
+    Vec<C> r = vzero<C>();
+    if constexpr (BM == BM_BORDER || BM == BM_CLAMP) {
+        int x, y, z;
+        unflat32(v, dout, x, y, z);
+        const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
+        const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
+        const float4 pos = sample_pos_cm<CM>(tab.cam[p], make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
+                                             mip_mode != MIP_NONE,
+                                             BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f);
+        if (filter == F_LINEAR || filter == F_NEAREST) r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
+    }
     store<C>(out, (int64_t)tab.out_slot[p] * nv + v, r);
+}
+
+template <int C, typename S, int BM>
+static void st_fwd_cm(int cm, dim3 blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
+                      const PairTable& t) {
+#define GFT_ST(CMV)                                                                                              \
+    k_sample_transform<C, S, BM, CMV><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, \
+                                                                    ms, out, t)
+    switch (cm) {
+        case CM_LINDEPTH: GFT_ST(CM_LINDEPTH); break;
+        case CM_TRANSFORM: GFT_ST(CM_TRANSFORM); break;
+        case CM_LINDEPTH_REVERSE: GFT_ST(CM_LINDEPTH_REVERSE); break;
+        default: GFT_ST(CM_TRANSFORM_REVERSE); break;
+    }
+#undef GFT_ST
 }
 
 template <int C, typename S>
 static void st_fwd(int bm, dim3 blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
                    const PairTable& t) {
     switch (bm) {
-        case BM_BORDER:
-            k_sample_transform<C, S, BM_BORDER><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
-                                                                             a.cco, a.coord_mode, ms, out, t);
-            break;
-        case BM_CLAMP:
-            k_sample_transform<C, S, BM_CLAMP><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
-                                                                            a.cco, a.coord_mode, ms, out, t);
-            break;
+        case BM_BORDER: st_fwd_cm<C, S, BM_BORDER>(a.coord_mode, blocks, s, a, ms, out, t); break;
+        case BM_CLAMP: st_fwd_cm<C, S, BM_CLAMP>(a.coord_mode, blocks, s, a, ms, out, t); break;
         default:
-            k_sample_transform<C, S, BM_WRAP><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias,
-                                                                           a.cco, a.coord_mode, ms, out, t);
+            k_sample_transform<C, S, BM_WRAP, CM_LINDEPTH><<<blocks, RS_THREADS, 0, s>>>(
+                a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, ms, out, t);
             break;
     }
 }
