@@ -232,32 +232,39 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     from gft.pipeline import RenderAdvectStep
     out = {}
     # ---- e2e: pinned host inputs -> device, graph step, loss -> host ----------
-    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
-            (('d', inputs['d_prev']), ('vx', inputs['vx'][None]), ('vy', inputs['vy'][None]),
-             ('vz', inputs['vz'][None]), ('t', inputs['target']))}
-    dsts = {'d': step.s_d, 'vx': step.s_vx, 'vy': step.s_vy, 'vz': step.s_vz, 't': step.s_t}
-    h2d = sum(v.numel() * v.element_size() for v in host.values())
-    loss_host = torch.empty(1, dtype=torch.float32).pin_memory()
-
-    def e2e_step():
-        with torch.no_grad():
-            for k, v in host.items():
-                dsts[k].copy_(v, non_blocking=True)
-        loss, _ = step.replay()
-        loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
-
-    k = min(max(3, args.steps // 2), 50)
-    for _ in range(2):
-        e2e_step()
+    # Through the public streaming API (gft.pipeline.StreamedSteps): every
+    # step copies its own inputs (two frames' inputs alternate) from pinned
+    # host memory and reads its loss back; the copy of step i+1's inputs
+    # overlaps step i.  e2e_serial: one step at a time, the host waiting for
+    # each loss before it copies the next inputs.
+    from gft.pipeline import StreamedSteps
+    hosts = [StreamedSteps.host_inputs(inputs), StreamedSteps.host_inputs(step.make_inputs(frame=1))]
+    h2d = StreamedSteps.h2d_bytes(hosts[0])
+    streamed = StreamedSteps(step, inputs, warmup=args.warmup)
+    k = min(max(6, args.steps // 2), 60)
+    streamed.run([hosts[i % 2] for i in range(4)])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(k):
-        e2e_step()
-        torch.cuda.current_stream().synchronize()
-        float(loss_host[0])
+    losses = streamed.run([hosts[i % 2] for i in range(k)])
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / k
     out['e2e'] = {'value': 1000.0 / e2e_ms, 'unit': 'iters/s', 'h2d_bytes_per_step': int(h2d),
-                  'd2h_bytes_per_step': 4, 'ms_per_step': e2e_ms}
+                  'd2h_bytes_per_step': 4, 'ms_per_step': e2e_ms, 'steps': k,
+                  'what': 'StreamedSteps: per-step H2D of pinned inputs overlapping the previous step, loss read '
+                          'back one step later', 'loss_last': losses[-1]}
+
+    def serial_step(host):
+        return streamed.run([host])[0]
+
+    for i in range(2):
+        serial_step(hosts[i % 2])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(k):
+        serial_step(hosts[i % 2])
+    ser_ms = (time.perf_counter() - t0) * 1000.0 / k
+    out['e2e_serial'] = {'value': 1000.0 / ser_ms, 'unit': 'iters/s', 'ms_per_step': ser_ms,
+                         'what': 'one step at a time: copy inputs, replay, read the loss, wait'}
+    del streamed
 
     # ---- plain: per-camera launches, composed advection, no graph -----------
     plain = RenderAdvectStep(args.config, dev, storage_dtype=None, mode='plain')

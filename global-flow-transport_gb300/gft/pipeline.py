@@ -191,6 +191,83 @@ class RenderAdvectStep:
         return self.step(self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
 
 
+class StreamedSteps:
+    """Runs the graph-captured step over a stream of host inputs with the
+    transfers overlapped: two captured copies of the step, each with its own
+    input slot, alternate; the host-to-device copy of step i+1's inputs (from
+    pinned host memory, on a copy stream) runs while step i computes, and each
+    step's loss is copied back to pinned host memory on the compute stream and
+    read by the host one step later, so the host never stalls the device.
+    Every step still copies its own inputs and reads its own loss.
+
+    step: a RenderAdvectStep (batched mode) whose configuration both slots
+    use; example: inputs as make_inputs returns them (to set up the slots)."""
+
+    KEYS = ('d', 'vx', 'vy', 'vz', 't')
+
+    def __init__(self, step, example, warmup=3):
+        self.dev = step.dev
+        self.slots = [step, RenderAdvectStep(step.cfg, step.dev, storage_dtype=step.storage_dtype, mode=step.mode)]
+        for st in self.slots:
+            st.setup_static(example)
+            st.capture(warmup=warmup)
+        self.copy_stream = torch.cuda.Stream(self.dev)
+        self.copied = [torch.cuda.Event() for _ in self.slots]
+        self.done = [torch.cuda.Event() for _ in self.slots]
+        self.loss_ready = [torch.cuda.Event() for _ in self.slots]
+        self.loss_host = [torch.empty(1, dtype=torch.float32).pin_memory() for _ in self.slots]
+        for ev in self.done:
+            ev.record(torch.cuda.current_stream(self.dev))
+
+    @staticmethod
+    def host_inputs(inputs):
+        """Pinned host tensors of make_inputs' arrays, keyed d, vx, vy, vz, t."""
+        import numpy as _np
+        arrays = (inputs['d_prev'], inputs['vx'][None], inputs['vy'][None], inputs['vz'][None], inputs['target'])
+        return {k: torch.from_numpy(_np.ascontiguousarray(a)).pin_memory() for k, a in zip(StreamedSteps.KEYS, arrays)}
+
+    @staticmethod
+    def h2d_bytes(host):
+        return sum(v.numel() * v.element_size() for v in host.values())
+
+    def _enqueue(self, i, host):
+        k = i % len(self.slots)
+        st = self.slots[k]
+        dsts = (st.s_d, st.s_vx, st.s_vy, st.s_vz, st.s_t)
+        cur = torch.cuda.current_stream(self.dev)
+        with torch.cuda.stream(self.copy_stream), torch.no_grad():
+            self.copy_stream.wait_event(self.done[k])  # the slot's previous step has consumed its inputs
+            for key, dst in zip(self.KEYS, dsts):
+                dst.copy_(host[key], non_blocking=True)
+            self.copied[k].record(self.copy_stream)
+        cur.wait_event(self.copied[k])
+        loss, _ = st.replay()
+        self.done[k].record(cur)
+        self.loss_host[k].copy_(loss.detach().reshape(1), non_blocking=True)
+        self.loss_ready[k].record(cur)
+
+    def _read(self, i):
+        k = i % len(self.slots)
+        self.loss_ready[k].synchronize()
+        return float(self.loss_host[k][0])
+
+    def run(self, host_inputs):
+        """Steps over an iterable of host_inputs() dicts; returns the losses."""
+        losses = []
+        i = -1
+        for i, host in enumerate(host_inputs):
+            self._enqueue(i, host)
+            if i >= 1:
+                losses.append(self._read(i - 1))
+        if i >= 0:
+            losses.append(self._read(i))
+        return losses
+
+    def grads(self, i):
+        """Gradients of step i (valid until that slot runs again, two steps later)."""
+        return self.slots[i % len(self.slots)].g_grads
+
+
 class _Holder:
     """GridTransform view used for the falloff computation."""
 

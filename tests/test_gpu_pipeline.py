@@ -37,6 +37,32 @@ def test_graph_replay_equals_eager(gpu):
         assert rel_l2(_np(a), b) <= 1e-4
 
 
+def test_streamed_steps_equal_single_steps(gpu):
+    """StreamedSteps (inputs copied while the previous step runs, losses read
+    one step late) gives each step the loss and gradients of running that
+    step alone on the same inputs."""
+    from gft.pipeline import RenderAdvectStep, StreamedSteps
+    s = RenderAdvectStep('tiny', gpu)
+    frames = [s.make_inputs(frame=f) for f in range(3)]
+    ref = []
+    for inp in frames:
+        r = RenderAdvectStep('tiny', gpu)
+        r.setup_static(inp)
+        loss, grads = r.run_static()
+        ref.append((float(loss), [_np(g) for g in grads]))
+    streamed = StreamedSteps(s, frames[0])
+    hosts = [StreamedSteps.host_inputs(inp) for inp in frames]
+    order = [0, 1, 2, 1, 0]
+    losses = streamed.run([hosts[i] for i in order])
+    assert len(losses) == len(order)
+    for j, i in enumerate(order):
+        assert abs(losses[j] - ref[i][0]) <= 1e-5 * abs(ref[i][0])
+    # the gradients of the last step (slot 0) before that slot runs again
+    torch.cuda.synchronize()
+    for a, b in zip(streamed.grads(len(order) - 1), ref[order[-1]][1]):
+        assert rel_l2(_np(a), b) <= 1e-4
+
+
 def test_batched_equals_plain(gpu):
     from gft.pipeline import RenderAdvectStep
     a = RenderAdvectStep('tiny', gpu, mode='batched')
