@@ -513,7 +513,10 @@ def kernel_roofline(step, dev, timed):
     s, C = 4, 4
     pix = V * H * W
     samples = pix * D
-    stored = _clipped_samples(step) * C * 4  # bytes of the sample store written / read
+    # bytes of the sample store written / read: the samples the forward stored
+    # (inside the clipped ranges and outside empty occupancy blocks)
+    n_stored = ops.stored_sample_count(smp, shape5, V, step.res)
+    stored = n_stored * C * 4
     bytes_fwd = nvox * C * s + pix * C * 4 + stored
     # scatter pass: stored samples read, image + adjoint read, per-camera
     # reciprocal weights read, gradient read-modify-write
@@ -530,6 +533,8 @@ def kernel_roofline(step, dev, timed):
         'raymarch_bwd_scatter_resampling': {'ms': tr, 'alg_bytes': bytes_resample, 'GBps': bytes_resample / tr / 1e6,
                                             'what': 'the same pass re-sampling the grid (no sample store)'},
         'raymarch_samples_stored_bytes': stored,
+        'raymarch_samples_in_clipped_ranges': _clipped_samples(step),
+        'raymarch_samples_stored': n_stored,
         'raymarch_bwd_weights': {'ms': tw, 'alg_bytes': bytes_weights, 'GBps': bytes_weights / tw / 1e6,
                                  'samples_per_s': samples / tw * 1e3},
         'raymarch_bwd_reference': {'ms': tb_ref, 'what': 'whole op: weights + inversion + scatter'},

@@ -261,7 +261,7 @@ size_t gft_raymarch_grid_transform_samples_size(const int64_t input_shape[5], in
         return 0;
     std::vector<Pair> pairs((size_t)input_shape[0] * (separate_camera_batch ? (size_t)num_cameras : 1));
     set_uniform_images(pairs, output_shape[0], output_shape[1], output_shape[2]);
-    return align256(sizeof(float) * (size_t)raymarch_samples_floats(pairs, (int)input_shape[4]));
+    return align256(raymarch_store_bytes(pairs, (int)input_shape[4], (int)input_shape[0], dims_of(input_shape)));
 }
 
 static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
@@ -306,9 +306,10 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
     if (samples != nullptr) {
-        if (samples_bytes < sizeof(float) * (size_t)raymarch_samples_floats(pairs, a.C))
+        if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
-        a.samples_out = samples;
+        a.store = raymarch_store_layout(samples, pairs, a.C, a.N, a.din);
+        if (!launch_raymarch_occupancy(a, as_stream(stream))) return GFT_ERR_CUDA;
     }
     if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
     return GFT_OK;
@@ -409,9 +410,9 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
     if (samples != nullptr) {
-        if (samples_bytes < sizeof(float) * (size_t)raymarch_samples_floats(pairs, a.C))
+        if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
-        a.samples_in = samples;
+        a.store = raymarch_store_layout(const_cast<float*>(samples), pairs, a.C, a.N, a.din);
     }
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
     if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,

@@ -75,13 +75,22 @@ struct RaymarchArgs {
     int filter, boundary, blend;
     int layout = LAYOUT_FLAT;  // cell layout of the input and its gradient
     int n_slots;  // output slots = N * (separate ? V : 1)
-    // Sample store (LINEAR only): the forward writes each clipped-range sample,
-    // the adjoint reads it instead of re-sampling (raymarch_samples_floats).
-    float* samples_out = nullptr;
-    const float* samples_in = nullptr;
+    // Sample store (LINEAR only): the forward writes the samples it blends, the
+    // adjoint reads them instead of re-sampling (store.samples != nullptr).
+    struct Store {
+        float* samples = nullptr;     // cells of C floats, sample_index
+        uint32_t* words = nullptr;    // per pair, tile, step and warp: the lanes that stored a sample
+        uint8_t* occ = nullptr;       // per input slice and 4^3-voxel block: 0 = no non-zero voxel in
+                                      // the block grown by one voxel at its upper faces
+        int nbx = 0, nby = 0, nbz = 0;
+    } store;
 };
-// Floats of the sample store of these pairs (uniform or per-pair images).
-int64_t raymarch_samples_floats(const std::vector<Pair>& pairs, int C);
+// Bytes of the sample store of these pairs (samples, ballot words,
+// occupancy map of the N input slices), and its parts at `base`.
+size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din);
+RaymarchArgs::Store raymarch_store_layout(void* base, const std::vector<Pair>& pairs, int C, int N, Dims din);
+// Fills a.store.occ from the input (before the storing forward).
+bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s);
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
 // Per-pair reciprocal weight sums of the reference-normalised adjoint (pass 1).
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s);

@@ -110,22 +110,137 @@ static unsigned set_ray_tiles(PairTable& t, int64_t* cells = nullptr) {
     return (unsigned)b;
 }
 
-int64_t raymarch_samples_floats(const std::vector<Pair>& pairs, int C) {
+// ---- sample store ----------------------------------------------------------------
+// The differentiable forward keeps the samples it blends for the adjoint.  Only
+// samples that can be non-zero are written: a sample whose 8 corners lie in a
+// 4^3-voxel block without a non-zero voxel (grown by one voxel at its upper
+// faces, so that it holds every corner of a sample with its base cell in the
+// block) is exactly zero, and the forward neither fetches nor stores it; per
+// warp and step a ballot word records which lanes stored one, and the adjoint
+// reads a sample where its bit is set and uses zero elsewhere.
+constexpr int OCC_SHIFT = 2;  // 4^3-voxel occupancy blocks
+
+static int64_t store_cells(const std::vector<Pair>& pairs) {
     int64_t f = 0;
     for (const Pair& p : pairs) f += (int64_t)ray_tiles(p.W, p.H) * p.D * (RM_BX * RM_BY);
-    return f * C;
+    return f;
+}
+static Dims occ_dims(Dims d) {
+    const int b = 1 << OCC_SHIFT;
+    return Dims{(d.x + b - 1) / b, (d.y + b - 1) / b, (d.z + b - 1) / b};
+}
+static size_t align256u(size_t n) { return (n + 255) & ~size_t(255); }
+
+size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din) {
+    const int64_t cells = store_cells(pairs);
+    return align256u(sizeof(float) * cells * C) + align256u(sizeof(uint32_t) * (cells / 32)) +
+           align256u((size_t)voxels(occ_dims(din)) * N);
 }
 
-// Cell index of this lane's step i in the sample store.
+RaymarchArgs::Store raymarch_store_layout(void* base, const std::vector<Pair>& pairs, int C, int N, Dims din) {
+    RaymarchArgs::Store st;
+    const int64_t cells = store_cells(pairs);
+    char* p = static_cast<char*>(base);
+    st.samples = reinterpret_cast<float*>(p);
+    p += align256u(sizeof(float) * cells * C);
+    st.words = reinterpret_cast<uint32_t*>(p);
+    p += align256u(sizeof(uint32_t) * (cells / 32));
+    st.occ = reinterpret_cast<uint8_t*>(p);
+    const Dims od = occ_dims(din);
+    st.nbx = od.x;
+    st.nby = od.y;
+    st.nbz = od.z;
+    return st;
+}
+
+// Cell index of this lane's step i in the sample store, and of its warp's
+// ballot word (a pair's cells and words start at smp0 and smp0 / 32).
 __device__ __forceinline__ int64_t sample_index(const PairTable& tab, int p, int D, int i) {
     const int tid = threadIdx.y * RM_BX + threadIdx.x;
     return tab.smp0[p] + ((int64_t)(blockIdx.x - tab.tile0[p]) * D + i) * (RM_BX * RM_BY) + tid;
+}
+__device__ __forceinline__ int64_t sample_word_index(const PairTable& tab, int p, int D, int i) {
+    const int tid = threadIdx.y * RM_BX + threadIdx.x;
+    return (tab.smp0[p] >> 5) + ((int64_t)(blockIdx.x - tab.tile0[p]) * D + i) * (RM_BX * RM_BY / 32) + (tid >> 5);
+}
+
+// Occupancy of one input slice per block: a non-zero voxel marks the blocks
+// whose grown region holds it (its own, and the lower neighbour along each axis
+// where it lies on the block's lower face); all writers store 1.
+template <int C, typename S, int L>
+__global__ void k_raymarch_occupancy(const S* __restrict__ in, Dims d, uint8_t* __restrict__ occ, Dims od) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= voxels(d)) return;
+    const int n = blockIdx.y;
+    int x, y, z;
+    unflat32(v, d, x, y, z);
+    const Vec<C> a = Load<C, S>::at(in + (size_t)n * slice_cells<L>(d) * C, cell_index<L>(x, y, z, d));
+    bool nonzero = false;
+#pragma unroll
+    for (int c = 0; c < C; ++c) nonzero = nonzero || a.v[c] != 0.f;  // NaN counts as non-zero
+    if (!nonzero) return;
+    const int bx = x >> OCC_SHIFT, by = y >> OCC_SHIFT, bz = z >> OCC_SHIFT;
+    const int mask = (1 << OCC_SHIFT) - 1;
+    const int ex = (x & mask) == 0 && bx > 0, ey = (y & mask) == 0 && by > 0, ez = (z & mask) == 0 && bz > 0;
+    uint8_t* o = occ + (size_t)n * voxels(od);
+    for (int k = 0; k <= ez; ++k)
+        for (int j = 0; j <= ey; ++j)
+            for (int i = 0; i <= ex; ++i) o[((size_t)(bz - k) * od.y + (by - j)) * od.x + (bx - i)] = 1;
+}
+
+template <int C, typename S, int L>
+static void occ_launch(const RaymarchArgs& a, cudaStream_t s) {
+    const Dims od{a.store.nbx, a.store.nby, a.store.nbz};
+    const dim3 grid((unsigned)((voxels(a.din) + 255) / 256), (unsigned)a.N);
+    k_raymarch_occupancy<C, S, L><<<grid, 256, 0, s>>>((const S*)a.input, a.din, a.store.occ, od);
+}
+
+bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s) {
+    const Dims od{a.store.nbx, a.store.nby, a.store.nbz};
+    if (!cuda_ok(cudaMemsetAsync(a.store.occ, 0, (size_t)voxels(od) * a.N, s), "zero occupancy")) return false;
+    // ballot words of steps no warp marches stay 0, so the store is fully defined
+    const size_t words = reinterpret_cast<const char*>(a.store.occ) - reinterpret_cast<const char*>(a.store.words);
+    if (!cuda_ok(cudaMemsetAsync(a.store.words, 0, words, s), "zero sample words")) return false;
+    const bool brick = a.layout == LAYOUT_BRICK;
+    if (a.dtype == 0) {
+        if (a.C == 4) brick ? occ_launch<4, float, LAYOUT_BRICK>(a, s) : occ_launch<4, float, LAYOUT_FLAT>(a, s);
+        else if (a.C == 2) brick ? occ_launch<2, float, LAYOUT_BRICK>(a, s) : occ_launch<2, float, LAYOUT_FLAT>(a, s);
+        else brick ? occ_launch<1, float, LAYOUT_BRICK>(a, s) : occ_launch<1, float, LAYOUT_FLAT>(a, s);
+    } else {
+        if (a.C == 4) brick ? occ_launch<4, __nv_bfloat16, LAYOUT_BRICK>(a, s) : occ_launch<4, __nv_bfloat16, LAYOUT_FLAT>(a, s);
+        else if (a.C == 2) brick ? occ_launch<2, __nv_bfloat16, LAYOUT_BRICK>(a, s) : occ_launch<2, __nv_bfloat16, LAYOUT_FLAT>(a, s);
+        else brick ? occ_launch<1, __nv_bfloat16, LAYOUT_BRICK>(a, s) : occ_launch<1, __nv_bfloat16, LAYOUT_FLAT>(a, s);
+    }
+    return launched(1, "raymarch occupancy launch");
+}
+
+// True where the sample at p is exactly zero by the occupancy map, without a
+// fetch: its corners that the boundary mode reads lie in the grown region of
+// one block without a non-zero voxel.  BORDER and CLAMP: the block of the base
+// cell clamped to the grid (corners outside read 0 resp. the clamped border
+// voxels, which that block holds); WRAP: interior base cells only (all 8
+// corners inside).  Non-finite positions are fetched.
+template <int BM>
+__device__ __forceinline__ bool sample_empty(Dims d, float px, float py, float pz, const uint8_t* __restrict__ occ,
+                                             int nbx, int nby) {
+    if (!(fabsf(px) <= 3.0e9f && fabsf(py) <= 3.0e9f && fabsf(pz) <= 3.0e9f)) return false;
+    int x0 = (int)floorf(px), y0 = (int)floorf(py), z0 = (int)floorf(pz);
+    if constexpr (BM == BM_WRAP) {
+        if (!((unsigned)x0 < (unsigned)(d.x - 1) && (unsigned)y0 < (unsigned)(d.y - 1) &&
+              (unsigned)z0 < (unsigned)(d.z - 1)))
+            return false;
+    } else {
+        x0 = min(max(x0, 0), d.x - 1);
+        y0 = min(max(y0, 0), d.y - 1);
+        z0 = min(max(z0, 0), d.z - 1);
+    }
+    return __ldg(occ + ((uint32_t)(z0 >> OCC_SHIFT) * nby + (uint32_t)(y0 >> OCC_SHIFT)) * nbx + (x0 >> OCC_SHIFT)) == 0;
 }
 
 template <int C, typename S, int BM, bool LIN, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_fwd(const S* __restrict__ in, Dims din, int filter, int blend_mode, float* __restrict__ out,
-                   float* __restrict__ samples, const __grid_constant__ PairTable tab) {
+                   const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
     RayPix r;
     const bool live = ray_pixel(tab, r);  // every lane stays to the warp's clip reduction
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
@@ -139,16 +254,21 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     float3 pos = nearp;
     Vec<C> acc = vzero<C>();
     int i0 = 0, i1 = D - 1, w0 = 0, w1 = D - 1;
+    // Storing samples (LINEAR): every lane stays in the loop to the warp's
+    // last step, for the per-step ballot of the lanes that stored one.
+    const bool storing = LIN && st.samples != nullptr;
     // MIN/MAX samples outside are +-FLOAT_MAX, and BEER_LAMBERT_EXCLUSIVE
     // multiplies a zero sample by exp(-density sum), which overflows for
     // sums below -88: neither is clipped.
     if (BM == BM_BORDER && (LIN || filter == F_NEAREST) && (C == 1 || blend_mode != BL_BEER_LAMBERT_EXCLUSIVE)) {
         const bool hit = live && ray_clip(nearp, step, D, din, i0, i1);
-        warp_clip_range(hit, D, i0, i1, w0, w1);
-        if (!live) return;
-        if (!hit) {
-            store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
-            return;
+        warp_clip_range(hit, D, i0, i1, w0, w1);  // i0 > i1 where !hit
+        if (!storing) {
+            if (!live) return;
+            if (!hit) {
+                store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
+                return;
+            }
         }
         for (int i = 0; i < w0; ++i) {
             pos.x += step.x;
@@ -156,23 +276,38 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             pos.z += step.z;
         }
     } else if (!live) {
-        return;
+        if (!storing) return;
+        i0 = D;
+        i1 = -1;
     }
+    const uint8_t* occ = storing ? st.occ + (size_t)tab.in_batch[p] * st.nbx * st.nby * st.nbz : nullptr;
     for (int i = w0; i <= w1; ++i) {
+        bool stored = false;
         if (i >= i0 && i <= i1) {
             Vec<C> smp;
             if constexpr (LIN) {
-                smp = fetch_linear<C, S, BM, L>(g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
-                if (samples) store_stream<C>(samples, sample_index(tab, p, D, i), smp);
+                const float qx = pos.x - 0.5f, qy = pos.y - 0.5f, qz = pos.z - 0.5f;
+                const bool empty = storing && sample_empty<BM>(din, qx, qy, qz, occ, st.nbx, st.nby);
+                smp = empty ? vzero<C>() : fetch_linear<C, S, BM, L>(g, din, qx, qy, qz);
+                if (storing && !empty) {
+                    store_stream<C>(st.samples, sample_index(tab, p, D, i), smp);
+                    stored = true;
+                }
             } else {
                 smp = fetch<C, S, BM, true>(filter, g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
             }
             acc = blend<C>(blend_mode, acc, smp);
         }
+        if (storing) {
+            const unsigned word = __ballot_sync(0xffffffffu, stored);
+            if ((threadIdx.x & 31u) == 0 && (threadIdx.y & 3u) == 0)
+                st.words[sample_word_index(tab, p, D, i)] = word;
+        }
         pos.x += step.x;
         pos.y += step.y;
         pos.z += step.z;
     }
+    if (!live) return;
     store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
 }
 
@@ -362,7 +497,7 @@ template <int C, typename S, int BM, int MODE, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
-                       const float* __restrict__ samples, const __grid_constant__ PairTable tab) {
+                       const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
     RayPix r;
     const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
@@ -370,9 +505,10 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     ray_far_step(tab.cam[p], x, y, W, H, D, pos, step, nearp);
     // With a sample store: the forward's own clip range (front-to-back steps
     // [s_lo, s_hi], computed from the same near point and step as there); its
-    // samples outside are zero (BORDER), elsewhere it stored all D.
+    // samples outside are zero (BORDER), inside it stored the non-zero ones.
+    const bool use_store = MODE != 2 && st.samples != nullptr;
     int s_lo = 0, s_hi = D - 1;
-    if (MODE != 2 && samples != nullptr && BM == BM_BORDER)
+    if (use_store && BM == BM_BORDER)
         if (!ray_clip(nearp, step, D, din, s_lo, s_hi)) {
             s_lo = D;
             s_hi = -1;
@@ -407,25 +543,23 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     // Not unrolled: the step body is large, and unrolled copies stalled on
     // instruction fetch (unroll 2 / 4: 13 % / 36 % slower normalised pass at
     // 480x270x192; capping registers at 64 or 72 spilled and was slower too).
-    // Stored samples: step k reads the forward's step D - 1 - k (zero outside
-    // the forward's range) and prefetches the next step's line into L2, so
-    // that the stream's DRAM latency overlaps a step (measured at 480x270x192:
-    // normalised pass 0.92 -> 0.87 ms; holding the next sample in registers
-    // instead was as fast but took 93 registers and slowed the re-sampling
-    // path).
-    const bool use_store = MODE != 2 && samples != nullptr;
+    // Stored samples: step k reads the forward's step i = D - 1 - k: zero
+    // outside the forward's range or where the warp's ballot word for that
+    // step has this lane's bit clear, else the stored sample.  (Words are only
+    // read for steps inside the lane's own forward range, which the forward's
+    // warp wrote; a warp's words of consecutive steps share a cache line.)
+    const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;
 #pragma unroll 1
     for (int k = w_lo; k <= w_hi; ++k) {
         const bool on = k >= k_lo && k <= k_hi;
         const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
-        if (use_store && k < w_hi)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(samples + sample_index(tab, p, D, D - 2 - k) * C));
         Vec<C> val = vfill<C>(1.f);
         if (MODE != 2 && on) {
             Vec<C> smp;
             if (use_store) {
                 const int i = D - 1 - k;
-                smp = i >= s_lo && i <= s_hi ? load_stream<C>(samples, sample_index(tab, p, D, i)) : vzero<C>();
+                const uint32_t word = i >= s_lo && i <= s_hi ? __ldg(st.words + sample_word_index(tab, p, D, i)) : 0u;
+                smp = (word >> lane) & 1u ? load_stream<C>(st.samples, sample_index(tab, p, D, i)) : vzero<C>();
             } else {
                 smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             }
@@ -444,13 +578,13 @@ static void fwd_dispatch_lin(bool lin, dim3 grid, dim3 block, cudaStream_t s, co
     // the brick layout is produced for the LINEAR render path only
     if (a.layout == LAYOUT_BRICK)
         k_raymarch_fwd<C, S, BM, true, LAYOUT_BRICK><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
-                                                                           out, a.samples_out, t);
+                                                                           out, a.store, t);
     else if (lin)
         k_raymarch_fwd<C, S, BM, true, LAYOUT_FLAT><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
-                                                                          out, a.samples_out, t);
+                                                                          out, a.store, t);
     else
         k_raymarch_fwd<C, S, BM, false, LAYOUT_FLAT><<<grid, block, 0, s>>>((const S*)in, a.din, a.filter, a.blend,
-                                                                           out, nullptr, t);
+                                                                           out, RaymarchArgs::Store{}, t);
 }
 
 template <int C, typename S>
@@ -488,10 +622,10 @@ static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, co
                            const float* dout, float* grad, const float* cnt, const PairTable& t) {
     if (exact)
         k_raymarch_scatter<C, S, BM, 0, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.samples_in, t);
+                                                                     cnt, a.store, t);
     else
         k_raymarch_scatter<C, S, BM, 1, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.samples_in, t);
+                                                                     cnt, a.store, t);
 }
 
 template <int C, typename S, int BM>
@@ -517,7 +651,7 @@ template <int BM>
 static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
                              const PairTable& t) {
     k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(nullptr, a.din, a.blend, nullptr, nullptr,
-                                                                               cnt, nullptr, nullptr, t);
+                                                                               cnt, nullptr, RaymarchArgs::Store{}, t);
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel).

@@ -189,6 +189,18 @@ def set_raymarch_sample_store(enabled):
     _state['sample_store'] = bool(enabled)
 
 
+def stored_sample_count(samples, shape5, nv, out_shape, separate=True):
+    """Samples a storing raymarch forward wrote into ``samples`` (the set bits
+    of its per-warp ballot words, which follow the 256-byte aligned sample
+    cells: per camera, 8x16-pixel tile, depth sample and lane)."""
+    D, H, W = out_shape
+    pairs = shape5[0] * (nv if separate else 1)
+    cells = pairs * ((W + 7) // 8) * ((H + 15) // 16) * D * 128
+    off = (cells * shape5[4] * 4 + 255) // 256 * 256
+    words = samples.view(torch.uint8)[off:off + cells // 8].cpu().numpy()
+    return int(np.unpackbits(words).sum())
+
+
 def _samples_buffer(shape5, nv, out_shape, separate, device):
     n = _lib.load().gft_raymarch_grid_transform_samples_size(_lib.i64(shape5), nv, _lib.i32(out_shape),
                                                                int(separate))

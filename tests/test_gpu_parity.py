@@ -197,6 +197,44 @@ def test_raymarch_sample_store(ops, C, blend, boundary, mode):
     assert rel_l2(grads[1], grads[0]) <= 1e-5
 
 
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_sample_store_sparse_grid(ops, boundary, mode):
+    """A grid that is zero outside a sub-box: the storing forward skips the
+    samples of empty occupancy blocks (exactly zero), its output is identical
+    to the plain forward's, it stores fewer samples than its rays take (none
+    for an all-zero grid under BORDER and CLAMP, where the boundary samples are
+    covered too), and the gradient equals the re-sampling one."""
+    _, _, M, V, P, F = scene((12, 14, 13), 3, (13, 9, 11))
+    x = small_grid((12, 14, 13), 4, 31) * 0.4
+    x[:, :3] = 0.0
+    x[:, 9:] = 0.0
+    x[:, :, 10:] = 0.0
+    x[:, :, :, :4] = 0.0
+    dy = cuda(np.random.default_rng(32).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+    grads, outs = [], []
+    for store in (False, True):
+        ops.set_raymarch_sample_store(store)
+        try:
+            xt = cuda(x).requires_grad_(True)
+            with ops.grad_mode(mode):
+                y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11), 'LINEAR', boundary)
+                y.backward(dy)
+        finally:
+            ops.set_raymarch_sample_store(True)
+        grads.append(np_(xt.grad))
+        outs.append(np_(y))
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(grads[1], grads[0]) <= 1e-5
+    counts = []
+    for grid in (x, np.zeros_like(x)):
+        smp = ops._samples_buffer(grid.shape, 3, (13, 9, 11), True, 'cuda')
+        ops._raymarch_fwd(cuda(grid), M, V, P, F, (13, 9, 11), 1, BOUNDS.index(boundary), 0, True, samples=smp)
+        counts.append(ops.stored_sample_count(smp, grid.shape, 3, (13, 9, 11)))
+    assert 0 < counts[0] < 3 * 9 * 11 * 13
+    assert counts[1] == 0 if boundary != 'WRAP' else counts[1] < counts[0]
+
+
 def test_raymarch_sample_store_many_pairs(ops):
     """More (batch, camera) pairs than one launch table holds (2 x 9 = 18):
     the store offsets continue across the tables."""

@@ -78,8 +78,9 @@ def test_argument_errors_without_a_gpu(lib):
                                        ctypes.c_void_p(1), None)
     assert st == lib.ERR_INVALID_ARGUMENT and b'2^32' in L.gft_last_error()
     # sample store: LINEAR only, a large enough store, a store pointer
-    assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == ((8 + 7) // 8) * ((4 + 15) // 16) * 4 \
-        * 128 * 4 * 4
+    # one 8x16-pixel tile x 4 steps x 128 lanes of 4 floats, a ballot word per
+    # warp and step, a 2x2x2 occupancy map (256-byte aligned parts)
+    assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == 4 * 128 * 4 * 4 + 256 + 256
     st = L.gft_raymarch_grid_transform_store(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 0, 0, 0, 1,
                                              ctypes.c_void_p(1), ctypes.c_void_p(1), 1 << 20, None)
     assert st == lib.ERR_INVALID_ARGUMENT and b'LINEAR' in L.gft_last_error()
