@@ -405,22 +405,33 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 #pragma unroll
             for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? w[k] : w[k] * val.v[c];
     }
-    for (int r = 1; r <= rounds; ++r) {
-        const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
-                    mz = __shfl_down_sync(0xffffffffu, wz, r);
-        float mv[C];
-        if constexpr (MODE != 2) {
+    if constexpr (MODE == 2) {
+        // Weight sums: a member's 8 sums are its own weights (members never
+        // accumulate), so the head pulls them as they are; zero weights add 0.
+        nz = 0xffu;
+        for (int r = 1; r <= rounds; ++r) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float t = __shfl_down_sync(0xffffffffu, acc[k][0], r);
+                if (r <= n) acc[k][0] += t;
+            }
+        }
+    } else {
+        for (int r = 1; r <= rounds; ++r) {
+            const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
+                        mz = __shfl_down_sync(0xffffffffu, wz, r);
+            float mv[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) mv[c] = __shfl_down_sync(0xffffffffu, val.v[c], r);
-        }
-        if (r <= n) {
-            nz |= zero_weight_mask(mx, my, mz);
-            float w[8];
-            corner_weights(mx, my, mz, w);
+            if (r <= n) {
+                nz |= zero_weight_mask(mx, my, mz);
+                float w[8];
+                corner_weights(mx, my, mz, w);
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
+                for (int k = 0; k < 8; ++k)
 #pragma unroll
-                for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? acc[k][c] + w[k] : fmaf(w[k], mv[c], acc[k][c]);
+                    for (int c = 0; c < C; ++c) acc[k][c] = fmaf(w[k], mv[c], acc[k][c]);
+            }
         }
     }
     if (!head) return;
