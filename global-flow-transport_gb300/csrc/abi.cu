@@ -604,11 +604,17 @@ static size_t mip_ws_bytes(const int64_t* s, int mip, int num) {
     const int L = usable_mip_levels(dims_of(s), num);
     return sizeof(float) * mip_workspace_floats(dims_of(s), L, (int)s[4]) * (size_t)s[0];
 }
+// SampleGridTransform's workspace: the mips, then (with mips) the occupancy
+// maps of the N input slices.
+static size_t transform_ws_bytes(const int64_t* s, int mip, int num) {
+    const size_t m = mip_ws_bytes(s, mip, num);
+    return m == 0 ? 0 : align256(m) + occupancy_bytes(dims_of(s)) * (size_t)s[0];
+}
 
 size_t gft_sample_grid_transform_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps) {
     std::string why;
     if (!grid_shape_ok(input_shape, why)) return 0;
-    return mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+    return transform_ws_bytes(input_shape, mipmapping, num_mipmaps);
 }
 
 static bool build_batch_mips(const void* input, int dtype, const int64_t* s, int mip, int num, void* ws,
@@ -653,12 +659,29 @@ gft_status gft_sample_grid_transform(const void* input, int32_t input_dtype, con
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
     if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
-    const size_t need = mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
+    const size_t need = transform_ws_bytes(input_shape, mipmapping, num_mipmaps);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "mip workspace too small");
     std::vector<MipSet> sets;
     if (!build_batch_mips(input, input_dtype, input_shape, mipmapping, num_mipmaps, workspace, sets, as_stream(stream)))
         return GFT_ERR_CUDA;
+    // Occupancy (forward modes, whose input is a volume, often mostly empty;
+    // BORDER / CLAMP with LINEAR or NEAREST filtering): samples reading only
+    // zeros skip their LOD and fetches.
+    if (need > 0 && (coordinate_mode == 0 || coordinate_mode == 3) &&
+        (boundary == GFT_BOUNDARY_BORDER || boundary == GFT_BOUNDARY_CLAMP) &&
+        (interpolation == GFT_FILTER_LINEAR || interpolation == GFT_FILTER_NEAREST)) {
+        const Dims d = dims_of(input_shape);
+        const size_t esz = input_dtype == GFT_DTYPE_BF16 ? 2 : 4, ob = occupancy_bytes(d);
+        uint8_t* occ = reinterpret_cast<uint8_t*>(workspace) + align256(mip_ws_bytes(input_shape, mipmapping, num_mipmaps));
+        for (int b = 0; b < (int)input_shape[0]; ++b) {
+            const void* base = reinterpret_cast<const char*>(input) + (size_t)b * voxels(d) * input_shape[4] * esz;
+            uint8_t* raw = occ + ob * b;
+            if (!launch_occupancy(base, input_dtype, (int)input_shape[4], d, sets[b].levels, raw, raw + ob / 2,
+                                  as_stream(stream), &sets[b]))
+                return GFT_ERR_CUDA;
+        }
+    }
     SampleArgs a;
     a.input = input;
     a.dtype = input_dtype;

@@ -54,9 +54,21 @@ struct MipSet {
     const float* lvl[MAX_MIPS + 1];
     Dims dims[MAX_MIPS + 1];
     int levels;  // L
+    // Optional occupancy of level 0 per 8^3-voxel block, grown by the
+    // footprint of every level's fetch (occupancy_radius): 0 = every sample
+    // whose (clamped) floor position lies in the block reads only zeros.
+    const uint8_t* occ = nullptr;
+    Dims occ_dims{0, 0, 0};
 };
 int usable_mip_levels(Dims d, int num_mips);
 size_t mip_workspace_floats(Dims d, int levels, int C);
+// Occupancy map of a sampled grid (SampleGridTransform, forward coordinate
+// modes): bytes per batch slice, and the map build (raw blocks into `raw`,
+// grown into set->occ) for one slice.
+constexpr int OCC_BLOCK_SHIFT = 3;
+size_t occupancy_bytes(Dims d);
+bool launch_occupancy(const void* input, int dtype, int C, Dims d, int levels, uint8_t* raw, uint8_t* grown,
+                      cudaStream_t s, MipSet* set);
 
 // error helpers
 void set_error(const std::string& msg);

@@ -189,6 +189,105 @@ bool launch_build_mips(const void* input, int dtype, int C, Dims d, int levels, 
     return true;
 }
 
+// ---- occupancy of a sampled grid -------------------------------------------------
+// A transform-mode sample at level-0 position p reads, at mip level m, the
+// level-m cells around p * 2^-m, i.e. level-0 voxels within 1.5 * 2^m of p;
+// with the floor of the folded position (a few ulp from the exact one) and
+// up to L levels, within 1.5 * 2^L + 3 voxels of floor(p).  Under CLAMP a
+// position beyond the grid reads the clamped border cells of level m, at most
+// 2^(m+1) - 2 voxels from the clamped floor position (level dims = dims >> m).
+// So every voxel read lies within R = max(1.5 * 2^L + 3, 2^(L+1)) voxels of
+// the clamped floor(p).  A block's grown flag ORs the raw flags of the blocks
+// within ceil(R / 8) blocks, so 0 means that every sample with its clamped
+// floor position in the block reads zeros at every level: exactly zero.
+__host__ __device__ inline int occupancy_radius_blocks(int levels) {
+    const int R = max((3 << levels) / 2 + 3, 2 << levels);
+    return (R + (1 << OCC_BLOCK_SHIFT) - 1) >> OCC_BLOCK_SHIFT;
+}
+static Dims occ_block_dims(Dims d) {
+    const int b = 1 << OCC_BLOCK_SHIFT;
+    return Dims{(d.x + b - 1) / b, (d.y + b - 1) / b, (d.z + b - 1) / b};
+}
+size_t occupancy_bytes(Dims d) { return 2 * (((size_t)voxels(occ_block_dims(d)) + 255) & ~size_t(255)); }
+
+// Raw flags: one thread per 8-voxel x-run of a block row (coalesced reads,
+// one flag store per run with a non-zero voxel).
+template <int C, typename S>
+__global__ void k_occupancy_raw(const S* __restrict__ g, Dims d, uint8_t* __restrict__ raw, Dims od) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t runs = (uint32_t)od.x * d.y * d.z;
+    if (t >= runs) return;
+    const int bx = (int)(t % (uint32_t)od.x);
+    const uint32_t r = t / (uint32_t)od.x;  // z * H + y
+    const int y = (int)(r % (uint32_t)d.y), z = (int)(r / (uint32_t)d.y);
+    const int x0 = bx << OCC_BLOCK_SHIFT, x1 = min(x0 + (1 << OCC_BLOCK_SHIFT), d.x);
+    bool nonzero = false;
+    for (int x = x0; x < x1; ++x) {
+        const Vec<C> a = Load<C, S>::at(g, (int64_t)r * d.x + x);
+#pragma unroll
+        for (int c = 0; c < C; ++c) nonzero = nonzero || a.v[c] != 0.f;  // NaN counts as non-zero
+    }
+    if (nonzero) raw[((size_t)(z >> OCC_BLOCK_SHIFT) * od.y + (y >> OCC_BLOCK_SHIFT)) * od.x + bx] = 1;
+}
+
+// Grown flags: one thread per block ORs the raw flags within rb blocks (RB: rb
+// known at compile time, the loads of a row independent; 0: any rb).
+template <int RB>
+__global__ void __launch_bounds__(64) k_occupancy_grow(const uint8_t* __restrict__ raw, Dims od, int rb,
+                                                       uint8_t* __restrict__ grown) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= voxels(od)) return;
+    int x, y, z;
+    unflat32(v, od, x, y, z);
+    const int r = RB > 0 ? RB : rb;
+    unsigned any = 0;
+    for (int k = max(z - r, 0); k <= min(z + r, od.z - 1); ++k)
+        for (int j = max(y - r, 0); j <= min(y + r, od.y - 1); ++j) {
+            const uint8_t* row = raw + ((size_t)k * od.y + j) * od.x;
+            if constexpr (RB > 0) {
+#pragma unroll
+                for (int o = -RB; o <= RB; ++o) {
+                    const int i = x + o;
+                    if (i >= 0 && i < od.x) any |= __ldg(row + i);
+                }
+            } else {
+                for (int i = max(x - r, 0); i <= min(x + r, od.x - 1); ++i) any |= __ldg(row + i);
+            }
+        }
+    grown[v] = any != 0;
+}
+
+template <int C, typename S>
+static void occ_raw_launch(const void* input, Dims d, uint8_t* raw, Dims od, cudaStream_t s) {
+    const int64_t runs = (int64_t)od.x * d.y * d.z;
+    k_occupancy_raw<C, S><<<(unsigned)((runs + 255) / 256), 256, 0, s>>>((const S*)input, d, raw, od);
+}
+
+bool launch_occupancy(const void* input, int dtype, int C, Dims d, int levels, uint8_t* raw, uint8_t* grown,
+                      cudaStream_t s, MipSet* set) {
+    const Dims od = occ_block_dims(d);
+    const int64_t nb = voxels(od);
+    if (!cuda_ok(cudaMemsetAsync(raw, 0, (size_t)nb, s), "zero occupancy")) return false;
+    if (dtype == 0) {
+        if (C == 4) occ_raw_launch<4, float>(input, d, raw, od, s);
+        else if (C == 2) occ_raw_launch<2, float>(input, d, raw, od, s);
+        else occ_raw_launch<1, float>(input, d, raw, od, s);
+    } else {
+        if (C == 4) occ_raw_launch<4, __nv_bfloat16>(input, d, raw, od, s);
+        else if (C == 2) occ_raw_launch<2, __nv_bfloat16>(input, d, raw, od, s);
+        else occ_raw_launch<1, __nv_bfloat16>(input, d, raw, od, s);
+    }
+    const int rb = occupancy_radius_blocks(levels);
+    const unsigned gb = (unsigned)((nb + 63) / 64);
+    if (rb == 1) k_occupancy_grow<1><<<gb, 64, 0, s>>>(raw, od, rb, grown);
+    else if (rb == 2) k_occupancy_grow<2><<<gb, 64, 0, s>>>(raw, od, rb, grown);
+    else k_occupancy_grow<0><<<gb, 64, 0, s>>>(raw, od, rb, grown);
+    if (!launched(2, "occupancy launch")) return false;
+    set->occ = grown;
+    set->occ_dims = od;
+    return true;
+}
+
 // Sampler2::sample3D / Sampling::sample3D with mips (sampling.hpp:551-620, 690-712).
 // Level 0 is read with the storage type S, coarser levels are fp32.
 template <int C, typename S, int BM>
@@ -252,9 +351,13 @@ __device__ __forceinline__ float3 dehom_lod(float4 h) {
     return make_float3(h.x * iw, h.y * iw, h.z * iw);
 }
 
+// With an occupancy map (forward modes): a sample whose clamped floor
+// position lies in an empty grown block reads only zeros at every level and is
+// returned with w = -1 (exactly zero, no position, LOD or fetch needed).
 template <int CM>
 __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float3 din, float3 dout_inv, bool lod,
-                                                bool outside_zero = false) {
+                                                bool outside_zero = false, const uint8_t* occ = nullptr,
+                                                Dims od = Dims{0, 0, 0}) {
     float3 p, f, ex, ey, ez;
     if constexpr (CM == CM_TRANSFORM || CM == CM_LINDEPTH) {
         float4 ndc = idx_to_ndc(idx, dout_inv);
@@ -268,6 +371,12 @@ __device__ __forceinline__ float4 sample_pos_cm(const CamX& c, float3 idx, float
             const float m = 0.5f + 1e-3f * fmaxf(fabsf(f.x), fmaxf(fabsf(f.y), fabsf(f.z)));
             if (f.x <= -m || f.x >= din.x + m || f.y <= -m || f.y >= din.y + m || f.z <= -m || f.z >= din.z + m)
                 return make_float4(f.x, f.y, f.z, 0.f);
+        }
+        if (occ != nullptr && fabsf(f.x) <= 3.0e9f && fabsf(f.y) <= 3.0e9f && fabsf(f.z) <= 3.0e9f) {
+            const int bx = min(max((int)floorf(f.x), 0), (int)din.x - 1) >> OCC_BLOCK_SHIFT;
+            const int by = min(max((int)floorf(f.y), 0), (int)din.y - 1) >> OCC_BLOCK_SHIFT;
+            const int bz = min(max((int)floorf(f.z), 0), (int)din.z - 1) >> OCC_BLOCK_SHIFT;
+            if (__ldg(occ + ((size_t)bz * od.y + by) * od.x + bx) == 0) return make_float4(f.x, f.y, f.z, -1.f);
         }
         p = CM == CM_TRANSFORM ? idx_to_os(c, idx, dout_inv) : idx_to_os_lindepth(c, idx, dout_inv);
         if (!lod || skip_lod<CM>(p, din, outside_zero)) return make_float4(p.x, p.y, p.z, 0.f);
@@ -333,8 +442,10 @@ __global__ void __launch_bounds__(RS_THREADS)
         const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
         const float4 pos = sample_pos_cm<CM>(tab.cam[p], make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
                                              mip_mode != MIP_NONE,
-                                             BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f);
-        if (filter == F_LINEAR || filter == F_NEAREST) r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
+                                             BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f, ms.occ,
+                                             ms.occ_dims);
+        if ((filter == F_LINEAR || filter == F_NEAREST) && !(pos.w < 0.f))
+            r = sample_mip<C, S, BM>(filter, mip_mode, ms, pos, bias, cco);
     }
     store<C>(out, (int64_t)tab.out_slot[p] * nv + v, r);
 }

@@ -371,6 +371,35 @@ def test_sample_transform_forward(ops, cm, filt, boundary, mip):
         assert rel_l2(np_(y), ref) <= FWD_TOL
 
 
+@pytest.mark.parametrize('cm', ['TRANSFORM_LINDEPTH', 'TRANSFORM'])
+@pytest.mark.parametrize('filt', ['NEAREST', 'LINEAR'])
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+@pytest.mark.parametrize('mip', ['NEAREST', 'LINEAR'])
+def test_sample_transform_sparse_volume(ops, cm, filt, boundary, mip):
+    """A volume that is zero outside a small box (volume -> frustum with mips):
+    samples reading only zeros at every level, by the occupancy map of 8^3-voxel
+    blocks grown by the mip footprint, skip their LOD and fetches; the result
+    still matches the oracle."""
+    from oracle import resample as R
+    from oracle import transforms as OT
+    shape, res = (96, 100, 96), (24, 30, 32)  # 12x13x12 blocks, the box in blocks 5-8
+    _, _, M, V, P, F = scene(shape, 2, res)
+    x = np.zeros((1,) + shape + (1,), np.float32)
+    x[:, 40:64, 40:66, 40:64] = small_grid((24, 26, 24), 1, 33)
+    ocm = OT.LINDEPTH if cm == 'TRANSFORM_LINDEPTH' else OT.TRANSFORM
+    y = ops.sample_grid_transform(cuda(x), M, V, P, F, res, filt, boundary, mip, 2, 0.3, cm)
+    ref = R.sample_grid_transform(x, M, V, P, F, res, ['NEAREST', 'LINEAR'].index(filt),
+                                  ['BORDER', 'CLAMP'].index(boundary), ['NONE', 'NEAREST', 'LINEAR'].index(mip), 2,
+                                  0.3, ocm)
+    assert np.abs(ref).max() > 0 and (ref == 0).mean() > 0.3
+    if filt == 'NEAREST' or mip == 'NEAREST':
+        bad = np.any(np.abs(np_(y) - ref) > 1e-5, axis=-1)
+        assert bad.mean() <= 0.02
+        assert rel_l2(np_(y)[~bad], ref[~bad]) <= FWD_TOL
+    else:
+        assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
 @pytest.mark.parametrize('cm', CMS)
 @pytest.mark.parametrize('boundary', BOUNDS)
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])

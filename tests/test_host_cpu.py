@@ -132,10 +132,12 @@ def test_argument_errors_without_a_gpu(lib):
 def test_workspace_sizes(lib):
     L = lib.load()
     s = lib.i64([2, 16, 20, 12, 2])
-    # mips: levels 1..3 for both batch slices, 256 B aligned
+    # mips: levels 1..3 for both batch slices, 256 B aligned; then per slice
+    # two occupancy maps of 2x3x2 8^3-voxel blocks (256 B aligned each)
     n = L.gft_sample_grid_transform_workspace_size(s, 2, 3)
     lv = [(16 >> m) * (20 >> m) * (12 >> m) * 2 for m in (1, 2, 3)]
-    assert n == 2 * 4 * sum((v + 63) // 64 * 64 for v in lv)
+    mips = 2 * 4 * sum((v + 63) // 64 * 64 for v in lv)
+    assert n == (mips + 255) // 256 * 256 + 2 * 2 * 256
     assert L.gft_sample_grid_transform_workspace_size(s, 0, 3) == 0
     assert L.gft_advect_workspace_size(s, 1) == 0 and L.gft_advect_workspace_size(s, 2) >= 16 * 20 * 12 * 2 * 4
 
