@@ -188,11 +188,45 @@ __global__ void k_raymarch_occupancy(const S* __restrict__ in, Dims d, uint8_t* 
             for (int i = 0; i <= ex; ++i) o[((size_t)(bz - k) * od.y + (by - j)) * od.x + (bx - i)] = 1;
 }
 
+// Brick layout: one thread per 2x2x2-voxel brick (its 8 cells contiguous); a
+// non-zero brick marks its block and, where it lies on the block's lower face
+// along an axis (even brick coordinate), the lower neighbour too: at least
+// every block that a non-zero voxel of it marks (more is safe).
+template <int C, typename S>
+__global__ void k_raymarch_occupancy_bricks(const S* __restrict__ in, Dims d, uint8_t* __restrict__ occ, Dims od) {
+    const Dims bd{(d.x + 1) / 2, (d.y + 1) / 2, (d.z + 1) / 2};
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= voxels(bd)) return;
+    const int n = blockIdx.y;
+    const S* g = in + (size_t)n * brick_cells(d) * C + (size_t)b * 8 * C;
+    bool nonzero = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const Vec<C> a = Load<C, S>::at(g, k);  // cells outside the grid hold zeros or are never read
+#pragma unroll
+        for (int c = 0; c < C; ++c) nonzero = nonzero || a.v[c] != 0.f;  // NaN counts as non-zero
+    }
+    if (!nonzero) return;
+    int x2, y2, z2;
+    unflat32(b, bd, x2, y2, z2);
+    const int bx = x2 >> (OCC_SHIFT - 1), by = y2 >> (OCC_SHIFT - 1), bz = z2 >> (OCC_SHIFT - 1);
+    const int ex = (x2 & 1) == 0 && bx > 0, ey = (y2 & 1) == 0 && by > 0, ez = (z2 & 1) == 0 && bz > 0;
+    uint8_t* o = occ + (size_t)n * voxels(od);
+    for (int k = 0; k <= ez; ++k)
+        for (int j = 0; j <= ey; ++j)
+            for (int i = 0; i <= ex; ++i) o[((size_t)(bz - k) * od.y + (by - j)) * od.x + (bx - i)] = 1;
+}
+
 template <int C, typename S, int L>
 static void occ_launch(const RaymarchArgs& a, cudaStream_t s) {
     const Dims od{a.store.nbx, a.store.nby, a.store.nbz};
-    const dim3 grid((unsigned)((voxels(a.din) + 255) / 256), (unsigned)a.N);
-    k_raymarch_occupancy<C, S, L><<<grid, 256, 0, s>>>((const S*)a.input, a.din, a.store.occ, od);
+    if constexpr (L == LAYOUT_BRICK) {
+        const dim3 grid((unsigned)((brick_cells(a.din) / 8 + 255) / 256), (unsigned)a.N);
+        k_raymarch_occupancy_bricks<C, S><<<grid, 256, 0, s>>>((const S*)a.input, a.din, a.store.occ, od);
+    } else {
+        const dim3 grid((unsigned)((voxels(a.din) + 255) / 256), (unsigned)a.N);
+        k_raymarch_occupancy<C, S, L><<<grid, 256, 0, s>>>((const S*)a.input, a.din, a.store.occ, od);
+    }
 }
 
 bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s) {

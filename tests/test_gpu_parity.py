@@ -237,22 +237,28 @@ def test_raymarch_sample_store_sparse_grid(ops, boundary, mode):
 
 def test_raymarch_sample_store_many_pairs(ops):
     """More (batch, camera) pairs than one launch table holds (2 x 9 = 18):
-    the store offsets continue across the tables."""
+    the store offsets continue across the tables, and each batch slice skips
+    by its own occupancy map."""
     _, _, M, V, P, F = scene((10, 14, 12), 9, (13, 9, 11))
-    x = small_grid((10, 14, 12), 4, 29) * 0.4
-    x = np.concatenate([x, x[:, ::-1].copy()], axis=0)
+    # two slices zero outside different boxes: each slice has its own occupancy
+    x = np.zeros((2, 10, 14, 12, 4), np.float32)
+    x[0, 1:5, 2:9, 6:12] = small_grid((4, 7, 6), 4, 29)[0] * 0.4
+    x[1, 5:10, 7:14, 0:6] = small_grid((5, 7, 6), 4, 34)[0] * 0.4
     M2 = np.stack([M[0], M[0]]) if np.asarray(M).ndim == 3 else M
     dy = cuda(np.random.default_rng(30).standard_normal((2, 9, 9, 11, 4)).astype(np.float32))
-    grads = []
+    grads, outs = [], []
     for store in (False, True):
         ops.set_raymarch_sample_store(store)
         try:
             xt = cuda(x).requires_grad_(True)
             with ops.grad_mode('REFERENCE'):
-                ops.raymarch_grid_transform(xt, M2, V, P, F, (13, 9, 11)).backward(dy)
+                y = ops.raymarch_grid_transform(xt, M2, V, P, F, (13, 9, 11))
+                y.backward(dy)
         finally:
             ops.set_raymarch_sample_store(True)
         grads.append(np_(xt.grad))
+        outs.append(np_(y))
+    assert np.array_equal(outs[0], outs[1])
     assert rel_l2(grads[1], grads[0]) <= 1e-5
 
 
@@ -375,7 +381,8 @@ def test_sample_transform_forward(ops, cm, filt, boundary, mip):
 @pytest.mark.parametrize('filt', ['NEAREST', 'LINEAR'])
 @pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
 @pytest.mark.parametrize('mip', ['NEAREST', 'LINEAR'])
-def test_sample_transform_sparse_volume(ops, cm, filt, boundary, mip):
+@pytest.mark.parametrize('N', [1, 2])
+def test_sample_transform_sparse_volume(ops, cm, filt, boundary, mip, N):
     """A volume that is zero outside a small box (volume -> frustum with mips):
     samples reading only zeros at every level, by the occupancy map of 8^3-voxel
     blocks grown by the mip footprint, skip their LOD and fetches; the result
@@ -384,8 +391,11 @@ def test_sample_transform_sparse_volume(ops, cm, filt, boundary, mip):
     from oracle import transforms as OT
     shape, res = (96, 100, 96), (24, 30, 32)  # 12x13x12 blocks, the box in blocks 5-8
     _, _, M, V, P, F = scene(shape, 2, res)
-    x = np.zeros((1,) + shape + (1,), np.float32)
-    x[:, 40:64, 40:66, 40:64] = small_grid((24, 26, 24), 1, 33)
+    x = np.zeros((N,) + shape + (1,), np.float32)
+    x[0, 40:64, 40:66, 40:64] = small_grid((24, 26, 24), 1, 33)[0]
+    if N == 2:  # another box: each slice has its own occupancy map
+        x[1, 10:30, 60:90, 50:80] = small_grid((20, 30, 30), 1, 35)[0]
+        M = np.stack([M[0], M[0]])
     ocm = OT.LINDEPTH if cm == 'TRANSFORM_LINDEPTH' else OT.TRANSFORM
     y = ops.sample_grid_transform(cuda(x), M, V, P, F, res, filt, boundary, mip, 2, 0.3, cm)
     ref = R.sample_grid_transform(x, M, V, P, F, res, ['NEAREST', 'LINEAR'].index(filt),
@@ -568,11 +578,18 @@ def test_raymarch_multi_argument_errors(ops):
 @pytest.mark.parametrize('C', [1, 2, 4])
 @pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP', 'WRAP'])
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
-def test_raymarch_bricked_equals_rows(ops, C, boundary, mode):
+@pytest.mark.parametrize('sparse', [False, True])
+def test_raymarch_bricked_equals_rows(ops, C, boundary, mode, sparse):
     """Odd grid sizes (padded bricks), forward bit-identical, gradient in the
-    brick layout equal to the row gradient."""
+    brick layout equal to the row gradient; sparse: zero outside a box whose
+    faces cut through bricks, so the sample store's occupancy map of the
+    bricked grid (built per brick) and of the row grid (per voxel) differ."""
     _, _, M, V, P, F = scene((9, 13, 11), 3, (13, 9, 11))
     x = small_grid((9, 13, 11), C, 51) * 0.4
+    if sparse:
+        box = np.zeros_like(x)
+        box[:, 3:8, 5:10, 1:6] = x[:, 3:8, 5:10, 1:6]
+        x = box
     dy = cuda(np.random.default_rng(52).standard_normal((1, 3, 9, 11, C)).astype(np.float32))
     xr = cuda(x).requires_grad_(True)
     xb = ops.to_bricks(cuda(x)).requires_grad_(True)
