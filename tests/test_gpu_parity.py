@@ -494,6 +494,51 @@ def test_advect_odd_voxel_count(ops, order, boundary):
     test_advect(ops, order, 'MC_SMOOTH' if order == 2 else 'NONE', boundary, 'REFERENCE', shape=(9, 11, 7))
 
 
+@pytest.mark.parametrize('C', [1, 4])
+@pytest.mark.parametrize('field', ['smooth', 'integer'])
+@pytest.mark.parametrize('boundary', BOUNDS)
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_advect_merged_scatter(ops, C, field, boundary, mode):
+    """The adjoint scatters merge the corners that consecutive voxels along x
+    share: a smooth field (lookups one cell apart, nearly every lane merges)
+    and an integer one (lookups on cell corners, where the ceil corner is the
+    floor corner and counts 2).  Rows of 45 voxels cross the warps, the last
+    block is partial, and two density slices share the velocity (the first
+    slice writes the lookup gradient, the second adds to it)."""
+    from oracle import advect as OA
+    D, H, W = 5, 6, 45
+    rng = np.random.default_rng(60 + C)
+    d = np.stack([small_grid((D, H, W), C, 61 + C)[0], small_grid((D, H, W), C, 62 + C)[0]])
+    if field == 'smooth':
+        def comp(shape, base):
+            z, y, x = np.meshgrid(*[np.arange(n, dtype=np.float64) for n in shape], indexing='ij')
+            return (base + 0.05 * np.sin(0.3 * x + 0.2 * y + 0.1 * z)).astype(np.float32)[None, ..., None]
+        vx, vy, vz = comp((D, H, W + 1), 0.37), comp((D, H + 1, W), -0.21), comp((D + 1, H, W), 0.13)
+        dt = 1.3
+    else:
+        vx = np.full((1, D, H, W + 1, 1), 1.0, np.float32)
+        vy = np.full((1, D, H + 1, W, 1), -1.0, np.float32)
+        vz = np.zeros((1, D + 1, H, W, 1), np.float32)
+        dt = 1.0
+    bi = BOUNDS.index(boundary)
+    dtn = cuda(d).requires_grad_(True)
+    vs = [cuda(v).requires_grad_(True) for v in (vx, vy, vz)]
+    go = rng.standard_normal(d.shape).astype(np.float32)
+    with ops.grad_mode(mode):
+        y = ops.advect(dtn, *vs, dt=dt, order=2, clamp='MC_SMOOTH', boundary=boundary)
+        y.backward(cuda(go))
+    gv_want = [np.zeros(v.shape[1:]) for v in (vx, vy, vz)]
+    for n in range(2):
+        ref = OA.warp(d[n], vx[0], vy[0], vz[0], dt, 2, 'MC_SMOOTH', bi)
+        assert rel_l2(np_(y)[n], ref) <= FWD_TOL
+        gd, *gv = OA.warp_grad(d[n], vx[0], vy[0], vz[0], go[n], dt, 2, 'MC_SMOOTH', bi, exact=(mode == 'EXACT'))
+        assert rel_l2(np_(dtn.grad)[n], gd) <= GRAD_TOL
+        for acc, g in zip(gv_want, gv):
+            acc += g
+    for got, want in zip(vs, gv_want):
+        assert rel_l2(np_(got.grad)[0], want) <= GRAD_TOL
+
+
 # ------------------------------------------------------------------ raymarch, uneven camera batches
 UNEVEN = [(13, 9, 11), (7, 6, 5), (11, 12, 16)]  # (depth samples, height, width) per camera
 
