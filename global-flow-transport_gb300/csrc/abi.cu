@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -200,6 +201,28 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// Vector accesses need aligned device pointers: a tensor of C channels is
+// read and written C elements at a time (16 bytes for C == 4 fp32, 8 for
+// C == 4 bf16), the RGB-plus-density images and lookup tables as float4, and
+// workspaces and sample stores hold float4 / float2 regions.  cudaMalloc and
+// the torch allocator return 256-byte aligned buffers; a misaligned pointer
+// is an argument error here instead of a misaligned access in a kernel.
+size_t vec_bytes(int64_t C, int32_t dtype) { return (size_t)C * (dtype == GFT_DTYPE_BF16 ? 2 : 4); }
+
+gft_status check_aligned(std::initializer_list<const void*> ptrs, size_t a) {
+    for (const void* p : ptrs)
+        if (reinterpret_cast<uintptr_t>(p) % a != 0)
+            return fail(GFT_ERR_INVALID_ARGUMENT,
+                        "device pointer not aligned to its " + std::to_string(a) + "-byte channel vector");
+    return GFT_OK;
+}
+
+gft_status check_workspace_aligned(const void* ws) {
+    if (reinterpret_cast<uintptr_t>(ws) % 16 != 0)
+        return fail(GFT_ERR_WORKSPACE, "workspace or sample store not 16-byte aligned");
+    return GFT_OK;
+}
+
 // Raymarch pairs of one image size: pair k writes output slot out_slot.
 void set_uniform_images(std::vector<Pair>& pairs, int D, int H, int W) {
     for (Pair& p : pairs) {
@@ -308,6 +331,11 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
     if (samples != nullptr) {
         if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
+    }
+    if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(a.C, 0))) != GFT_OK || (st = check_workspace_aligned(samples)) != GFT_OK)
+        return st;
+    if (samples != nullptr) {
         a.store = raymarch_store_layout(samples, pairs, a.C, a.N, a.din);
         if (!launch_raymarch_occupancy(a, as_stream(stream))) return GFT_ERR_CUDA;
     }
@@ -414,6 +442,10 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
         a.store = raymarch_store_layout(const_cast<float*>(samples), pairs, a.C, a.N, a.din);
     }
+    if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
+        (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
+        (st = check_workspace_aligned(samples)) != GFT_OK || (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
     if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
                              cnt, as_stream(stream)))
@@ -439,6 +471,7 @@ gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5]
                                                                         separate_camera_batch, GFT_GRAD_REFERENCE);
     if (workspace == nullptr || workspace_bytes < need)
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    if ((st = check_workspace_aligned(workspace)) != GFT_OK) return st;
     RaymarchArgs a{};
     a.N = (int)input_shape[0];
     a.C = (int)input_shape[4];
@@ -515,6 +548,9 @@ gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dt
     a.blend = blending_mode;
     const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
     a.n_slots = (int)pairs.size();
+    if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(a.C, 0))) != GFT_OK)
+        return st;
     if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
     return GFT_OK;
 }
@@ -563,6 +599,10 @@ gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t inp
     a.blend = blending_mode;
     const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
     a.n_slots = (int)pairs.size();
+    if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
+        (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
     if (!launch_raymarch_bwd(a, pairs, output, output_grad, grad_mode == GFT_GRAD_EXACT, weights_ready, input_grad,
                              cnt, as_stream(stream)))
@@ -585,6 +625,7 @@ gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_sh
                                                                               GFT_GRAD_REFERENCE);
     if (workspace == nullptr || workspace_bytes < need)
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
+    if ((st = check_workspace_aligned(workspace)) != GFT_OK) return st;
     RaymarchArgs a{};
     a.N = (int)input_shape[0];
     a.C = (int)input_shape[4];
@@ -662,6 +703,10 @@ gft_status gft_sample_grid_transform(const void* input, int32_t input_dtype, con
     const size_t need = transform_ws_bytes(input_shape, mipmapping, num_mipmaps);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "mip workspace too small");
+    if ((st = check_aligned({input}, vec_bytes(input_shape[4], input_dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(input_shape[4], 0))) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     std::vector<MipSet> sets;
     if (!build_batch_mips(input, input_dtype, input_shape, mipmapping, num_mipmaps, workspace, sets, as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -739,6 +784,9 @@ gft_status gft_sample_grid_transform_grad(const int64_t input_shape[5], const fl
     const size_t need = gft_sample_grid_transform_grad_workspace_size(input_shape);
     if (grad_mode == GFT_GRAD_REFERENCE && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "sample count workspace too small");
+    if ((st = check_aligned({output_grad, input_grad}, vec_bytes(input_shape[4], 0))) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     const auto pairs = make_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, (int)input_shape[0],
                                   separate_camera_batch != 0);
     const Dims dout{(int)output_grad_shape[4], (int)output_grad_shape[3], (int)output_grad_shape[2]};
@@ -786,6 +834,10 @@ gft_status gft_sample_grid_lut(const void* input, int32_t input_dtype, const int
     const size_t need = mip_ws_bytes(input_shape, mipmapping, num_mipmaps);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "mip workspace too small");
+    if ((st = check_aligned({input}, vec_bytes(input_shape[4], input_dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(input_shape[4], 0))) != GFT_OK ||
+        (st = check_aligned({lookup}, 16)) != GFT_OK || (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     std::vector<MipSet> sets;
     if (!build_batch_mips(input, input_dtype, input_shape, mipmapping, num_mipmaps, workspace, sets, as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -831,6 +883,9 @@ gft_status gft_sample_grid_lut_grad(const float* input, const int64_t input_shap
     const size_t need = gft_sample_grid_lut_grad_workspace_size(input_shape);
     if (grad_mode == GFT_GRAD_REFERENCE && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "sample count workspace too small");
+    if ((st = check_aligned({input, output_grad, input_grad}, vec_bytes(input_shape[4], 0))) != GFT_OK ||
+        (st = check_aligned({lookup, lookup_grad}, 16)) != GFT_OK || (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     LutArgs a;
     a.input = input;
     a.dtype = 0;
@@ -862,6 +917,7 @@ gft_status gft_lod_transform(const int32_t input_shape[3], const float* matrix_m
         return fail(GFT_ERR_INVALID_ARGUMENT, "All shape dimensions must be positive");
     if (!matrix_mv || !matrix_p || !frustum || num <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "camera batch size mismatch");
     if (!output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (const gft_status st = check_aligned({output}, 16); st != GFT_OK) return st;
     const auto pairs = make_pairs(nullptr, 1, matrix_mv, matrix_p, frustum, num, num, false);
     const Dims din{input_shape[2], input_shape[1], input_shape[0]};
     const Dims dout{output_shape[2], output_shape[1], output_shape[0]};
@@ -878,6 +934,7 @@ gft_status gft_reduce_grid_blend(const float* input, const int64_t input_shape[5
     if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blending mode");
     if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (const gft_status st = check_aligned({input, output}, vec_bytes(input_shape[4], 0)); st != GFT_OK) return st;
     if (!launch_blend_fwd(input, (int)input_shape[0], (int)input_shape[4], dims_of(input_shape), blending_mode,
                           keep_dims != 0, output, as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -896,6 +953,9 @@ gft_status gft_reduce_grid_blend_grad(const float* output_grad, const float* out
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blending mode");
     if (!enum_in(grad_mode, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (!output_grad || !output || !input || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (const gft_status st = check_aligned({output_grad, output, input, input_grad}, vec_bytes(input_shape[4], 0));
+        st != GFT_OK)
+        return st;
     if (!launch_blend_bwd(output_grad, output, input, (int)input_shape[0], (int)input_shape[4], dims_of(input_shape),
                           blending_mode, keep_dims != 0, grad_mode == GFT_GRAD_EXACT, input_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -931,6 +991,10 @@ gft_status gft_advect(const void* density, int32_t density_dtype, const int64_t 
     const size_t need = gft_advect_workspace_size(density_shape, order);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "advect workspace too small");
+    if ((st = check_aligned({density}, vec_bytes(density_shape[4], density_dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(density_shape[4], 0))) != GFT_OK ||
+        (st = check_aligned({vel_x, vel_y, vel_z}, 4)) != GFT_OK || (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     AdvectArgs a;
     a.density = density;
     a.dtype = density_dtype;
@@ -973,6 +1037,10 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     const size_t need = gft_advect_grad_workspace_size(density_shape, order);
     if (workspace == nullptr || workspace_bytes < need) return fail(GFT_ERR_WORKSPACE, "advect gradient workspace too small");
+    if ((st = check_aligned({density, output_grad, density_grad}, vec_bytes(density_shape[4], 0))) != GFT_OK ||
+        (st = check_aligned({vel_x, vel_y, vel_z, vel_x_grad, vel_y_grad, vel_z_grad}, 4)) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     AdvectArgs a;
     a.density = density;
     a.dtype = 0;
@@ -1006,6 +1074,7 @@ gft_status gft_transmittance(const float* input, const int64_t shape[5], float* 
     std::string why;
     if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (const gft_status st = check_aligned({input, output}, 4); st != GFT_OK) return st;
     if (!launch_transmittance(input, (int)shape[0], dims_of(shape), output, as_stream(stream))) return GFT_ERR_CUDA;
     return GFT_OK;
 }
@@ -1015,6 +1084,7 @@ gft_status gft_transmittance_grad(const float* output, const float* output_grad,
     std::string why;
     if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    if (const gft_status st = check_aligned({output, output_grad, input_grad}, 4); st != GFT_OK) return st;
     if (!launch_transmittance_grad(output, output_grad, (int)shape[0], dims_of(shape), input_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
@@ -1031,6 +1101,10 @@ gft_status gft_light_compose(const float* density, const float* transmittance, c
     if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
     if (!density || !transmittance || !light_color || !output)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({density, transmittance, light_color}, 4)) != GFT_OK ||
+        (st = check_aligned({output}, 16)) != GFT_OK)
+        return st;
     if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], dims_of(shape), ambient, scale,
                               output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, output, as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -1047,6 +1121,10 @@ gft_status gft_light_compose_grad(const float* density, const float* transmittan
     if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
     if (!density || !transmittance || !light_color || !output_grad || !density_grad || !transmittance_grad)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({density, transmittance, light_color, density_grad, transmittance_grad}, 4)) != GFT_OK ||
+        (st = check_aligned({output_grad}, 16)) != GFT_OK)
+        return st;
     if (!launch_light_compose_grad(density, transmittance, light_color, output_grad, (int)shape[0], dims_of(shape),
                                    ambient, scale, output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, density_grad,
                                    transmittance_grad, as_stream(stream)))
@@ -1065,6 +1143,10 @@ gft_status gft_image_loss(const float* image, const float* target, const float b
     if (!image || !target || !background || !loss) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
     if (workspace == nullptr || workspace_bytes < gft_image_loss_workspace_size(pixels))
         return fail(GFT_ERR_WORKSPACE, "image loss workspace too small");
+    gft_status st;
+    if ((st = check_aligned({image}, 16)) != GFT_OK || (st = check_aligned({target, loss}, 4)) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
     if (!launch_image_loss(image, target, pixels, background, reinterpret_cast<float*>(workspace), loss,
                            as_stream(stream)))
         return GFT_ERR_CUDA;
@@ -1076,6 +1158,9 @@ gft_status gft_image_loss_grad(const float* image, const float* target, const fl
     if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
     if (!image || !target || !background || !loss_grad || !image_grad)
         return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({image, image_grad}, 16)) != GFT_OK || (st = check_aligned({target, loss_grad}, 4)) != GFT_OK)
+        return st;
     if (!launch_image_loss_grad(image, target, pixels, background, loss_grad, image_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;

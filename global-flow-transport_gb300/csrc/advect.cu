@@ -307,15 +307,15 @@ __global__ void __launch_bounds__(AD_THREADS)
         sy += gback.v[i] * ddy.v[i];
         sz += gback.v[i] * ddz.v[i];
     }
-    float* gl = glut + t * 3;
-    if (first) {  // the slice's first lookup-gradient term: written, not added
+    float* gl = glut + t;  // three planes (x, y, z components) of nv floats
+    if (first) {           // the slice's first lookup-gradient term: written, not added
         gl[0] = -sx;
-        gl[1] = -sy;
-        gl[2] = -sz;
+        gl[nv] = -sy;
+        gl[2 * nv] = -sz;
     } else {
         gl[0] -= sx;
-        gl[1] -= sy;
-        gl[2] -= sz;
+        gl[nv] -= sy;
+        gl[2 * nv] -= sz;
     }
 }
 
@@ -369,15 +369,15 @@ __global__ void __launch_bounds__(AD_THREADS)
         sy += gf.v[i] * ddy.v[i];
         sz += gf.v[i] * ddz.v[i];
     }
-    float* gl = glut + t * 3;
-    if (first) {  // the slice's first lookup-gradient term: written, not added
+    float* gl = glut + t;  // three planes (x, y, z components) of nv floats
+    if (first) {           // the slice's first lookup-gradient term: written, not added
         gl[0] = sx;
-        gl[1] = sy;
-        gl[2] = sz;
+        gl[nv] = sy;
+        gl[2 * nv] = sz;
     } else {
         gl[0] += sx;
-        gl[1] += sy;
-        gl[2] += sz;
+        gl[nv] += sy;
+        gl[2 * nv] += sz;
     }
 }
 
@@ -402,9 +402,13 @@ __global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restric
 }
 
 // Velocity gradient: g_centred = -dt * g_lut, then the adjoint of the face
-// average (each face receives half of both adjacent cells).
+// average (each face receives half of both adjacent cells).  glut holds the
+// lookup gradient as three planes (x, y, z components) of voxels(dm) floats.
 __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, float dt, float* __restrict__ gvx,
                                    float* __restrict__ gvy, float* __restrict__ gvz) {
+    const float* __restrict__ gx = glut;
+    const float* __restrict__ gy = glut + voxels(dm);
+    const float* __restrict__ gz = glut + 2 * voxels(dm);
     // nx + ny + nz < 2^32 (checked by the launcher): 32-bit index arithmetic
     const uint32_t nx = (uint32_t)(dm.x + 1) * dm.y * dm.z;
     const uint32_t ny = (uint32_t)dm.x * (dm.y + 1) * dm.z;
@@ -415,8 +419,8 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
         const uint32_t r = t / (uint32_t)(dm.x + 1);  // z*H + y
         const int i = (int)(t - r * (uint32_t)(dm.x + 1));
         float a = 0.f;
-        if (i > 0) a += glut[((int64_t)r * dm.x + i - 1) * 3 + 0];
-        if (i < dm.x) a += glut[((int64_t)r * dm.x + i) * 3 + 0];
+        if (i > 0) a += gx[r * (uint32_t)dm.x + i - 1];
+        if (i < dm.x) a += gx[r * (uint32_t)dm.x + i];
         gvx[t] = h * a;
         return;
     }
@@ -425,8 +429,8 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
         int x, j, z;
         unflat32(t, Dims{dm.x, dm.y + 1, dm.z}, x, j, z);
         float a = 0.f;
-        if (j > 0) a += glut[((((int64_t)z * dm.y) + j - 1) * dm.x + x) * 3 + 1];
-        if (j < dm.y) a += glut[((((int64_t)z * dm.y) + j) * dm.x + x) * 3 + 1];
+        if (j > 0) a += gy[((uint32_t)z * dm.y + j - 1) * dm.x + x];
+        if (j < dm.y) a += gy[((uint32_t)z * dm.y + j) * dm.x + x];
         gvy[t] = h * a;
         return;
     }
@@ -436,8 +440,8 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
         const int64_t k = t / plane;
         const int64_t xy = t - (uint32_t)k * plane;
         float a = 0.f;
-        if (k > 0) a += glut[((k - 1) * plane + xy) * 3 + 2];
-        if (k < dm.z) a += glut[(k * plane + xy) * 3 + 2];
+        if (k > 0) a += gz[(k - 1) * plane + xy];
+        if (k < dm.z) a += gz[k * plane + xy];
         gvz[t] = h * a;
     }
 }
@@ -588,6 +592,14 @@ gft_status gft_advect_noalloc(const void* density, int32_t density_dtype, const 
     }
     if (!density || !vel_x || !vel_y || !vel_z || !output) {
         set_error("tensor pointer is NULL");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
+    // the density and output are accessed as C-element vectors
+    const uintptr_t vin = (uintptr_t)C * (density_dtype == GFT_DTYPE_BF16 ? 2 : 4), vout = (uintptr_t)C * 4;
+    if (reinterpret_cast<uintptr_t>(density) % vin != 0 || reinterpret_cast<uintptr_t>(output) % vout != 0 ||
+        reinterpret_cast<uintptr_t>(vel_x) % 4 != 0 || reinterpret_cast<uintptr_t>(vel_y) % 4 != 0 ||
+        reinterpret_cast<uintptr_t>(vel_z) % 4 != 0) {
+        set_error("device pointer not aligned to its channel vector");
         return GFT_ERR_INVALID_ARGUMENT;
     }
     const double elems = (double)density_shape[1] * (double)density_shape[2] * (double)density_shape[3] * (double)C;

@@ -699,11 +699,18 @@ static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const Raymar
                                                                                cnt, nullptr, RaymarchArgs::Store{}, t);
 }
 
-// Weight sums -> their reciprocals (0 where no sample reached the voxel).
-__global__ void k_invert_weights(float* __restrict__ w, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v = w[i];
-        w[i] = v > 0.f ? 1.f / v : 0.f;
+// Weight sums -> their reciprocals (0 where no sample reached the voxel), 16
+// bytes per access: the workspace is 16-byte aligned (checked at the C ABI)
+// and holds brick_cells (a multiple of 8) floats per pair; n4 = floats / 4.
+__device__ __forceinline__ float inv_or_zero(float v) { return v > 0.f ? 1.f / v : 0.f; }
+__global__ void k_invert_weights(float4* __restrict__ w, int64_t n4) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 v = w[i];
+        v.x = inv_or_zero(v.x);
+        v.y = inv_or_zero(v.y);
+        v.z = inv_or_zero(v.z);
+        v.w = inv_or_zero(v.w);
+        w[i] = v;
     }
 }
 
@@ -724,8 +731,10 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t want = (n + 255) / 256, cap = (int64_t)std::max(sms, 1) * 8;
-    k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), 256, 0, s>>>(ws_cnt, n);
+    const int64_t cap = (int64_t)std::max(sms, 1) * 8;
+    const int64_t want = (n / 4 + 255) / 256;
+    k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), 256, 0, s>>>(
+        reinterpret_cast<float4*>(ws_cnt), n / 4);
     return launched(1, "raymarch weight inversion launch");
 }
 

@@ -9,6 +9,13 @@
  *     resample_grid.cc:330-331);
  *   - tensor data pointers are DEVICE pointers; the caller allocates every
  *     output, gradient and workspace buffer (query sizes with *_workspace_size);
+ *   - alignment: a tensor of C channels is accessed C elements at a time, so
+ *     its pointer is a multiple of C x element bytes (16 for C == 4 fp32, 8
+ *     for C == 4 bf16); RGB + density images, light-composition outputs and
+ *     lookup tables (4 floats per entry) are 16-byte aligned; workspaces and
+ *     sample stores are 16-byte aligned.  cudaMalloc and the torch allocator
+ *     give 256 bytes.  A misaligned tensor is GFT_ERR_INVALID_ARGUMENT, a
+ *     misaligned workspace or sample store GFT_ERR_WORKSPACE;
  *   - 4x4 matrices and frustum parameters are HOST pointers (the reference
  *     declares them HostMemory, resample_grid.cc:1070-1105): 16 floats read
  *     column-major, i.e. numpy ``matrix.transpose()`` flattened, as

@@ -129,6 +129,48 @@ def test_argument_errors_without_a_gpu(lib):
         assert st == lib.ERR_INVALID_ARGUMENT and b'FORWARD_READY' in L.gft_last_error()
 
 
+def test_misaligned_pointers_are_rejected(lib):
+    """Device pointers off their channel vector's alignment (C x element bytes,
+    16 for the float4 images) and workspaces or sample stores off 16 bytes are
+    argument / workspace errors, found before any launch (no GPU needed)."""
+    L = lib.load()
+    eye = np.eye(4, dtype=np.float32).reshape(-1)
+    fr = np.array([1, 3, -1, 1, 1, -1], dtype=np.float32)
+    bkg = np.zeros(3, dtype=np.float32)
+    p = eye.ctypes.data_as(ctypes.c_void_p)
+    f = fr.ctypes.data_as(ctypes.c_void_p)
+    out = lib.i32([4, 4, 4])
+    shape4 = lib.i64([1, 8, 8, 8, 4])
+    al = ctypes.c_void_p(1 << 20)  # aligned fake device addresses, never dereferenced
+    off4 = ctypes.c_void_p((1 << 20) + 4)
+    off2 = ctypes.c_void_p((1 << 20) + 2)
+    # a four-channel fp32 input, then an output, 4 bytes off a 16-byte boundary
+    st = L.gft_raymarch_grid_transform(off4, 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 1, al, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+    st = L.gft_raymarch_grid_transform(al, 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 1, off4, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+    # a sample store and a gradient workspace 4 bytes off 16
+    st = L.gft_raymarch_grid_transform_store(al, 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 1, al, off4, 1 << 20,
+                                             None)
+    assert st == lib.ERR_WORKSPACE and b'16-byte' in L.gft_last_error()
+    st = L.gft_raymarch_grid_transform_grad(al, 0, shape4, al, al, p, 1, p, p, f, 1, out, 1, 0, 0, 1, 0, al, off4,
+                                            1 << 20, None)
+    assert st == lib.ERR_WORKSPACE and b'16-byte' in L.gft_last_error()
+    st = L.gft_raymarch_grid_transform_grad_weights(shape4, p, 1, p, p, f, 1, out, 0, 1, off4, 1 << 20, None)
+    assert st == lib.ERR_WORKSPACE
+    # a two-channel bf16 density needs 4 bytes, a two-channel fp32 output 8
+    shape2 = lib.i64([1, 8, 8, 8, 2])
+    st = L.gft_advect(off2, 1, shape2, al, al, al, 1.0, 1, 0, 1, al, None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+    st = L.gft_advect(al, 0, shape2, al, al, al, 1.0, 1, 0, 1, off4, None, 0, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+    st = L.gft_advect_noalloc(off2, 1, shape2, al, al, al, 1.0, 1, 0, 1, al, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+    # the image loss reads RGB + density pixels as float4
+    st = L.gft_image_loss(off4, al, bkg.ctypes.data_as(ctypes.c_void_p), 16, al, al, 1 << 20, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
+
+
 def test_workspace_sizes(lib):
     L = lib.load()
     s = lib.i64([2, 16, 20, 12, 2])
