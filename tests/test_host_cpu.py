@@ -41,6 +41,48 @@ def test_library_exports_every_declared_symbol(lib):
     assert b'sm_103a' in L.gft_version()
 
 
+def _prototypes():
+    """name -> (return type, [parameter declarations]) of every gft.h function."""
+    text = re.sub(r'/\*.*?\*/', '', open(HEADER).read(), flags=re.S)
+    protos = {}
+    for m in re.finditer(r'([A-Za-z_][\w ]*?\**)\s*\b(gft_\w+)\s*\(([^;{]*?)\)\s*;', text):
+        params = [p.strip() for p in m.group(3).split(',')]
+        protos[m.group(2)] = (m.group(1).strip(), [] if params in ([''], ['void']) else params)
+    return protos
+
+
+def _kind_of_decl(decl):
+    if '*' in decl or '[' in decl:
+        return 'ptr'
+    # size_t and unsigned long long: one 64-bit unsigned type on the LP64 hosts
+    for key, kind in (('size_t', 'u64'), ('int64_t', 'i64'), ('int32_t', 'i32'), ('float', 'f32'),
+                      ('unsigned long long', 'u64'), ('gft_status', 'i32')):
+        if key in decl:
+            return kind
+    raise AssertionError('unclassified declaration: ' + decl)
+
+
+def _kind_of_ctype(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return 'ptr'
+    if t in (ctypes.c_size_t, ctypes.c_ulonglong):
+        return 'u64' if ctypes.sizeof(t) == 8 else 'u32'
+    return {ctypes.c_int64: 'i64', ctypes.c_int32: 'i32', ctypes.c_float: 'f32'}[t]
+
+
+def test_bindings_match_the_header_prototypes(lib):
+    """Every ctypes signature of gft._lib has the parameter count, parameter
+    kinds (pointer / f32 / i32 / i64 / u64) and return kind of its gft.h
+    prototype, so a changed prototype cannot be bound with a stale layout."""
+    protos = _prototypes()
+    assert set(protos) == set(lib._SIGS)
+    for name, (ret, params) in protos.items():
+        sig_ret, sig_args = lib._SIGS[name]
+        assert len(sig_args) == len(params), name
+        assert [_kind_of_ctype(t) for t in sig_args] == [_kind_of_decl(p) for p in params], name
+        assert _kind_of_ctype(sig_ret) == _kind_of_decl(ret), name
+
+
 def test_argument_errors_without_a_gpu(lib):
     L = lib.load()
     shape3 = lib.i64([1, 8, 8, 8, 3])
