@@ -1,0 +1,27 @@
+"""bench.py's reference arm runs on the host cores alone (the FP64 oracle port
+of the step on a bounded sample): one JSON line with the metric, unit and
+value of the GPU arm's workload, its cpu_baseline record and an end-to-end
+record without transfers, on a short CPU budget."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_json_line():
+    out = subprocess.run([sys.executable, 'bench.py', '--impl', 'reference', '--cpu-budget', '1', '--steps', '1',
+                          '--warmup', '3'], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line['impl'] == 'reference'
+    assert line['metric'] == 'fwd+bwd render+advect iters/s' and line['unit'] == 'iters/s'
+    assert line['value'] > 0 and line['higher_is_better'] is True and line['n_gpus'] == 1
+    assert line['config']['workload'].startswith('cfg2')
+    cb = line['cpu_baseline']
+    assert cb['kind'] == 'port' and cb['cores'] >= 1 and cb['sample'] and cb['value'] == line['value']
+    assert line['e2e'] == {'value': line['value'], 'unit': 'iters/s', 'h2d_bytes_per_step': 0,
+                           'd2h_bytes_per_step': 0}
