@@ -25,3 +25,14 @@ def test_reference_arm_prints_one_json_line():
     assert cb['kind'] == 'port' and cb['cores'] >= 1 and cb['sample'] and cb['value'] == line['value']
     assert line['e2e'] == {'value': line['value'], 'unit': 'iters/s', 'h2d_bytes_per_step': 0,
                            'd2h_bytes_per_step': 0}
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    """Under torchrun with N > 1 only rank 0 times and prints; rank 1 exits 0
+    and prints nothing."""
+    env = dict(os.environ, RANK='1', LOCAL_RANK='1', WORLD_SIZE='2')
+    out = subprocess.run([sys.executable, 'bench.py', '--impl', 'reference', '--gpus', '2', '--cpu-budget', '1',
+                          '--steps', '1', '--warmup', '3'], cwd=ROOT, env=env, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip() == ''
