@@ -1,17 +1,20 @@
 """Benchmark: fwd+bwd render + advect iterations per second on one GB300.
 
-Workload (default ``cfg2``, the multi-view frame configuration): plume density
-128x227x128 advected one MacCormack step (MC_SMOOTH, CLAMP) by a staggered
-curl-noise velocity field, spot light with a 256x196x196 shadow frustum (3 mip
-levels, inverse-resampling gradients), 5 perspective views of 480x270 with 192
-depth samples, fused Beer-Lambert raymarch, L2 image loss against seeded target
-renders; one step = forward + backward to the previous density and all three
-velocity components.  Synthetic seeded data stand in for ScalarFlow.
+Workload (default ``cfg5``, the largest configuration, with BF16 storage and
+FP32 arithmetic): plume density 256x455x256 advected one MacCormack step
+(MC_SMOOTH, CLAMP) by a staggered curl-noise velocity field, spot light with a
+256x196x196 shadow frustum (4 mip levels, inverse-resampling gradients), 5
+perspective views of 960x540 with 256 depth samples, fused Beer-Lambert
+raymarch, L2 image loss against seeded target renders; one step = forward +
+backward to the previous density and all three velocity components, replayed
+from one CUDA graph.  Synthetic seeded data stand in for ScalarFlow.
 
 Arms:
   default            this repo: batched kernels, whole step in one CUDA graph
-  --impl reference   the FP64 NumPy port of the reference ops on the host cores
-                     (the reference's ops are CUDA-only TensorFlow kernels)
+  --impl reference   the reference's path on the host cores: its ops are
+                     CUDA-only TensorFlow kernels, so its CPU stand-in is the
+                     FP64 NumPy port in oracle/, run as whole iterations on all
+                     cores (oracle/cpu_step.py FullStep)
 
 One JSON line on stdout (rank 0).
 """
@@ -31,6 +34,8 @@ for _p in (ROOT, PKG):
 
 METRIC = 'fwd+bwd render+advect iters/s'
 L2_BYTES = 129 * 1024 * 1024
+DEFAULT_CONFIG = 'cfg5'
+DEFAULT_STORAGE = 'bf16'
 
 
 def _peaks():
@@ -138,6 +143,78 @@ def _ddp():
     return ws, rank, local
 
 
+
+
+# ---------------------------------------------------------------- workload
+def _storage_dtype(name):
+    import torch
+    return torch.bfloat16 if name == 'bf16' else None
+
+
+def workload_config(config, storage, grad_mode):
+    """The ``config`` object both arms print: the workload they run."""
+    from gft.pipeline import CONFIGS
+    c = CONFIGS[config]
+    D, H, W = c['grid']
+    Wi, Hi = c['image']
+    return {'workload': '%s: density %dx%dx%d (%s storage, fp32 arithmetic), MacCormack advect (MC_SMOOTH, CLAMP), '
+                        'spot-light shadow %s (%d mips), %d views %dx%d x%d samples, L2 image loss, fwd+bwd'
+                        % (config, D, H, W, storage, 'x'.join(map(str, c['shadow'])), c['mips'], c['views'], Wi, Hi,
+                           c['samples']),
+            'config': config, 'storage': storage, 'grad_mode': grad_mode,
+            'l2': 'inputs larger than L2 (129 MB); the GPU arm also flushes L2 between timed steps'}
+
+
+def alg_bytes(step, storage_bytes):
+    """Compulsory unique bytes of one iteration by the per-op formulas of the
+    path (s = bytes per stored grid element; the grids the shadow pass
+    resamples, the velocities and every gradient are fp32):
+      mips          sum over the 4 pyramids (two resampled grids, two resampled
+                    gradients) of sum_m (N_m + N_m+1) * 4
+      render fwd    N*4*s + P*4*4                 (P = views * H * W pixels)
+      render bwd    N*4*s + 2*P*4*4 + 2*N*4*4
+      shadow        2 * (N*4 + 2*S*4 + S*4 + N*4) (forward and its inverse-
+                    resampling gradient; S frustum cells)
+      advect fwd    N*s + F*4 + N*4               (F velocity faces)
+      advect bwd    (2*N + 2*F)*4 + N*s
+    Returns (total, per-part dict)."""
+    import numpy as np
+    D, H, W = step.shape
+    N = D * H * W
+    Dc, Hi, Wi = step.res
+    P = len(step.cams) * Hi * Wi
+    Ds, Hs, Ws = step.shadow_res
+    S = Ds * Hs * Ws
+    F = (W + 1) * H * D + W * (H + 1) * D + W * H * (D + 1)
+    s = storage_bytes
+
+    def pyramid(dims, L):
+        tot, d = 0, tuple(dims)
+        for _ in range(L):
+            nxt = tuple(max(1, x // 2) for x in d)
+            tot += (int(np.prod(d)) + int(np.prod(nxt))) * 4
+            d = nxt
+        return tot
+    L = step.rs.num_mips
+    parts = {
+        'mips': 2 * pyramid((D, H, W), L) + 2 * pyramid((Ds, Hs, Ws), L),
+        'render_fwd': N * 4 * s + P * 16,
+        'render_bwd': N * 4 * s + 2 * P * 16 + 2 * N * 16,
+        'shadow': 2 * (N * 4 + 2 * S * 4 + S * 4 + N * 4),
+        'advect_fwd': N * s + F * 4 + N * 4,
+        'advect_bwd': (2 * N + 2 * F) * 4 + N * s,
+    }
+    return sum(parts.values()), parts
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the dominant kernel, from one ncu capture of
+#   python bench.py --kernel-only raymarch_scatter --config <c> --storage <s>
+# (summaries in profiles/raymarch_scatter_<c>.md)
+SCATTER_TRAFFIC = {}
+
+
+# ------------------------------------------------------------------ our arm
 def bench_ours(args):
     import numpy as np
     import torch
@@ -151,7 +228,7 @@ def bench_ours(args):
         import torch.distributed as dist
         dist.init_process_group('nccl', device_id=dev)
     lib = _lib.load()
-    storage = torch.bfloat16 if args.storage == 'bf16' else None
+    storage = _storage_dtype(args.storage)
     ops.set_grad_mode(args.grad_mode)
 
     step = RenderAdvectStep(args.config, dev, storage_dtype=storage, mode='batched')
@@ -199,23 +276,23 @@ def bench_ours(args):
             torch.distributed.destroy_process_group()
         return
     value = ws * 1000.0 / ms
+    total_bytes, parts = alg_bytes(step, 2 if storage is not None else 4)
+    peak, src = _peaks()
     line = {
         'metric': METRIC, 'value': value, 'unit': 'iters/s', 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'f32' if storage is None else 'bf16-storage/f32',
+        'vs_baseline': None, 'dtype': 'bf16-storage/f32' if storage is not None else 'f32',
         'data': 'synthetic (seeded plume + curl-noise velocity; ScalarFlow absent)',
-        'config': {'workload': '%s: density %s, MacCormack advect, spot-light shadow %s (%d mips), %d views %dx%d x%d '
-                               'samples, L2 image loss, fwd+bwd' % (args.config, 'x'.join(map(str, step.shape)),
-                                                                   'x'.join(map(str, step.shadow_res)), step.rs.num_mips,
-                                                                   len(step.cams), step.res[1], step.res[2],
-                                                                   step.res[0]),
-                   'grad_mode': args.grad_mode, 'cuda_graph': True,
-                   'l2': 'flushed between timed steps (write of 258 MB)', 'parallelism': 'replicas' if ws > 1 else 'single'},
+        'config': workload_config(args.config, args.storage, args.grad_mode),
+        'cuda_graph': True, 'parallelism': 'replicas' if ws > 1 else 'single',
         'gpu_launches': int(launches_per_step * args.steps),
         'launches_per_step': int(launches_per_step),
         'loss': loss_val,
         'wall_s_timed': t_wall,
         'clocks': clocks,
+        'step_roofline': {'alg_bytes': total_bytes, 'parts': parts, 'achieved_GBps': total_bytes / ms / 1e6,
+                          'peak': peak, 'frac': total_bytes / ms / 1e6 / peak, 'unit': 'GB/s',
+                          'what': 'whole iteration: compulsory bytes by the per-op formulas / step time'},
     }
     line.update(result)
     print(json.dumps(line), flush=True)
@@ -223,13 +300,26 @@ def bench_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _grads_of(step):
+    import torch
+    loss, grads = step.replay()
+    torch.cuda.synchronize()
+    return float(loss), [g.detach().float().clone() for g in grads]
+
+
+def _rel(a, b):
+    import torch
+    n = float(torch.linalg.norm(b.double()))
+    return float(torch.linalg.norm((a - b).double())) / (n if n > 0 else 1.0)
+
+
 def extras(args, step, dev, timed, storage, inputs, ms):
-    """e2e through the public API, the plain per-op path, per-kernel roofline
-    and the CPU baseline."""
+    """e2e through the public API, the FP32 step beside the headline, the
+    plain per-op FP32 path, the accuracy of BF16 storage, per-kernel
+    roofline, the other workloads and the CPU baseline."""
     import numpy as np
     import torch
-    from gft import ops
-    from gft.pipeline import RenderAdvectStep
+    from gft.pipeline import RenderAdvectStep, StreamedSteps
     out = {}
     # ---- e2e: pinned host inputs -> device, graph step, loss -> host ----------
     # Through the public streaming API (gft.pipeline.StreamedSteps): every
@@ -237,7 +327,6 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     # host memory and reads its loss back; the copy of step i+1's inputs
     # overlaps step i.  e2e_serial: one step at a time, the host waiting for
     # each loss before it copies the next inputs.
-    from gft.pipeline import StreamedSteps
     hosts = [StreamedSteps.host_inputs(inputs), StreamedSteps.host_inputs(step.make_inputs(frame=1))]
     h2d = StreamedSteps.h2d_bytes(hosts[0])
     streamed = StreamedSteps(step, inputs, warmup=args.warmup)
@@ -265,34 +354,89 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     out['e2e_serial'] = {'value': 1000.0 / ser_ms, 'unit': 'iters/s', 'ms_per_step': ser_ms,
                          'what': 'one step at a time: copy inputs, replay, read the loss, wait'}
     del streamed
+    torch.cuda.empty_cache()
 
-    # ---- plain: per-camera launches, composed advection, no graph -----------
+    # ---- the same batched graph step with FP32 storage ------------------------
+    f32 = step
+    if storage is not None:
+        f32 = RenderAdvectStep(args.config, dev, storage_dtype=None, mode='batched')
+        f32.setup_static(inputs)
+        f32.capture(warmup=args.warmup)
+        for _ in range(3):
+            f32.replay()
+        t = timed(f32.replay, min(max(5, args.steps), 50))
+        out['batched_f32'] = {'value': 1000.0 / float(np.mean(t)), 'unit': 'iters/s',
+                              'ms_per_step': float(np.mean(t)),
+                              'what': 'the headline step with FP32 storage'}
+        # accuracy of BF16 storage against the FP32 step on the same inputs
+        # (the FP32 path is held to the FP64 oracle by the -m gpu tests)
+        lb, gb = _grads_of(step)
+        lf, gf = _grads_of(f32)
+        out['bf16_accuracy'] = {'loss_rel': abs(lb - lf) / abs(lf),
+                                'grad_rel_l2': dict(zip(('density', 'vel_x', 'vel_y', 'vel_z'),
+                                                        [_rel(a, b) for a, b in zip(gb, gf)])),
+                                'against': 'FP32 storage, same inputs (FP32 is within 1e-4 of FP64: '
+                                           'tests/test_gpu_configs.py)'}
+    ms_f32 = out.get('batched_f32', {}).get('ms_per_step', ms)
+
+    # ---- plain: per-camera launches, composed advection, no graph, FP32 ------
     plain = RenderAdvectStep(args.config, dev, storage_dtype=None, mode='plain')
     plain.setup_static(inputs)
     for _ in range(2):
         plain.run_static()
     torch.cuda.synchronize()
-    pt = timed(plain.run_static, min(max(3, args.steps // 3), 30))
+    pt = timed(plain.run_static, min(max(3, args.steps // 3), 20))
     out['plain'] = {'value': 1000.0 / float(np.mean(pt)), 'unit': 'iters/s', 'ms_per_step': float(np.mean(pt)),
-                    'what': 'same step, one raymarch launch per camera, advection from 4 SampleGridLut calls + '
-                            'elementwise ops, no CUDA graph'}
+                    'what': 'FP32 storage, one raymarch launch per camera, advection from 4 SampleGridLut calls + '
+                            'elementwise ops, tensor-op glue, no CUDA graph'}
     out['batched_vs_plain'] = out['plain']['ms_per_step'] / ms
+    out['batched_f32_vs_plain'] = out['plain']['ms_per_step'] / ms_f32
     del plain
+    torch.cuda.empty_cache()
 
     # ---- per-kernel timing of the dominant ops (roofline) -------------------
-    out.update(kernel_roofline(step, dev, timed))
+    out.update(kernel_roofline(step, dev, timed, storage))
+    if f32 is not step:
+        del f32
+        torch.cuda.empty_cache()
     out['static_cameras'] = static_cameras(args, dev, timed, storage, inputs)
     out['uneven_views'] = uneven_views(dev, timed)
-    out['transport_chain'] = transport_chain(step, dev, timed)
+    out['cfg2'] = other_config('cfg2', args, dev, timed)
+    out['transport_chain'] = transport_chain('cfg2', dev, timed, frames=16, every=4)
+    if not args.no_chain5:
+        out['transport_chain_cfg5'] = transport_chain(args.config, dev, timed, frames=args.chain_frames, every=8,
+                                                      storage=storage, iters=2)
 
     # ---- CPU baseline ------------------------------------------------------------
     if not args.no_cpu:
         try:
             from oracle import cpu_step
-            out['cpu_baseline'] = cpu_step.time_step(step, inputs, budget_s=args.cpu_budget, workers=1)
+            out['cpu_baseline'] = cpu_step.time_step(budget_s=args.cpu_budget, workers=1, config=args.config)
         except Exception as e:  # the baseline is reported, not required
             out['cpu_baseline'] = {'error': repr(e)}
     return out
+
+
+def other_config(config, args, dev, timed):
+    """The headline's graph step on another configuration, FP32 and BF16."""
+    import numpy as np
+    import torch
+    from gft.pipeline import RenderAdvectStep
+    res = {}
+    inputs = None
+    for name, dt in (('f32', None), ('bf16', torch.bfloat16)):
+        st = RenderAdvectStep(config, dev, storage_dtype=dt, mode='batched')
+        inputs = inputs or st.make_inputs()
+        st.setup_static(inputs)
+        st.capture(warmup=3)
+        for _ in range(3):
+            st.replay()
+        t = timed(st.replay, 30)
+        res[name] = {'ms_per_step': float(np.mean(t)), 'value': 1000.0 / float(np.mean(t)), 'unit': 'iters/s'}
+        del st
+        torch.cuda.empty_cache()
+    res['workload'] = workload_config(config, 'f32|bf16', args.grad_mode)['workload']
+    return res
 
 
 def static_cameras(args, dev, timed, storage, inputs):
@@ -301,6 +445,7 @@ def static_cameras(args, dev, timed, storage, inputs):
     the geometry alone, so they are computed once and reused instead of in
     every step (opt-in; the headline number recomputes them every step)."""
     import numpy as np
+    import torch
     from gft import ops
     from gft.pipeline import RenderAdvectStep
     if args.grad_mode != 'REFERENCE':
@@ -317,59 +462,76 @@ def static_cameras(args, dev, timed, storage, inputs):
                 'what': 'cached raymarch weight sums (fixed cameras), otherwise the timed step'}
     finally:
         ops.set_raymarch_weight_cache(False)
+        torch.cuda.empty_cache()
 
 
-def transport_chain(step, dev, timed, frames=16, every=4):
-    """The global-transport chain on the step's workload: an initial density
-    and 15 seeded staggered velocity fields, MacCormack advection through 16
-    frames, every frame rendered by the 5 views and compared with its target,
-    gradients to the initial density and all velocities, the adjoint
-    recomputing each 4-frame segment from its stored first density
-    (gft.chain.TransportChain).  One CUDA graph per iteration when capture
-    succeeds, else eager."""
+def transport_chain(config, dev, timed, frames=16, every=4, storage=None, iters=5):
+    """The global-transport chain on a configuration's workload: an initial
+    density and frames-1 seeded staggered velocity fields, MacCormack advection
+    through all frames, every frame rendered by the views and compared with
+    its target, gradients to the initial density and all velocities, the
+    adjoint recomputing each segment of ``every`` frames from its stored first
+    density (gft.chain.TransportChain).  One CUDA graph per iteration when
+    capture succeeds, else eager.  Reports the peak device memory."""
     import numpy as np
     import torch
     from gft import synthetic as syn
     from gft.chain import TransportChain
-    shape = step.shape
-    d0 = torch.from_numpy(syn.plume_density(shape, 3000)).to(dev).requires_grad_(True)
-    vels = []
-    for t in range(frames - 1):
-        vx, vy, vz = syn.curl_velocity(shape, 3100 + t)
-        vels.append(tuple(torch.from_numpy(v).to(dev).requires_grad_(True) for v in (vx, vy, vz)))
-    with torch.no_grad():
-        targets = [step.render(torch.from_numpy(syn.plume_density(shape, 3200 + t, t)).to(dev))[..., :3].contiguous()
-                   for t in range(frames)]
-    chain = TransportChain(step, frames=frames, checkpoint_every=every)
-    params = [d0] + [v for tr in vels for v in tr]
-
-    def it():
-        loss = chain.loss(d0, vels, targets)
-        return loss, torch.autograd.grad(loss, params)
-
-    graph, why = None, None
+    from gft.pipeline import RenderAdvectStep
     try:
-        side = torch.cuda.Stream(dev)
-        side.wait_stream(torch.cuda.current_stream(dev))
-        with torch.cuda.stream(side):
-            for _ in range(2):
-                it()
-        torch.cuda.current_stream(dev).wait_stream(side)
-        torch.cuda.synchronize(dev)
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            out = it()
-        run = graph.replay
-    except Exception as e:
-        graph, why = None, repr(e)[:200]
-        torch.cuda.synchronize(dev)
-        run = it
-    run()
-    ms = float(np.median(timed(run, 5, flush_l2=False)))
-    return {'workload': '%d frames, density %s, 5 views, MacCormack chain, fwd+bwd to the initial density and all '
-                        'velocities, checkpoint every %d frames' % (frames, 'x'.join(map(str, shape)), every),
-            'ms_per_iteration': ms, 'iters_per_s': 1000.0 / ms, 'cuda_graph': graph is not None,
-            'frames_per_s': frames * 1000.0 / ms, **({'capture_error': why} if why else {})}
+        step = RenderAdvectStep(config, dev, storage_dtype=storage, mode='batched')
+        shape = step.shape
+        torch.cuda.empty_cache()
+        torch.cuda.reset_peak_memory_stats(dev)
+        base = torch.cuda.memory_allocated(dev)
+        d0 = torch.from_numpy(syn.plume_density(shape, 3000)).to(dev).requires_grad_(True)
+        vels = []
+        for t in range(frames - 1):
+            vx, vy, vz = syn.curl_velocity_device(shape, 3100 + t, dev)
+            vels.append(tuple(v.requires_grad_(True) for v in (vx, vy, vz)))
+        with torch.no_grad():
+            targets = [step.render(syn.plume_density_device(shape, 3200 + t, dev, t))[..., :3].contiguous()
+                       for t in range(frames)]
+        chain = TransportChain(step, frames=frames, checkpoint_every=every)
+        params = [d0] + [v for tr in vels for v in tr]
+
+        def it():
+            loss = chain.loss(d0, vels, targets)
+            return loss, torch.autograd.grad(loss, params)
+
+        graph, why = None, None
+        try:
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(side):
+                for _ in range(2):
+                    it()
+            torch.cuda.current_stream(dev).wait_stream(side)
+            torch.cuda.synchronize(dev)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                out = it()
+            run = graph.replay
+        except Exception as e:
+            graph, why = None, repr(e)[:200]
+            torch.cuda.synchronize(dev)
+            run = it
+        run()
+        ms = float(np.median(timed(run, iters, flush_l2=False)))
+        peak = torch.cuda.max_memory_allocated(dev) - base
+        res = {'workload': '%d frames, density %s (%s storage), %d views, MacCormack chain, fwd+bwd to the initial '
+                           'density and all velocities, checkpoint every %d frames'
+                           % (frames, 'x'.join(map(str, shape)), 'bf16' if storage is not None else 'f32',
+                              len(step.cams), every),
+               'ms_per_iteration': ms, 'iters_per_s': 1000.0 / ms, 'cuda_graph': graph is not None,
+               'frames_per_s': frames * 1000.0 / ms, 'peak_hbm_bytes': int(peak),
+               **({'capture_error': why} if why else {})}
+        del graph, chain, vels, targets, d0, params
+        torch.cuda.empty_cache()
+        return res
+    except Exception as e:  # reported, not required
+        torch.cuda.empty_cache()
+        return {'error': repr(e)[:300]}
 
 
 def uneven_views(dev, timed):
@@ -419,60 +581,17 @@ def uneven_views(dev, timed):
             'sizes': [s[1] for s in shapes], 'one_launch_ms': tm, 'per_view_ms': tp, 'speedup': tp / tm}
 
 
-SCATTER_PROFILE = os.path.join(ROOT, 'profiles', 'raymarch_scatter_cfg2.md')
-
-
-def _profiled_traffic():
-    """DRAM bytes per launch of the raymarch adjoint scatter pass from the
-    committed ncu summary (its ``dram_bytes_per_launch:`` line), else None."""
-    try:
-        with open(SCATTER_PROFILE) as f:
-            for line in f:
-                if line.strip().startswith('dram_bytes_per_launch:'):
-                    return int(line.split(':', 1)[1].strip().split()[0])
-    except (OSError, ValueError):
-        pass
-    return None
-
-
-def _clipped_samples(step):
-    """Ray samples inside the raymarch's clipped step ranges at this workload
-    (the kernels' BORDER slab test, in float64): the samples the forward
-    stores and the adjoint reads back."""
-    import numpy as np
-    D, H, W = step.res
-    gz, gy, gx = step.shape
-    m = np.asarray(step.M, np.float64)[0].T
-    ys, xs = np.meshgrid(np.arange(H) + 0.5, np.arange(W) + 0.5, indexing='ij')
-    zmax = max(D - 1, 1)
-    hi = np.array([gx, gy, gz], np.float64) + 0.55
-    total = 0
-    for c in range(len(step.cams)):
-        inv = np.linalg.inv(np.asarray(step.V, np.float64)[c].T @ m) @ np.linalg.inv(np.asarray(step.P, np.float64)[c].T)
-
-        def os_at(zi):
-            ndc = np.stack([xs / W * 2 - 1, ys / H * 2 - 1, np.full_like(xs, zi / D * 2 - 1), np.ones_like(xs)], -1)
-            h = ndc @ inv.T
-            return h[..., :3] / h[..., 3:4]
-        near = os_at(0.5)
-        st = (os_at(zmax + 0.5) - near) / zmax
-        with np.errstate(divide='ignore', invalid='ignore'):
-            a, b = (-1.05 - near) / st, (hi - near) / st
-        t0 = np.maximum(0.0, np.max(np.minimum(a, b), -1))
-        t1 = np.minimum(D - 1.0, np.min(np.maximum(a, b), -1))
-        i0, i1 = np.maximum(0, np.floor(t0) - 1), np.minimum(D - 1, np.ceil(t1) + 1)
-        total += int(np.sum(np.where(t0 <= t1, i1 - i0 + 1, 0)))
-    return total
-
-
-def kernel_roofline(step, dev, timed):
+def kernel_roofline(step, dev, timed, storage=None):
     """Times the render kernels alone with CUDA events on their stream (L2
-    flushed before each launch) and converts the algorithmic bytes per launch
-    into GB/s against the measured HBM peak.  The dominant kernel is the
-    raymarch adjoint's scatter pass (k_raymarch_scatter, one launch for the 5
-    views) as the step runs it: reading the samples the forward stored, with
-    its per-camera weight sums precomputed (GFT_GRAD_WEIGHTS_READY: a gradient
-    memset plus the scatter launch)."""
+    flushed before each launch).  The dominant kernel is the raymarch
+    adjoint's scatter pass (k_raymarch_scatter, one launch for all views) as
+    the step runs it: reading the samples the forward stored, with its
+    per-camera weight sums precomputed (GFT_GRAD_WEIGHTS_READY: a gradient
+    memset plus the scatter launch).  ``alg_bytes`` is the render-backward
+    formula (N*4*s + 2*P*4*4 + 2*N*4*4: the grid read once, image and adjoint,
+    gradient read-modify-write); ``impl_bytes`` adds what this implementation
+    moves on top of it (the stored samples it reads instead of re-gathering,
+    the per-camera reciprocal weight sums)."""
     import numpy as np
     import torch
     from gft import ops
@@ -482,6 +601,9 @@ def kernel_roofline(step, dev, timed):
         light = d * (step.shadow(d) * step.falloff_col + step.ambient)
         # the raymarch input in the brick layout the step uses
         data = ops.to_bricks((torch.cat([light, d], dim=-1) * step.depth_step).contiguous())
+        if storage is not None:
+            data = data.to(storage)
+        del d, light
     grid = step.shape
     D, H, W = step.res
     V = len(step.cams)
@@ -499,78 +621,70 @@ def kernel_roofline(step, dev, timed):
     ws = weights()
     scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
                                         ops.GRAD['REFERENCE'], weights=ws, grid=grid, samples=smp)
-    resample = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                         ops.GRAD['REFERENCE'], weights=ws, grid=grid)
     for _ in range(2):
-        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter(), resample()
+        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter()
     tf = float(np.median(timed(fwd, 7)))
     tb_ref = float(np.median(timed(lambda: bwd('REFERENCE'), 7)))
     tb_ex = float(np.median(timed(lambda: bwd('EXACT'), 7)))
     tw = float(np.median(timed(weights, 7)))
     ts = float(np.median(timed(scatter, 7)))
-    tr = float(np.median(timed(resample, 7)))
     nvox = int(np.prod(step.shape))
-    s, C = 4, 4
+    s = 2 if storage is not None else 4
+    C = 4
     pix = V * H * W
     samples = pix * D
-    # bytes of the sample store written / read: the samples the forward stored
-    # (inside the clipped ranges and outside empty occupancy blocks)
     n_stored = ops.stored_sample_count(smp, shape5, V, step.res)
     stored = n_stored * C * 4
-    bytes_fwd = nvox * C * s + pix * C * 4 + stored
-    # scatter pass: stored samples read, image + adjoint read, per-camera
-    # reciprocal weights read, gradient read-modify-write
-    bytes_scatter = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
-    bytes_resample = nvox * C * s + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
-    bytes_exact = stored + 2 * pix * C * 4 + 2 * nvox * C * 4
-    bytes_weights = 2 * V * nvox * 4
+    alg_fwd = nvox * C * s + pix * C * 4
+    alg_bwd = nvox * C * s + 2 * pix * C * 4 + 2 * nvox * C * 4
+    impl_scatter = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
     kern = {
-        'raymarch_fwd': {'ms': tf, 'alg_bytes': bytes_fwd, 'GBps': bytes_fwd / tf / 1e6,
-                         'samples_per_s': samples / tf * 1e3},
-        'raymarch_bwd_scatter': {'ms': ts, 'alg_bytes': bytes_scatter, 'GBps': bytes_scatter / ts / 1e6,
-                                 'samples_per_s': samples / ts * 1e3,
+        'raymarch_fwd': {'ms': tf, 'alg_bytes': alg_fwd, 'GBps': alg_fwd / tf / 1e6,
+                         'impl_bytes': alg_fwd + stored, 'samples_per_s': samples / tf * 1e3},
+        'raymarch_bwd_scatter': {'ms': ts, 'alg_bytes': alg_bwd, 'GBps': alg_bwd / ts / 1e6,
+                                 'impl_bytes': impl_scatter, 'samples_per_s': samples / ts * 1e3,
                                  'what': 'reference normalisation, weights ready, stored samples'},
-        'raymarch_bwd_scatter_resampling': {'ms': tr, 'alg_bytes': bytes_resample, 'GBps': bytes_resample / tr / 1e6,
-                                            'what': 'the same pass re-sampling the grid (no sample store)'},
-        'raymarch_samples_stored_bytes': stored,
-        'raymarch_samples_in_clipped_ranges': _clipped_samples(step),
         'raymarch_samples_stored': n_stored,
-        'raymarch_bwd_weights': {'ms': tw, 'alg_bytes': bytes_weights, 'GBps': bytes_weights / tw / 1e6,
-                                 'samples_per_s': samples / tw * 1e3},
-        'raymarch_bwd_reference': {'ms': tb_ref, 'what': 'whole op: weights + inversion + scatter'},
-        'raymarch_bwd_exact': {'ms': tb_ex, 'alg_bytes': bytes_exact, 'GBps': bytes_exact / tb_ex / 1e6,
-                               'samples_per_s': samples / tb_ex * 1e3},
+        'raymarch_samples_stored_bytes': stored,
+        'raymarch_bwd_weights': {'ms': tw, 'impl_bytes': 2 * V * nvox * 4, 'samples_per_s': samples / tw * 1e3,
+                                 'what': 'geometry-only pass of the reference normalisation (per-camera weight sums)'},
+        'raymarch_bwd_reference': {'ms': tb_ref, 'alg_bytes': alg_bwd, 'GBps': alg_bwd / tb_ref / 1e6,
+                                   'what': 'whole op: weights + inversion + scatter'},
+        'raymarch_bwd_exact': {'ms': tb_ex, 'alg_bytes': alg_bwd, 'GBps': alg_bwd / tb_ex / 1e6},
         'grad_mode': mode,
     }
-    traffic = _profiled_traffic()
-    return {'roofline': {'kernel': 'k_raymarch_scatter (raymarch adjoint scatter pass, 5 views)', 'bound': 'hbm',
-                         'achieved': kern['raymarch_bwd_scatter']['GBps'], 'peak': peak, 'unit': 'GB/s',
-                         'frac': kern['raymarch_bwd_scatter']['GBps'] / peak, 'peak_source': src,
-                         'traffic': traffic, 'alg_bytes': bytes_scatter,
-                         'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, '
-                                           'profiles/raymarch_scatter_cfg2.md' if traffic else None,
-                         'note': 'algorithmic bytes = compulsory unique traffic (the stored samples the pass '
-                                 'reads, image and adjoint, reciprocal weights, gradient read-modify-write); the '
-                                 'pass is bound by the L1/L2 path of its merged trilinear gradient reductions and '
-                                 'by latency, not by HBM'},
+    traffic = SCATTER_TRAFFIC.get((step.config_name, 'bf16' if storage is not None else 'f32'))
+    del smp, ws, data, y, dy
+    torch.cuda.empty_cache()
+    return {'roofline': {'kernel': 'k_raymarch_scatter (raymarch adjoint scatter pass, %d views)' % V,
+                         'bound': 'hbm', 'achieved': kern['raymarch_bwd_scatter']['GBps'], 'peak': peak,
+                         'unit': 'GB/s', 'frac': kern['raymarch_bwd_scatter']['GBps'] / peak, 'peak_source': src,
+                         'traffic': traffic, 'alg_bytes': alg_bwd, 'impl_bytes': impl_scatter,
+                         'traffic_source': ('ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch'
+                                            if traffic else None),
+                         'note': 'alg_bytes = the render-backward formula; the pass is bound by the L1/L2 path of '
+                                 'its merged trilinear gradient reductions and by latency, not by HBM'},
             'kernels': kern}
 
 
 def kernel_only(args):
-    """Runs one op of the cfg workload ``args.repeat`` times without a graph
+    """Runs one op of the workload ``args.repeat`` times without a graph
     (for ncu captures of a single kernel)."""
     import torch
     from gft import ops
     from gft.pipeline import RenderAdvectStep
     dev = torch.device('cuda', 0)
     ops.set_grad_mode(args.grad_mode)
-    step = RenderAdvectStep(args.config, dev, mode='batched')
+    storage = _storage_dtype(args.storage)
+    step = RenderAdvectStep(args.config, dev, mode='batched', storage_dtype=storage)
     inputs = step.make_inputs()
     step.setup_static(inputs)
     with torch.no_grad():
         d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
         light = d * (step.shadow(d) * step.falloff_col + step.ambient)
         data = ops.to_bricks((torch.cat([light, d], dim=-1) * step.depth_step).contiguous())
+        if storage is not None:
+            data = data.to(storage)
         grid = step.shape
         smp = ops._samples_buffer((1,) + tuple(grid) + (4,), len(step.cams), step.res, True, dev)
         y = ops._raymarch_fwd(data, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True, grid=grid, samples=smp)
@@ -602,38 +716,57 @@ def kernel_only(args):
     print(json.dumps({'kernel_only': args.kernel_only, 'repeat': args.repeat, 'ok': True}))
 
 
+# ------------------------------------------------------------ reference arm
 def bench_reference(args):
-    """The reference's own implementation of the path is CUDA-only TensorFlow
-    ops; its CPU stand-in is the FP64 NumPy port in oracle/, timed on a bounded
-    sample of the same workload with all host cores."""
+    """The reference's own implementation of the path is CUDA-only
+    TensorFlow ops; its CPU stand-in is the FP64 NumPy port in oracle/, run
+    as whole iterations of the same workload on all host cores
+    (oracle/cpu_step.py FullStep).  A whole iteration of the default workload
+    takes on the order of a minute, so the arm runs as many as fit in
+    ``--ref-budget`` seconds (at least one) and reports the steps it ran."""
     ws, rank, _ = _ddp()
     if rank != 0:
         return
     from oracle import cpu_step
     workers = os.cpu_count() or 1
-    res = cpu_step.time_step(None, None, budget_s=args.cpu_budget, workers=workers, config=args.config)
-    v = res['value']
-    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'iters/s', 'n_gpus': ws, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': 1000.0 / v if v else None, 'higher_is_better': True,
-            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-            'config': {'workload': args.config + ' (same step as the GPU arm)'},
-            'cpu_baseline': res,
-            'e2e': {'value': v, 'unit': 'iters/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    t0 = time.perf_counter()
+    res = cpu_step.time_full_steps(args.config, workers=workers, budget_s=args.ref_budget, max_steps=args.steps)
+    wall = time.perf_counter() - t0
+    times = res['seconds_per_step']
+    sec = sum(times) / len(times)
+    v = 1.0 / sec
+    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'iters/s', 'n_gpus': ws,
+            'steps': len(times), 'warmup': 0, 'steps_requested': args.steps, 'warmup_requested': args.warmup,
+            'ms_per_step': 1000.0 * sec, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic (seeded plume + curl-noise velocity; ScalarFlow absent)',
+            'config': workload_config(args.config, args.storage, args.grad_mode),
+            'cpu_baseline': {'value': v, 'unit': 'iters/s', 'cores': res['workers'], 'kind': 'port',
+                             'sample': 'whole iterations (every voxel, ray and frustum cell), FP64 NumPy port of '
+                                       'the reference ops, %d spawned workers sharing memory; per-stage seconds '
+                                       'per step: %s' % (res['workers'], json.dumps(
+                                           {k: round(x, 2) for k, x in res['stages_s'].items()})),
+                             'seconds_per_step': times},
+            'e2e': {'value': v, 'unit': 'iters/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+            'wall_s': wall, 'loss': res['loss'][-1]}
     print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=200)
+    ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--config', default='cfg2')
-    ap.add_argument('--storage', default='f32', choices=['f32', 'bf16'])
+    ap.add_argument('--config', default=DEFAULT_CONFIG)
+    ap.add_argument('--storage', default=DEFAULT_STORAGE, choices=['f32', 'bf16'])
     ap.add_argument('--grad-mode', default='REFERENCE', choices=['REFERENCE', 'EXACT'])
     ap.add_argument('--quick', action='store_true', help='only the timed graph replays')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-chain5', action='store_true', help='skip the long transport chain on the headline grid')
+    ap.add_argument('--chain-frames', type=int, default=120)
     ap.add_argument('--cpu-budget', type=float, default=20.0)
+    ap.add_argument('--ref-budget', type=float, default=240.0,
+                    help='reference arm: seconds of whole FP64 iterations to run (at least one)')
     ap.add_argument('--save-clocks', default=None, metavar='CSV', help='write every clock sample to this file')
     ap.add_argument('--kernel-only', default=None,
                     choices=['raymarch_fwd', 'raymarch_bwd', 'raymarch_weights', 'raymarch_scatter', 'advect_fwd',

@@ -535,7 +535,7 @@ bool launch_advect_bwd(const AdvectArgs& a, bool exact, bool forward_ready, cons
 // NOALLOC_MAX_ELEMENTS floats (16 MiB); every device that loads the library
 // keeps it until the process exits.  Host code cannot pass the array's name to a
 // kernel (on the host it is only a stand-in symbol), so its device address is
-// looked up once per device with cudaGetSymbolAddress.
+// looked up with cudaGetSymbolAddress.
 constexpr size_t NOALLOC_MAX_ELEMENTS = size_t(1) << 22;
 static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_MAX_ELEMENTS];
 
@@ -543,22 +543,37 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_noalloc_mu;
 static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of g_noalloc_scratch on the current device; the lookup runs on
-// the first call per device and is cached.
-static bool noalloc_scratch(float** out) {
+// Device address of g_noalloc_scratch on the current device.  Outside stream
+// capture the address is looked up on every call (cheap), so a context that
+// was reset and reloaded the module never sees a stale pointer; the result is
+// cached per device for calls made while `s` is being captured, where the
+// lookup (which may load the module) is not made.
+static bool noalloc_scratch(cudaStream_t s, float** out) {
     int dev = -1;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
         set_error("gft_advect_noalloc: device ordinal out of range");
         return false;
     }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (g_noalloc_ptr[dev] == nullptr) {
-        void* p = nullptr;
-        if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)"))
-            return false;
-        g_noalloc_ptr[dev] = reinterpret_cast<float*>(p);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        (void)cudaGetLastError();  // reset the last-error state the failed query set
+        cap = cudaStreamCaptureStatusActive;  // unknown: do not risk an unsafe call
     }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (g_noalloc_ptr[dev] == nullptr) {
+            set_error("gft_advect_noalloc: first call on this device made during stream capture; "
+                      "call it once before capturing");
+            return false;
+        }
+        *out = g_noalloc_ptr[dev];
+        return true;
+    }
+    void* p = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)"))
+        return false;
+    g_noalloc_ptr[dev] = reinterpret_cast<float*>(p);
     *out = g_noalloc_ptr[dev];
     return true;
 }
@@ -582,6 +597,10 @@ gft_status gft_advect_noalloc(const void* density, int32_t density_dtype, const 
             set_error("Invalid input shape (NDHWC): all dimensions must be positive");
             return GFT_ERR_INVALID_ARGUMENT;
         }
+    if (density_shape[1] > INT32_MAX || density_shape[2] > INT32_MAX || density_shape[3] > INT32_MAX) {
+        set_error("grid dimension too large");
+        return GFT_ERR_INVALID_ARGUMENT;
+    }
     const int64_t C = density_shape[4];
     if (!(C == 1 || C == 2 || C == 4)) {
         set_error("Only 1,2 and 4 Channel supported.");
@@ -612,7 +631,7 @@ gft_status gft_advect_noalloc(const void* density, int32_t density_dtype, const 
         return GFT_ERR_INVALID_ARGUMENT;
     }
     float* scratch = nullptr;
-    if (order == 2 && !noalloc_scratch(&scratch)) return GFT_ERR_CUDA;
+    if (order == 2 && !noalloc_scratch(reinterpret_cast<cudaStream_t>(stream), &scratch)) return GFT_ERR_CUDA;
     AdvectArgs a;
     a.density = density;
     a.dtype = density_dtype;

@@ -21,10 +21,9 @@ constexpr int RM_BX = 8, RM_BY = 16;
 // dims up to dims + 0.5), and blending a zero sample leaves the accumulator
 // unchanged.  So a ray only needs the steps i whose position p0 + i*st can lie
 // in that box: [i_lo, i_hi] from a slab test, widened by a margin (0.05 voxels
-// and one step) far above the rounding of the iterated positions.  The steps
-// before i_lo are still iterated as additions, so the positions of the
-// processed samples are bit-identical to those of the full march.  Returns
-// false when no step can reach the box.
+// and one step) far above the rounding of the positions.  Sample i lies at
+// fmaf(i, step, p0) (ray_sample), so the processed samples sit exactly where
+// the full march puts them.  Returns false when no step can reach the box.
 __device__ __forceinline__ bool ray_clip(float3 p0, float3 st, int n, Dims d, int& i_lo, int& i_hi) {
     float t0 = 0.f, t1 = (float)(n - 1);
     const float lo = -1.05f;
@@ -53,6 +52,19 @@ __device__ __forceinline__ bool ray_clip(float3 p0, float3 st, int n, Dims d, in
 struct RayPix {
     int p, x, y, W, H, D;
 };
+
+// Position of sample i of a ray: near + i * step with one rounding per
+// coordinate.  The reference walks the ray by repeated addition
+// (raymarch_grid.cu.cc:122-140, its adjoint by repeated subtraction from the far
+// end, :354-370), whose rounding error grows along the ray: at 960x540x256 on a
+// 256x455x256 grid that drift changes the unnormalised (exact) adjoint by
+// ~3e-4 rel-L2 against fp64 positions, against ~2e-5 here.  The forward and
+// every adjoint pass evaluate the same expression, so they sample the same
+// points bit for bit.
+__device__ __forceinline__ float3 ray_sample(float3 nearp, float3 step, int i) {
+    const float t = (float)i;
+    return make_float3(fmaf(t, step.x, nearp.x), fmaf(t, step.y, nearp.y), fmaf(t, step.z, nearp.z));
+}
 __device__ __forceinline__ bool ray_pixel(const PairTable& tab, RayPix& r) {
     const int b = blockIdx.x;
     int p = 0;
@@ -285,7 +297,6 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     const float3 nearp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, 0.5f), dinv);
     const float3 farp = idx_to_os(cam, make_float3(x + 0.5f, y + 0.5f, zmax + 0.5f), dinv);
     const float3 step = make_float3((farp.x - nearp.x) / zmax, (farp.y - nearp.y) / zmax, (farp.z - nearp.z) / zmax);
-    float3 pos = nearp;
     Vec<C> acc = vzero<C>();
     int i0 = 0, i1 = D - 1, w0 = 0, w1 = D - 1;
     // Storing samples (LINEAR): every lane stays in the loop to the warp's
@@ -304,11 +315,6 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
                 return;
             }
         }
-        for (int i = 0; i < w0; ++i) {
-            pos.x += step.x;
-            pos.y += step.y;
-            pos.z += step.z;
-        }
     } else if (!live) {
         if (!storing) return;
         i0 = D;
@@ -318,6 +324,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     for (int i = w0; i <= w1; ++i) {
         bool stored = false;
         if (i >= i0 && i <= i1) {
+            const float3 pos = ray_sample(nearp, step, i);
             Vec<C> smp;
             if constexpr (LIN) {
                 const float qx = pos.x - 0.5f, qy = pos.y - 0.5f, qz = pos.z - 0.5f;
@@ -337,17 +344,14 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             if ((threadIdx.x & 31u) == 0 && (threadIdx.y & 3u) == 0)
                 st.words[sample_word_index(tab, p, D, i)] = word;
         }
-        pos.x += step.x;
-        pos.y += step.y;
-        pos.z += step.z;
     }
     if (!live) return;
     store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
 }
 
-// Ray set-up shared by the adjoint kernels: far end point and step (the
-// reference's grad kernel walks from farPos by -step, raymarch_grid.cu.cc:354-370).
-// (nearp: the forward's start point, for the forward's clip range.)
+// Ray set-up shared by the adjoint kernels: near point, far point and step,
+// computed as the forward computes them (the adjoint visits the forward's
+// samples i = D-1 .. 0 at ray_sample(nearp, step, i)).
 __device__ __forceinline__ void ray_far_step(const CamX& cam, int x, int y, int W, int H, int D, float3& farp,
                                              float3& step, float3& nearp) {
     const float3 dinv = make_float3(1.f / (float)W, 1.f / (float)H, 1.f / (float)D);
@@ -546,8 +550,8 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
     RayPix r;
     const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
-    float3 pos, step, nearp;
-    ray_far_step(tab.cam[p], x, y, W, H, D, pos, step, nearp);
+    float3 farp, step, nearp;
+    ray_far_step(tab.cam[p], x, y, W, H, D, farp, step, nearp);
     // With a sample store: the forward's own clip range (front-to-back steps
     // [s_lo, s_hi], computed from the same near point and step as there); its
     // samples outside are zero (BORDER), inside it stored the non-zero ones.
@@ -568,19 +572,18 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         acc = loadf<C>(out, pix);
         go = loadf<C>(dout, pix);
     }
-    // the adjoint samples far - k*step, k in [0, D), back to front
+    // the adjoint visits the forward's samples back to front: step k is
+    // sample i = D - 1 - k
     int k_lo = 0, k_hi = D - 1, w_lo = 0, w_hi = D - 1;
     if constexpr (BM == BM_BORDER) {
         const bool clip = MODE == 2 || C == 1 || blend_mode == BL_ADDITIVE || blend_mode == BL_ALPHA_ADDITIVE ||
                           ((blend_mode == BL_BEER_LAMBERT || blend_mode == BL_BEER_LAMBERT_EXCLUSIVE) &&
                            acc.v[C - 1] >= 0.f);
-        const bool hit = live && (!clip || ray_clip(pos, make_float3(-step.x, -step.y, -step.z), D, din, k_lo, k_hi));
+        int i_lo = 0, i_hi = D - 1;
+        const bool hit = live && (!clip || ray_clip(nearp, step, D, din, i_lo, i_hi));
+        k_lo = D - 1 - i_hi;
+        k_hi = D - 1 - i_lo;
         warp_clip_range(hit, D, k_lo, k_hi, w_lo, w_hi);
-        for (int k = 0; k < w_lo; ++k) {  // iterated subtraction, as the full march
-            pos.x -= step.x;
-            pos.y -= step.y;
-            pos.z -= step.z;
-        }
     } else if (!live) {
         k_lo = D;
         k_hi = -1;
@@ -597,6 +600,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
 #pragma unroll 1
     for (int k = w_lo; k <= w_hi; ++k) {
         const bool on = k >= k_lo && k <= k_hi;
+        const float3 pos = ray_sample(nearp, step, D - 1 - k);
         const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
         Vec<C> val = vfill<C>(1.f);
         if (MODE != 2 && on) {
@@ -611,9 +615,6 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
         scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val);
-        pos.x -= step.x;
-        pos.y -= step.y;
-        pos.z -= step.z;
     }
 }
 

@@ -56,9 +56,14 @@ CONFIGS = {
 
 
 class RenderAdvectStep:
-    def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched'):
-        cfg = CONFIGS[config] if isinstance(config, str) else config
+    def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None):
+        self.config_name = config if isinstance(config, str) else None
+        cfg = dict(CONFIGS[config] if isinstance(config, str) else config)
+        if order is not None:
+            cfg['order'] = int(order)
         self.cfg = cfg
+        self.order = int(cfg.get('order', 2))  # 1 semi-Lagrangian, 2 MacCormack (+ MC_SMOOTH)
+        self.clamp = 'MC_SMOOTH' if self.order == 2 else 'NONE'
         self.dev = torch.device(device)
         self.storage_dtype = storage_dtype
         self.mode = mode
@@ -102,8 +107,8 @@ class RenderAdvectStep:
     # --------------------------------------------------------------- pieces
     def advect(self, d_prev, vx, vy, vz):
         if self.mode == 'plain':
-            return advect_composed(d_prev, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP')
-        return ops.advect(d_prev, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP',
+            return advect_composed(d_prev, vx, vy, vz, dt=1.0, order=self.order, clamp=self.clamp, boundary='CLAMP')
+        return ops.advect(d_prev, vx, vy, vz, dt=1.0, order=self.order, clamp=self.clamp, boundary='CLAMP',
                           storage_dtype=self.storage_dtype)
 
     def shadow(self, d):
@@ -207,7 +212,8 @@ class StreamedSteps:
 
     def __init__(self, step, example, warmup=3):
         self.dev = step.dev
-        self.slots = [step, RenderAdvectStep(step.cfg, step.dev, storage_dtype=step.storage_dtype, mode=step.mode)]
+        self.slots = [step, RenderAdvectStep(step.config_name or step.cfg, step.dev, storage_dtype=step.storage_dtype,
+                                             mode=step.mode, order=step.order)]
         for st in self.slots:
             st.setup_static(example)
             st.capture(warmup=warmup)

@@ -113,3 +113,64 @@ def hemisphere_cameras(n_random, samples, sizes=(64, 256), radius=2.5, fov=30.0,
         cams.append(Camera(t, nearFar=[near, far], fov=fov, aspect=1.0))
         shapes.append((samples, s, s))
     return cams, shapes
+
+
+# ---- device-side generators (for long chains of large grids) ----------------
+def _gauss_wrap_device(x, sigma):
+    """Periodic ('wrap') Gaussian filter of a 3-D device tensor by FFT."""
+    import torch
+    spec = torch.fft.rfftn(x)
+    out = spec
+    for axis, n in enumerate(x.shape):
+        f = torch.fft.fftfreq(n, device=x.device) if axis < 2 else torch.fft.rfftfreq(n, device=x.device)
+        g = torch.exp(-2.0 * (torch.pi * sigma * f) ** 2)
+        shape = [1, 1, 1]
+        shape[axis] = g.numel()
+        out = out * g.reshape(shape)
+    return torch.fft.irfftn(out, s=x.shape)
+
+
+def plume_density_device(shape_dhw, seed, device, frame=0, sigma=3.0, scale=0.05):
+    """plume_density generated on the device ([1, D, H, W, 1] fp32): the same
+    construction with the device's random generator and an FFT Gaussian."""
+    import torch
+    D, H, W = shape_dhw
+    g = torch.Generator(device=device).manual_seed(int(seed))
+    noise = torch.rand((D, H, W), generator=g, device=device)
+    d = torch.exp(_gauss_wrap_device(noise, sigma)) * scale
+    z = (torch.arange(D, device=device, dtype=torch.float32) + 0.5 - D / 2.0)[:, None, None]
+    x = (torch.arange(W, device=device, dtype=torch.float32) + 0.5 - W / 2.0)[None, None, :]
+    y = torch.arange(H, device=device, dtype=torch.float32)[None, :, None]
+    height = H * min(1.0, 0.35 + 0.04 * frame)
+    mask = (torch.sqrt(x * x + z * z) <= 0.3 * W) & (y < height)
+    return (d * mask).float()[None, ..., None].contiguous()
+
+
+def _faces_device(c, axis):
+    import torch
+    lo = c.narrow(axis, 0, 1)
+    hi = c.narrow(axis, c.shape[axis] - 1, 1)
+    p = torch.cat([lo, c, hi], dim=axis)
+    n = p.shape[axis]
+    return 0.5 * (p.narrow(axis, 0, n - 1) + p.narrow(axis, 1, n - 1))
+
+
+def curl_velocity_device(shape_dhw, seed, device, magnitude=1.0, upward=0.5, sigma=4.0):
+    """curl_velocity generated on the device: staggered components
+    [1, D, H, W+1, 1], [1, D, H+1, W, 1], [1, D+1, H, W, 1] fp32."""
+    import torch
+    D, H, W = shape_dhw
+    g = torch.Generator(device=device).manual_seed(int(seed))
+    A = [_gauss_wrap_device(torch.randn((D, H, W), generator=g, device=device), sigma) for _ in range(3)]
+    dAz_dy, = torch.gradient(A[2], dim=1)
+    dAy_dz, = torch.gradient(A[1], dim=0)
+    dAx_dz, = torch.gradient(A[0], dim=0)
+    dAz_dx, = torch.gradient(A[2], dim=2)
+    dAy_dx, = torch.gradient(A[1], dim=2)
+    dAx_dy, = torch.gradient(A[0], dim=1)
+    vx = dAz_dy - dAy_dz
+    vy = dAx_dz - dAz_dx
+    vz = dAy_dx - dAx_dy
+    s = magnitude / max(1e-12, float(torch.sqrt(vx * vx + vy * vy + vz * vz).max()))
+    vx, vy, vz = vx * s, vy * s + upward, vz * s
+    return tuple(_faces_device(v, a).float()[None, ..., None].contiguous() for v, a in ((vx, 2), (vy, 1), (vz, 0)))

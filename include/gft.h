@@ -276,12 +276,14 @@ gft_status gft_advect(
  * every device that loads the library until the process exits), so
  * D*H*W*C above that limit is rejected with GFT_ERR_INVALID_ARGUMENT (order 1
  * needs no scratch and has no limit).  The function calls no cudaMalloc /
- * cudaFree and no allocating library routine.  Its first call on a device (the
- * device current on the calling thread, which must own ``stream``) looks up
- * the array's device address once; make that first call before any stream
- * capture.  Every call shares the one array and each call overwrites it before
- * reading it, so nothing needs clearing, but calls whose kernels overlap on the
- * GPU (different streams without ordering) race on it. */
+ * cudaFree and no allocating library routine.  Each call outside stream
+ * capture looks up the array's device address on the current device (the
+ * device current on the calling thread, which must own ``stream``); a call
+ * made while ``stream`` is being captured reuses the address of that device's
+ * last lookup, so make a first call on each device before any stream capture.
+ * Every call shares the one array and each call overwrites it before reading
+ * it, so nothing needs clearing, but calls whose kernels overlap on the GPU
+ * (different streams without ordering) race on it. */
 size_t gft_advect_noalloc_max_elements(void);
 gft_status gft_advect_noalloc(
     const void* density, int32_t density_dtype, const int64_t density_shape[5],

@@ -45,19 +45,29 @@ def _cams(M, V, P, F, n, b, separate_camera_batch):
     return [(c, T.CameraXform(M[b], V[c], P[c], F[c])) for c in cams]
 
 
+def _window(rows, cols, c):
+    """Image window of camera index c: ``rows``/``cols`` are slices or, per
+    camera, lists of slices."""
+    r = rows[c] if isinstance(rows, (list, tuple)) else rows
+    k = cols[c] if isinstance(cols, (list, tuple)) else cols
+    return (slice(None) if r is None else r, slice(None) if k is None else k)
+
+
 def raymarch_fwd(x, M, V, P, F, out_shape, filter_mode=S.LINEAR, boundary=S.BORDER,
-                 blend_mode=B.BEER_LAMBERT, separate_camera_batch=True, rows=None):
+                 blend_mode=B.BEER_LAMBERT, separate_camera_batch=True, rows=None, cols=None):
     """x [N,D,H,W,C]; M [N,16]; V,P [V,16]; F [V,6]; out_shape (D,H,W) of the frustum.
-    Returns [N, V (or 1), H, W, C].  ``rows`` optionally restricts the work to a
-    subset of image rows (the rest stay 0), used for bounded CPU timing."""
+    Returns [N, V (or 1), H, W, C].  ``rows`` / ``cols`` optionally restrict the
+    work to a window of image rows and columns (slices, or one slice per
+    camera); the rest stay 0.  Used for bounded CPU timing and for checking
+    the rays that reach a sub-block of a large grid."""
     x = np.asarray(x, dtype=np.float64)
     N, C = x.shape[0], x.shape[4]
     D, H, W = out_shape
     nv = len(V) if separate_camera_batch else 1
     out = np.zeros((N, nv, H, W, C))
-    rsel = slice(None) if rows is None else rows
     for b in range(N):
         for vi, (c, cam) in enumerate(_cams(M, V, P, F, N, b, separate_camera_batch)):
+            rsel = _window(rows, cols, c)
             near, far, step = ray_endpoints(cam, H, W, D)
             near, step = near[rsel], step[rsel]
             acc = np.zeros(near.shape[:-1] + (C,))
@@ -69,34 +79,45 @@ def raymarch_fwd(x, M, V, P, F, out_shape, filter_mode=S.LINEAR, boundary=S.BORD
 
 
 def raymarch_bwd(x, y, dy, M, V, P, F, out_shape, boundary=S.BORDER,
-                 blend_mode=B.BEER_LAMBERT, separate_camera_batch=True, exact=False, rows=None):
+                 blend_mode=B.BEER_LAMBERT, separate_camera_batch=True, exact=False, rows=None, cols=None):
     """Gradient w.r.t. x of raymarch_fwd with LINEAR filtering (the only filter the
     gradient op accepts, raymarch_grid.cc:65).  y is the forward output, dy its
-    gradient.  Returns [N,D,H,W,C]."""
+    gradient.  Returns [N,D,H,W,C].  With a window (``rows`` / ``cols``) only
+    its rays contribute: exact at every voxel that no ray outside it reaches."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
     dy = np.asarray(dy, dtype=np.float64)
     N, C = x.shape[0], x.shape[4]
     D, H, W = out_shape
     gx = np.zeros_like(x)
-    rsel = slice(None) if rows is None else rows
     for b in range(N):
         for vi, (c, cam) in enumerate(_cams(M, V, P, F, N, b, separate_camera_batch)):
-            near, far, step = ray_endpoints(cam, H, W, D)
-            near, step = near[rsel], step[rsel]
             ov = vi if separate_camera_batch else 0
-            acc = y[b, ov][rsel].copy()
-            g = dy[b, ov][rsel].copy()
-            buf = np.zeros_like(x[b])
-            cnt = np.zeros(x.shape[1:4])
-            for i in range(D - 1, -1, -1):
-                pos = near + i * step
-                smp = _sample(x[b], pos, S.LINEAR, boundary)
-                gcell, g, acc = B.blend_gradients(blend_mode, g, smp, acc, exact)
-                S.scatter_linear(buf, pos - 0.5, gcell, boundary, cnt, count_weights=True, exact_window=exact)
+            buf, cnt = camera_scatter(x[b], y[b, ov], dy[b, ov], cam, out_shape, _window(rows, cols, c), boundary,
+                                      blend_mode, exact)
             if exact:
                 gx[b] += buf
             else:
                 nz = cnt > 0
                 gx[b][nz] += buf[nz] / cnt[nz][:, None]
     return gx
+
+
+def camera_scatter(xb, yv, dyv, cam, out_shape, window, boundary=S.BORDER, blend_mode=B.BEER_LAMBERT, exact=False):
+    """The per-camera part of raymarch_bwd before normalisation: the trilinear
+    scatter of the blend adjoint over the rays of ``window`` (rows, cols) of
+    one camera, and the per-voxel sum of the trilinear weights.
+    xb [D,H,W,C]; yv, dyv [H,W,C].  Returns (buf [D,H,W,C], weight_sum [D,H,W])."""
+    D, H, W = out_shape
+    near, far, step = ray_endpoints(cam, H, W, D)
+    near, step = near[window], step[window]
+    acc = np.asarray(yv, dtype=np.float64)[window].copy()
+    g = np.asarray(dyv, dtype=np.float64)[window].copy()
+    buf = np.zeros(xb.shape, dtype=np.float64)
+    cnt = np.zeros(xb.shape[:3])
+    for i in range(D - 1, -1, -1):
+        pos = near + i * step
+        smp = _sample(xb, pos, S.LINEAR, boundary)
+        gcell, g, acc = B.blend_gradients(blend_mode, g, smp, acc, exact)
+        S.scatter_linear(buf, pos - 0.5, gcell, boundary, cnt, count_weights=True, exact_window=exact)
+    return buf, cnt

@@ -16,31 +16,40 @@ def _out_coords(D, H, W):
 
 def sample_grid_transform(x, M, V, P, F, out_shape, filter_mode=S.LINEAR, boundary=S.BORDER,
                           mip_mode=S.MIP_NONE, num_mips=0, mip_bias=0.0,
-                          coord_mode=T.LINDEPTH, separate_camera_batch=True):
+                          coord_mode=T.LINDEPTH, separate_camera_batch=True, out_box=None, mips=None):
     """SampleGridTransform (resample_grid.cc:23-61, :268-447; kSample3D
     resample_grid.cu.cc:240-252; launcher :289-438).
     x [N,D,H,W,C] -> [N, V (or 1), Do, Ho, Wo, C].  Only LINEAR/NEAREST filtering
     and BORDER/CLAMP boundaries reach a fetch in this op (Sampler2::_internal_fetch3D,
-    sampling.hpp:567-585); other combinations give 0."""
+    sampling.hpp:567-585); other combinations give 0.  ``out_box`` = ((z0, z1),
+    (y0, y1), (x0, x1)) computes only that box of output cells and returns
+    [N, V (or 1), z1-z0, y1-y0, x1-x0, C].  ``mips``: the pyramid of a
+    one-slice input as build_mips returns it, if already built."""
     x = np.asarray(x, dtype=np.float64)
     N, C = x.shape[0], x.shape[4]
     Do, Ho, Wo = out_shape
     dims_in = S.dims_xyz(x[0])
     dims_out = np.array([Wo, Ho, Do], dtype=np.int64)
     nv = len(V) if separate_camera_batch else 1
-    out = np.zeros((N, nv, Do, Ho, Wo, C))
     use_mip = mip_mode != S.MIP_NONE
     L = S.usable_mip_levels(x.shape[1:4], num_mips) if use_mip else 0
     idx = _out_coords(Do, Ho, Wo) + 0.5
+    if out_box is not None:
+        (z0, z1), (y0, y1), (x0, x1) = out_box
+        idx = idx[z0:z1, y0:y1, x0:x1]
+    out = np.zeros((N, nv) + idx.shape[:3] + (C,))
     if filter_mode not in (S.LINEAR, S.NEAREST) or boundary not in (S.BORDER, S.CLAMP):
         return out
     for b in range(N):
-        mips = S.build_mips(x[b], L) if use_mip else [x[b]]
+        if mips is not None and N == 1:
+            pyr = mips[:L + 1] if use_mip else mips[:1]
+        else:
+            pyr = S.build_mips(x[b], L) if use_mip else [x[b]]
         cams = range(len(V)) if separate_camera_batch else [b]
         for vi, c in enumerate(cams):
             cam = T.CameraXform(M[b], V[c], P[c], F[c])
             pos = T.sample_positions(cam, coord_mode, idx, dims_in, dims_out, use_mip)
-            out[b, vi] = S.sample_mipmapped(mips, pos, filter_mode, boundary,
+            out[b, vi] = S.sample_mipmapped(pyr, pos, filter_mode, boundary,
                                             mip_mode if (use_mip and True) else S.MIP_NONE,
                                             mip_bias, 0.5, L)
     return out

@@ -129,3 +129,63 @@ def test_lindepth_round_trip():
     assert np.allclose(back, idx, atol=1e-9)
     back2 = T.os_to_idx(cam, T.idx_to_os(cam, idx, np.array([11, 9, 16.0])), np.array([11, 9, 16.0]))
     assert np.allclose(back2, idx, atol=1e-9)
+
+
+@pytest.mark.parametrize('order', [1, 2])
+def test_step_oracle_gradient_fd(order):
+    """The FP64 step oracle (oracle/step.py) with exact op adjoints and the
+    scatter adjoint for the shadow resamplings (no mips) is the true gradient
+    of its forward: directional derivatives against central differences for
+    the previous density and all three velocity components.  The density is
+    positive everywhere and noisy, so no Beer-Lambert max(., 0) kink sits at
+    the evaluation point; MacCormack runs without the MC_SMOOTH clamp, whose
+    selection ties (lookups clamped to one edge cell) make central differences
+    jump -- its adjoint is checked on random data by
+    test_advect_exact_adjoint_fd."""
+    from gft import synthetic as syn
+    from gft.pipeline import RenderAdvectStep
+    from oracle import step as OS
+    from scene_utils import step_scene
+    st = RenderAdvectStep('tiny', 'cpu', order=order)
+    sc = step_scene(st)
+    sc['mips'] = 0
+    sc['clamp'] = 'NONE'
+    rng = np.random.default_rng(11 + order)
+    d = syn.plume_density(st.shape, 7)[0].astype(np.float64) * 8 + 0.05 + 0.01 * rng.random(st.shape + (1,))
+    vel = [v[0].astype(np.float64) for v in syn.curl_velocity(st.shape, 8)]
+    tgt = rng.random((len(st.cams), st.res[1], st.res[2], 3)) * 0.3
+    _, _, grads = OS.step(sc, d, *vel, tgt, exact=True, shadow_grad='adjoint')
+    xs = [d] + vel
+    for k in range(4):
+        u = rng.standard_normal(xs[k].shape)
+
+        def loss(e):
+            a = [x.copy() for x in xs]
+            a[k] = a[k] + e * u
+            return OS.forward(sc, *a, tgt)[0]
+        fd = (loss(EPS) - loss(-EPS)) / (2 * EPS)
+        assert abs(fd - np.sum(grads[k] * u)) <= 1e-4 * abs(fd), (k, fd, np.sum(grads[k] * u))
+
+
+def test_step_oracle_forward_is_the_render_composition():
+    """The step oracle's image equals the oracle render composition
+    (shadow_transmission + render_fused) applied to the advected density."""
+    from gft import synthetic as syn
+    from gft.pipeline import RenderAdvectStep
+    from oracle import render as ORd
+    from oracle import step as OS
+    from scene_utils import step_scene
+    st = RenderAdvectStep('tiny', 'cpu')
+    sc = step_scene(st)
+    d = syn.plume_density(st.shape, 3)[0].astype(np.float64) * 8
+    vel = [v[0].astype(np.float64) for v in syn.curl_velocity(st.shape, 4)]
+    tgt = np.zeros((len(st.cams), st.res[1], st.res[2], 3))
+    _, parts = OS.forward(sc, d, *vel, tgt)
+    da = OA.warp(d, *vel, 1.0, 2, 'MC_SMOOTH', S.CLAMP)
+    trv = ORd.shadow_transmission(da[None], sc['M'], sc['Vs'], sc['Ps'], sc['Fs'], sc['shadow_res'],
+                                  sc['shadow_step'], num_mips=sc['mips'])
+    light = da * (trv * sc['falloff_col'] + sc['ambient'])
+    imgs = ORd.render_fused(np.concatenate([light, da], -1)[None], sc['M'], sc['V'], sc['P'], sc['F'], sc['res'],
+                            sc['depth_step'], cut_alpha=False)
+    ref = np.concatenate(imgs, 0)
+    assert np.max(np.abs(parts['img'] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
