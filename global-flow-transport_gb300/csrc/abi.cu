@@ -1092,6 +1092,74 @@ gft_status gft_transmittance_grad(const float* output, const float* output_grad,
 
 static bool layout_ok(int32_t layout) { return layout == 0 || layout == GFT_LAYOUT_BRICK; }
 
+// ---------------------------------------------------------------- FP64 checks
+gft_status gft_transmittance_check(const float* input, const float* output, const int64_t shape[5],
+                                   int32_t column_stride, double* result, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (column_stride < 1) return fail(GFT_ERR_INVALID_ARGUMENT, "column stride must be positive");
+    if (!input || !output || !result) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({input, output}, 4)) != GFT_OK || (st = check_aligned({result}, 16)) != GFT_OK) return st;
+    if (!launch_transmittance_check(input, output, (int)shape[0], dims_of(shape), column_stride, result,
+                                    as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_raymarch_check(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                              const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+                              const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+                              const float* output, int32_t ray_stride, double* result, void* stream) {
+    std::string why;
+    const int32_t layout = input_dtype & GFT_LAYOUT_BRICK;
+    const int32_t dtype = input_dtype & ~GFT_LAYOUT_BRICK;
+    if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
+    if (!enum_in(dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
+    if (output_shape == nullptr || output_shape[0] <= 0 || output_shape[1] <= 0 || output_shape[2] <= 0)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "invalid output shape");
+    if (ray_stride < 1) return fail(GFT_ERR_INVALID_ARGUMENT, "ray stride must be positive");
+    if (!input || !output || !result) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
+    if (st != GFT_OK) return st;
+    if ((st = check_aligned({input}, vec_bytes(input_shape[4], dtype))) != GFT_OK ||
+        (st = check_aligned({output}, vec_bytes(input_shape[4], 0))) != GFT_OK ||
+        (st = check_aligned({result}, 16)) != GFT_OK)
+        return st;
+    // every (batch, camera) pair with the camera inverses in double
+    std::vector<CheckTable> tabs;
+    const int N = (int)input_shape[0];
+    for (int b = 0; b < N; ++b)
+        for (int c = 0; c < num_cameras; ++c) {
+            if (tabs.empty() || tabs.back().n == MAX_PAIRS) {
+                tabs.emplace_back();
+                std::memset(&tabs.back(), 0, sizeof(CheckTable));
+            }
+            CheckTable& t = tabs.back();
+            double m[4][4], v[4][4], p[4][4], mv[4][4], mvi[4][4], pi[4][4];
+            mat_from_flat(matrix_m + 16 * (num_m == 1 ? 0 : b), m);
+            mat_from_flat(matrix_v + 16 * c, v);
+            mat_from_flat(matrix_p + 16 * c, p);
+            matmul4(v, m, mv);
+            inverse4(mv, mvi);
+            inverse4(p, pi);
+            for (int r = 0; r < 4; ++r)
+                for (int k = 0; k < 4; ++k) {
+                    t.cam[t.n].mvi[4 * r + k] = mvi[r][k];
+                    t.cam[t.n].pi[4 * r + k] = pi[r][k];
+                }
+            t.in_batch[t.n] = b;
+            t.out_slot[t.n] = b * num_cameras + c;
+            ++t.n;
+        }
+    if (!launch_raymarch_check(input, dtype, layout ? LAYOUT_BRICK : LAYOUT_FLAT, (int)input_shape[4],
+                               dims_of(input_shape), tabs, output_shape[2], output_shape[1], output_shape[0], output,
+                               ray_stride, result, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
 gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
                              const int64_t shape[5], float ambient, float scale, int32_t output_layout, float* output,
                              void* stream) {

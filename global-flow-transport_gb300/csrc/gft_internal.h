@@ -177,4 +177,19 @@ bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const f
 bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], const float* gloss,
                             float* gimg, cudaStream_t st);
 
+// FP64 check step (check.cu): double-precision camera inverses per pair
+struct CamD {
+    double mvi[16], pi[16];  // (V M)^-1 and P^-1, row-major
+};
+struct CheckTable {
+    CamD cam[MAX_PAIRS];
+    int in_batch[MAX_PAIRS];
+    int out_slot[MAX_PAIRS];
+    int n;
+};
+bool launch_transmittance_check(const float* x, const float* tr, int N, Dims d, int stride, double* result,
+                                cudaStream_t s);
+bool launch_raymarch_check(const void* in, int dtype, int layout, int C, Dims din, const std::vector<CheckTable>& tabs,
+                           int W, int H, int D, const float* img, int stride, double* result, cudaStream_t s);
+
 }  // namespace gft

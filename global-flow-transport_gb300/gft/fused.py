@@ -133,3 +133,21 @@ def image_loss(image, target, background):
         background = background.detach().cpu().numpy()
     bkg = np.ascontiguousarray(np.asarray(background, dtype=np.float32).reshape(3))
     return _ImageLoss.apply(img, tgt, bkg)
+
+
+def transmittance_check(x, tr, column_stride=1, out=None):
+    """FP64 recomputation of transmittance(x) on every column_stride-th
+    column: a device float64 tensor [max |tr - tr64|, max |tr64|]
+    (written into ``out`` when given, e.g. a slice of a buffer a captured
+    step reads back)."""
+    x = _cuda(x, 'input')
+    tr = _cuda(tr, 'output')
+    if x.shape != tr.shape or x.dim() != 5 or x.shape[4] != 1:
+        raise _lib.GftInvalidArgument('expected two [N, D, H, W, 1] grids, got %s and %s'
+                                      % (tuple(x.shape), tuple(tr.shape)))
+    res = out if out is not None else torch.empty(2, dtype=torch.float64, device=x.device)
+    lib = _lib.load()
+    with torch.cuda.device(x.device):
+        _lib.check(lib.gft_transmittance_check(_p(x), _p(tr), _shape(x), int(column_stride), _p(res),
+                                               _stream(x.device)), 'TransmittanceCheck')
+    return res

@@ -933,3 +933,28 @@ def advect(density, vel_x, vel_y, vel_z, dt=1.0, order=1, clamp='NONE', boundary
         raise NotImplementedError('MIM and MAX warp sampling have wrong gradients.')
     return _Advect.apply(d, vx, vy, vz, float(dt), int(order), _enum(CLAMP, c, 'clamp'),
                          _enum(BOUNDARY, boundary, 'boundary'), storage_dtype)
+
+
+def raymarch_check(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape, output, ray_stride=1,
+                   grid_shape=None, out=None):
+    """FP64 recomputation of the density (last) channel of a BEER_LAMBERT /
+    LINEAR / BORDER raymarch_grid_transform (separate camera batches) for
+    every ray_stride-th pixel: a device float64 tensor [max |fp32 - fp64|,
+    max |fp64|] of ``output`` [N, V, H, W, C] (written into ``out`` when
+    given; the ratio is the max-norm relative error).  ``grid_shape``: the input is in the brick layout
+    (raymarch_grid_transform_bricked)."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    y = _cuda(output, 'output')
+    lib = _lib.load()
+    Mh, nm = _mats(matrix_m)
+    Vh, nv = _mats(matrix_v)
+    Ph, _ = _mats(matrix_p)
+    Fh, _ = _frustum(frustum_params)
+    shape5, code = _grid5(x, tuple(grid_shape) if grid_shape is not None else None)
+    res = out if out is not None else torch.empty(2, dtype=torch.float64, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_check(_p(x), code, _lib.i64(shape5), _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
+                                    _lib.i32(_shape3(output_shape)), _p(y), int(ray_stride), _p(res),
+                                    _stream(x.device))
+    _lib.check(st, 'RaymarchCheck')
+    return res

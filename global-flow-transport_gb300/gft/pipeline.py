@@ -56,7 +56,8 @@ CONFIGS = {
 
 
 class RenderAdvectStep:
-    def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None):
+    def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None,
+                 fp64_check=False, check_strides=(7, 257)):
         self.config_name = config if isinstance(config, str) else None
         cfg = dict(CONFIGS[config] if isinstance(config, str) else config)
         if order is not None:
@@ -91,6 +92,13 @@ class RenderAdvectStep:
         self.bkg_host = np.array([0.0, 0.5, 1.0], dtype=np.float32)
         self.bkg = torch.from_numpy(self.bkg_host).to(self.dev)
         self.graph = None
+        # FP64 check step (batched mode): double-precision recomputation of the
+        # shadow transmittance (every check_strides[0]-th light-frustum column)
+        # and of the raymarch's accumulated density (every check_strides[1]-th
+        # ray) of each forward, into a device buffer read by fp64_errors()
+        self.fp64_check = bool(fp64_check) and mode != 'plain'
+        self.check_strides = tuple(int(v) for v in check_strides)
+        self.check_buf = torch.zeros(4, dtype=torch.float64, device=self.dev) if self.fp64_check else None
 
     # --------------------------------------------------------------- inputs
     def make_inputs(self, frame=0, target_seed_offset=7):
@@ -121,6 +129,9 @@ class RenderAdvectStep:
             tr = torch.exp(-sh)
         else:
             tr = fused.transmittance(sh.squeeze(0))  # a view: no zero-fill in the backward
+            if self.fp64_check:
+                fused.transmittance_check(sh.squeeze(0).detach(), tr.detach(), self.check_strides[0],
+                                          out=self.check_buf[0:2])
         trv = _InverseSampleGrad.apply(tr, self.M, self.Vs, self.Ps, self.Fs, self.shape,
                                        'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_LINDEPTH', self.rs, None)
         return trv.squeeze(0)  # [1,D,H,W,1]
@@ -140,7 +151,21 @@ class RenderAdvectStep:
         else:
             img = ops.raymarch_grid_transform_bricked(data, self.shape, self.M, self.V, self.P, self.F, self.res,
                                                       storage_dtype=self.storage_dtype)
+            if self.fp64_check:
+                xs = data.detach() if self.storage_dtype is None else data.detach().to(self.storage_dtype)
+                ops.raymarch_check(xs, self.M, self.V, self.P, self.F, self.res, img.detach(), self.check_strides[1],
+                                   grid_shape=self.shape, out=self.check_buf[2:4])
         return img.squeeze(0)  # [V,H,W,4]
+
+    def fp64_errors(self):
+        """Largest deviations of the last forward's FP32 results from their FP64
+        recomputation (needs fp64_check=True): transmittance and raymarch
+        density, absolute and relative to the largest FP64 value (max norm)."""
+        v = self.check_buf.cpu().tolist()
+        rel = lambda e, m: e / m if m > 0 else 0.0
+        return {'transmittance_abs': v[0], 'transmittance_rel': rel(v[0], v[1]), 'raymarch_density_abs': v[2],
+                'raymarch_density_rel': rel(v[2], v[3]),
+                'strides': {'transmittance_columns': self.check_strides[0], 'raymarch_rays': self.check_strides[1]}}
 
     def loss(self, d_prev, vx, vy, vz, target):
         if self.mode != 'plain' and torch.is_grad_enabled() and ops.get_grad_mode() == 'REFERENCE':

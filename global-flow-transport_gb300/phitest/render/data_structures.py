@@ -4,12 +4,26 @@ API (phitest/render/data_structures.py), on torch CUDA tensors.
 Only the members on the render + advect path are kept: staggered velocity
 layout, centring, warping of densities (fused into one CUDA pass per stage via
 gft.ops.advect) and of velocities (per staggered component, composed from the
-lookup sampler like the reference), and the frame-chain forward advection.
-IO, statistics, hulls and optimisation helpers are out of scope.
+lookup sampler like the reference), the frame-chain forward advection, and the
+.npz state files of the reference (DensityGrid / VelocityGrid / State /
+Sequence save and from_file, same keys and directory layout), so that a
+reconstruction saved by either can resume on the other.  Statistics and
+optimisation helpers are out of scope.
 """
 import copy
+import logging
+import os
 
+import numpy as np
 import torch
+
+LOG = logging.getLogger('Structs')
+
+
+def _numpy(t):
+    if isinstance(t, torch.Tensor):
+        return t.detach().float().cpu().numpy()
+    return np.asarray(t)
 
 from gft import ops as _gops
 
@@ -21,13 +35,57 @@ def _spatial(t):
 class DensityGrid:
     """data_structures.py:140-330 (subset).  ``d`` is [1, D, H, W, 1]."""
 
-    def __init__(self, shape, d=None, inflow=None, inflow_offset=None, scale_renderer=None, device=None, **kwargs):
+    def __init__(self, shape, d=None, inflow=None, inflow_offset=None, scale_renderer=None, device=None, hull=None,
+                 inflow_mask=None, **kwargs):
         self.shape = list(shape)
+        if isinstance(d, np.ndarray):
+            d = torch.from_numpy(np.ascontiguousarray(d, dtype=np.float32))
         dev = torch.device(device) if device is not None else (d.device if d is not None else torch.device('cuda'))
-        self._d = d if d is not None else torch.zeros([1] + self.shape + [1], dtype=torch.float32, device=dev)
-        self.inflow = inflow
-        self.inflow_offset = inflow_offset
+        self._d = d.to(dev) if d is not None else torch.zeros([1] + self.shape + [1], dtype=torch.float32, device=dev)
+        as_t = lambda v: torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).to(dev) \
+            if isinstance(v, np.ndarray) else v
+        self.inflow = as_t(inflow)
+        self.inflow_offset = list(inflow_offset) if inflow_offset is not None else None
+        self.inflow_mask = as_t(inflow_mask)
+        self.hull = as_t(hull)
         self.scale_renderer = scale_renderer
+
+    def save(self, path):
+        """Compressed .npz as the reference writes it (data_structures.py:332-353):
+        the density [1, D, H, W, 1] as the positional array 'arr_0', plus 'hull',
+        'inflow', 'inflow_mask' and 'inflow_offset' where present."""
+        save = {}
+        if self.hull is not None:
+            save['hull'] = _numpy(self.hull)
+        if self.inflow is not None:
+            save['inflow'] = _numpy(self.inflow)
+            if self.inflow_mask is not None:
+                save['inflow_mask'] = _numpy(self.inflow_mask)
+            save['inflow_offset'] = np.asarray(self.inflow_offset)
+        np.savez_compressed(path, _numpy(self._d), **save)
+
+    @classmethod
+    def from_file(cls, path, scale_renderer=None, hull=None, inflow=None, inflow_offset=None, inflow_mask=None,
+                  device=None, **kwargs):
+        """Loads a density .npz (data_structures.py:174-194); None (with a
+        warning) when it cannot be read."""
+        try:
+            with np.load(path) as f:
+                d = f['arr_0']
+                if 'hull' in f and hull is None:
+                    hull = f['hull']
+                if 'inflow' in f and inflow is None:
+                    inflow = f['inflow']
+                    if 'inflow_mask' in f and inflow_mask is None:
+                        inflow_mask = f['inflow_mask']
+                    if 'inflow_offset' in f and inflow_offset is None:
+                        inflow_offset = f['inflow_offset'].tolist()
+                grid = cls(list(d.shape[-4:-1]), d=d, inflow=inflow, inflow_offset=inflow_offset,
+                           scale_renderer=scale_renderer, device=device, hull=hull, inflow_mask=inflow_mask)
+        except Exception:
+            LOG.warning("Failed to load density from '%s':", path, exc_info=True)
+            return None
+        return grid
 
     @property
     def d(self):
@@ -76,6 +134,8 @@ class VelocityGrid:
         gen = torch.Generator(device='cpu').manual_seed(kwargs.get('seed', 0))
 
         def init(v, shape):
+            if isinstance(v, np.ndarray):
+                v = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).to(dev)
             if v is not None:
                 if list(v.shape[-4:-1]) != shape or v.shape[-1] != 1:
                     raise ValueError('Invalid shape of velocity component on assignment')
@@ -103,6 +163,33 @@ class VelocityGrid:
                                                           [GridTransform(cs)]).squeeze(1))
         return cls(shape, x=comps[0], y=comps[1], z=comps[2], scale_renderer=scale_renderer, device=centered.device,
                    **kwargs)
+
+    def save(self, path):
+        """Compressed .npz as the reference writes it (data_structures.py:680-681):
+        'centered_shape', 'vel_x', 'vel_y', 'vel_z'."""
+        np.savez_compressed(path, centered_shape=np.asarray(self.centered_shape), vel_x=_numpy(self._x),
+                            vel_y=_numpy(self._y), vel_z=_numpy(self._z))
+
+    @classmethod
+    def from_file(cls, path, scale_renderer=None, warp_renderer=None, device=None, **kwargs):
+        """Loads a velocity .npz (data_structures.py:487-504), including the
+        legacy layout without 'centered_shape'; None (with a warning) when it
+        cannot be read."""
+        try:
+            with np.load(path) as vel:
+                if 'centered_shape' not in vel:  # legacy: derived from the x component
+                    shape = list(vel['vel_x'].shape)
+                    shape[-2] -= 1
+                    shape = shape[1:-1]
+                else:
+                    shape = vel['centered_shape'].tolist()
+                grid = cls(shape, x=vel['vel_x'].astype(np.float32), y=vel['vel_y'].astype(np.float32),
+                           z=vel['vel_z'].astype(np.float32), scale_renderer=scale_renderer,
+                           warp_renderer=warp_renderer, device=device, **kwargs)
+        except Exception:
+            LOG.warning("Failed to load velocity from '%s':", path, exc_info=True)
+            return None
+        return grid
 
     @property
     def x(self):
@@ -282,9 +369,62 @@ class State:
     def get_density_transform(self):
         return self.transform.copy_new_data(self.density.d)
 
+    def save(self, path, suffix=None):
+        """density.npz and velocity.npz (or density_<suffix>.npz, ...) in ``path``
+        (data_structures.py:1213-1215); the directory is created if missing."""
+        os.makedirs(path, exist_ok=True)
+        self.density.save(os.path.join(path, 'density.npz' if suffix is None else 'density_' + suffix + '.npz'))
+        self.velocity.save(os.path.join(path, 'velocity.npz' if suffix is None else 'velocity_' + suffix + '.npz'))
+
+    @classmethod
+    def from_file(cls, path, frame, transform=None, scale_renderer=None, warp_renderer=None, device=None,
+                  density_filename='density.npz', velocity_filename='velocity.npz', **kwargs):
+        """data_structures.py:1123-1128."""
+        density = DensityGrid.from_file(os.path.join(path, density_filename), scale_renderer=scale_renderer,
+                                        device=device)
+        velocity = VelocityGrid.from_file(os.path.join(path, velocity_filename), scale_renderer=scale_renderer,
+                                          warp_renderer=warp_renderer, device=device)
+        return cls(density, velocity, frame, transform=transform)
+
 
 class Sequence(list):
     """Frame chain (data_structures.py:1242-1322, subset)."""
+
+    @property
+    def sequence(self):
+        return self
+
+    @classmethod
+    def from_file(cls, load_path, frames, transform=None, base_path=None, scale_renderer=None, warp_renderer=None,
+                  device=None, density_filename='density.npz', velocity_filename='velocity.npz',
+                  frame_callback=lambda idx, frame: None, **kwargs):
+        """Frames from load_path/frame_{frame:06d}/ with prev/next links
+        (data_structures.py:1241-1259)."""
+        seq, prev = [], None
+        for idx, frame in enumerate(frames):
+            frame_callback(idx, frame)
+            sub_dir = 'frame_{:06d}'.format(frame)
+            state = State.from_file(os.path.join(load_path, sub_dir), frame, transform=transform,
+                                    scale_renderer=scale_renderer, warp_renderer=warp_renderer, device=device,
+                                    density_filename=density_filename, velocity_filename=velocity_filename)
+            if base_path is not None:
+                state.data_path = os.path.join(base_path, sub_dir)
+                os.makedirs(state.data_path, exist_ok=True)
+            state.prev = prev
+            prev = state
+            seq.append(state)
+        for i in range(len(seq) - 1):
+            seq[i].next = seq[i + 1]
+        return cls(seq)
+
+    def save(self, path=None, suffix=None):
+        """Each frame into path/frame_{frame:06d}/ (or its data_path)
+        (data_structures.py:1302-1307)."""
+        for state in self:
+            if path is None and hasattr(state, 'data_path'):
+                state.save(state.data_path, suffix)
+            else:
+                state.save(os.path.join(path, 'frame_{:06d}'.format(state.frame)), suffix)
 
     def densities_advect_fwd(self, dt=1.0, order=1, clamp='NONE'):
         if clamp is None or clamp.upper() not in ('LOCAL', 'GLOBAL'):

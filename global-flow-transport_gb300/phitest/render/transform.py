@@ -87,6 +87,17 @@ class MatrixTransform(object):
     def transform(self, vector):
         return self.get_transform_matrix() @ np.asarray(vector)
 
+    def transform_AABB(self, corner_min=(0, 0, 0), corner_max=(1, 1, 1), expand_corners=False):
+        """World positions (w = 1) of an axis-aligned box's corners: min and max,
+        or all 8 with expand_corners, in the order of transform.py:104-117."""
+        a, b = [float(v) for v in corner_min], [float(v) for v in corner_max]
+        pts = [(a[0], a[1], a[2])]
+        if expand_corners:
+            pts += [(b[0], a[1], a[2]), (a[0], b[1], a[2]), (a[0], a[1], b[2]), (b[0], b[1], a[2]),
+                    (b[0], a[1], b[2]), (a[0], b[1], b[2])]
+        pts.append((b[0], b[1], b[2]))
+        return [self.transform([x, y, z, 1]) for x, y, z in pts]
+
     def __eq__(self, other):
         return np.array_equal(self.get_transform_matrix(), other.get_transform_matrix())
 

@@ -343,6 +343,30 @@ gft_status gft_image_loss(const float* image, const float* target, const float b
 gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
                                const float* loss_grad, float* image_grad, void* stream);
 
+/* ---- FP64 check step (no counterpart in the reference) ----
+ * Double-precision recomputations on the GPU of the two FP32 results of the
+ * step whose rounding compounds along a ray, on a strided sample, from the
+ * same FP32 inputs the step used.  result (device, 16-byte aligned): two
+ * doubles, overwritten: the largest |fp32 - fp64| and the largest |fp64|
+ * over the sample (their ratio is the max-norm relative error).
+ *
+ * gft_transmittance_check: input and output of gft_transmittance
+ * [N, D, H, W, 1]; every column_stride-th (n, h, w) column recomputed as
+ * exp(-sum) in double. */
+gft_status gft_transmittance_check(const float* input, const float* output, const int64_t shape[5],
+                                   int32_t column_stride, double* result, void* stream);
+/* gft_raymarch_check: the density (last) channel of a BEER_LAMBERT (C > 1:
+ * d = max(d + s, 0); C == 1: a sum), LINEAR, BORDER raymarch
+ * (gft_raymarch_grid_transform with separate camera batches) recomputed in
+ * double -- camera inverses, sample positions near + i*step, trilinear
+ * weights and the sum -- for every ray_stride-th pixel of every (batch,
+ * camera) pair, against output [N, V, H, W, C].  input_dtype may carry
+ * GFT_LAYOUT_BRICK. */
+gft_status gft_raymarch_check(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                              const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+                              const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+                              const float* output, int32_t ray_stride, double* result, void* stream);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -310,3 +310,91 @@ def test_brick_layout_conversion():
             for xx in range(W):
                 assert torch.equal(xb[0, cell(xx, yy, zz)], x[0, zz, yy, xx])
     assert torch.equal(ops.from_bricks(xb, (D, H, W)), x)
+
+
+def _golden_cameras(kind, res, n, seed=4000):
+    from gft import synthetic as syn
+    if kind == 'arc':
+        return syn.arc_cameras(n, tuple(res), radius=2.5, fov=30.0)
+    cams, _ = syn.hemisphere_cameras(n - 1, res[0], seed=seed)
+    return cams
+
+
+def test_camera_crops_match_the_reference_golden_values():
+    """Camera.copy_clipped_to_world_coords and copy_with_frustum_crop against
+    the values recorded from the reference's own Camera class
+    (tests/golden/make_camera_golden.py) for the benchmark scenes: the
+    density grid's 8 world corners, every camera of cfg1, cfg2 (pad 0 and 2),
+    cfg4's hemisphere views and cfg5."""
+    import json
+    from phitest.render.transform import GridTransform
+    path = os.path.join(ROOT, 'tests', 'golden', 'camera.json')
+    with open(path) as f:
+        golden = json.load(f)
+    for name, g in golden.items():
+        D, H, W = g['shape']
+        gt = GridTransform([D, H, W], center=True, normalize='MIN')
+        corners = gt.transform_AABB([0, 0, 0], [W, H, D], True)
+        np.testing.assert_allclose(np.asarray(corners), np.asarray(g['corners']), rtol=1e-6, atol=1e-7)
+        cams = _golden_cameras(g['kind'], g['res'], g['n'])
+        assert len(cams) == len(g['cameras'])
+        for cam, want in zip(cams, g['cameras']):
+            clipped, rect = cam.copy_clipped_to_world_coords(corners)
+            w = want['clipped']
+            np.testing.assert_allclose(clipped.clip, w['clip'], rtol=1e-6, err_msg=name)
+            np.testing.assert_allclose(clipped.trbl, w['trbl'], rtol=1e-6, atol=1e-7, err_msg=name)
+            np.testing.assert_allclose(np.asarray(rect), np.asarray(w['scissor_rect']), rtol=1e-6, atol=1e-7)
+            np.testing.assert_allclose(clipped.projection_matrix(), np.asarray(w['projection']), rtol=1e-6,
+                                       atol=1e-7)
+            crop = cam.copy_with_frustum_crop(corners, g['pad'])
+            w = want['crop']
+            assert [int(v) for v in crop.transform.grid_size] == w['grid_size'], name
+            assert [[int(a), int(b)] for a, b in crop.scissor_pad] == w['scissor_pad'], name
+            np.testing.assert_allclose(crop.clip, w['clip'], rtol=1e-6, err_msg=name)
+            np.testing.assert_allclose(crop.trbl, w['trbl'], rtol=1e-6, atol=1e-7, err_msg=name)
+            np.testing.assert_allclose(crop.projection_matrix(), np.asarray(w['projection']), rtol=1e-6, atol=1e-7)
+
+
+def test_state_npz_round_trip_and_reference_keys(tmp_path):
+    """DensityGrid / VelocityGrid / State / Sequence .npz files: the keys and
+    layout of the reference's files (data_structures.py:332-353, :680-681,
+    :1213-1215, :1302-1307), a lossless round trip, and the legacy velocity
+    file without 'centered_shape'."""
+    import torch
+    from phitest.render.data_structures import DensityGrid, Sequence, State, VelocityGrid
+    rng = np.random.default_rng(0)
+    shape = [5, 6, 4]
+    d = torch.from_numpy(rng.random([1] + shape + [1]).astype(np.float32))
+    hull = torch.from_numpy((rng.random([1] + shape + [1]) > 0.5).astype(np.float32))
+    inflow = torch.from_numpy(rng.random([1, 2, 3, 2, 1]).astype(np.float32))
+    dg = DensityGrid(shape, d=d, hull=hull, inflow=inflow, inflow_offset=[1, 2, 1], device='cpu')
+    dg.save(str(tmp_path / 'density.npz'))
+    with np.load(str(tmp_path / 'density.npz')) as f:
+        assert set(f.files) == {'arr_0', 'hull', 'inflow', 'inflow_offset'}
+        assert f['arr_0'].shape == (1, 5, 6, 4, 1) and f['inflow_offset'].tolist() == [1, 2, 1]
+    dl = DensityGrid.from_file(str(tmp_path / 'density.npz'), device='cpu')
+    assert dl.shape == shape and torch.equal(dl.d, d) and torch.equal(dl.hull, hull)
+    assert torch.equal(dl.inflow, inflow) and dl.inflow_offset == [1, 2, 1]
+    vg = VelocityGrid(shape, std=0.3, device='cpu')
+    vg.save(str(tmp_path / 'velocity.npz'))
+    with np.load(str(tmp_path / 'velocity.npz')) as f:
+        assert set(f.files) == {'centered_shape', 'vel_x', 'vel_y', 'vel_z'}
+        assert f['vel_x'].shape == (1, 5, 6, 5, 1) and f['vel_y'].shape == (1, 5, 7, 4, 1)
+    vl = VelocityGrid.from_file(str(tmp_path / 'velocity.npz'), device='cpu')
+    assert vl.centered_shape == shape and all(torch.equal(a, b) for a, b in zip((vl.x, vl.y, vl.z),
+                                                                                (vg.x, vg.y, vg.z)))
+    np.savez_compressed(str(tmp_path / 'legacy.npz'), vel_x=vg.x.numpy(), vel_y=vg.y.numpy(), vel_z=vg.z.numpy())
+    assert VelocityGrid.from_file(str(tmp_path / 'legacy.npz'), device='cpu').centered_shape == shape
+    assert DensityGrid.from_file(str(tmp_path / 'missing.npz'), device='cpu') is None
+    # a sequence of three frames: frame_{:06d}/density.npz, velocity.npz
+    states = [State(DensityGrid(shape, d=d * (i + 1), device='cpu'), VelocityGrid(shape, std=0.1 * (i + 1),
+                                                                                  device='cpu'), frame=10 + i)
+              for i in range(3)]
+    Sequence(states).save(str(tmp_path / 'seq'))
+    assert sorted(os.listdir(str(tmp_path / 'seq'))) == ['frame_000010', 'frame_000011', 'frame_000012']
+    seq = Sequence.from_file(str(tmp_path / 'seq'), [10, 11, 12], device='cpu')
+    assert [s.frame for s in seq] == [10, 11, 12] and seq[0].next is seq[1] and seq[2].prev is seq[1]
+    for a, b in zip(seq, states):
+        assert torch.equal(a.density.d, b.density.d) and torch.equal(a.velocity.z, b.velocity.z)
+    states[0].save(str(tmp_path / 'one'), suffix='it5')
+    assert sorted(os.listdir(str(tmp_path / 'one'))) == ['density_it5.npz', 'velocity_it5.npz']
