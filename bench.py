@@ -300,11 +300,22 @@ def bench_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def _grads_of(step):
+def _load_inputs(step, inputs):
+    """Copies make_inputs() arrays into a captured step's static inputs."""
     import torch
+    with torch.no_grad():
+        for dst, key, lead in ((step.s_d, 'd_prev', False), (step.s_vx, 'vx', True), (step.s_vy, 'vy', True),
+                               (step.s_vz, 'vz', True), (step.s_t, 'target', False)):
+            a = torch.from_numpy(inputs[key])
+            dst.copy_(a[None] if lead else a)
+
+
+def _grads_of(step, inputs):
+    import torch
+    _load_inputs(step, inputs)
     loss, grads = step.replay()
     torch.cuda.synchronize()
-    return float(loss), [g.detach().float().clone() for g in grads]
+    return float(loss.detach()), [g.detach().float().clone() for g in grads]
 
 
 def _rel(a, b):
@@ -370,8 +381,8 @@ def extras(args, step, dev, timed, storage, inputs, ms):
                               'what': 'the headline step with FP32 storage'}
         # accuracy of BF16 storage against the FP32 step on the same inputs
         # (the FP32 path is held to the FP64 oracle by the -m gpu tests)
-        lb, gb = _grads_of(step)
-        lf, gf = _grads_of(f32)
+        lb, gb = _grads_of(step, inputs)
+        lf, gf = _grads_of(f32, inputs)
         out['bf16_accuracy'] = {'loss_rel': abs(lb - lf) / abs(lf),
                                 'grad_rel_l2': dict(zip(('density', 'vel_x', 'vel_y', 'vel_z'),
                                                         [_rel(a, b) for a, b in zip(gb, gf)])),
@@ -399,8 +410,9 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     if f32 is not step:
         del f32
         torch.cuda.empty_cache()
+    out['fp64_check'] = fp64_check(args, dev, timed, storage, inputs, ms)
     out['static_cameras'] = static_cameras(args, dev, timed, storage, inputs)
-    out['uneven_views'] = uneven_views(dev, timed)
+    out['cfg4'] = uneven_batch(dev, timed, storage)
     out['cfg2'] = other_config('cfg2', args, dev, timed)
     out['transport_chain'] = transport_chain('cfg2', dev, timed, frames=16, every=4)
     if not args.no_chain5:
@@ -437,6 +449,32 @@ def other_config(config, args, dev, timed):
         torch.cuda.empty_cache()
     res['workload'] = workload_config(config, 'f32|bf16', args.grad_mode)['workload']
     return res
+
+
+def fp64_check(args, dev, timed, storage, inputs, ms):
+    """The headline step with the FP64 check step inside its graph
+    (RenderAdvectStep(fp64_check=True)): the largest deviations of the FP32
+    shadow transmittance (every 7th light-frustum column) and of the raymarch's
+    accumulated density (every 257th ray) from their double-precision
+    recomputation on the GPU, and the time the check adds to a step."""
+    import numpy as np
+    import torch
+    from gft.pipeline import RenderAdvectStep
+    try:
+        st = RenderAdvectStep(args.config, dev, storage_dtype=storage, mode='batched', fp64_check=True)
+        st.setup_static(inputs)
+        st.capture(warmup=3)
+        for _ in range(3):
+            st.replay()
+        t = float(np.mean(timed(st.replay, 10)))
+        res = st.fp64_errors()
+        res.update({'ms_per_step_with_check': t, 'check_ms': t - ms})
+        del st
+        torch.cuda.empty_cache()
+        return res
+    except Exception as e:  # reported, not required
+        torch.cuda.empty_cache()
+        return {'error': repr(e)[:300]}
 
 
 def static_cameras(args, dev, timed, storage, inputs):
@@ -534,51 +572,71 @@ def transport_chain(config, dev, timed, frames=16, every=4, storage=None, iters=
         return {'error': repr(e)[:300]}
 
 
-def uneven_views(dev, timed):
-    """One frame of the uneven-view batch workload: density 96x170x96 (C = 4
-    light + density), one fixed 256x256 view plus 8 seeded upper-hemisphere
-    views of 64-256 pixels square, 128 samples, reference-normalised gradient.
-    Raymarch forward + adjoint of all 9 views in one launch each
-    (raymarch_grid_transform_multi) against one launch per view (the
-    reference's structure: one call per image size)."""
+def uneven_batch(dev, timed, storage=None, frames=64, views=8):
+    """cfg4: 64 frames of 96x170x96 density, each rendered by 1 fixed view
+    (256^2) + 8 seeded upper-hemisphere views of 64-256 px square (cameras
+    narrowed to the grid's bounding box), 128 samples, Beer-Lambert + spot
+    light with shadow, L2 image loss; all 576 renders and their adjoints plus
+    the batched shadow pass in one CUDA graph (gft.pipeline.UnevenBatchStep).
+    Beside it, the raymarch alone (forward + reference-normalised adjoint) of
+    the 576 views: views bound to their frame in launches of 16
+    (raymarch_grid_transform_views) against one call per view (the reference's
+    structure: one call per camera image size)."""
     import numpy as np
     import torch
     from gft import ops
-    from gft import synthetic as syn
-    from phitest.render.transform import GridTransform
-    shape = (96, 170, 96)
-    gt = GridTransform(list(shape), center=True, normalize='MIN')
-    M = syn.model_matrix(gt)
-    cams, shapes = syn.hemisphere_cameras(8, 128, seed=4000)
-    V, P, F = syn.camera_params(cams)
-    d = torch.from_numpy(syn.plume_density(shape, 4000)).to(dev)
-    x = (torch.cat([d * 0.7, d * 0.5, d * 0.3, d], -1) * 0.02).contiguous()
-    ref = ops.GRAD['REFERENCE']
-    y = ops._raymarch_multi_fwd(x, M, V, P, F, [list(s) for s in shapes], 1, 0, 0)
-    torch.manual_seed(0)
-    dy = torch.randn_like(y) * 1e-3
-    sl = [list(s) for s in shapes]
+    from gft.pipeline import UnevenBatchStep
+    try:
+        st = UnevenBatchStep(frames=frames, views=views, device=dev, storage_dtype=storage)
+        inputs = st.make_inputs(seed=4000)
+        st.setup_static(inputs)
+        torch.cuda.reset_peak_memory_stats(dev)
+        st.capture(warmup=3)
+        for _ in range(2):
+            st.replay()
+        t = float(np.median(timed(st.replay, 5)))
+        nviews = len(st.shapes)
+        res = {'workload': '%d frames x (1 + %d) views of 64-256 px, density %s, %d samples, shadow + BEER_LAMBERT, '
+                           'fwd+bwd to every frame density, one CUDA graph' % (frames, views,
+                                                                               'x'.join(map(str, st.shape)),
+                                                                               st.shapes[0][0]),
+               'ms_per_iteration': t, 'iters_per_s': 1000.0 / t, 'renders_per_s': nviews * 1000.0 / t,
+               'views': nviews, 'pixels': st.pixels, 'peak_hbm_bytes': int(torch.cuda.max_memory_allocated(dev))}
+        # raymarch alone: one views op vs one call per view
+        with torch.no_grad():
+            x = (torch.from_numpy(inputs['d']).to(dev).repeat(1, 1, 1, 1, 4) * 0.02).contiguous()
+        cb, shapes = st.camera_batch, st.shapes
+        ref = ops.GRAD['REFERENCE']
+        y = ops._raymarch_views_fwd(x, st.M, st.V, st.P, st.F, cb, shapes, 1, 0, 0)
+        dy = torch.randn_like(y) * 1e-3
 
-    def multi():
-        yy = ops._raymarch_multi_fwd(x, M, V, P, F, sl, 1, 0, 0)
-        ops._raymarch_multi_bwd(x, yy, dy, M, V, P, F, sl, 1, 0, 0, ref)
+        def views_op():
+            yy = ops._raymarch_views_fwd(x, st.M, st.V, st.P, st.F, cb, shapes, 1, 0, 0)
+            ops._raymarch_views_bwd(x, yy, dy, st.M, st.V, st.P, st.F, cb, shapes, 1, 0, 0, ref)
 
-    offs = np.cumsum([0] + [h * w for _, h, w in shapes])
-    dys = [dy[:, offs[c]:offs[c + 1]].reshape(1, 1, shapes[c][1], shapes[c][2], 4).contiguous()
-           for c in range(len(shapes))]
+        offs = np.cumsum([0] + [h * w for _, h, w in shapes])
+        dys = [dy[offs[c]:offs[c + 1]].reshape(1, 1, shapes[c][1], shapes[c][2], 4).contiguous()
+               for c in range(len(shapes))]
 
-    def per_view():
-        for c, s in enumerate(shapes):
-            yc = ops._raymarch_fwd(x, M, V[c:c + 1], P[c:c + 1], F[c:c + 1], s, 1, 0, 0, True)
-            ops._raymarch_bwd(x, yc, dys[c], M, V[c:c + 1], P[c:c + 1], F[c:c + 1], s, 1, 0, 0, True, ref)
+        def per_view():
+            for c, s in enumerate(shapes):
+                b = cb[c]
+                xb = x[b:b + 1]
+                yc = ops._raymarch_fwd(xb, st.M[b:b + 1], st.V[c:c + 1], st.P[c:c + 1], st.F[c:c + 1], s, 1, 0, 0,
+                                       True)
+                ops._raymarch_bwd(xb, yc, dys[c], st.M[b:b + 1], st.V[c:c + 1], st.P[c:c + 1], st.F[c:c + 1], s, 1,
+                                  0, 0, True, ref)
 
-    for _ in range(2):
-        multi(), per_view()
-    tm = float(np.median(timed(multi, 7)))
-    tp = float(np.median(timed(per_view, 7)))
-    return {'workload': 'density 96x170x96, views 256^2 + 8 x (64-256)^2 upper hemisphere, 128 samples, '
-                        'raymarch fwd + reference-normalised adjoint',
-            'sizes': [s[1] for s in shapes], 'one_launch_ms': tm, 'per_view_ms': tp, 'speedup': tp / tm}
+        views_op(), per_view()
+        tv = float(np.median(timed(views_op, 3)))
+        tp = float(np.median(timed(per_view, 3)))
+        res['raymarch_only'] = {'views_op_ms': tv, 'per_view_calls_ms': tp, 'speedup': tp / tv}
+        del st, x, y, dy, dys
+        torch.cuda.empty_cache()
+        return res
+    except Exception as e:  # reported, not required
+        torch.cuda.empty_cache()
+        return {'error': repr(e)[:300]}
 
 
 def kernel_roofline(step, dev, timed, storage=None):

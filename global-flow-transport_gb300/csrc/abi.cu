@@ -506,9 +506,27 @@ static bool multi_shapes_ok(const int32_t* shapes, int32_t num_cameras, std::str
 
 // Every (batch, camera) pair with its own image; the output of batch slice n
 // holds the cameras' images one after another.
+// camera_batch == nullptr: every (batch, camera) pair, the output of batch
+// slice n holding the cameras' images one after another.  Otherwise one pair
+// per camera c, rendering batch slice camera_batch[c], the output holding the
+// cameras' images one after another.
 static std::vector<Pair> multi_pairs(const float* M, int num_m, const float* V, const float* P, const float* F,
-                                     int num_cameras, int batch, const int32_t* shapes) {
-    auto pairs = make_pairs(M, num_m, V, P, F, num_cameras, batch, true);
+                                     int num_cameras, int batch, const int32_t* shapes,
+                                     const int32_t* camera_batch = nullptr) {
+    std::vector<Pair> pairs;
+    if (camera_batch == nullptr) {
+        pairs = make_pairs(M, num_m, V, P, F, num_cameras, batch, true);
+    } else {
+        for (int c = 0; c < num_cameras; ++c) {
+            const int b = camera_batch[c];
+            Pair p;
+            p.cam = make_cam(M + 16 * (num_m == 1 ? 0 : b), V + 16 * c, P + 16 * c, F + 6 * c);
+            p.in_batch = b;
+            p.out_slot = c;
+            p.camera = c;
+            pairs.push_back(p);
+        }
+    }
     int64_t per_batch = 0;
     for (int c = 0; c < num_cameras; ++c) per_batch += (int64_t)shapes[3 * c + 1] * shapes[3 * c + 2];
     for (Pair& p : pairs) {
@@ -517,16 +535,29 @@ static std::vector<Pair> multi_pairs(const float* M, int num_m, const float* V, 
         p.D = shapes[3 * p.camera];
         p.H = shapes[3 * p.camera + 1];
         p.W = shapes[3 * p.camera + 2];
-        p.pix0 = (int64_t)p.in_batch * per_batch + off;
+        p.pix0 = (camera_batch == nullptr ? (int64_t)p.in_batch * per_batch : 0) + off;
     }
     return pairs;
 }
 
-gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dtype, const int64_t input_shape[5],
-                                             const float* matrix_m, int32_t num_m, const float* matrix_v,
-                                             const float* matrix_p, const float* frustum, int32_t num_cameras,
-                                             const int32_t* output_shapes, int32_t interpolation, int32_t boundary,
-                                             int32_t blending_mode, float* output, void* stream) {
+static bool camera_batch_ok(const int32_t* camera_batch, int num_cameras, int64_t batch, std::string& why) {
+    if (camera_batch == nullptr) {
+        why = "camera_batch is NULL";
+        return false;
+    }
+    for (int c = 0; c < num_cameras; ++c)
+        if (camera_batch[c] < 0 || camera_batch[c] >= batch) {
+            why = "camera_batch entries must lie in [0, batch)";
+            return false;
+        }
+    return true;
+}
+
+static gft_status multi_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                 const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                 const float* frustum, int32_t num_cameras, const int32_t* camera_batch,
+                                 const int32_t* output_shapes, int32_t interpolation, int32_t boundary,
+                                 int32_t blending_mode, float* output, void* stream) {
     std::string why;
     if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
@@ -536,6 +567,8 @@ gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dt
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
     if (st != GFT_OK) return st;
+    if (camera_batch != nullptr && !camera_batch_ok(camera_batch, num_cameras, input_shape[0], why))
+        return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!input || !output) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     RaymarchArgs a{};
     a.input = input;
@@ -546,7 +579,8 @@ gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dt
     a.filter = interpolation;
     a.boundary = boundary;
     a.blend = blending_mode;
-    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes,
+                                   camera_batch);
     a.n_slots = (int)pairs.size();
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
         (st = check_aligned({output}, vec_bytes(a.C, 0))) != GFT_OK)
@@ -555,19 +589,44 @@ gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dt
     return GFT_OK;
 }
 
+gft_status gft_raymarch_grid_transform_multi(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                             const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                             const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                             const int32_t* output_shapes, int32_t interpolation, int32_t boundary,
+                                             int32_t blending_mode, float* output, void* stream) {
+    return multi_fwd_impl(input, input_dtype, input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras,
+                          nullptr, output_shapes, interpolation, boundary, blending_mode, output, stream);
+}
+
+gft_status gft_raymarch_grid_transform_views(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                             const float* matrix_m, int32_t num_m, const float* matrix_v,
+                                             const float* matrix_p, const float* frustum, int32_t num_cameras,
+                                             const int32_t* camera_batch, const int32_t* output_shapes,
+                                             int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                             float* output, void* stream) {
+    if (camera_batch == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "camera_batch is NULL");
+    return multi_fwd_impl(input, input_dtype, input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras,
+                          camera_batch, output_shapes, interpolation, boundary, blending_mode, output, stream);
+}
+
+size_t gft_raymarch_grid_transform_views_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
+                                                             int32_t grad_mode) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why) || (grad_mode & ~GFT_GRAD_WEIGHTS_READY) == GFT_GRAD_EXACT) return 0;
+    return align256(sizeof(float) * (size_t)brick_cells(dims_of(input_shape)) * (size_t)std::max(num_cameras, 1));
+}
+
 size_t gft_raymarch_grid_transform_multi_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
                                                              int32_t grad_mode) {
     return gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras, 1, grad_mode);
 }
 
-gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t input_dtype,
-                                                  const int64_t input_shape[5], const float* output,
-                                                  const float* output_grad, const float* matrix_m, int32_t num_m,
-                                                  const float* matrix_v, const float* matrix_p, const float* frustum,
-                                                  int32_t num_cameras, const int32_t* output_shapes,
-                                                  int32_t interpolation, int32_t boundary, int32_t blending_mode,
-                                                  int32_t grad_mode, float* input_grad, void* workspace,
-                                                  size_t workspace_bytes, void* stream) {
+static gft_status multi_grad_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
+                                  const float* output, const float* output_grad, const float* matrix_m, int32_t num_m,
+                                  const float* matrix_v, const float* matrix_p, const float* frustum,
+                                  int32_t num_cameras, const int32_t* camera_batch, const int32_t* output_shapes,
+                                  int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t grad_mode,
+                                  float* input_grad, void* workspace, size_t workspace_bytes, void* stream) {
     std::string why;
     if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
@@ -584,8 +643,13 @@ gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t inp
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
     if (st != GFT_OK) return st;
+    if (camera_batch != nullptr && !camera_batch_ok(camera_batch, num_cameras, input_shape[0], why))
+        return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!input || !output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
-    const size_t need = gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, grad_mode);
+    const size_t need =
+        camera_batch != nullptr
+            ? gft_raymarch_grid_transform_views_grad_workspace_size(input_shape, num_cameras, grad_mode)
+            : gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, grad_mode);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
     RaymarchArgs a{};
@@ -597,7 +661,8 @@ gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t inp
     a.filter = interpolation;
     a.boundary = boundary;
     a.blend = blending_mode;
-    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes,
+                                   camera_batch);
     a.n_slots = (int)pairs.size();
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
         (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
@@ -610,19 +675,50 @@ gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t inp
     return GFT_OK;
 }
 
-gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_shape[5], const float* matrix_m,
-                                                          int32_t num_m, const float* matrix_v, const float* matrix_p,
-                                                          const float* frustum, int32_t num_cameras,
-                                                          const int32_t* output_shapes, int32_t boundary,
-                                                          void* workspace, size_t workspace_bytes, void* stream) {
+gft_status gft_raymarch_grid_transform_multi_grad(const void* input, int32_t input_dtype,
+                                                  const int64_t input_shape[5], const float* output,
+                                                  const float* output_grad, const float* matrix_m, int32_t num_m,
+                                                  const float* matrix_v, const float* matrix_p, const float* frustum,
+                                                  int32_t num_cameras, const int32_t* output_shapes,
+                                                  int32_t interpolation, int32_t boundary, int32_t blending_mode,
+                                                  int32_t grad_mode, float* input_grad, void* workspace,
+                                                  size_t workspace_bytes, void* stream) {
+    return multi_grad_impl(input, input_dtype, input_shape, output, output_grad, matrix_m, num_m, matrix_v, matrix_p,
+                           frustum, num_cameras, nullptr, output_shapes, interpolation, boundary, blending_mode,
+                           grad_mode, input_grad, workspace, workspace_bytes, stream);
+}
+
+gft_status gft_raymarch_grid_transform_views_grad(const void* input, int32_t input_dtype,
+                                                  const int64_t input_shape[5], const float* output,
+                                                  const float* output_grad, const float* matrix_m, int32_t num_m,
+                                                  const float* matrix_v, const float* matrix_p, const float* frustum,
+                                                  int32_t num_cameras, const int32_t* camera_batch,
+                                                  const int32_t* output_shapes, int32_t interpolation,
+                                                  int32_t boundary, int32_t blending_mode, int32_t grad_mode,
+                                                  float* input_grad, void* workspace, size_t workspace_bytes,
+                                                  void* stream) {
+    if (camera_batch == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "camera_batch is NULL");
+    return multi_grad_impl(input, input_dtype, input_shape, output, output_grad, matrix_m, num_m, matrix_v, matrix_p,
+                           frustum, num_cameras, camera_batch, output_shapes, interpolation, boundary, blending_mode,
+                           grad_mode, input_grad, workspace, workspace_bytes, stream);
+}
+
+static gft_status multi_weights_impl(const int64_t input_shape[5], const float* matrix_m, int32_t num_m,
+                                     const float* matrix_v, const float* matrix_p, const float* frustum,
+                                     int32_t num_cameras, const int32_t* camera_batch, const int32_t* output_shapes,
+                                     int32_t boundary, void* workspace, size_t workspace_bytes, void* stream) {
     std::string why;
     if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!multi_shapes_ok(output_shapes, num_cameras, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!enum_in(boundary, 0, 2)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid boundary mode");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
     if (st != GFT_OK) return st;
-    const size_t need = gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras,
-                                                                              GFT_GRAD_REFERENCE);
+    if (camera_batch != nullptr && !camera_batch_ok(camera_batch, num_cameras, input_shape[0], why))
+        return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    const size_t need =
+        camera_batch != nullptr
+            ? gft_raymarch_grid_transform_views_grad_workspace_size(input_shape, num_cameras, GFT_GRAD_REFERENCE)
+            : gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, GFT_GRAD_REFERENCE);
     if (workspace == nullptr || workspace_bytes < need)
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
     if ((st = check_workspace_aligned(workspace)) != GFT_OK) return st;
@@ -632,11 +728,32 @@ gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_sh
     a.din = dims_of(input_shape);
     a.filter = GFT_FILTER_LINEAR;
     a.boundary = boundary;
-    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes);
+    const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes,
+                                   camera_batch);
     a.n_slots = (int)pairs.size();
     if (!launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
+}
+
+gft_status gft_raymarch_grid_transform_multi_grad_weights(const int64_t input_shape[5], const float* matrix_m,
+                                                          int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                                          const float* frustum, int32_t num_cameras,
+                                                          const int32_t* output_shapes, int32_t boundary,
+                                                          void* workspace, size_t workspace_bytes, void* stream) {
+    return multi_weights_impl(input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, nullptr,
+                              output_shapes, boundary, workspace, workspace_bytes, stream);
+}
+
+gft_status gft_raymarch_grid_transform_views_grad_weights(const int64_t input_shape[5], const float* matrix_m,
+                                                          int32_t num_m, const float* matrix_v, const float* matrix_p,
+                                                          const float* frustum, int32_t num_cameras,
+                                                          const int32_t* camera_batch, const int32_t* output_shapes,
+                                                          int32_t boundary, void* workspace, size_t workspace_bytes,
+                                                          void* stream) {
+    if (camera_batch == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "camera_batch is NULL");
+    return multi_weights_impl(input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, camera_batch,
+                              output_shapes, boundary, workspace, workspace_bytes, stream);
 }
 
 // ---------------------------------------------------------------- resample

@@ -72,6 +72,13 @@ _SIGS = {
                                                       _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
     'gft_raymarch_grid_transform_multi_grad_weights': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32, _P,
                                                               _SZ, _P]),
+    'gft_raymarch_grid_transform_views': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32P,
+                                                 _I32, _I32, _I32, _P, _P]),
+    'gft_raymarch_grid_transform_views_grad_workspace_size': (_SZ, [_I64P, _I32, _I32]),
+    'gft_raymarch_grid_transform_views_grad': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
+                                                      _I32P, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
+    'gft_raymarch_grid_transform_views_grad_weights': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32P,
+                                                              _I32, _P, _SZ, _P]),
     'gft_sample_grid_transform_workspace_size': (_SZ, [_I64P, _I32, _I32]),
     'gft_sample_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                          _I32, _I32, _I32, _I32, _F, _I32, _F, _I32, _P, _P, _SZ, _P]),

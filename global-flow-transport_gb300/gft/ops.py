@@ -598,6 +598,123 @@ def raymarch_grid_transform_multi(input, matrix_m, matrix_v, matrix_p, frustum_p
     return [part.view(x.shape[0], h, w, x.shape[4]) for part, (_, h, w) in zip(torch.split(y, sizes, dim=1), shapes)]
 
 
+# ------------------------------------------------------------------ views bound to batch slices
+def _views_args(M, V, P, F, camera_batch, shapes):
+    Mh, nm = _mats(M)
+    Vh, nv = _mats(V)
+    Ph, npj = _mats(P)
+    Fh, nf = _frustum(F)
+    if not (nv == npj == nf == len(camera_batch) == len(shapes)):
+        raise _lib.GftInvalidArgument('camera batch size mismatch')
+    return Mh, nm, Vh, Ph, Fh, nv, _lib.i32(camera_batch), _lib.i32(sum(shapes, []))
+
+
+def _raymarch_views_weights(x_shape, device, M, V, P, F, camera_batch, shapes, boundary):
+    lib = _lib.load()
+    Mh, nm, Vh, Ph, Fh, nv, cb, sh = _views_args(M, V, P, F, camera_batch, shapes)
+    shape = _lib.i64(x_shape)
+    ws = _workspace(lib.gft_raymarch_grid_transform_views_grad_workspace_size(shape, nv, GRAD['REFERENCE']), device)
+    with torch.cuda.device(device):
+        st = lib.gft_raymarch_grid_transform_views_grad_weights(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv, cb, sh,
+                                                                boundary, _p(ws), ws.numel(), _stream(device))
+    _lib.check(st, 'RaymarchGridTransformViews weights')
+    return ws
+
+
+def _raymarch_views_fwd(x, M, V, P, F, camera_batch, shapes, interp, boundary, blend):
+    lib = _lib.load()
+    Mh, nm, Vh, Ph, Fh, nv, cb, sh = _views_args(M, V, P, F, camera_batch, shapes)
+    npix = sum(h * w for _, h, w in shapes)
+    out = torch.empty((npix, x.shape[4]), dtype=torch.float32, device=x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_views(_p(x), _dtype_code(x), _lib.i64(x.shape), _p(Mh), nm, _p(Vh),
+                                                   _p(Ph), _p(Fh), nv, cb, sh, interp, boundary, blend, _p(out),
+                                                   _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformViews')
+    return out
+
+
+def _raymarch_views_bwd(x, y, dy, M, V, P, F, camera_batch, shapes, interp, boundary, blend, gmode, weights=None):
+    lib = _lib.load()
+    Mh, nm, Vh, Ph, Fh, nv, cb, sh = _views_args(M, V, P, F, camera_batch, shapes)
+    shape = _lib.i64(x.shape)
+    grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    if weights is not None and gmode == GRAD['REFERENCE']:
+        ws = weights
+        gmode = gmode | WEIGHTS_READY
+    else:
+        ws = _workspace(lib.gft_raymarch_grid_transform_views_grad_workspace_size(shape, nv, gmode), x.device)
+    with torch.cuda.device(x.device):
+        st = lib.gft_raymarch_grid_transform_views_grad(_p(x), _dtype_code(x), shape, _p(y), _p(dy), _p(Mh), nm,
+                                                        _p(Vh), _p(Ph), _p(Fh), nv, cb, sh, interp, boundary, blend,
+                                                        gmode, _p(grad), _p(ws), ws.numel(), _stream(x.device))
+    _lib.check(st, 'RaymarchGridTransformViewsGrad')
+    return grad
+
+
+class _RaymarchViews(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, M, V, P, F, camera_batch, shapes, interp, boundary, blend, storage_dtype):
+        xs = _storage(x, storage_dtype)
+        ctx.weights = None
+        if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
+                and interp == FILTER['LINEAR']):
+            cur = torch.cuda.current_stream(xs.device)
+            side = _side_stream(xs.device)
+            side.wait_stream(cur)
+            with torch.cuda.stream(side):
+                ws = _raymarch_views_weights(tuple(xs.shape), xs.device, M, V, P, F, camera_batch, shapes, boundary)
+                ev = torch.cuda.Event()
+                ev.record(side)
+            ctx.weights = (ws, ev)
+        y = _raymarch_views_fwd(xs, M, V, P, F, camera_batch, shapes, interp, boundary, blend)
+        ctx.save_for_backward(xs, y)
+        ctx.args = (M, V, P, F, camera_batch, shapes, interp, boundary, blend)
+        ctx.in_dtype = x.dtype
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        xs, y = ctx.saved_tensors
+        M, V, P, F, camera_batch, shapes, interp, boundary, blend = ctx.args
+        ws = None
+        if ctx.weights is not None:
+            ws, ev = ctx.weights
+            torch.cuda.current_stream(xs.device).wait_event(ev)
+        g = _raymarch_views_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, camera_batch, shapes, interp, boundary,
+                                blend, GRAD[get_grad_mode()], weights=ws)
+        ctx.weights = None
+        return (g.to(ctx.in_dtype),) + (None,) * 10
+
+
+def raymarch_grid_transform_views(input, camera_batch, matrix_m, matrix_v, matrix_p, frustum_params, output_shapes,
+                                  interpolation='LINEAR', boundary='BORDER', blending_mode='BEER_LAMBERT',
+                                  storage_dtype=None):
+    """RaymarchGridTransform of views bound to batch slices, in one launch per
+    16 views: camera c renders only batch slice camera_batch[c] into an image of
+    output_shapes[c] = (depth samples, height, width).  Returns the images as
+    one [sum_c H_c W_c, C] buffer, the cameras one after another (split it with
+    views_split); camera c's image equals
+    raymarch_grid_transform(input[b:b+1], M[b], camera c alone, output_shapes[c])
+    with b = camera_batch[c]."""
+    x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
+    if x.dim() != 5 or x.shape[4] > 4:
+        raise _lib.GftInvalidArgument('Invalid input shape (NDHWC): %s' % (tuple(x.shape),))
+    nv = _mats(matrix_v)[1]
+    shapes = _shapes3(output_shapes, nv)
+    cb = [int(b) for b in camera_batch]
+    return _RaymarchViews.apply(x, matrix_m, matrix_v, matrix_p, frustum_params, cb, shapes,
+                                _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
+                                _enum(BLEND, blending_mode, 'blending_mode'), storage_dtype)
+
+
+def views_split(y, output_shapes):
+    """The per-camera [H_c, W_c, C] images of a raymarch_grid_transform_views output."""
+    sizes = [int(h) * int(w) for _, h, w in output_shapes]
+    return [part.view(int(h), int(w), y.shape[-1]) for part, (_, h, w) in zip(torch.split(y, sizes, dim=0),
+                                                                             output_shapes)]
+
+
 # ------------------------------------------------------------------ SampleGridTransform
 def _sample_transform_fwd(x, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco, separate):
     lib = _lib.load()

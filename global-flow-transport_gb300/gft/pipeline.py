@@ -221,6 +221,114 @@ class RenderAdvectStep:
         return self.step(self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
 
 
+class UnevenBatchStep:
+    """A batch of frames rendered by views bound to their frame (the uneven-view
+    workload): per frame one fixed view plus ``views`` seeded cameras on the
+    upper hemisphere with square images of 64-256 pixels, all with ``samples``
+    depth samples; each frame lit by the spot light with its shadow pass; loss =
+    mean squared difference of every view's image (background composite) to its
+    target; forward + backward to every frame's density.  The raymarch of all
+    frames' views runs as gft.ops.raymarch_grid_transform_views (16 views per
+    launch), the shadow pass and the light composition batched over the frames,
+    the whole step capturable in one CUDA graph.
+
+    clip_cameras: each camera's top/right/bottom/left narrowed to the density
+    grid's world bounding box (Camera.copy_clipped_to_world_coords with
+    preserve_clip, so the depth step stays that of the original camera), as the
+    reference fits its render cameras to the density's hull, so fewer rays
+    miss the grid."""
+
+    def __init__(self, frames=64, views=8, shape=(96, 170, 96), samples=128, device='cuda', storage_dtype=None,
+                 clip_cameras=True, seed=4000, shadow=(128, 128, 128), mips=3, sizes=(64, 256)):
+        self.dev = torch.device(device)
+        self.frames = int(frames)
+        self.shape = tuple(shape)
+        self.storage_dtype = storage_dtype
+        self.gt = syn.grid_transform(self.shape)
+        D, H, W = self.shape
+        corners = self.gt.transform_AABB([0, 0, 0], [W, H, D], True)
+        Vs, Ps, Fs, self.shapes, self.camera_batch, steps = [], [], [], [], [], []
+        for f in range(self.frames):
+            cams, shp = syn.hemisphere_cameras(views, samples, sizes=sizes, seed=seed + f)
+            if clip_cameras:
+                cams = [c.copy_clipped_to_world_coords(corners, preserve_clip=True)[0] for c in cams]
+            V, P, F = syn.camera_params(cams)
+            Vs.append(V), Ps.append(P), Fs.append(F)
+            self.shapes += [list(s) for s in shp]
+            self.camera_batch += [f] * len(cams)
+            steps += [c.depth_step for c in cams]
+        self.V, self.P, self.F = np.concatenate(Vs), np.concatenate(Ps), np.concatenate(Fs)
+        self.depth_step = float(steps[0])
+        if not np.allclose(steps, self.depth_step):
+            raise ValueError('the views of a batch must share one depth step')
+        self.M = np.concatenate([syn.model_matrix(self.gt)] * self.frames)
+        self.spot = SpotLight(Transform(translation=[0, 0, 2.0], parent=Transform(rotation_deg=[-40, 0, 0])),
+                              intensity=0.85, cast_shadows=True, shadow_clip=[0.85, 3.15], range_scale=0.825,
+                              angle_deg=60.0, shadow_resolution=list(shadow), cone_mask=False)
+        self.ambient = 0.64
+        self.rs = RenderSettings(mips)
+        self.Vs, self.Ps, self.Fs = syn.camera_params([self.spot.shadow_cam])
+        self.shadow_step = float(self.spot.shadow_cam.depth_step)
+        self.shadow_res = tuple(shadow)
+        fall = self.spot.falloff(_Holder(self.gt), self.dev)
+        col = torch.tensor(self.spot.c * np.float32(self.spot.i), dtype=torch.float32, device=self.dev)
+        self.falloff_col = (fall * col)[None].contiguous()
+        self.bkg_host = np.array([0.0, 0.5, 1.0], dtype=np.float32)
+        self.pixels = sum(h * w for _, h, w in self.shapes)
+        self.graph = None
+
+    def make_inputs(self, seed=0, target_seed_offset=7):
+        """Seeded frame densities [F, D, H, W, 1] (plumes rising with the frame)
+        and targets [pixels, 3] rendered from perturbed plumes."""
+        d = np.concatenate([syn.plume_density(self.shape, seed + f, f) for f in range(self.frames)], 0)
+        dt = np.concatenate([syn.plume_density(self.shape, seed + f + target_seed_offset, f + 1)
+                             for f in range(self.frames)], 0)
+        with torch.no_grad():
+            tgt = self.render(torch.from_numpy(dt).to(self.dev))[..., :3].contiguous()
+        return dict(d=d, target=tgt.cpu().numpy())
+
+    def shadow(self, d):
+        from phitest.render.renderer import _InverseSampleGrad
+        sh = _InverseSampleGrad.apply(d * self.shadow_step, self.M, self.Vs, self.Ps, self.Fs, self.shadow_res,
+                                      'TRANSFORM_LINDEPTH', 'TRANSFORM_LINDEPTH_REVERSE', self.rs, None)
+        tr = fused.transmittance(sh[:, 0])
+        trv = _InverseSampleGrad.apply(tr, self.M, self.Vs, self.Ps, self.Fs, self.shape,
+                                       'TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_LINDEPTH', self.rs, None)
+        return trv[:, 0]  # [F,D,H,W,1]
+
+    def render(self, d):
+        """Images of all views, [pixels, 4], the views one after another."""
+        data = fused.light_compose(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step)
+        return ops.raymarch_grid_transform_views(data, self.camera_batch, self.M, self.V, self.P, self.F,
+                                                 self.shapes, storage_dtype=self.storage_dtype)
+
+    def step(self, d, target):
+        loss = fused.image_loss(self.render(d), target, self.bkg_host)
+        (g,) = torch.autograd.grad(loss, [d])
+        return loss, g
+
+    def setup_static(self, inputs):
+        self.s_d = torch.from_numpy(inputs['d']).to(self.dev).requires_grad_(True)
+        self.s_t = torch.from_numpy(inputs['target']).to(self.dev)
+
+    def capture(self, warmup=3):
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self.step(self.s_d, self.s_t)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        torch.cuda.synchronize(self.dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.g_loss, self.g_grad = self.step(self.s_d, self.s_t)
+        torch.cuda.synchronize(self.dev)
+
+    def replay(self):
+        self.graph.replay()
+        return self.g_loss, self.g_grad
+
+
 class StreamedSteps:
     """Runs the graph-captured step over a stream of host inputs with the
     transfers overlapped: two captured copies of the step, each with its own

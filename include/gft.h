@@ -194,6 +194,35 @@ gft_status gft_raymarch_grid_transform_multi_grad_weights(
     const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
     const float* frustum, int32_t num_cameras, const int32_t* output_shapes,
     int32_t boundary, void* workspace, size_t workspace_bytes, void* stream);
+/* ---- RaymarchGridTransform over views bound to batch slices ----
+ * No counterpart op in the reference.  As the _multi functions, but camera c
+ * renders only batch slice camera_batch[c] (int32, host, num_cameras entries
+ * in [0, N)): a batch of frames, each seen by its own cameras of their own
+ * image sizes (the reference renders them with one call per frame and image
+ * size).  output (and output_grad) hold the cameras' images one after another,
+ * camera c starting at pixel P_c = sum over the cameras before c of H W; the
+ * input gradient of slice n sums the adjoints of the cameras that render it.
+ * The workspace of the reference-normalised gradient holds one weight-sum
+ * grid per camera.  Up to 16 cameras per launch. */
+gft_status gft_raymarch_grid_transform_views(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* camera_batch, const int32_t* output_shapes,
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, float* output, void* stream);
+size_t gft_raymarch_grid_transform_views_grad_workspace_size(
+    const int64_t input_shape[5], int32_t num_cameras, int32_t grad_mode);
+gft_status gft_raymarch_grid_transform_views_grad(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* output, const float* output_grad,
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* camera_batch, const int32_t* output_shapes,
+    int32_t interpolation, int32_t boundary, int32_t blending_mode,
+    int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
+gft_status gft_raymarch_grid_transform_views_grad_weights(
+    const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t* camera_batch, const int32_t* output_shapes,
+    int32_t boundary, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- SampleGridTransform (resample_grid.cc:23-61, :268-447; launcher resample_grid.cu.cc:289-438) ----
  * output [N, separate_camera_batch ? num_cameras : 1, Do, Ho, Wo, C] fp32.

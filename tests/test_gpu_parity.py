@@ -619,6 +619,66 @@ def test_raymarch_multi_argument_errors(ops):
         ops.raymarch_grid_transform_multi(cuda(x), M, V, P, F, [(13, 9, 11), (7, 0, 5), (11, 12, 16)])
 
 
+# ------------------------------------------------------------------ raymarch, views bound to batch slices
+def _views_scene(C, seed, frames=3, per_frame=6):
+    """frames batch slices, each seen by its own per_frame cameras of uneven
+    image sizes (18 views: two launches of up to 16)."""
+    from gft import synthetic as syn
+    _, _, M, _, _, _ = scene((10, 14, 12), 1, (13, 9, 11))
+    x = np.concatenate([small_grid((10, 14, 12), C, seed + b) for b in range(frames)], 0) * 0.4
+    Vs, Ps, Fs, shapes, cb = [], [], [], [], []
+    for f in range(frames):
+        cams, shp = syn.hemisphere_cameras(per_frame - 1, 11, sizes=(5, 13), radius=2.0, fov=40.0, seed=seed + 10 * f,
+                                           fixed_size=9)
+        V, P, F = syn.camera_params(cams)
+        Vs.append(V), Ps.append(P), Fs.append(F)
+        shapes += [list(s) for s in shp]
+        cb += [f] * per_frame
+    return x, np.concatenate([M] * frames, 0), np.concatenate(Vs), np.concatenate(Ps), np.concatenate(Fs), cb, shapes
+
+
+@pytest.mark.parametrize('C', [1, 4])
+def test_raymarch_views_forward_equals_per_camera(ops, C):
+    x, M, V, P, F, cb, shapes = _views_scene(C, 51)
+    y = ops.raymarch_grid_transform_views(cuda(x), cb, M, V, P, F, shapes)
+    imgs = ops.views_split(y, shapes)
+    for c, (b, shp) in enumerate(zip(cb, shapes)):
+        one = ops.raymarch_grid_transform(cuda(x[b:b + 1]), M[b:b + 1], V[c:c + 1], P[c:c + 1], F[c:c + 1], shp)
+        assert torch.equal(imgs[c], one[0, 0])
+
+
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_views_backward_equals_per_camera_sum(ops, mode):
+    x, M, V, P, F, cb, shapes = _views_scene(4, 53)
+    rng = np.random.default_rng(54)
+    dys = [cuda(rng.standard_normal((h, w, 4)).astype(np.float32)) for _, h, w in shapes]
+    with ops.grad_mode(mode):
+        xt = cuda(x).requires_grad_(True)
+        y = ops.raymarch_grid_transform_views(xt, cb, M, V, P, F, shapes)
+        (y * torch.cat([d.reshape(-1, 4) for d in dys])).sum().backward()
+        g = torch.zeros_like(xt)
+        for c, (b, shp) in enumerate(zip(cb, shapes)):
+            xc = cuda(x[b:b + 1]).requires_grad_(True)
+            one = ops.raymarch_grid_transform(xc, M[b:b + 1], V[c:c + 1], P[c:c + 1], F[c:c + 1], shp)
+            one.backward(dys[c][None, None])
+            g[b:b + 1] += xc.grad
+    assert rel_l2(np_(xt.grad), np_(g)) <= 1e-5
+
+
+def test_raymarch_views_oracle_and_errors(ops):
+    from gft import _lib
+    from oracle import raymarch as RM
+    x, M, V, P, F, cb, shapes = _views_scene(4, 57, frames=2, per_frame=3)
+    y = ops.views_split(ops.raymarch_grid_transform_views(cuda(x), cb, M, V, P, F, shapes), shapes)
+    for c, (b, shp) in enumerate(zip(cb, shapes)):
+        ref = RM.raymarch_fwd(x[b:b + 1], M[b:b + 1], V[c:c + 1], P[c:c + 1], F[c:c + 1], shp)
+        assert rel_l2(np_(y[c]), ref[0, 0]) <= FWD_TOL
+    with pytest.raises(_lib.GftInvalidArgument):
+        ops.raymarch_grid_transform_views(cuda(x), [0, 1, 2, 0, 1, 1], M, V, P, F, shapes)  # slice 2 of 2
+    with pytest.raises(_lib.GftInvalidArgument):
+        ops.raymarch_grid_transform_views(cuda(x), cb[:-1], M, V, P, F, shapes)
+
+
 # ------------------------------------------------------------------ raymarch, brick layout
 @pytest.mark.parametrize('C', [1, 2, 4])
 @pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP', 'WRAP'])

@@ -113,3 +113,34 @@ def test_checkpointed_chain_gradients(gpu):
     assert abs(res[0][0] - res[1][0]) <= 1e-6 * abs(res[1][0])
     for a, b in zip(res[0][1], res[1][1]):
         assert rel_l2(a, b) <= 1e-4
+
+
+def test_uneven_batch_step_equals_per_frame_steps(gpu):
+    """The uneven-view batch step (frames x their own views in one
+    raymarch_grid_transform_views call, batched shadow and light composition,
+    one CUDA graph) equals the frames computed one at a time: the loss is the
+    pixel-weighted mean of the per-frame losses and each frame's gradient the
+    per-frame gradient scaled by its share of the pixels."""
+    from gft.pipeline import UnevenBatchStep
+    kw = dict(views=3, shape=(12, 16, 10), samples=14, device=gpu, shadow=(10, 10, 10), mips=2, sizes=(6, 12))
+    both = UnevenBatchStep(frames=2, seed=70, **kw)
+    rng = np.random.default_rng(71)
+    d = (rng.random((2, 12, 16, 10, 1)) * 0.3).astype(np.float32)
+    tgt = (rng.random((both.pixels, 3)) * 0.2).astype(np.float32)
+    both.setup_static({'d': d, 'target': tgt})
+    both.capture(warmup=2)
+    loss, g = both.replay()
+    torch.cuda.synchronize()
+    loss, g = float(loss.detach()), _np(g)
+    parts, grads, off = [], [], 0
+    for f in range(2):
+        one = UnevenBatchStep(frames=1, seed=70 + f, **kw)
+        n = one.pixels
+        one.setup_static({'d': d[f:f + 1], 'target': tgt[off:off + n]})
+        lf, gf = one.step(one.s_d, one.s_t)
+        parts.append((float(lf.detach()), n))
+        grads.append(_np(gf) * n)
+        off += n
+    total = sum(n for _, n in parts)
+    assert abs(loss - sum(l * n for l, n in parts) / total) <= 1e-5 * abs(loss)
+    assert rel_l2(g, np.concatenate(grads, 0) / total) <= 1e-5
