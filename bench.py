@@ -234,6 +234,12 @@ def bench_ours(args):
     step = RenderAdvectStep(args.config, dev, storage_dtype=storage, mode='batched')
     inputs = step.make_inputs(frame=rank)
     step.setup_static(inputs)
+    tune_log = {}
+    if not args.no_autotune:
+        # launch-configuration knobs timed on this workload before the capture
+        from gft import autotune
+        statics = (step.s_d, step.s_vx, step.s_vy, step.s_vz, step.s_t)
+        step.knobs = autotune.tune(lambda: step.step(*statics), key=autotune.step_key(step), log=tune_log)
     n0 = lib.gft_launch_count()
     step.capture(warmup=args.warmup)
     launches_per_step = (lib.gft_launch_count() - n0) // (args.warmup + 1)
@@ -290,6 +296,7 @@ def bench_ours(args):
         'loss': loss_val,
         'wall_s_timed': t_wall,
         'clocks': clocks,
+        'autotune': {'knobs': step.knobs, 'candidates_ms': tune_log} if step.knobs else None,
         'step_roofline': {'alg_bytes': total_bytes, 'parts': parts, 'achieved_GBps': total_bytes / ms / 1e6,
                           'peak': peak, 'frac': total_bytes / ms / 1e6 / peak, 'unit': 'GB/s',
                           'what': 'whole iteration: compulsory bytes by the per-op formulas / step time'},
@@ -821,6 +828,7 @@ def main():
     ap.add_argument('--quick', action='store_true', help='only the timed graph replays')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-chain5', action='store_true', help='skip the long transport chain on the headline grid')
+    ap.add_argument('--no-autotune', action='store_true', help='default launch configuration (no tuning)')
     ap.add_argument('--chain-frames', type=int, default=120)
     ap.add_argument('--cpu-budget', type=float, default=20.0)
     ap.add_argument('--ref-budget', type=float, default=240.0,

@@ -1,6 +1,7 @@
 // extern "C" entry points of libgft.so (declared in include/gft.h): argument
 // checks with the reference ops' error classes, camera set-up and dispatch to
 // the launchers.  No entry point allocates device memory or synchronises.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -25,6 +26,21 @@ bool cuda_ok(cudaError_t e, const char* what) {
 }
 
 static std::atomic<unsigned long long> g_launches{0};
+
+// launch-configuration knobs, defaults as documented in gft.h
+static std::atomic<int> g_knobs[GFT_KNOB_COUNT] = {{0}, {256}, {256}, {8}};
+int knob_value(int k) { return (k >= 0 && k < GFT_KNOB_COUNT) ? g_knobs[k].load(std::memory_order_relaxed) : 0; }
+int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(sms, 1);
+}
+unsigned raymarch_blocks(int tiles) {
+    const int k = knob_value(GFT_KNOB_RAYMARCH_BLOCKS_PER_SM);
+    if (k <= 0) return (unsigned)std::max(tiles, 1);
+    return (unsigned)std::max(1, std::min(tiles, k * sm_count()));
+}
 
 bool launched(int n, const char* what) {
     g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed);
@@ -242,6 +258,22 @@ const char* gft_last_error(void) { return g_last_error.c_str(); }
 const char* gft_version(void) { return "gft-gb300 0.1 (sm_103a)"; }
 
 unsigned long long gft_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+gft_status gft_set_knob(int32_t knob, int32_t value) {
+    bool ok = false;
+    switch (knob) {
+        case GFT_KNOB_RAYMARCH_BLOCKS_PER_SM: ok = value >= 0 && value <= 32; break;
+        case GFT_KNOB_ADVECT_THREADS:
+        case GFT_KNOB_RESAMPLE_THREADS: ok = value == 64 || value == 128 || value == 256; break;
+        case GFT_KNOB_SCAN_SEGMENTS: ok = value == 4 || value == 8 || value == 16; break;
+        default: return fail(GFT_ERR_INVALID_ARGUMENT, "unknown knob");
+    }
+    if (!ok) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid knob value");
+    g_knobs[knob].store(value, std::memory_order_relaxed);
+    return GFT_OK;
+}
+
+int32_t gft_get_knob(int32_t knob) { return knob_value(knob); }
 
 // ---------------------------------------------------------------- raymarch
 static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],

@@ -15,7 +15,8 @@
 
 namespace gft {
 
-constexpr int AD_THREADS = 256;
+constexpr int AD_THREADS = 256;  // the largest block (launch bounds); GFT_KNOB_ADVECT_THREADS picks the size
+static int adv_threads() { return knob_value(GFT_KNOB_ADVECT_THREADS); }
 constexpr int CLAMP_NONE = 0, CLAMP_MC_SMOOTH = 1, CLAMP_NEGATIVE = 2;
 
 // lut = -dt * centred velocity at voxel (x, y, z) (centered, data_structures.py:819-833)
@@ -125,30 +126,31 @@ __global__ void __launch_bounds__(AD_THREADS)
 template <int C, typename S>
 static bool adv_fwd_c(const AdvectArgs& a, float* out, float* ws, cudaStream_t s) {
     const int64_t nv = voxels(a.d);
-    const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
+    const int T = adv_threads();
+    const unsigned blocks = (unsigned)((nv + T - 1) / T);
     for (int b = 0; b < a.N; ++b) {
         const S* db = reinterpret_cast<const S*>(a.density) + (size_t)b * nv * C;
         float* ob = out + (size_t)b * nv * C;
         if (a.order == 1) {
             const bool neg = a.clamp == CLAMP_NEGATIVE;
             switch (a.boundary) {
-                case BM_BORDER: k_adv_sl<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
-                case BM_CLAMP: k_adv_sl<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
-                default: k_adv_sl<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+                case BM_BORDER: k_adv_sl<C, S, BM_BORDER><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+                case BM_CLAMP: k_adv_sl<C, S, BM_CLAMP><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
+                default: k_adv_sl<C, S, BM_WRAP><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, neg, ob); break;
             }
         } else {
             switch (a.boundary) {
                 case BM_BORDER:
-                    k_adv_sl<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
-                    k_adv_mc<C, S, BM_BORDER><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    k_adv_sl<C, S, BM_BORDER><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_BORDER><<<blocks, T, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
                     break;
                 case BM_CLAMP:
-                    k_adv_sl<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
-                    k_adv_mc<C, S, BM_CLAMP><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    k_adv_sl<C, S, BM_CLAMP><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_CLAMP><<<blocks, T, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
                     break;
                 default:
-                    k_adv_sl<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
-                    k_adv_mc<C, S, BM_WRAP><<<blocks, AD_THREADS, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
+                    k_adv_sl<C, S, BM_WRAP><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, ws);
+                    k_adv_mc<C, S, BM_WRAP><<<blocks, T, 0, s>>>(db, ws, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp, ob);
                     break;
             }
         }
@@ -452,7 +454,8 @@ template <int C, int BM, int COUNT>
 static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* dy, float* gd, float* gvx, float* gvy,
                          float* gvz, float* ws, cudaStream_t s) {
     const int64_t nv = voxels(a.d);
-    const unsigned blocks = (unsigned)((nv + AD_THREADS - 1) / AD_THREADS);
+    const int T = adv_threads();
+    const unsigned blocks = (unsigned)((nv + T - 1) / T);
     const size_t vc = (size_t)nv * C;
     // packed: the two scatter targets hold (sum, count) pairs at even offsets
     // (8-byte aligned with ws), no counters
@@ -480,23 +483,23 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
             if (COUNT && !PACK && !cuda_ok(cudaMemsetAsync(cnt2, 0, sizeof(unsigned int) * nv, s), "zero counter"))
                 return false;
             if (!forward_ready)  // else fwd holds this slice's semi-Lagrangian grid already
-                k_adv_sl<C, float, BM><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
-            k_adv_bwd_back<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
+                k_adv_sl<C, float, BM><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
+            k_adv_bwd_back<C, BM, COUNT><<<blocks, T, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
                                                                       dyb, gdb, gfwd_sc, cnt2, gdir, glut, b == 0);
-            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
+            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
                                                                      gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut, false);
         } else {
             if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
-            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, AD_THREADS, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
+            k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
                                                                      a.clamp == CLAMP_NEGATIVE, dyb, nullptr,
                                                                      nullptr, gd_sc, cnt3, glut, b == 0);
         }
-        k_adv_bwd_density<C, COUNT><<<blocks, AD_THREADS, 0, s>>>(gdb, gd_sc, cnt3, nv);
+        k_adv_bwd_density<C, COUNT><<<blocks, T, 0, s>>>(gdb, gd_sc, cnt3, nv);
         if (!launched(a.order == 2 ? (forward_ready ? 3 : 4) : 2, "advect gradient launch")) return false;
     }
     const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
                           (int64_t)a.d.x * a.d.y * (a.d.z + 1);
-    k_adv_bwd_velocity<<<(unsigned)((nstag + AD_THREADS - 1) / AD_THREADS), AD_THREADS, 0, s>>>(glut, a.d, a.dt, gvx,
+    k_adv_bwd_velocity<<<(unsigned)((nstag + T - 1) / T), T, 0, s>>>(glut, a.d, a.dt, gvx,
                                                                                                  gvy, gvz);
     return launched(1, "velocity gradient launch");
 }

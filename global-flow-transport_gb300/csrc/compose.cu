@@ -39,9 +39,10 @@ static unsigned grid_for(int64_t n, int threads) {
 // shadow frustum alone would give one thread per column too few threads to
 // hide the latency of 256 dependent steps.)  The sums associate differently
 // from a sequential scan: rounding only.
-constexpr int TS_COLS = 32, TS_SEGS = 8;
+// TS_SEGS: 4, 8 (default) or 16 segments, GFT_KNOB_SCAN_SEGMENTS.
+constexpr int TS_COLS = 32;
 
-template <bool REVERSE>
+template <bool REVERSE, int TS_SEGS>
 __global__ void __launch_bounds__(TS_COLS* TS_SEGS)
     k_transmittance_seg(const float* __restrict__ a, const float* __restrict__ b, int N, Dims d,
                         float* __restrict__ out) {
@@ -86,18 +87,25 @@ __global__ void __launch_bounds__(TS_COLS* TS_SEGS)
     }
 }
 
-bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st) {
+template <bool REVERSE>
+static void scan_launch(const float* a, const float* b, int N, Dims d, float* out, cudaStream_t st) {
     const int64_t cols = (int64_t)d.x * d.y * N;
-    k_transmittance_seg<false><<<(unsigned)((cols + TS_COLS - 1) / TS_COLS), dim3(TS_COLS, TS_SEGS), 0, st>>>(
-        s, nullptr, N, d, out);
+    const unsigned blocks = (unsigned)((cols + TS_COLS - 1) / TS_COLS);
+    switch (knob_value(GFT_KNOB_SCAN_SEGMENTS)) {
+        case 4: k_transmittance_seg<REVERSE, 4><<<blocks, dim3(TS_COLS, 4), 0, st>>>(a, b, N, d, out); break;
+        case 16: k_transmittance_seg<REVERSE, 16><<<blocks, dim3(TS_COLS, 16), 0, st>>>(a, b, N, d, out); break;
+        default: k_transmittance_seg<REVERSE, 8><<<blocks, dim3(TS_COLS, 8), 0, st>>>(a, b, N, d, out); break;
+    }
+}
+
+bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st) {
+    scan_launch<false>(s, nullptr, N, d, out, st);
     return launched(1, "transmittance launch");
 }
 
 // tr, g: the forward output and its adjoint
 bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st) {
-    const int64_t cols = (int64_t)d.x * d.y * N;
-    k_transmittance_seg<true><<<(unsigned)((cols + TS_COLS - 1) / TS_COLS), dim3(TS_COLS, TS_SEGS), 0, st>>>(
-        tr, g, N, d, gs);
+    scan_launch<true>(tr, g, N, d, gs, st);
     return launched(1, "transmittance gradient launch");
 }
 

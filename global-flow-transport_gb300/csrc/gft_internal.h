@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "gft.h"
 #include "gft_common.cuh"
 
 namespace gft {
@@ -69,6 +70,14 @@ constexpr int OCC_BLOCK_SHIFT = 3;
 size_t occupancy_bytes(Dims d);
 bool launch_occupancy(const void* input, int dtype, int C, Dims d, int levels, uint8_t* raw, uint8_t* grown,
                       cudaStream_t s, MipSet* set);
+
+// Launch-configuration knobs (gft_set_knob; values checked there): read when
+// a launch is issued, so a captured graph keeps the values of its capture.
+int knob_value(int knob);
+int sm_count();  // SMs of the current device
+// Blocks of a raymarch launch over `tiles` pixel tiles under
+// GFT_KNOB_RAYMARCH_BLOCKS_PER_SM.
+unsigned raymarch_blocks(int tiles);
 
 // error helpers
 void set_error(const std::string& msg);

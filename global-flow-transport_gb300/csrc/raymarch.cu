@@ -50,6 +50,7 @@ __device__ __forceinline__ bool ray_clip(float3 p0, float3 st, int n, Dims d, in
 // differ in image size and sample count.  Sets this thread's pair, pixel and
 // the pair's geometry; false for pixels outside the pair's image.
 struct RayPix {
+    int tile;  // pixel tile of the launch (set by the caller)
     int p, x, y, W, H, D;
 };
 
@@ -66,7 +67,7 @@ __device__ __forceinline__ float3 ray_sample(float3 nearp, float3 step, int i) {
     return make_float3(fmaf(t, step.x, nearp.x), fmaf(t, step.y, nearp.y), fmaf(t, step.z, nearp.z));
 }
 __device__ __forceinline__ bool ray_pixel(const PairTable& tab, RayPix& r) {
-    const int b = blockIdx.x;
+    const int b = r.tile;
     int p = 0;
     while (p + 1 < tab.n && b >= tab.tile0[p + 1]) ++p;
     r.p = p;
@@ -167,13 +168,13 @@ RaymarchArgs::Store raymarch_store_layout(void* base, const std::vector<Pair>& p
 
 // Cell index of this lane's step i in the sample store, and of its warp's
 // ballot word (a pair's cells and words start at smp0 and smp0 / 32).
-__device__ __forceinline__ int64_t sample_index(const PairTable& tab, int p, int D, int i) {
+__device__ __forceinline__ int64_t sample_index(const PairTable& tab, int tile, int p, int D, int i) {
     const int tid = threadIdx.y * RM_BX + threadIdx.x;
-    return tab.smp0[p] + ((int64_t)(blockIdx.x - tab.tile0[p]) * D + i) * (RM_BX * RM_BY) + tid;
+    return tab.smp0[p] + ((int64_t)(tile - tab.tile0[p]) * D + i) * (RM_BX * RM_BY) + tid;
 }
-__device__ __forceinline__ int64_t sample_word_index(const PairTable& tab, int p, int D, int i) {
+__device__ __forceinline__ int64_t sample_word_index(const PairTable& tab, int tile, int p, int D, int i) {
     const int tid = threadIdx.y * RM_BX + threadIdx.x;
-    return (tab.smp0[p] >> 5) + ((int64_t)(blockIdx.x - tab.tile0[p]) * D + i) * (RM_BX * RM_BY / 32) + (tid >> 5);
+    return (tab.smp0[p] >> 5) + ((int64_t)(tile - tab.tile0[p]) * D + i) * (RM_BX * RM_BY / 32) + (tid >> 5);
 }
 
 // Occupancy of one input slice per block: a non-zero voxel marks the blocks
@@ -284,10 +285,11 @@ __device__ __forceinline__ bool sample_empty(Dims d, float px, float py, float p
 }
 
 template <int C, typename S, int BM, bool LIN, int L>
-__global__ void __launch_bounds__(RM_BX* RM_BY)
-    k_raymarch_fwd(const S* __restrict__ in, Dims din, int filter, int blend_mode, float* __restrict__ out,
-                   const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+__device__ __forceinline__ void raymarch_fwd_tile(const S* __restrict__ in, Dims din, int filter, int blend_mode,
+                                                  float* __restrict__ out, const RaymarchArgs::Store& st,
+                                                  const PairTable& tab, int tile) {
     RayPix r;
+    r.tile = tile;
     const bool live = ray_pixel(tab, r);  // every lane stays to the warp's clip reduction
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     const CamX& cam = tab.cam[p];
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
                 const bool empty = storing && sample_empty<BM>(din, qx, qy, qz, occ, st.nbx, st.nby);
                 smp = empty ? vzero<C>() : fetch_linear<C, S, BM, L>(g, din, qx, qy, qz);
                 if (storing && !empty) {
-                    store_stream<C>(st.samples, sample_index(tab, p, D, i), smp);
+                    store_stream<C>(st.samples, sample_index(tab, r.tile, p, D, i), smp);
                     stored = true;
                 }
             } else {
@@ -342,11 +344,25 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         if (storing) {
             const unsigned word = __ballot_sync(0xffffffffu, stored);
             if ((threadIdx.x & 31u) == 0 && (threadIdx.y & 3u) == 0)
-                st.words[sample_word_index(tab, p, D, i)] = word;
+                st.words[sample_word_index(tab, r.tile, p, D, i)] = word;
         }
     }
     if (!live) return;
     store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);
+}
+
+// The raymarch kernels walk the pixel tiles of their launch: one block per
+// tile, or (a persistent grid, the launch-configuration knob
+// GFT_KNOB_RAYMARCH_BLOCKS_PER_SM) a fixed number of blocks per SM taking
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Every thread of a block walks
+// the same tiles, so the warp-collective steps of a tile see all 32 lanes.
+template <int C, typename S, int BM, bool LIN, int L>
+__global__ void __launch_bounds__(RM_BX* RM_BY)
+    k_raymarch_fwd(const S* __restrict__ in, Dims din, int filter, int blend_mode, float* __restrict__ out,
+                   const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+    const int tiles = tab.tile0[tab.n];
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+        raymarch_fwd_tile<C, S, BM, LIN, L>(in, din, filter, blend_mode, out, st, tab, tile);
 }
 
 // Ray set-up shared by the adjoint kernels: near point, far point and step,
@@ -543,11 +559,12 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 // Every lane stays in the loop to its warp's last step (scatter_step is
 // warp-collective); lanes without a sample at a step pass act = false.
 template <int C, typename S, int BM, int MODE, int L>
-__global__ void __launch_bounds__(RM_BX* RM_BY)
-    k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
-                       const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
-                       const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+__device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, Dims din, int blend_mode,
+                                                      const float* __restrict__ out, const float* __restrict__ dout,
+                                                      float* __restrict__ grad, const float* __restrict__ cnt,
+                                                      const RaymarchArgs::Store& st, const PairTable& tab, int tile) {
     RayPix r;
+    r.tile = tile;
     const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     float3 farp, step, nearp;
@@ -607,8 +624,8 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
             Vec<C> smp;
             if (use_store) {
                 const int i = D - 1 - k;
-                const uint32_t word = i >= s_lo && i <= s_hi ? __ldg(st.words + sample_word_index(tab, p, D, i)) : 0u;
-                smp = (word >> lane) & 1u ? load_stream<C>(st.samples, sample_index(tab, p, D, i)) : vzero<C>();
+                const uint32_t word = i >= s_lo && i <= s_hi ? __ldg(st.words + sample_word_index(tab, r.tile, p, D, i)) : 0u;
+                smp = (word >> lane) & 1u ? load_stream<C>(st.samples, sample_index(tab, r.tile, p, D, i)) : vzero<C>();
             } else {
                 smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             }
@@ -616,6 +633,19 @@ __global__ void __launch_bounds__(RM_BX* RM_BY)
         }
         scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val);
     }
+}
+
+// At least 6 resident blocks per SM: the tile loop would otherwise take 90
+// registers (5 blocks); with the bound it stays at the 80 of one tile per
+// block, without spills.
+template <int C, typename S, int BM, int MODE, int L>
+__global__ void __launch_bounds__(RM_BX* RM_BY, 6)
+    k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
+                       const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
+                       const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+    const int tiles = tab.tile0[tab.n];
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+        raymarch_scatter_tile<C, S, BM, MODE, L>(in, din, blend_mode, out, dout, grad, cnt, st, tab, tile);
 }
 
 template <int C, typename S, int BM>
@@ -648,7 +678,7 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
     const dim3 block(RM_BX, RM_BY, 1);
     int64_t cells = 0;
     for (PairTable& t : make_tables(pairs)) {
-        const dim3 grid(set_ray_tiles(t, &cells));
+        const dim3 grid(raymarch_blocks((int)set_ray_tiles(t, &cells)));
         if (a.dtype == 0) {
             if (a.C == 4) fwd_dispatch_bm<4, float>(grid, block, s, a, out, t);
             else if (a.C == 2) fwd_dispatch_bm<2, float>(grid, block, s, a, out, t);
@@ -720,7 +750,7 @@ bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pai
     if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * cells * pairs.size(), s), "zero weights")) return false;
     const dim3 block(RM_BX, RM_BY, 1);
     for (PairTable& t : make_tables(pairs)) {
-        const dim3 grid(set_ray_tiles(t));
+        const dim3 grid(raymarch_blocks((int)set_ray_tiles(t)));
         switch (a.boundary) {
             case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, t); break;
             case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, t); break;
@@ -748,7 +778,7 @@ bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
     const dim3 block(RM_BX, RM_BY, 1);
     int64_t smp_cells = 0;
     for (PairTable& t : make_tables(pairs)) {
-        const dim3 grid(set_ray_tiles(t, &smp_cells));
+        const dim3 grid(raymarch_blocks((int)set_ray_tiles(t, &smp_cells)));
         if (a.dtype == 0) {
             if (a.C == 4) bwd_dispatch_bm<4, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
             else if (a.C == 2) bwd_dispatch_bm<2, float>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);

@@ -451,11 +451,11 @@ __global__ void __launch_bounds__(RS_THREADS)
 }
 
 template <int C, typename S, int BM>
-static void st_fwd_cm(int cm, dim3 blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
+static void st_fwd_cm(int cm, dim3 blocks, int T, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
                       const PairTable& t) {
-#define GFT_ST(CMV)                                                                                              \
-    k_sample_transform<C, S, BM, CMV><<<blocks, RS_THREADS, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, \
-                                                                    ms, out, t)
+#define GFT_ST(CMV)                                                                                             \
+    k_sample_transform<C, S, BM, CMV><<<blocks, T, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, ms, \
+                                                           out, t)
     switch (cm) {
         case CM_LINDEPTH: GFT_ST(CM_LINDEPTH); break;
         case CM_TRANSFORM: GFT_ST(CM_TRANSFORM); break;
@@ -466,14 +466,14 @@ static void st_fwd_cm(int cm, dim3 blocks, cudaStream_t s, const SampleArgs& a, 
 }
 
 template <int C, typename S>
-static void st_fwd(int bm, dim3 blocks, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
+static void st_fwd(int bm, dim3 blocks, int T, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
                    const PairTable& t) {
     switch (bm) {
-        case BM_BORDER: st_fwd_cm<C, S, BM_BORDER>(a.coord_mode, blocks, s, a, ms, out, t); break;
-        case BM_CLAMP: st_fwd_cm<C, S, BM_CLAMP>(a.coord_mode, blocks, s, a, ms, out, t); break;
+        case BM_BORDER: st_fwd_cm<C, S, BM_BORDER>(a.coord_mode, blocks, T, s, a, ms, out, t); break;
+        case BM_CLAMP: st_fwd_cm<C, S, BM_CLAMP>(a.coord_mode, blocks, T, s, a, ms, out, t); break;
         default:
-            k_sample_transform<C, S, BM_WRAP, CM_LINDEPTH><<<blocks, RS_THREADS, 0, s>>>(
-                a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, ms, out, t);
+            k_sample_transform<C, S, BM_WRAP, CM_LINDEPTH><<<blocks, T, 0, s>>>(a.dout, a.filter, a.mip_mode,
+                                                                                a.mip_bias, a.cco, ms, out, t);
             break;
     }
 }
@@ -486,16 +486,17 @@ bool launch_sample_transform_fwd(const SampleArgs& a, const std::vector<Pair>& p
         std::vector<Pair> pb;
         for (const Pair& p : pairs)
             if (p.in_batch == b) pb.push_back(p);
+        const int T = knob_value(GFT_KNOB_RESAMPLE_THREADS);  // <= RS_THREADS, the launch bounds
         for (const PairTable& t : make_tables(pb)) {
-            const dim3 blocks((unsigned)((nv + RS_THREADS - 1) / RS_THREADS), t.n);
+            const dim3 blocks((unsigned)((nv + T - 1) / T), t.n);
             if (a.dtype == 0) {
-                if (a.C == 4) st_fwd<4, float>(a.boundary, blocks, s, a, mips[b], out, t);
-                else if (a.C == 2) st_fwd<2, float>(a.boundary, blocks, s, a, mips[b], out, t);
-                else st_fwd<1, float>(a.boundary, blocks, s, a, mips[b], out, t);
+                if (a.C == 4) st_fwd<4, float>(a.boundary, blocks, T, s, a, mips[b], out, t);
+                else if (a.C == 2) st_fwd<2, float>(a.boundary, blocks, T, s, a, mips[b], out, t);
+                else st_fwd<1, float>(a.boundary, blocks, T, s, a, mips[b], out, t);
             } else {
-                if (a.C == 4) st_fwd<4, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
-                else if (a.C == 2) st_fwd<2, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
-                else st_fwd<1, __nv_bfloat16>(a.boundary, blocks, s, a, mips[b], out, t);
+                if (a.C == 4) st_fwd<4, __nv_bfloat16>(a.boundary, blocks, T, s, a, mips[b], out, t);
+                else if (a.C == 2) st_fwd<2, __nv_bfloat16>(a.boundary, blocks, T, s, a, mips[b], out, t);
+                else st_fwd<1, __nv_bfloat16>(a.boundary, blocks, T, s, a, mips[b], out, t);
             }
             if (!launched(1, "sample transform launch")) return false;
         }

@@ -44,6 +44,8 @@ _SIGS = {
     'gft_last_error': (ctypes.c_char_p, []),
     'gft_version': (ctypes.c_char_p, []),
     'gft_launch_count': (ctypes.c_ulonglong, []),
+    'gft_set_knob': (_I32, [_I32, _I32]),
+    'gft_get_knob': (_I32, [_I32]),
     'gft_raymarch_grid_transform': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                            _I32, _I32, _I32, _I32, _P, _P]),
     'gft_raymarch_grid_transform_store': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,

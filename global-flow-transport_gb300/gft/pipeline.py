@@ -57,7 +57,7 @@ CONFIGS = {
 
 class RenderAdvectStep:
     def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None,
-                 fp64_check=False, check_strides=(7, 257)):
+                 fp64_check=False, check_strides=(7, 257), autotune=False):
         self.config_name = config if isinstance(config, str) else None
         cfg = dict(CONFIGS[config] if isinstance(config, str) else config)
         if order is not None:
@@ -92,6 +92,9 @@ class RenderAdvectStep:
         self.bkg_host = np.array([0.0, 0.5, 1.0], dtype=np.float32)
         self.bkg = torch.from_numpy(self.bkg_host).to(self.dev)
         self.graph = None
+        # launch-configuration knobs chosen by gft.autotune before the capture
+        self.autotune = bool(autotune)
+        self.knobs, self.tune_log = None, {}
         # FP64 check step (batched mode): double-precision recomputation of the
         # shadow transmittance (every check_strides[0]-th light-frustum column)
         # and of the raymarch's accumulated density (every check_strides[1]-th
@@ -196,8 +199,12 @@ class RenderAdvectStep:
         return (self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
 
     def capture(self, warmup=3):
-        """Captures step() on the static inputs into one CUDA graph."""
+        """Captures step() on the static inputs into one CUDA graph (after
+        tuning the launch-configuration knobs on them, with autotune)."""
         args = (self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
+        if self.autotune:
+            from . import autotune as _at
+            self.knobs = _at.tune(lambda: self.step(*args), key=_at.step_key(self), log=self.tune_log)
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):

@@ -372,6 +372,32 @@ gft_status gft_image_loss(const float* image, const float* target, const float b
 gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
                                const float* loss_grad, float* image_grad, void* stream);
 
+/* ---- Launch-configuration knobs (no counterpart in the reference) ----
+ * Process-wide settings of how some kernels are launched, chosen per workload
+ * by gft.autotune (which times the candidates with CUDA events).  They change
+ * the launch shape only: results are the same for every value (bit for bit
+ * for the gathers; up to the association of the sums for the segmented scans
+ * and the order of the floating-point atomic additions for the scatters).  A launch reads them when it is issued, so a
+ * captured CUDA graph keeps the values of its capture.
+ *   GFT_KNOB_RAYMARCH_BLOCKS_PER_SM  0 (default): one block per 8x16-pixel tile;
+ *                                    1-32: a persistent grid of that many
+ *                                    blocks per SM walking the tiles
+ *   GFT_KNOB_ADVECT_THREADS          threads per block of the advection
+ *                                    kernels: 64, 128 or 256 (default)
+ *   GFT_KNOB_RESAMPLE_THREADS        threads per block of the
+ *                                    SampleGridTransform forward: 64, 128 or
+ *                                    256 (default)
+ *   GFT_KNOB_SCAN_SEGMENTS           depth segments per column of the
+ *                                    transmittance scans: 4, 8 (default) or 16
+ * gft_set_knob returns GFT_ERR_INVALID_ARGUMENT for an unknown knob or value. */
+#define GFT_KNOB_RAYMARCH_BLOCKS_PER_SM 0
+#define GFT_KNOB_ADVECT_THREADS 1
+#define GFT_KNOB_RESAMPLE_THREADS 2
+#define GFT_KNOB_SCAN_SEGMENTS 3
+#define GFT_KNOB_COUNT 4
+gft_status gft_set_knob(int32_t knob, int32_t value);
+int32_t gft_get_knob(int32_t knob);
+
 /* ---- FP64 check step (no counterpart in the reference) ----
  * Double-precision recomputations on the GPU of the two FP32 results of the
  * step whose rounding compounds along a ray, on a strided sample, from the

@@ -398,3 +398,23 @@ def test_state_npz_round_trip_and_reference_keys(tmp_path):
         assert torch.equal(a.density.d, b.density.d) and torch.equal(a.velocity.z, b.velocity.z)
     states[0].save(str(tmp_path / 'one'), suffix='it5')
     assert sorted(os.listdir(str(tmp_path / 'one'))) == ['density_it5.npz', 'velocity_it5.npz']
+
+
+def test_launch_knobs_validate_and_round_trip(lib):
+    """gft_set_knob / gft_get_knob (no launch): every documented value is
+    accepted and read back, anything else is rejected and leaves the knob."""
+    from gft import autotune as at
+    before = at.knobs()
+    try:
+        for name, (_, cands, default) in at.KNOBS.items():
+            for v in cands:
+                at.set_knob(name, v)
+                assert at.get_knob(name) == v
+            at.set_knob(name, default)
+            with pytest.raises(ValueError):
+                at.set_knob(name, -3)
+            assert at.get_knob(name) == default
+        L = lib.load()
+        assert L.gft_set_knob(99, 1) == 1 and b"unknown knob" in L.gft_last_error()
+    finally:
+        at.apply(before)
