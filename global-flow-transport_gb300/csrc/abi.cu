@@ -375,13 +375,28 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
     return GFT_OK;
 }
 
+// Raymarch gradient workspace for `pairs` (batch, camera) pairs: the
+// per-pair reciprocal weight sums of the reference normalisation, plus the
+// integer accumulators of the deterministic adjoint.
+static size_t raymarch_grad_ws(const int64_t* input_shape, size_t pairs, int32_t grad_mode) {
+    const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC);
+    if (det) return raymarch_det_bytes((int)input_shape[0], (int)input_shape[4], dims_of(input_shape), pairs);
+    if (grad_mode == GFT_GRAD_EXACT) return 0;
+    return align256(sizeof(float) * (size_t)brick_cells(dims_of(input_shape)) * pairs);
+}
+
 size_t gft_raymarch_grid_transform_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
                                                        int32_t separate_camera_batch, int32_t grad_mode) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why) || (grad_mode & ~GFT_GRAD_WEIGHTS_READY) == GFT_GRAD_EXACT) return 0;
-    const size_t cells = (size_t)brick_cells(dims_of(input_shape));
+    if (!grid_shape_ok(input_shape, why)) return 0;
     const size_t pairs = (size_t)input_shape[0] * (separate_camera_batch ? (size_t)std::max(num_cameras, 1) : 1);
-    return align256(sizeof(float) * cells * pairs);
+    return raymarch_grad_ws(input_shape, pairs, grad_mode);
+}
+
+// The deterministic adjoint's bound holds for these blend modes.
+static bool det_blend_ok(int blend, int64_t C) {
+    return C == 1 || blend == GFT_BLEND_BEER_LAMBERT || blend == GFT_BLEND_ADDITIVE;
 }
 
 static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
@@ -438,18 +453,24 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
     const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
-    grad_mode &= ~GFT_GRAD_WEIGHTS_READY;
+    const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    const int32_t ws_mode = grad_mode;
+    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC);
     const int layout = (input_dtype & GFT_LAYOUT_BRICK) ? LAYOUT_BRICK : LAYOUT_FLAT;
     input_dtype &= ~GFT_LAYOUT_BRICK;
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
+    if (det && weights_ready)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_DETERMINISTIC computes its own weight sums");
+    if (det && !det_blend_ok(blending_mode, input_shape[4]))
+        return fail(GFT_ERR_UNIMPLEMENTED, "deterministic gradient: BEER_LAMBERT or ADDITIVE blending only");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
     if (!input || !output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     const size_t need = gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras,
-                                                                        separate_camera_batch, grad_mode);
+                                                                        separate_camera_batch, ws_mode);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
     RaymarchArgs a;
@@ -469,6 +490,7 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
                             separate_camera_batch != 0);
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
+    a.det = det;
     if (samples != nullptr) {
         if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
@@ -644,8 +666,8 @@ gft_status gft_raymarch_grid_transform_views(const void* input, int32_t input_dt
 size_t gft_raymarch_grid_transform_views_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
                                                              int32_t grad_mode) {
     std::string why;
-    if (!grid_shape_ok(input_shape, why) || (grad_mode & ~GFT_GRAD_WEIGHTS_READY) == GFT_GRAD_EXACT) return 0;
-    return align256(sizeof(float) * (size_t)brick_cells(dims_of(input_shape)) * (size_t)std::max(num_cameras, 1));
+    if (!grid_shape_ok(input_shape, why)) return 0;
+    return raymarch_grad_ws(input_shape, (size_t)std::max(num_cameras, 1), grad_mode);
 }
 
 size_t gft_raymarch_grid_transform_multi_grad_workspace_size(const int64_t input_shape[5], int32_t num_cameras,
@@ -669,10 +691,16 @@ static gft_status multi_grad_impl(const void* input, int32_t input_dtype, const 
     if (!enum_in(blending_mode, 0, 4) || blending_mode == GFT_BLEND_BEER_LAMBERT_EXCLUSIVE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
     const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
-    grad_mode &= ~GFT_GRAD_WEIGHTS_READY;
+    const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    const int32_t ws_mode = grad_mode;
+    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC);
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
+    if (det && weights_ready)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_DETERMINISTIC computes its own weight sums");
+    if (det && !det_blend_ok(blending_mode, input_shape[4]))
+        return fail(GFT_ERR_UNIMPLEMENTED, "deterministic gradient: BEER_LAMBERT or ADDITIVE blending only");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras, 1);
     if (st != GFT_OK) return st;
     if (camera_batch != nullptr && !camera_batch_ok(camera_batch, num_cameras, input_shape[0], why))
@@ -680,8 +708,8 @@ static gft_status multi_grad_impl(const void* input, int32_t input_dtype, const 
     if (!input || !output || !output_grad || !input_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     const size_t need =
         camera_batch != nullptr
-            ? gft_raymarch_grid_transform_views_grad_workspace_size(input_shape, num_cameras, grad_mode)
-            : gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, grad_mode);
+            ? gft_raymarch_grid_transform_views_grad_workspace_size(input_shape, num_cameras, ws_mode)
+            : gft_raymarch_grid_transform_multi_grad_workspace_size(input_shape, num_cameras, ws_mode);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
     RaymarchArgs a{};
@@ -696,6 +724,7 @@ static gft_status multi_grad_impl(const void* input, int32_t input_dtype, const 
     const auto pairs = multi_pairs(matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras, a.N, output_shapes,
                                    camera_batch);
     a.n_slots = (int)pairs.size();
+    a.det = det;
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
         (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
         (st = check_workspace_aligned(workspace)) != GFT_OK)
@@ -1170,6 +1199,14 @@ size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t or
     return align256(sizeof(float) * (nv * (4 * C + 3)) + sizeof(unsigned int) * 2 * nv + 16);
 }
 
+size_t gft_advect_grad_workspace_size_mode(const int64_t density_shape[5], int32_t order, int32_t grad_mode) {
+    if ((grad_mode & GFT_GRAD_DETERMINISTIC) == 0) return gft_advect_grad_workspace_size(density_shape, order);
+    std::string why;
+    if (!grid_shape_ok(density_shape, why)) return 0;
+    const size_t nv = (size_t)density_shape[1] * density_shape[2] * density_shape[3];
+    return align256(advect_det_ws_bytes(nv, (size_t)density_shape[4]));
+}
+
 gft_status gft_advect_grad(const float* density, const int64_t density_shape[5], const float* vel_x,
                            const float* vel_y, const float* vel_z, float dt, int32_t order, int32_t clamp,
                            int32_t boundary, int32_t grad_mode, const float* output_grad, float* density_grad,
@@ -1177,14 +1214,15 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
                            size_t workspace_bytes, void* stream) {
     gft_status st = check_advect(density_shape, vel_x, vel_y, vel_z, order, clamp, boundary);
     if (st != GFT_OK) return st;
+    const size_t need = gft_advect_grad_workspace_size_mode(density_shape, order, grad_mode);
     const bool forward_ready = (grad_mode & GFT_GRAD_FORWARD_READY) != 0;
-    grad_mode &= ~GFT_GRAD_FORWARD_READY;
+    const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    grad_mode &= ~(GFT_GRAD_FORWARD_READY | GFT_GRAD_DETERMINISTIC);
     if (!enum_in(grad_mode, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (forward_ready && (order != 2 || density_shape[0] != 1))
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_FORWARD_READY needs order 2 and one batch slice");
     if (!density || !output_grad || !density_grad || !vel_x_grad || !vel_y_grad || !vel_z_grad)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
-    const size_t need = gft_advect_grad_workspace_size(density_shape, order);
     if (workspace == nullptr || workspace_bytes < need) return fail(GFT_ERR_WORKSPACE, "advect gradient workspace too small");
     if ((st = check_aligned({density, output_grad, density_grad}, vec_bytes(density_shape[4], 0))) != GFT_OK ||
         (st = check_aligned({vel_x, vel_y, vel_z, vel_x_grad, vel_y_grad, vel_z_grad}, 4)) != GFT_OK ||
@@ -1203,6 +1241,7 @@ gft_status gft_advect_grad(const float* density, const int64_t density_shape[5],
     a.order = order;
     a.clamp = clamp;
     a.boundary = boundary;
+    a.det = det;
     if (!launch_advect_bwd(a, grad_mode == GFT_GRAD_EXACT, forward_ready, output_grad, density_grad, vel_x_grad,
                            vel_y_grad, vel_z_grad, reinterpret_cast<float*>(workspace), as_stream(stream)))
         return GFT_ERR_CUDA;

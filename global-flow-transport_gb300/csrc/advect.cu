@@ -7,6 +7,7 @@
 // MacCormack runs in two passes: (1) the semi-Lagrangian value, (2) the back
 // lookup of (1), the correction and the MC_SMOOTH clamp, with the MIN/MAX of
 // the forward footprint taken from the same 8 gathers as the forward value.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -202,9 +203,13 @@ constexpr bool packed_count() {
 // for the lane that gives.  All 32 lanes call it; act = this lane scatters.
 // COUNT 0: exact (BORDER: the fetch window); 1: uint counters, 2: packed
 // (sum, count) pairs (C == 1), both with the reference's (-1, dims) window.
-template <int C, int BM, int COUNT>
+// DET (deterministic adjoint; COUNT 0 or 1): the contributions, scaled by the
+// power of two iscale and rounded, are added to int64 accumulators (C per
+// voxel) instead of buf; integer sums do not depend on the order of the adds.
+template <int C, int BM, int COUNT, bool DET = false>
 __device__ __forceinline__ void scatter_merged(float* __restrict__ buf, unsigned int* __restrict__ cnt, Dims d,
-                                               bool act, float px, float py, float pz, Vec<C> val) {
+                                               bool act, float px, float py, float pz, Vec<C> val,
+                                               unsigned long long* __restrict__ iacc = nullptr, float iscale = 0.f) {
     constexpr bool PACK = packed_count<C, COUNT>();
     constexpr unsigned FULL = 0xffffffffu;
     if constexpr (BM == BM_BORDER) {
@@ -247,6 +252,13 @@ __device__ __forceinline__ void scatter_merged(float* __restrict__ buf, unsigned
         if ((BM == BM_BORDER && !ok) || (sx && give)) continue;
         const int64_t f = flat3(sx ? c.x1 : c.x0, sy ? c.y1 : c.y0, sz ? c.z1 : c.z0, d);
         const bool two = !sx && take;
+        if constexpr (DET) {
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch)
+                atomicAdd(iacc + f * C + ch, (unsigned long long)__float2ll_rn(v[k].v[ch] * iscale));
+            if constexpr (COUNT == 1) atomicAdd(cnt + f, two ? 2u : 1u);
+            continue;
+        }
         if constexpr (PACK) {
             atomicAdd(reinterpret_cast<float2*>(buf) + f, make_float2(v[k].v[0], two ? 2.f : 1.f));
         } else {
@@ -254,6 +266,74 @@ __device__ __forceinline__ void scatter_merged(float* __restrict__ buf, unsigned
             if constexpr (COUNT == 1) atomicAdd(cnt + f, two ? 2u : 1u);
         }
     }
+}
+
+// ---- deterministic adjoint (GFT_GRAD_DETERMINISTIC) ---------------------------
+// The two lookup scatters add fixed-point int64 contributions.  Their scales
+// are powers of two from bounds of every voxel's partial sums, computed on the
+// GPU from maxima (independent of the evaluation order): the back lookup
+// scatters -0.5 g_corr (|.| <= 0.5 max|dy|) with trilinear weights summing to
+// one per lookup, so no voxel's sum exceeds 0.5 max|dy| N; the forward lookup
+// scatters the fwd adjoint, whose largest magnitude a max pass measures, times
+// N.  scale = 2^(61 - ceil(log2 bound)) keeps every partial sum below 2^61.
+template <int C>
+__device__ __forceinline__ Vec<C> det_load(const unsigned long long* __restrict__ acc, int64_t t, float scale) {
+    Vec<C> r;
+    const double inv = 1.0 / (double)scale;
+#pragma unroll
+    for (int c = 0; c < C; ++c) r.v[c] = (float)((double)(long long)acc[t * C + c] * inv);
+    return r;
+}
+__device__ __forceinline__ void adv_warp_absmax(unsigned int* out, float m) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float x = __shfl_down_sync(0xffffffffu, m, o);
+        m = (x > m || x != x) ? x : m;  // NaN propagates
+    }
+    if ((threadIdx.x & 31u) == 0) atomicMax(out, __float_as_uint(m));
+}
+// max |dy| of one slice
+__global__ void k_adv_det_absmax(const float* __restrict__ v, int64_t n, unsigned int* __restrict__ out) {
+    float m = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = fabsf(v[i]);
+        m = (x > m || x != x) ? x : m;
+    }
+    adv_warp_absmax(out, m);
+}
+// max |fwd adjoint| = max |gdir + (normalised) back-lookup scatter|
+template <int C, int COUNT>
+__global__ void k_adv_det_gfmax(const float* __restrict__ gdir, const unsigned long long* __restrict__ iacc,
+                                const float* __restrict__ iscale, const unsigned int* __restrict__ cnt, int64_t nv,
+                                unsigned int* __restrict__ out) {
+    float m = 0.f;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += (int64_t)gridDim.x * blockDim.x) {
+        Vec<C> sc = det_load<C>(iacc, t, *iscale);
+        if (COUNT) {
+            const unsigned int n = cnt[t];
+            if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+        }
+        const Vec<C> g = loadf<C>(gdir, t);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const float x = fabsf(g.v[c] + sc.v[c]);
+            m = (x > m || x != x) ? x : m;
+        }
+    }
+    adv_warp_absmax(out, m);
+}
+// scale <- 2^(61 - ceil(log2(factor * max))), NaN for a non-finite bound
+__global__ void k_adv_det_scale(const unsigned int* __restrict__ maxbits, double factor, float* __restrict__ scale) {
+    const double t = (double)__uint_as_float(*maxbits) * factor;
+    float sc;
+    if (!(t < 1e300)) {
+        sc = __int_as_float(0x7fc00000);
+    } else if (t <= 0.0) {
+        sc = 1.f;
+    } else {
+        sc = ldexpf(1.f, 61 - max(-60, (int)ceil(log2(t))));
+    }
+    *scale = sc;
 }
 
 // (sum / count where count > 0) of a packed pair, as the uint-counter form
@@ -269,12 +349,13 @@ __device__ __forceinline__ float packed_normalised(const float* __restrict__ buf
 // of the back lookup (whose lut is -lut).
 // Single channel: at most 64 registers (4 blocks of 256 per SM instead of 3,
 // 16 bytes spilled) for the latency of the two corner gathers.
-template <int C, int BM, int COUNT>
+template <int C, int BM, int COUNT, bool DET = false>
 __global__ void __launch_bounds__(AD_THREADS, C == 1 ? 4 : 1)
     k_adv_bwd_back(const float* __restrict__ d, const float* __restrict__ fwd, Dims dm, const float* __restrict__ vx,
                    const float* __restrict__ vy, const float* __restrict__ vz, float dt, int clamp,
                    const float* __restrict__ dy, float* __restrict__ gd, float* __restrict__ gfwd_sc,
-                   unsigned int* __restrict__ cnt2, float* __restrict__ gdir, float* __restrict__ glut, bool first) {
+                   unsigned int* __restrict__ cnt2, float* __restrict__ gdir, float* __restrict__ glut, bool first,
+                   unsigned long long* __restrict__ iacc, const float* __restrict__ iscale) {
     const int64_t nv = voxels(dm), t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = t0 < nv;  // lanes past the end stay for the merged scatter
     const int64_t t = in ? t0 : nv - 1;
@@ -302,7 +383,7 @@ __global__ void __launch_bounds__(AD_THREADS, C == 1 ? 4 : 1)
         store<C>(gd, t, vscale(gcorr, 0.5f));
         store<C>(gdir, t, g);
     }
-    scatter_merged<C, BM, COUNT>(gfwd_sc, cnt2, dm, in, bx, by, bz, gback);
+    scatter_merged<C, BM, COUNT, DET>(gfwd_sc, cnt2, dm, in, bx, by, bz, gback, iacc, DET ? *iscale : 0.f);
     if (!in) return;
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
@@ -326,13 +407,15 @@ __global__ void __launch_bounds__(AD_THREADS, C == 1 ? 4 : 1)
 // Stage C: fwd adjoint = direct term + (normalised) back-lookup scatter; scatter
 // it into the density through the forward lookup and accumulate that lookup's
 // gradient.  first_order: the fwd adjoint is the output gradient itself.
-template <int C, int BM, int COUNT>
+template <int C, int BM, int COUNT, bool DET = false>
 __global__ void __launch_bounds__(AD_THREADS)
     k_adv_bwd_fwd(const float* __restrict__ d, Dims dm, const float* __restrict__ vx, const float* __restrict__ vy,
                   const float* __restrict__ vz, float dt, bool first_order, bool negative,
                   const float* __restrict__ gdir, const float* __restrict__ gfwd_sc,
                   const unsigned int* __restrict__ cnt2, float* __restrict__ gd_sc, unsigned int* __restrict__ cnt3,
-                  float* __restrict__ glut, bool first) {
+                  float* __restrict__ glut, bool first, const unsigned long long* __restrict__ iacc_in,
+                  const float* __restrict__ iscale_in, unsigned long long* __restrict__ iacc_out,
+                  const float* __restrict__ iscale_out) {
     const int64_t nv = voxels(dm), t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = t0 < nv;  // lanes past the end stay for the merged scatter
     const int64_t t = in ? t0 : nv - 1;
@@ -353,7 +436,13 @@ __global__ void __launch_bounds__(AD_THREADS)
     }
     if (!first_order) {
         Vec<C> sc;
-        if constexpr (packed_count<C, COUNT>()) {
+        if constexpr (DET) {
+            sc = det_load<C>(iacc_in, t, *iscale_in);
+            if (COUNT) {
+                const unsigned int n = cnt2[t];
+                if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+            }
+        } else if constexpr (packed_count<C, COUNT>()) {
             sc.v[0] = packed_normalised(gfwd_sc, t);
         } else {
             sc = loadf<C>(gfwd_sc, t);
@@ -364,7 +453,7 @@ __global__ void __launch_bounds__(AD_THREADS)
         }
         gf = vadd(gf, sc);
     }
-    scatter_merged<C, BM, COUNT>(gd_sc, cnt3, dm, in, px, py, pz, gf);
+    scatter_merged<C, BM, COUNT, DET>(gd_sc, cnt3, dm, in, px, py, pz, gf, iacc_out, DET ? *iscale_out : 0.f);
     if (!in) return;
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
@@ -386,14 +475,21 @@ __global__ void __launch_bounds__(AD_THREADS)
 }
 
 // Stage D: density gradient = direct term + (normalised) forward-lookup scatter.
-template <int C, int COUNT>
+template <int C, int COUNT, bool DET = false>
 __global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restrict__ gd_sc,
-                                  const unsigned int* __restrict__ cnt3, int64_t nv) {
+                                  const unsigned int* __restrict__ cnt3, int64_t nv,
+                                  const unsigned long long* __restrict__ iacc, const float* __restrict__ iscale) {
     constexpr bool NORM = COUNT != 0;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nv) return;
     Vec<C> sc;
-    if constexpr (packed_count<C, COUNT>()) {
+    if constexpr (DET) {
+        sc = det_load<C>(iacc, t, *iscale);
+        if (NORM) {
+            const unsigned int n = cnt3[t];
+            if (n > 0) sc = vscale(sc, 1.0f / (float)n);
+        }
+    } else if constexpr (packed_count<C, COUNT>()) {
         sc.v[0] = packed_normalised(gd_sc, t);
     } else {
         sc = loadf<C>(gd_sc, t);
@@ -450,6 +546,93 @@ __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, floa
     }
 }
 
+// Workspace of the deterministic adjoint: fwd | gdir | glut (3 planes) | two
+// counter planes | the two int64 scatter targets | maxima and scales.
+struct AdvDetLayout {
+    size_t fwd, gdir, glut, cnt2, cnt3, acc2, acc3, small, total;  // byte offsets
+};
+static AdvDetLayout adv_det_layout(size_t nv, size_t C) {
+    AdvDetLayout l;
+    const size_t vc = nv * C;
+    l.fwd = 0;
+    l.gdir = l.fwd + 4 * vc;
+    l.glut = l.gdir + 4 * vc;
+    l.cnt2 = l.glut + 12 * nv;
+    l.cnt3 = l.cnt2 + 4 * nv;
+    l.acc2 = (l.cnt3 + 4 * nv + 7) & ~size_t(7);
+    l.acc3 = l.acc2 + 8 * vc;
+    l.small = l.acc3 + 8 * vc;
+    l.total = l.small + 16;
+    return l;
+}
+
+size_t advect_det_ws_bytes(size_t nv, size_t C) { return adv_det_layout(nv, C).total; }
+
+static unsigned det_reduce_blocks(int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8));
+}
+
+template <int C, int BM, int COUNT>
+static bool adv_bwd_det(const AdvectArgs& a, bool forward_ready, const float* dy, float* gd, float* gvx, float* gvy,
+                        float* gvz, float* ws, cudaStream_t s) {
+    const int64_t nv = voxels(a.d);
+    const int T = adv_threads();
+    const unsigned blocks = (unsigned)((nv + T - 1) / T);
+    const size_t vc = (size_t)nv * C;
+    const AdvDetLayout L = adv_det_layout((size_t)nv, C);
+    char* base = reinterpret_cast<char*>(ws);
+    float* fwd = reinterpret_cast<float*>(base + L.fwd);
+    float* gdir = reinterpret_cast<float*>(base + L.gdir);
+    float* glut = reinterpret_cast<float*>(base + L.glut);
+    unsigned int* cnt2 = reinterpret_cast<unsigned int*>(base + L.cnt2);
+    unsigned int* cnt3 = reinterpret_cast<unsigned int*>(base + L.cnt3);
+    unsigned long long* acc2 = reinterpret_cast<unsigned long long*>(base + L.acc2);
+    unsigned long long* acc3 = reinterpret_cast<unsigned long long*>(base + L.acc3);
+    unsigned int* maxbits = reinterpret_cast<unsigned int*>(base + L.small);
+    float* scale = reinterpret_cast<float*>(base + L.small + 8);
+    const float* dens = reinterpret_cast<const float*>(a.density);
+    const unsigned rb = det_reduce_blocks((int64_t)vc);
+    for (int b = 0; b < a.N; ++b) {
+        const float* db = dens + (size_t)b * vc;
+        const float* dyb = dy + (size_t)b * vc;
+        float* gdb = gd + (size_t)b * vc;
+        // counters (when used) and both accumulators are contiguous from cnt2
+        if (!cuda_ok(cudaMemsetAsync(base + L.cnt2, 0, L.small + 8 - L.cnt2, s), "zero scatter")) return false;
+        int n = 0;
+        if (a.order == 2) {
+            if (!forward_ready)
+                k_adv_sl<C, float, BM><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd), ++n;
+            // back-lookup scatter of -0.5 g_corr: |sum| <= 0.5 max|dy| * voxels
+            k_adv_det_absmax<<<rb, 256, 0, s>>>(dyb, (int64_t)vc, maxbits);
+            k_adv_det_scale<<<1, 1, 0, s>>>(maxbits, 0.5 * (double)nv, scale);
+            k_adv_bwd_back<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
+                                                                    dyb, gdb, nullptr, cnt2, gdir, glut, b == 0,
+                                                                    acc2, scale);
+            k_adv_det_gfmax<C, COUNT><<<rb, 256, 0, s>>>(gdir, acc2, scale, cnt2, nv, maxbits + 1);
+            k_adv_det_scale<<<1, 1, 0, s>>>(maxbits + 1, (double)nv, scale + 1);
+            k_adv_bwd_fwd<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
+                                                                   gdir, nullptr, cnt2, nullptr, cnt3, glut, false,
+                                                                   acc2, scale, acc3, scale + 1);
+            n += 6;
+        } else {
+            if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
+            k_adv_det_absmax<<<rb, 256, 0, s>>>(dyb, (int64_t)vc, maxbits + 1);
+            k_adv_det_scale<<<1, 1, 0, s>>>(maxbits + 1, (double)nv, scale + 1);
+            k_adv_bwd_fwd<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
+                                                                   a.clamp == CLAMP_NEGATIVE, dyb, nullptr, nullptr,
+                                                                   nullptr, cnt3, glut, b == 0, nullptr, nullptr,
+                                                                   acc3, scale + 1);
+            n += 3;
+        }
+        k_adv_bwd_density<C, COUNT, true><<<blocks, T, 0, s>>>(gdb, nullptr, cnt3, nv, acc3, scale + 1);
+        if (!launched(n + 1, "advect gradient launch")) return false;
+    }
+    const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
+                          (int64_t)a.d.x * a.d.y * (a.d.z + 1);
+    k_adv_bwd_velocity<<<(unsigned)((nstag + T - 1) / T), T, 0, s>>>(glut, a.d, a.dt, gvx, gvy, gvz);
+    return launched(1, "velocity gradient launch");
+}
+
 template <int C, int BM, int COUNT>
 static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* dy, float* gd, float* gvx, float* gvy,
                          float* gvz, float* ws, cudaStream_t s) {
@@ -485,16 +668,19 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
             if (!forward_ready)  // else fwd holds this slice's semi-Lagrangian grid already
                 k_adv_sl<C, float, BM><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
             k_adv_bwd_back<C, BM, COUNT><<<blocks, T, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
-                                                                      dyb, gdb, gfwd_sc, cnt2, gdir, glut, b == 0);
+                                                                      dyb, gdb, gfwd_sc, cnt2, gdir, glut, b == 0,
+                                                              nullptr, nullptr);
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
-                                                                     gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut, false);
+                                                                     gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut, false,
+                                                             nullptr, nullptr, nullptr, nullptr);
         } else {
             if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
                                                                      a.clamp == CLAMP_NEGATIVE, dyb, nullptr,
-                                                                     nullptr, gd_sc, cnt3, glut, b == 0);
+                                                                     nullptr, gd_sc, cnt3, glut, b == 0, nullptr,
+                                                             nullptr, nullptr, nullptr);
         }
-        k_adv_bwd_density<C, COUNT><<<blocks, T, 0, s>>>(gdb, gd_sc, cnt3, nv);
+        k_adv_bwd_density<C, COUNT><<<blocks, T, 0, s>>>(gdb, gd_sc, cnt3, nv, nullptr, nullptr);
         if (!launched(a.order == 2 ? (forward_ready ? 3 : 4) : 2, "advect gradient launch")) return false;
     }
     const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
@@ -507,6 +693,10 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
 template <int C, int BM>
 static bool adv_bwd_bm(const AdvectArgs& a, bool exact, bool fr, const float* dy, float* gd, float* gvx, float* gvy,
                        float* gvz, float* ws, cudaStream_t s) {
+    if (a.det) {
+        if (exact) return adv_bwd_det<C, BM, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+        return adv_bwd_det<C, BM, 1>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
+    }
     if (exact) return adv_bwd_impl<C, BM, 0>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);
     if constexpr (C == 1) {
         if ((reinterpret_cast<uintptr_t>(ws) & 7u) == 0) return adv_bwd_impl<C, BM, 2>(a, fr, dy, gd, gvx, gvy, gvz, ws, s);

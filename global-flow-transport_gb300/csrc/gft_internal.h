@@ -105,7 +105,14 @@ struct RaymarchArgs {
                                       // the block grown by one voxel at its upper faces
         int nbx = 0, nby = 0, nbz = 0;
     } store;
+    // Deterministic adjoint (GFT_GRAD_DETERMINISTIC): integer accumulation in
+    // the workspace after the reciprocal weight sums (raymarch_det_bytes).
+    bool det = false;
+    unsigned long long* det_acc = nullptr;  // set by launch_raymarch_bwd
+    const float* det_scale = nullptr;
 };
+// Workspace bytes of the deterministic adjoint for `pairs` (batch, camera) pairs.
+size_t raymarch_det_bytes(int N, int C, Dims din, size_t pairs);
 // Bytes of the sample store of these pairs (samples, ballot words,
 // occupancy map of the N input slices), and its parts at `base`.
 size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din);
@@ -166,7 +173,9 @@ struct AdvectArgs {
     const float *vx, *vy, *vz;
     float dt;
     int order, clamp, boundary;
+    bool det = false;  // deterministic adjoint: int64 scatters, workspace advect_det_ws_bytes
 };
+size_t advect_det_ws_bytes(size_t voxels, size_t channels);
 bool launch_advect_fwd(const AdvectArgs& a, float* out, float* ws, cudaStream_t s);
 // forward_ready: ws starts with the semi-Lagrangian grid of launch_advect_fwd
 // (order 2, N == 1), which is then not recomputed.

@@ -6,6 +6,7 @@
 // with a host constant-buffer upload in between.  A warp covers an 8x4 pixel
 // tile so that the 32 rays of a warp gather from neighbouring voxels.
 #include <algorithm>
+#include <cmath>
 
 #include "gft_internal.h"
 
@@ -421,9 +422,15 @@ __device__ __forceinline__ unsigned zero_weight_mask(float fx, float fy, float f
 // accumulate into one gradient) and skips corners with no weight.  Zero-weight
 // contributions are skipped; the ceil corner is floor + 1 (the reference's
 // ceil(p) equals floor(p) only where the ceil weight is 0).
+// iacc != nullptr (deterministic adjoint): the corner sums go, scaled by the
+// power of two iscale and rounded to integers, into int64 accumulators
+// (MODE 2: one per brick cell of the pair; MODE 0/1: C per cell of the batch
+// slice) instead of the float reductions; integer addition is associative, so
+// the sums do not depend on the order in which the warps add them.
 template <int C, int BM, int MODE, int L>
 __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
-                                             bool act, float px, float py, float pz, Vec<C> val) {
+                                             bool act, float px, float py, float pz, Vec<C> val,
+                                             unsigned long long* __restrict__ iacc = nullptr, float iscale = 0.f) {
     const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;  // blockDim.x == RM_BX
     if constexpr (BM == BM_BORDER) {
         if constexpr (MODE != 0)
@@ -528,6 +535,20 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
         Vec<C> a;
 #pragma unroll
         for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];
+        if (iacc != nullptr) {
+            if constexpr (MODE == 2) {
+                atomicAdd(iacc + bi, (unsigned long long)__float2ll_rn(a.v[0] * iscale));
+            } else {
+                float inv = 1.f;
+                if constexpr (MODE == 1) inv = __ldg(cnt + bi);
+                if (inv > 0.f) {
+#pragma unroll
+                    for (int c = 0; c < C; ++c)
+                        atomicAdd(iacc + (uint64_t)ci * C + c, (unsigned long long)__float2ll_rn(a.v[c] * inv * iscale));
+                }
+            }
+            continue;
+        }
         if constexpr (MODE == 1) {
             const float inv = __ldg(cnt + bi);
             if (inv > 0.f) atomic_add<C>(grad, ci, vscale(a, inv));
@@ -562,11 +583,16 @@ template <int C, typename S, int BM, int MODE, int L>
 __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, Dims din, int blend_mode,
                                                       const float* __restrict__ out, const float* __restrict__ dout,
                                                       float* __restrict__ grad, const float* __restrict__ cnt,
+                                                      unsigned long long* __restrict__ iacc, float iscale,
                                                       const RaymarchArgs::Store& st, const PairTable& tab, int tile) {
     RayPix r;
     r.tile = tile;
     const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
+    unsigned long long* idst =
+        iacc == nullptr ? nullptr
+        : MODE == 2     ? iacc + (size_t)(tab.pair_base + p) * brick_cells(din)
+                        : iacc + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     float3 farp, step, nearp;
     ray_far_step(tab.cam[p], x, y, W, H, D, farp, step, nearp);
     // With a sample store: the forward's own clip range (front-to-back steps
@@ -631,7 +657,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             }
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
-        scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val);
+        scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val, idst, iscale);
     }
 }
 
@@ -642,10 +668,15 @@ template <int C, typename S, int BM, int MODE, int L>
 __global__ void __launch_bounds__(RM_BX* RM_BY, 6)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
+                       unsigned long long* __restrict__ iacc, const float* __restrict__ iscale_ptr, float wscale,
                        const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+    // integer accumulation: MODE 2 with the host's weight scale, the adjoint
+    // with the scale its bound kernel wrote
+    const float iscale = iacc == nullptr ? 0.f : MODE == 2 ? wscale : *iscale_ptr;
     const int tiles = tab.tile0[tab.n];
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
-        raymarch_scatter_tile<C, S, BM, MODE, L>(in, din, blend_mode, out, dout, grad, cnt, st, tab, tile);
+        raymarch_scatter_tile<C, S, BM, MODE, L>(in, din, blend_mode, out, dout, grad, cnt, iacc, iscale, st, tab,
+                                                 tile);
 }
 
 template <int C, typename S, int BM>
@@ -698,10 +729,10 @@ static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, co
                            const float* dout, float* grad, const float* cnt, const PairTable& t) {
     if (exact)
         k_raymarch_scatter<C, S, BM, 0, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.store, t);
+                                                                     cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
     else
         k_raymarch_scatter<C, S, BM, 1, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.store, t);
+                                                                     cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
 }
 
 template <int C, typename S, int BM>
@@ -725,9 +756,9 @@ static void bwd_dispatch_bm(bool exact, dim3 grid, dim3 block, cudaStream_t s, c
 
 template <int BM>
 static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
-                             const PairTable& t) {
-    k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(nullptr, a.din, a.blend, nullptr, nullptr,
-                                                                               cnt, nullptr, RaymarchArgs::Store{}, t);
+                             unsigned long long* wacc, float wscale, const PairTable& t) {
+    k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(
+        nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, wacc, nullptr, wscale, RaymarchArgs::Store{}, t);
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel), 16
@@ -745,36 +776,230 @@ __global__ void k_invert_weights(float4* __restrict__ w, int64_t n4) {
     }
 }
 
-bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
+// ---- deterministic adjoint (GFT_GRAD_DETERMINISTIC) ---------------------------------
+// Every float reduction of the adjoint becomes an exact int64 sum of
+// fixed-point contributions, so the gradient is the same bit for bit on every
+// run.  The weight sums use a fixed point of scale 2^(61 - ceil(log2 of the
+// largest sample count of a pair)): a voxel's weight sum never exceeds the
+// number of samples, so no sum overflows.  The adjoint's scale comes from a
+// bound on every voxel's partial sums, computed on the GPU from maxima (which
+// do not depend on the order of evaluation): each sample's blend adjoint is at
+// most B = max|dy| (ADDITIVE, or one channel) or, for BEER_LAMBERT with C > 1,
+// max|dy| (1 + (C-1) D max|x|) (the density channel sums the later samples'
+// light times the light adjoint, attenuated by exp(-density) <= 1); a voxel's
+// reference-normalised gradient is a sum over cameras of weighted means of
+// them (at most pairs * B) and its exact gradient at most B times its summed
+// trilinear weights (at most pairs * the largest weight sum).  The scale is
+// 2^(61 - ceil(log2 bound)), so no partial sum exceeds 2^61.
+static int64_t det_weights_offset(int64_t cells, size_t pairs) {
+    return (int64_t)align256u(sizeof(float) * cells * pairs);
+}
+size_t raymarch_det_bytes(int N, int C, Dims din, size_t pairs) {
+    const int64_t cells = brick_cells(din);  // >= voxels: covers both layouts
+    return (size_t)det_weights_offset(cells, pairs) + align256u(sizeof(unsigned long long) * cells * pairs) +
+           align256u(sizeof(unsigned long long) * cells * (size_t)N * C) + 256;
+}
+
+// largest sample count of a pair -> fixed-point scale of the weight sums
+static float det_weight_scale(const std::vector<Pair>& pairs, const RaymarchArgs& a) {
+    double most = 1.0;
+    for (const Pair& p : pairs) {
+        const double n = (double)(p.W > 0 ? p.W : a.W) * (p.H > 0 ? p.H : a.H) * (p.D > 0 ? p.D : a.D);
+        most = std::max(most, n);
+    }
+    const int e = (int)std::ceil(std::log2(most + 1.0));
+    return std::ldexp(1.0f, 61 - e);
+}
+
+__global__ void k_det_invert_weights(const unsigned long long* __restrict__ wacc, float wscale, float* __restrict__ w,
+                                     int64_t n, unsigned long long* __restrict__ wmax) {
+    unsigned long long m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long q = wacc[i];
+        w[i] = q > 0 ? (float)((double)wscale / (double)q) : 0.f;
+        m = q > m ? q : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31u) == 0 && m > 0) atomicMax(wmax, m);
+}
+
+// max |v| over n floats -> atomicMax on the bits (non-negative floats order like
+// their bits; NaN compares above every finite value)
+__device__ __forceinline__ void warp_absmax_to(unsigned int* out, float m) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31u) == 0) atomicMax(out, __float_as_uint(m));
+}
+__global__ void k_det_absmax(const float* __restrict__ v, int64_t n, unsigned int* __restrict__ out) {
+    float m = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = fabsf(v[i]);
+        m = (x > m || x != x) ? x : m;
+    }
+    warp_absmax_to(out, m);
+}
+// the input grid's voxels (not the brick padding), all channels
+template <int C, typename S, int L>
+__global__ void k_det_absmax_grid(const S* __restrict__ in, Dims d, int N, unsigned int* __restrict__ out) {
+    float m = 0.f;
+    const int64_t nv = voxels(d) * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = i / voxels(d);
+        int x, y, z;
+        unflat32((uint32_t)(i - b * voxels(d)), d, x, y, z);
+        const Vec<C> a = Load<C, S>::at(in + (size_t)b * slice_cells<L>(d) * C, cell_index<L>(x, y, z, d));
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const float x2 = fabsf(a.v[c]);
+            m = (x2 > m || x2 != x2) ? x2 : m;
+        }
+    }
+    warp_absmax_to(out, m);
+}
+// bounds: [0] max|dy| bits, [1] max|x| bits; wmax: the largest integer weight
+// sum (EXACT); scale <- 2^(61 - ceil(log2 bound)), NaN for a non-finite bound
+__global__ void k_det_scale(const unsigned int* __restrict__ bounds, const unsigned long long* __restrict__ wmax,
+                            float wscale, int C, int D, int blend, int pairs, bool exact, float* __restrict__ scale) {
+    const double dy = (double)__uint_as_float(bounds[0]), x = (double)__uint_as_float(bounds[1]);
+    double b = dy;
+    if (C > 1 && blend == BL_BEER_LAMBERT) b = dy * (1.0 + (double)(C - 1) * D * x);
+    double f = (double)pairs;
+    if (exact) f *= (double)(*wmax) / (double)wscale;
+    const double t = b * f;
+    float sc;
+    if (!(t < 1e300)) {
+        sc = __int_as_float(0x7fc00000);  // non-finite inputs: the gradient becomes NaN
+    } else if (t <= 0.0) {
+        sc = 1.f;
+    } else {
+        const int e = max(-60, (int)ceil(log2(t)));
+        sc = ldexpf(1.f, 61 - e);
+    }
+    *scale = sc;
+}
+__global__ void k_det_convert(const unsigned long long* __restrict__ acc, const float* __restrict__ scale,
+                              float* __restrict__ grad, int64_t n) {
+    const double inv = 1.0 / (double)(*scale);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        grad[i] = (float)((double)(long long)acc[i] * inv);
+}
+
+static unsigned grid_stride_blocks(int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8));
+}
+
+struct DetLayout {
+    unsigned long long* wacc;
+    unsigned long long* gacc;
+    unsigned int* bounds;           // [0] max|dy| bits, [1] max|x| bits
+    unsigned long long* wmax;       // largest weight sum
+    float* scale;                   // the adjoint's fixed-point scale
+};
+static DetLayout det_layout(float* ws, const RaymarchArgs& a, size_t pairs) {
     const int64_t cells = brick_cells(a.din);
-    if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * cells * pairs.size(), s), "zero weights")) return false;
+    char* base = reinterpret_cast<char*>(ws);
+    DetLayout L;
+    L.wacc = reinterpret_cast<unsigned long long*>(base + det_weights_offset(cells, pairs));
+    char* g = reinterpret_cast<char*>(L.wacc) + align256u(sizeof(unsigned long long) * cells * pairs);
+    L.gacc = reinterpret_cast<unsigned long long*>(g);
+    char* t = g + align256u(sizeof(unsigned long long) * cells * (size_t)a.N * a.C);
+    L.bounds = reinterpret_cast<unsigned int*>(t);
+    L.wmax = reinterpret_cast<unsigned long long*>(t + 16);
+    L.scale = reinterpret_cast<float*>(t + 32);
+    return L;
+}
+
+// Pass 1 of the reference-normalised adjoint: per-pair weight sums into
+// ws_cnt, inverted to reciprocals (deterministic: exact integer sums first,
+// and the largest sum into the layout's wmax).
+static bool raymarch_weights_impl(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, bool det,
+                                  cudaStream_t s) {
+    const int64_t cells = brick_cells(a.din);
+    const int64_t n = cells * (int64_t)pairs.size();
+    DetLayout L{};
+    float wscale = 0.f;
+    if (det) {
+        L = det_layout(ws_cnt, a, pairs.size());
+        wscale = det_weight_scale(pairs, a);
+        if (!cuda_ok(cudaMemsetAsync(L.wacc, 0, sizeof(unsigned long long) * n, s), "zero weights") ||
+            !cuda_ok(cudaMemsetAsync(L.wmax, 0, sizeof(unsigned long long), s), "zero weight max"))
+            return false;
+    } else if (!cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * n, s), "zero weights")) {
+        return false;
+    }
     const dim3 block(RM_BX, RM_BY, 1);
     for (PairTable& t : make_tables(pairs)) {
         const dim3 grid(raymarch_blocks((int)set_ray_tiles(t)));
         switch (a.boundary) {
-            case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, t); break;
-            case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, t); break;
-            default: weights_dispatch<BM_WRAP>(grid, block, s, a, ws_cnt, t); break;
+            case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, L.wacc, wscale, t); break;
+            case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, L.wacc, wscale, t); break;
+            default: weights_dispatch<BM_WRAP>(grid, block, s, a, ws_cnt, L.wacc, wscale, t); break;
         }
         if (!launched(1, "raymarch weight launch")) return false;
     }
-    const int64_t n = cells * (int64_t)pairs.size();
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t cap = (int64_t)std::max(sms, 1) * 8;
+    if (det) {
+        k_det_invert_weights<<<grid_stride_blocks(n), 256, 0, s>>>(L.wacc, wscale, ws_cnt, n, L.wmax);
+        return launched(1, "raymarch weight inversion launch");
+    }
     const int64_t want = (n / 4 + 255) / 256;
-    k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min(want, cap)), 256, 0, s>>>(
+    k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * 8)), 256, 0, s>>>(
         reinterpret_cast<float4*>(ws_cnt), n / 4);
     return launched(1, "raymarch weight inversion launch");
 }
 
-bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
+bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
+    return raymarch_weights_impl(a, pairs, ws_cnt, false, s);
+}
+
+template <int C, typename S, int L>
+static void det_absmax_grid(const RaymarchArgs& a, unsigned int* out, cudaStream_t s) {
+    k_det_absmax_grid<C, S, L><<<grid_stride_blocks(voxels(a.din) * a.N), 256, 0, s>>>((const S*)a.input, a.din, a.N,
+                                                                                      out);
+}
+
+bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pairs, const float* out,
                          const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s) {
+    RaymarchArgs a = a_in;
     const int64_t cells = a.layout == LAYOUT_BRICK ? brick_cells(a.din) : voxels(a.din);
-    if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * cells * a.C * a.N, s), "zero gradient")) return false;
-    if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
+    const int64_t n = cells * a.C * a.N;
+    if (!a.det) {
+        if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * n, s), "zero gradient")) return false;
+        if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
+    } else {
+        // integer sums into gacc, then converted into grad
+        const DetLayout L = det_layout(ws_cnt, a, pairs.size());
+        if (!cuda_ok(cudaMemsetAsync(L.gacc, 0, sizeof(unsigned long long) * n, s), "zero gradient") ||
+            !cuda_ok(cudaMemsetAsync(L.bounds, 0, 8, s), "zero bounds"))
+            return false;
+        if (!raymarch_weights_impl(a, pairs, ws_cnt, true, s)) return false;
+        int64_t pix = 0;
+        int dmax = a.D;
+        for (const Pair& p : pairs) {
+            pix += (int64_t)(p.W > 0 ? p.W : a.W) * (p.H > 0 ? p.H : a.H);
+            dmax = std::max(dmax, p.D);
+        }
+        k_det_absmax<<<grid_stride_blocks(pix * a.C), 256, 0, s>>>(dout, pix * a.C, L.bounds);
+        const bool brick = a.layout == LAYOUT_BRICK;
+        if (a.dtype == 0) {
+            if (a.C == 4) brick ? det_absmax_grid<4, float, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<4, float, LAYOUT_FLAT>(a, L.bounds + 1, s);
+            else if (a.C == 2) brick ? det_absmax_grid<2, float, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<2, float, LAYOUT_FLAT>(a, L.bounds + 1, s);
+            else brick ? det_absmax_grid<1, float, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<1, float, LAYOUT_FLAT>(a, L.bounds + 1, s);
+        } else {
+            if (a.C == 4) brick ? det_absmax_grid<4, __nv_bfloat16, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<4, __nv_bfloat16, LAYOUT_FLAT>(a, L.bounds + 1, s);
+            else if (a.C == 2) brick ? det_absmax_grid<2, __nv_bfloat16, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<2, __nv_bfloat16, LAYOUT_FLAT>(a, L.bounds + 1, s);
+            else brick ? det_absmax_grid<1, __nv_bfloat16, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<1, __nv_bfloat16, LAYOUT_FLAT>(a, L.bounds + 1, s);
+        }
+        k_det_scale<<<1, 1, 0, s>>>(L.bounds, L.wmax, det_weight_scale(pairs, a), a.C, dmax, a.blend, (int)pairs.size(),
+                                    exact, L.scale);
+        if (!launched(3, "deterministic bound launch")) return false;
+        a.det_acc = L.gacc;
+        a.det_scale = L.scale;
+    }
     const dim3 block(RM_BX, RM_BY, 1);
     int64_t smp_cells = 0;
     for (PairTable& t : make_tables(pairs)) {
@@ -789,6 +1014,10 @@ bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
             else bwd_dispatch_bm<1, __nv_bfloat16>(exact, grid, block, s, a, out, dout, grad, ws_cnt, t);
         }
         if (!launched(1, "raymarch backward launch")) return false;
+    }
+    if (a.det) {
+        k_det_convert<<<grid_stride_blocks(n), 256, 0, s>>>(a.det_acc, a.det_scale, grad, n);
+        return launched(1, "deterministic gradient conversion launch");
     }
     return true;
 }

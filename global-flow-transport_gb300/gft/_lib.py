@@ -101,6 +101,7 @@ _SIGS = {
     'gft_advect_noalloc_max_elements': (_SZ, []),
     'gft_advect_noalloc': (_I32, [_P, _I32, _I64P, _P, _P, _P, _F, _I32, _I32, _I32, _P, _P]),
     'gft_advect_grad_workspace_size': (_SZ, [_I64P, _I32]),
+    'gft_advect_grad_workspace_size_mode': (_SZ, [_I64P, _I32, _I32]),
     'gft_advect_grad': (_I32, [_P, _I64P, _P, _P, _P, _F, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P,
                                _P, _SZ, _P]),
 }

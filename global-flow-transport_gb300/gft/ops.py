@@ -22,7 +22,39 @@ COORD = {'TRANSFORM_LINDEPTH': 0, 'TRANSFORM_LINDEPTH_REVERSE': 1, 'TRANSFORM': 
 GRAD = {'REFERENCE': 0, 'EXACT': 1}
 CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
 
-_state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True}
+_state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True, 'deterministic': False}
+DETERMINISTIC = 0x400  # GFT_GRAD_DETERMINISTIC
+
+
+def set_deterministic(enabled):
+    """Deterministic gradients of the raymarch and advection ops: their
+    scatters add fixed-point integers instead of floats (gft.h
+    GFT_GRAD_DETERMINISTIC), so repeated backward passes give bit-identical
+    gradients.  Raymarch: BEER_LAMBERT or ADDITIVE blending."""
+    _state['deterministic'] = bool(enabled)
+
+
+def is_deterministic():
+    return _state['deterministic']
+
+
+class deterministic:
+    """Context manager switching deterministic gradients on (or off)."""
+
+    def __init__(self, enabled=True):
+        self.enabled = bool(enabled)
+
+    def __enter__(self):
+        self.prev = _state['deterministic']
+        _state['deterministic'] = self.enabled
+
+    def __exit__(self, *a):
+        _state['deterministic'] = self.prev
+
+
+def _scatter_gmode():
+    """grad_mode of the raymarch and advection gradient calls."""
+    return GRAD[get_grad_mode()] | (DETERMINISTIC if _state['deterministic'] else 0)
 
 
 def set_grad_mode(mode):
@@ -343,6 +375,8 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
     and geometry takes it over; until then it holds one float per voxel and
     camera.  Under CUDA-graph capture that raymarch and its backward must be
     captured too (they join the side stream)."""
+    if _state['deterministic']:
+        return  # the deterministic gradient computes its own (integer) weight sums
     dev = _cuda_device(device)
     out_shape = _shape3(output_shape)
     b = _enum(BOUNDARY, boundary, 'boundary')
@@ -392,7 +426,8 @@ class _Raymarch(torch.autograd.Function):
         xs = _storage(x, storage_dtype)
         shape5 = _grid5(xs, grid)[0]
         ctx.weights = None
-        if ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+        if (ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']
+                and not _state['deterministic']):
             cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
             if cached is not None:
                 ctx.weights = (cached, None)
@@ -421,7 +456,7 @@ class _Raymarch(torch.autograd.Function):
             if ev is not None:
                 torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                          GRAD[get_grad_mode()], weights=ws, grid=grid, samples=samples)
+                          _scatter_gmode(), weights=ws, grid=grid, samples=samples)
         ctx.weights = None
         return (g.to(ctx.in_dtype),) + (None,) * 11
 
@@ -549,7 +584,7 @@ class _RaymarchMulti(torch.autograd.Function):
         xs = _storage(x, storage_dtype)
         ctx.weights = None
         if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
-                and interp == FILTER['LINEAR']):
+                and interp == FILTER['LINEAR'] and not _state['deterministic']):
             cur = torch.cuda.current_stream(xs.device)
             side = _side_stream(xs.device)
             side.wait_stream(cur)
@@ -573,7 +608,7 @@ class _RaymarchMulti(torch.autograd.Function):
             ws, ev = ctx.weights
             torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_multi_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, shapes, interp, boundary, blend,
-                                GRAD[get_grad_mode()], weights=ws)
+                                _scatter_gmode(), weights=ws)
         ctx.weights = None
         return (g.to(ctx.in_dtype),) + (None,) * 9
 
@@ -658,7 +693,7 @@ class _RaymarchViews(torch.autograd.Function):
         xs = _storage(x, storage_dtype)
         ctx.weights = None
         if (ctx.needs_input_grad[0] and _state['side_weights'] and get_grad_mode() == 'REFERENCE'
-                and interp == FILTER['LINEAR']):
+                and interp == FILTER['LINEAR'] and not _state['deterministic']):
             cur = torch.cuda.current_stream(xs.device)
             side = _side_stream(xs.device)
             side.wait_stream(cur)
@@ -682,7 +717,7 @@ class _RaymarchViews(torch.autograd.Function):
             ws, ev = ctx.weights
             torch.cuda.current_stream(xs.device).wait_event(ev)
         g = _raymarch_views_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, camera_batch, shapes, interp, boundary,
-                                blend, GRAD[get_grad_mode()], weights=ws)
+                                blend, _scatter_gmode(), weights=ws)
         ctx.weights = None
         return (g.to(ctx.in_dtype),) + (None,) * 10
 
@@ -979,8 +1014,12 @@ def _advect_fwd(d, vx, vy, vz, dt, order, clamp, boundary, ws=None):
     return out
 
 
-def _advect_grad_workspace(shape, order, device):
-    return _workspace(_lib.load().gft_advect_grad_workspace_size(_lib.i64(shape), order), device)
+def _advect_grad_bytes(shape, order, gmode):
+    return int(_lib.load().gft_advect_grad_workspace_size_mode(_lib.i64(shape), order, gmode))
+
+
+def _advect_grad_workspace(shape, order, device, gmode=0):
+    return _workspace(_advect_grad_bytes(shape, order, gmode), device)
 
 
 def _advect_bwd(d, vx, vy, vz, dy, dt, order, clamp, boundary, gmode, ws=None):
@@ -991,7 +1030,7 @@ def _advect_bwd(d, vx, vy, vz, dy, dt, order, clamp, boundary, gmode, ws=None):
     gd = torch.empty(d.shape, dtype=torch.float32, device=d.device)
     gvx, gvy, gvz = (torch.empty(v.shape, dtype=torch.float32, device=d.device) for v in (vx, vy, vz))
     if ws is None:
-        ws = _advect_grad_workspace(d.shape, order, d.device)
+        ws = _advect_grad_workspace(d.shape, order, d.device, gmode)
     with torch.cuda.device(d.device):
         st = lib.gft_advect_grad(_p(d), shape, _p(vx), _p(vy), _p(vz), float(dt), order, clamp, boundary, gmode,
                                  _p(dy), _p(gd), _p(gvx), _p(gvy), _p(gvz), _p(ws), ws.numel(), _stream(d.device))
@@ -1016,7 +1055,7 @@ class _Advect(torch.autograd.Function):
         # semi-Lagrangian grid instead of recomputing it
         ws = None
         if any(ctx.needs_input_grad[:4]) and order == 2 and ds.shape[0] == 1 and ds is d and d.dtype == torch.float32:
-            ws = _advect_grad_workspace(d.shape, order, d.device)
+            ws = _advect_grad_workspace(d.shape, order, d.device, _scatter_gmode())
         y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary, ws=ws)
         # the workspace is a saved tensor, so that checkpointing drops and recomputes it
         ctx.save_for_backward(d, vx, vy, vz, ws)
@@ -1027,7 +1066,9 @@ class _Advect(torch.autograd.Function):
     def backward(ctx, dy):
         d, vx, vy, vz, ws = ctx.saved_tensors
         dt, order, clamp, boundary = ctx.args
-        gmode = GRAD[get_grad_mode()]
+        gmode = _scatter_gmode()
+        if ws is not None and ws.numel() < _advect_grad_bytes(d.shape, order, gmode):
+            ws = None  # the deterministic mode was switched on after the forward: recompute the intermediate
         gd, gvx, gvy, gvz = _advect_bwd(d.float().contiguous(), vx, vy, vz, _cuda(dy, 'output_grad'), dt, order,
                                         clamp, boundary, gmode | (FORWARD_READY if ws is not None else 0), ws=ws)
         return gd.to(d.dtype), gvx.view_as(vx), gvy.view_as(vy), gvz.view_as(vz), None, None, None, None, None

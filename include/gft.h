@@ -159,6 +159,23 @@ gft_status gft_raymarch_grid_transform_grad_stored(
  * geometry and workspace, and skips the pass.  No counterpart in the
  * reference, whose gradient kernel accumulates the sums itself. */
 #define GFT_GRAD_WEIGHTS_READY 0x100
+/* OR'ed into grad_mode of the raymarch gradients (_grad, _grad_stored,
+ * _multi_grad, _views_grad) and of gft_advect_grad: a deterministic adjoint.
+ * No counterpart in the reference, whose gradient scatters accumulate with
+ * floating-point atomics in whatever order the threads arrive, so its
+ * gradients differ from run to run in the last bits.  Here every scatter adds
+ * fixed-point int64 contributions (integer addition does not depend on the
+ * order) whose power-of-two scale comes from a bound on each voxel's partial
+ * sums computed on the GPU from maxima of the inputs; the result is then
+ * converted to fp32.  Gradients are bit-identical from run to run and as
+ * accurate as the float path or more.  Raymarch: BEER_LAMBERT or ADDITIVE
+ * blending (any mode with C == 1), not with GFT_GRAD_WEIGHTS_READY; the
+ * workspace size queries take the flag (larger workspaces; for the advection
+ * gradient gft_advect_grad_workspace_size_mode).  Advection: both lookup
+ * scatters; with GFT_GRAD_FORWARD_READY the workspace must be that size and
+ * hold gft_advect's intermediate at its start as usual.  Non-finite inputs
+ * give a NaN gradient. */
+#define GFT_GRAD_DETERMINISTIC 0x400
 gft_status gft_raymarch_grid_transform_grad_weights(
     const int64_t input_shape[5],
     const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
@@ -329,6 +346,9 @@ gft_status gft_advect_noalloc(
  * lookups. */
 #define GFT_GRAD_FORWARD_READY 0x200
 size_t gft_advect_grad_workspace_size(const int64_t density_shape[5], int32_t order);
+/* The workspace of gft_advect_grad for grad_mode (with its flags): larger with
+ * GFT_GRAD_DETERMINISTIC (int64 scatter targets), else the size above. */
+size_t gft_advect_grad_workspace_size_mode(const int64_t density_shape[5], int32_t order, int32_t grad_mode);
 gft_status gft_advect_grad(
     const float* density, const int64_t density_shape[5],
     const float* vel_x, const float* vel_y, const float* vel_z, float dt,
