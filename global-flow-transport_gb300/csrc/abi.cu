@@ -1390,36 +1390,63 @@ gft_status gft_light_compose_grad(const float* density, const float* transmittan
 
 size_t gft_image_loss_workspace_size(int64_t pixels) {
     if (pixels <= 0) return 0;
-    return align256(sizeof(float) * (size_t)image_loss_blocks(pixels));
+    return align256(sizeof(float) * image_loss_ws_floats(pixels));
+}
+
+static gft_status image_loss_args(const float* image, const float* target, const float background[3], int64_t pixels,
+                                  int32_t tonemap, const void* out) {
+    if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
+    if (pixels > (int64_t(1) << 40)) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count too large");
+    if (!enum_in(tonemap, GFT_TONEMAP_NONE, GFT_TONEMAP_NORMALIZE)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid tonemap");
+    if (!image || !target || !background || !out) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    return GFT_OK;
+}
+
+gft_status gft_image_loss_tonemap(const float* image, const float* target, const float background[3], int64_t pixels,
+                                  int32_t tonemap, float* loss, void* workspace, size_t workspace_bytes,
+                                  void* stream) {
+    gft_status st = image_loss_args(image, target, background, pixels, tonemap, loss);
+    if (st != GFT_OK) return st;
+    if (workspace == nullptr || workspace_bytes < gft_image_loss_workspace_size(pixels))
+        return fail(GFT_ERR_WORKSPACE, "image loss workspace too small");
+    if ((st = check_aligned({image}, 16)) != GFT_OK || (st = check_aligned({target, loss}, 4)) != GFT_OK ||
+        (st = check_workspace_aligned(workspace)) != GFT_OK)
+        return st;
+    if (!launch_image_loss(image, target, pixels, background, tonemap, reinterpret_cast<float*>(workspace), loss,
+                           as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
 }
 
 gft_status gft_image_loss(const float* image, const float* target, const float background[3], int64_t pixels,
                           float* loss, void* workspace, size_t workspace_bytes, void* stream) {
-    if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
-    if (!image || !target || !background || !loss) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
-    if (workspace == nullptr || workspace_bytes < gft_image_loss_workspace_size(pixels))
-        return fail(GFT_ERR_WORKSPACE, "image loss workspace too small");
-    gft_status st;
-    if ((st = check_aligned({image}, 16)) != GFT_OK || (st = check_aligned({target, loss}, 4)) != GFT_OK ||
-        (st = check_workspace_aligned(workspace)) != GFT_OK)
+    return gft_image_loss_tonemap(image, target, background, pixels, GFT_TONEMAP_NONE, loss, workspace,
+                                  workspace_bytes, stream);
+}
+
+gft_status gft_image_loss_tonemap_grad(const float* image, const float* target, const float background[3],
+                                       int64_t pixels, int32_t tonemap, const float* loss_grad, float* image_grad,
+                                       void* workspace, size_t workspace_bytes, void* stream) {
+    gft_status st = image_loss_args(image, target, background, pixels, tonemap, image_grad);
+    if (st != GFT_OK) return st;
+    if (!loss_grad) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    if (tonemap == GFT_TONEMAP_NORMALIZE) {
+        if (workspace == nullptr || workspace_bytes < gft_image_loss_workspace_size(pixels))
+            return fail(GFT_ERR_WORKSPACE, "image loss workspace too small");
+        if ((st = check_workspace_aligned(workspace)) != GFT_OK) return st;
+    }
+    if ((st = check_aligned({image, image_grad}, 16)) != GFT_OK || (st = check_aligned({target, loss_grad}, 4)) != GFT_OK)
         return st;
-    if (!launch_image_loss(image, target, pixels, background, reinterpret_cast<float*>(workspace), loss,
-                           as_stream(stream)))
+    if (!launch_image_loss_grad(image, target, pixels, background, tonemap, reinterpret_cast<float*>(workspace),
+                                loss_grad, image_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }
 
 gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
                                const float* loss_grad, float* image_grad, void* stream) {
-    if (pixels <= 0) return fail(GFT_ERR_INVALID_ARGUMENT, "pixel count must be positive");
-    if (!image || !target || !background || !loss_grad || !image_grad)
-        return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
-    gft_status st;
-    if ((st = check_aligned({image, image_grad}, 16)) != GFT_OK || (st = check_aligned({target, loss_grad}, 4)) != GFT_OK)
-        return st;
-    if (!launch_image_loss_grad(image, target, pixels, background, loss_grad, image_grad, as_stream(stream)))
-        return GFT_ERR_CUDA;
-    return GFT_OK;
+    return gft_image_loss_tonemap_grad(image, target, background, pixels, GFT_TONEMAP_NONE, loss_grad, image_grad,
+                                       nullptr, 0, stream);
 }
 
 }  // extern "C"

@@ -8,8 +8,9 @@
 //                    (lighting.py:236-262), a segmented depth scan;
 //   light compose    out = concat(d * (tr * color + ambient), d) * scale
 //                    (lighting.py:106-121, renderer.py:1012-1030);
-//   image loss       mean((img.rgb + bkg * exp(-img.a) - target)^2) with its
-//                    background composite (renderer.py:1048-1052).
+//   image loss       mean((tone(img.rgb + bkg * exp(-img.a)) - target)^2) with
+//                    its background composite and tonemapping
+//                    (renderer.py:528-541, :632-640, :1048-1052).
 //
 // Elementwise products and sums use __fmul_rn / __fadd_rn so that they round
 // exactly like the separate tensor ops they replace (no FMA contraction).
@@ -189,18 +190,26 @@ bool launch_light_compose_grad(const float* dens, const float* tr, const float* 
 }
 
 // --- image loss ------------------------------------------------------------------
+// loss = mean((tone(img.rgb + bkg * exp(-img.a)) - target)^2) over pixels and
+// rgb.  tone is the renderer's tonemapping (renderer.py:528-541): NONE;
+// CLIP_NEGATIVE max(c, 0); SATURATE clip(c, 0, 1); NORMALIZE over the whole
+// batch: y = c - min(c) where min(c) < 0 (else c), then y / max(y) where
+// max(y) > 0 (else y).  Adjoints follow the frameworks' rules: max(c, 0) and
+// clip pass the gradient where 0 <= c (<= 1); the gradient of a full min / max
+// reduction is shared evenly by the elements equal to it.
 struct Bkg {
     float c[3];
 };
 
-// Per-block partial sums of the squared differences (fixed order), then one
-// block sums the partials in index order: deterministic.
+// Per-block partial sums (fixed order), then one block sums the partials in
+// index order: deterministic.
 constexpr int LOSS_BLOCKS_MAX = 1024;
 
 __device__ __forceinline__ float block_sum(float v, float* sh) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();  // sh may still be read by a previous call
     if (l == 0) sh[w] = v;
     __syncthreads();
     float r = 0.f;
@@ -210,9 +219,91 @@ __device__ __forceinline__ float block_sum(float v, float* sh) {
     return r;
 }
 
+// NaN-propagating min / max (a NaN pixel makes the normalisation NaN, as the
+// tensor reductions do)
+__device__ __forceinline__ float nan_min(float a, float b) { return (b < a || b != b) ? b : a; }
+__device__ __forceinline__ float nan_max(float a, float b) { return (b > a || b != b) ? b : a; }
+
+template <bool MAX>
+__device__ __forceinline__ float block_ext(float v, float* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float x = __shfl_xor_sync(0xffffffffu, v, o);
+        v = MAX ? nan_max(v, x) : nan_min(v, x);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    float r = sh[0];
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = MAX ? nan_max(r, sh[i]) : nan_min(r, sh[i]);
+    }
+    return r;
+}
+
+// Composite of pixel i, channel c, and exp(-alpha)
+__device__ __forceinline__ float composite(float px, float bkg, float e) { return __fadd_rn(px, __fmul_rn(bkg, e)); }
+
+// Statistics of NORMALIZE in the workspace: st[0] = min(c), st[1] = max(y)
+// (max(c) - min(c) where min(c) < 0), st[2] and st[3] the adjoint's shares of
+// the max and min reductions.
+__device__ __forceinline__ float tone(int tm, float c, const float* st) {
+    switch (tm) {
+        case GFT_TONEMAP_CLIP_NEGATIVE: return c < 0.f ? 0.f : c;
+        case GFT_TONEMAP_SATURATE: return c < 0.f ? 0.f : (c > 1.f ? 1.f : c);
+        case GFT_TONEMAP_NORMALIZE: {
+            const float mn = st[0], mx = st[1];
+            const float y = mn < 0.f ? __fadd_rn(c, -mn) : c;
+            return mx > 0.f ? __fdiv_rn(y, mx) : y;
+        }
+        default: return c;
+    }
+}
+
 __global__ void __launch_bounds__(CP_THREADS)
-    k_image_loss_partial(const float* __restrict__ img, const float* __restrict__ tgt, int64_t npix, Bkg bkg,
-                         float* __restrict__ partial) {
+    k_tone_stats_partial(const float* __restrict__ img, int64_t npix, Bkg bkg, float* __restrict__ part) {
+    __shared__ float sh[CP_THREADS / 32];
+    float mn = INFINITY, mx = -INFINITY;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = reinterpret_cast<const float4*>(img)[i];
+        const float e = expf(-a.w);
+        const float px[3] = {a.x, a.y, a.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float v = composite(px[c], bkg.c[c], e);
+            mn = nan_min(mn, v);
+            mx = nan_max(mx, v);
+        }
+    }
+    const float rmn = block_ext<false>(mn, sh);
+    const float rmx = block_ext<true>(mx, sh);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = rmn;
+        part[2 * blockIdx.x + 1] = rmx;
+    }
+}
+
+__global__ void __launch_bounds__(CP_THREADS)
+    k_tone_stats_final(const float* __restrict__ part, int nparts, float* __restrict__ st) {
+    __shared__ float sh[CP_THREADS / 32];
+    float mn = INFINITY, mx = -INFINITY;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        mn = nan_min(mn, part[2 * i]);
+        mx = nan_max(mx, part[2 * i + 1]);
+    }
+    const float rmn = block_ext<false>(mn, sh);
+    const float rmx = block_ext<true>(mx, sh);
+    if (threadIdx.x == 0) {
+        st[0] = rmn;
+        // max over y = c - min is max(c) - min: rounding is monotonic
+        st[1] = rmn < 0.f ? __fadd_rn(rmx, -rmn) : rmx;
+    }
+}
+
+__global__ void __launch_bounds__(CP_THREADS)
+    k_image_loss_partial(const float* __restrict__ img, const float* __restrict__ tgt, int64_t npix, Bkg bkg, int tm,
+                         const float* __restrict__ st, float* __restrict__ partial) {
     __shared__ float sh[CP_THREADS / 32];
     float acc = 0.f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
@@ -221,7 +312,7 @@ __global__ void __launch_bounds__(CP_THREADS)
         const float px[3] = {a.x, a.y, a.z};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float diff = __fadd_rn(__fadd_rn(px[c], __fmul_rn(bkg.c[c], e)), -tgt[i * 3 + c]);
+            const float diff = __fadd_rn(tone(tm, composite(px[c], bkg.c[c], e), st), -tgt[i * 3 + c]);
             acc = fmaf(diff, diff, acc);
         }
     }
@@ -238,10 +329,92 @@ __global__ void __launch_bounds__(CP_THREADS)
     if (threadIdx.x == 0) *loss = r * inv_n;
 }
 
-// d loss / d rgb_c = 2 (rgb_c - t_c) / n; d rgb_c / d a = -bkg_c exp(-a).
+// NORMALIZE adjoint, first pass: with G = d loss / d z = 2 (z - t) / n,
+// per block: sum G z, sum G, #(y == max y), #(c == min c).
 __global__ void __launch_bounds__(CP_THREADS)
-    k_image_loss_grad(const float* __restrict__ img, const float* __restrict__ tgt, int64_t npix, Bkg bkg,
-                      float two_inv_n, const float* __restrict__ gloss, float* __restrict__ gimg) {
+    k_tone_grad_partial(const float* __restrict__ img, const float* __restrict__ tgt, int64_t npix, Bkg bkg,
+                        float two_inv_n, const float* __restrict__ gloss, const float* __restrict__ st,
+                        float* __restrict__ part, unsigned int* __restrict__ cnt) {
+    __shared__ float sh[CP_THREADS / 32];
+    const float gs = __fmul_rn(*gloss, two_inv_n);
+    const float mn = st[0], mx = st[1];
+    float sgz = 0.f, sg = 0.f;
+    unsigned int nmax = 0, nmin = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = reinterpret_cast<const float4*>(img)[i];
+        const float e = expf(-a.w);
+        const float px[3] = {a.x, a.y, a.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float v = composite(px[c], bkg.c[c], e);
+            const float y = mn < 0.f ? __fadd_rn(v, -mn) : v;
+            const float z = mx > 0.f ? __fdiv_rn(y, mx) : y;
+            const float g = __fmul_rn(gs, __fadd_rn(z, -tgt[i * 3 + c]));
+            sgz = fmaf(g, z, sgz);
+            sg += g;
+            nmax += (y == mx) ? 1u : 0u;
+            nmin += (v == mn) ? 1u : 0u;
+        }
+    }
+    const float r0 = block_sum(sgz, sh);
+    const float r1 = block_sum(sg, sh);
+    // counts: exact integer sums, one warp reduction each
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nmax += __shfl_xor_sync(0xffffffffu, nmax, o);
+        nmin += __shfl_xor_sync(0xffffffffu, nmin, o);
+    }
+    __shared__ unsigned int shc[2][CP_THREADS / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        shc[0][w] = nmax;
+        shc[1][w] = nmin;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int a = 0, b = 0;
+        for (int k = 0; k < CP_THREADS / 32; ++k) a += shc[0][k], b += shc[1][k];
+        part[2 * blockIdx.x] = r0;
+        part[2 * blockIdx.x + 1] = r1;
+        cnt[2 * blockIdx.x] = a;
+        cnt[2 * blockIdx.x + 1] = b;
+    }
+}
+
+// st[2] = (d loss / d max y) / #max, st[3] = (d loss / d min c) / #min (0 when
+// that normalisation step is not taken): d loss / d max = -sum G z / max, and
+// d loss / d min = -sum_i d loss / d y_i.
+__global__ void __launch_bounds__(CP_THREADS)
+    k_tone_grad_final(const float* __restrict__ part, const unsigned int* __restrict__ cnt, int nparts,
+                      float* __restrict__ st) {
+    __shared__ float sh[CP_THREADS / 32];
+    float a = 0.f, b = 0.f;
+    unsigned long long na = 0, nb = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    const float sgz = block_sum(a, sh);
+    const float sg = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < nparts; ++i) na += cnt[2 * i], nb += cnt[2 * i + 1];
+        const float mn = st[0], mx = st[1];
+        float gmax = 0.f, gy_sum = sg;
+        if (mx > 0.f) {
+            const float dmx = -sgz / mx;
+            gmax = na > 0 ? dmx / (float)na : 0.f;
+            gy_sum = sg / mx + dmx;
+        }
+        st[2] = gmax;
+        st[3] = (mn < 0.f && nb > 0) ? -gy_sum / (float)nb : 0.f;
+    }
+}
+
+// d loss / d rgb_c = tone'(c) 2 (tone(c) - t_c) / n; d c / d a = -bkg_c exp(-a).
+__global__ void __launch_bounds__(CP_THREADS)
+    k_image_loss_grad(const float* __restrict__ img, const float* __restrict__ tgt, int64_t npix, Bkg bkg, int tm,
+                      const float* __restrict__ st, float two_inv_n, const float* __restrict__ gloss,
+                      float* __restrict__ gimg) {
     const float gs = __fmul_rn(*gloss, two_inv_n);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 a = reinterpret_cast<const float4*>(img)[i];
@@ -250,9 +423,21 @@ __global__ void __launch_bounds__(CP_THREADS)
         float g[3], ga = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float diff = __fadd_rn(__fadd_rn(px[c], __fmul_rn(bkg.c[c], e)), -tgt[i * 3 + c]);
-            g[c] = __fmul_rn(gs, diff);
-            ga = __fadd_rn(ga, __fmul_rn(g[c], bkg.c[c]));
+            const float v = composite(px[c], bkg.c[c], e);
+            const float diff = __fadd_rn(tone(tm, v, st), -tgt[i * 3 + c]);
+            float gc = __fmul_rn(gs, diff);
+            if (tm == GFT_TONEMAP_CLIP_NEGATIVE) {
+                gc = v >= 0.f ? gc : 0.f;
+            } else if (tm == GFT_TONEMAP_SATURATE) {
+                gc = (v >= 0.f && v <= 1.f) ? gc : 0.f;
+            } else if (tm == GFT_TONEMAP_NORMALIZE) {
+                const float mn = st[0], mx = st[1];
+                const float y = mn < 0.f ? __fadd_rn(v, -mn) : v;
+                if (mx > 0.f) gc = __fadd_rn(__fdiv_rn(gc, mx), y == mx ? st[2] : 0.f);
+                if (mn < 0.f && v == mn) gc = __fadd_rn(gc, st[3]);
+            }
+            g[c] = gc;
+            ga = __fadd_rn(ga, __fmul_rn(gc, bkg.c[c]));
         }
         reinterpret_cast<float4*>(gimg)[i] = make_float4(g[0], g[1], g[2], -__fmul_rn(ga, e));
     }
@@ -262,21 +447,48 @@ int image_loss_blocks(int64_t npix) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((npix + CP_THREADS - 1) / CP_THREADS, LOSS_BLOCKS_MAX));
 }
 
-bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], float* partial,
+// ws floats: [0, 4) statistics, [4, 4 + nb) loss partials, then 2 nb floats of
+// the statistics / adjoint partials and 2 nb uint counts
+size_t image_loss_ws_floats(int64_t npix) { return 4 + (size_t)image_loss_blocks(npix) * 5; }
+
+bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], int tonemap, float* ws,
                        float* loss, cudaStream_t st) {
     const int nb = image_loss_blocks(npix);
     const Bkg b{{bkg[0], bkg[1], bkg[2]}};
-    k_image_loss_partial<<<nb, CP_THREADS, 0, st>>>(img, tgt, npix, b, partial);
+    float* stats = ws;
+    float* partial = ws + 4;
+    float* part2 = partial + nb;
+    int n = 2;
+    if (tonemap == GFT_TONEMAP_NORMALIZE) {
+        k_tone_stats_partial<<<nb, CP_THREADS, 0, st>>>(img, npix, b, part2);
+        k_tone_stats_final<<<1, CP_THREADS, 0, st>>>(part2, nb, stats);
+        n += 2;
+    }
+    k_image_loss_partial<<<nb, CP_THREADS, 0, st>>>(img, tgt, npix, b, tonemap, stats, partial);
     k_image_loss_final<<<1, CP_THREADS, 0, st>>>(partial, nb, 1.f / (float)(npix * 3), loss);
-    return launched(2, "image loss launch");
+    return launched(n, "image loss launch");
 }
 
-bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], const float* gloss,
-                            float* gimg, cudaStream_t st) {
+bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], int tonemap,
+                            float* ws, const float* gloss, float* gimg, cudaStream_t st) {
     const Bkg b{{bkg[0], bkg[1], bkg[2]}};
-    k_image_loss_grad<<<grid_for(npix, CP_THREADS), CP_THREADS, 0, st>>>(img, tgt, npix, b,
-                                                                          2.f / (float)(npix * 3), gloss, gimg);
-    return launched(1, "image loss gradient launch");
+    const float two_inv_n = 2.f / (float)(npix * 3);
+    int n = 1;
+    if (tonemap == GFT_TONEMAP_NORMALIZE) {
+        const int nb = image_loss_blocks(npix);
+        float* stats = ws;
+        float* part2 = ws + 4 + nb;
+        unsigned int* cnt = reinterpret_cast<unsigned int*>(part2 + 2 * nb);
+        k_tone_stats_partial<<<nb, CP_THREADS, 0, st>>>(img, npix, b, part2);
+        k_tone_stats_final<<<1, CP_THREADS, 0, st>>>(part2, nb, stats);
+        k_tone_grad_partial<<<nb, CP_THREADS, 0, st>>>(img, tgt, npix, b, two_inv_n, gloss, stats, part2, cnt);
+        k_tone_grad_final<<<1, CP_THREADS, 0, st>>>(part2, cnt, nb, stats);
+        n += 4;
+    }
+    k_image_loss_grad<<<grid_for(npix, CP_THREADS), CP_THREADS, 0, st>>>(img, tgt, npix, b, tonemap,
+                                                                          tonemap == GFT_TONEMAP_NORMALIZE ? ws : nullptr,
+                                                                          two_inv_n, gloss, gimg);
+    return launched(n, "image loss gradient launch");
 }
 
 }  // namespace gft

@@ -190,10 +190,12 @@ bool launch_light_compose(const float* dens, const float* tr, const float* color
 bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
                                float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st);
 int image_loss_blocks(int64_t npix);
-bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], float* partial,
+size_t image_loss_ws_floats(int64_t npix);
+bool launch_image_loss(const float* img, const float* tgt, int64_t npix, const float bkg[3], int tonemap, float* ws,
                        float* loss, cudaStream_t st);
-bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], const float* gloss,
-                            float* gimg, cudaStream_t st);
+// ws: the workspace of the forward's size (only NORMALIZE uses it)
+bool launch_image_loss_grad(const float* img, const float* tgt, int64_t npix, const float bkg[3], int tonemap,
+                            float* ws, const float* gloss, float* gimg, cudaStream_t st);
 
 // FP64 check step (check.cu): double-precision camera inverses per pair
 struct CamD {

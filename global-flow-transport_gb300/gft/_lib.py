@@ -65,6 +65,8 @@ _SIGS = {
     'gft_image_loss_workspace_size': (_SZ, [ctypes.c_int64]),
     'gft_image_loss': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _SZ, _P]),
     'gft_image_loss_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),
+    'gft_image_loss_tonemap': (_I32, [_P, _P, _P, ctypes.c_int64, _I32, _P, _P, _SZ, _P]),
+    'gft_image_loss_tonemap_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _I32, _P, _P, _P, _SZ, _P]),
     'gft_transmittance_check': (_I32, [_P, _P, _I64P, _I32, _P, _P]),
     'gft_raymarch_check': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _P, _I32, _P, _P]),
     'gft_raymarch_grid_transform_multi': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,

@@ -32,7 +32,7 @@ class TransportChain:
                 rgb = img[..., :3] + s.bkg * torch.exp(-img[..., 3:])
                 loss = loss + torch.mean((rgb - targets[t]) ** 2)
             else:
-                loss = loss + fused.image_loss(img, targets[t], s.bkg_host)
+                loss = loss + fused.image_loss(img, targets[t], s.bkg_host, getattr(s, "tonemap", "NONE"))
             if t + 1 < self.T:
                 vx, vy, vz = vels[t]
                 d = s.advect(d, vx, vy, vz)

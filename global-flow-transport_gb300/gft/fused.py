@@ -94,45 +94,54 @@ def light_compose(density, transmittance, light_color, ambient, scale, brick=Fal
     return _LightCompose.apply(d, tr, color.detach(), ambient, scale, bool(brick))
 
 
+TONEMAP = {'NONE': 0, 'CLIP_NEGATIVE': 1, 'SATURATE': 2, 'NORMALIZE': 3}
+
+
 class _ImageLoss(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, img, target, bkg):
+    def forward(ctx, img, target, bkg, tonemap):
         lib = _lib.load()
         npix = img.numel() // 4
         loss = torch.empty((), dtype=torch.float32, device=img.device)
         ws = _workspace(lib.gft_image_loss_workspace_size(npix), img.device)
         with torch.cuda.device(img.device):
-            _lib.check(lib.gft_image_loss(_p(img), _p(target), _p(bkg), npix, _p(loss), _p(ws), ws.numel(),
-                                          _stream(img.device)), 'ImageLoss')
-        ctx.save_for_backward(img, target)
+            _lib.check(lib.gft_image_loss_tonemap(_p(img), _p(target), _p(bkg), npix, tonemap, _p(loss), _p(ws),
+                                                  ws.numel(), _stream(img.device)), 'ImageLoss')
+        ctx.save_for_backward(img, target, ws)
         ctx.bkg = bkg
+        ctx.tonemap = tonemap
         return loss
 
     @staticmethod
     def backward(ctx, g):
-        img, target = ctx.saved_tensors
+        img, target, ws = ctx.saved_tensors
         lib = _lib.load()
         gi = torch.empty_like(img)
         g = g.contiguous()
         with torch.cuda.device(img.device):
-            _lib.check(lib.gft_image_loss_grad(_p(img), _p(target), _p(ctx.bkg), img.numel() // 4, _p(g), _p(gi),
-                                               _stream(img.device)), 'ImageLossGrad')
-        return gi, None, None
+            _lib.check(lib.gft_image_loss_tonemap_grad(_p(img), _p(target), _p(ctx.bkg), img.numel() // 4,
+                                                       ctx.tonemap, _p(g), _p(gi), _p(ws), ws.numel(),
+                                                       _stream(img.device)), 'ImageLossGrad')
+        return gi, None, None, None
 
 
-def image_loss(image, target, background):
-    """mean((image[..., :3] + background * exp(-image[..., 3:]) - target) ** 2)
+def image_loss(image, target, background, tonemap='NONE'):
+    """mean((tone(image[..., :3] + background * exp(-image[..., 3:])) - target) ** 2)
     for image [..., 4], target [..., 3] and a background colour of 3 floats
     (host values; a CUDA tensor is copied to the host, which a CUDA-graph
-    capture does not allow)."""
+    capture does not allow).  tonemap: the renderer's tonemapping, 'NONE',
+    'CLIP_NEGATIVE', 'SATURATE' or 'NORMALIZE' (over all pixels of the call)."""
     img = _cuda(image, 'image')
     tgt = _cuda(target, 'target')
     if img.shape[-1] != 4 or tuple(tgt.shape) != tuple(img.shape[:-1]) + (3,):
         raise _lib.GftInvalidArgument('image must be [..., 4] and target [..., 3] of the same pixels')
+    tm = str(tonemap).upper()
+    if tm not in TONEMAP:
+        raise _lib.GftInvalidArgument('unknown tonemapping %r' % (tonemap,))
     if isinstance(background, torch.Tensor):
         background = background.detach().cpu().numpy()
     bkg = np.ascontiguousarray(np.asarray(background, dtype=np.float32).reshape(3))
-    return _ImageLoss.apply(img, tgt, bkg)
+    return _ImageLoss.apply(img, tgt, bkg, TONEMAP[tm])
 
 
 def transmittance_check(x, tr, column_stride=1, out=None):

@@ -57,8 +57,10 @@ CONFIGS = {
 
 class RenderAdvectStep:
     def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None,
-                 fp64_check=False, check_strides=(7, 257), autotune=False):
+                 fp64_check=False, check_strides=(7, 257), autotune=False, tonemap='NONE'):
         self.config_name = config if isinstance(config, str) else None
+        # tonemapping of the composited images before the loss (renderer.py:639-640)
+        self.tonemap = str(tonemap).upper()
         cfg = dict(CONFIGS[config] if isinstance(config, str) else config)
         if order is not None:
             cfg['order'] = int(order)
@@ -178,9 +180,9 @@ class RenderAdvectStep:
         d = self.advect(d_prev, vx, vy, vz)
         img = self.render(d)
         if self.mode != 'plain':
-            return fused.image_loss(img, target, self.bkg_host)
+            return fused.image_loss(img, target, self.bkg_host, self.tonemap)
         rgb = img[..., :3] + self.bkg * torch.exp(-img[..., 3:])
-        return torch.mean((rgb - target) ** 2)
+        return torch.mean((tonemap_tensor(rgb, self.tonemap) - target) ** 2)
 
     def step(self, d_prev, vx, vy, vz, target):
         """Forward + backward; returns (loss, (g_d_prev, g_vx, g_vy, g_vz))."""
@@ -439,6 +441,22 @@ def centered_lut(vx, vy, vz, dt):
     cz = (vz[:, 1:] + vz[:, :-1]) * 0.5
     v = torch.cat([cx, cy, cz], dim=-1) * (-dt)
     return torch.nn.functional.pad(v, (0, 1))
+
+
+def tonemap_tensor(image, mode='NONE'):
+    """The renderer's tonemapping as tensor ops (phitest/render/renderer.py:528-541)."""
+    if mode == 'NONE':
+        return image
+    if mode == 'CLIP_NEGATIVE':
+        return torch.clamp_min(image, 0)
+    if mode == 'SATURATE':
+        return torch.clamp(image, 0, 1)
+    if mode == 'NORMALIZE':
+        mn = torch.min(image)
+        image = torch.where(mn < 0, image - mn, image)
+        mx = torch.max(image)
+        return torch.where(mx > 0, image / mx, image)
+    raise ValueError(mode)
 
 
 def advect_composed(d, vx, vy, vz, dt=1.0, order=2, clamp='MC_SMOOTH', boundary='CLAMP'):

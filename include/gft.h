@@ -391,6 +391,27 @@ gft_status gft_image_loss(const float* image, const float* target, const float b
                           float* loss, void* workspace, size_t workspace_bytes, void* stream);
 gft_status gft_image_loss_grad(const float* image, const float* target, const float background[3], int64_t pixels,
                                const float* loss_grad, float* image_grad, void* stream);
+/* gft_image_loss_tonemap(_grad): the same loss of the tonemapped composite,
+ * mean((tone(rgb + background * exp(-density)) - target)^2), with the
+ * renderer's tonemapping folded in (phitest/render/renderer.py:528-541,
+ * applied at :639-640): GFT_TONEMAP_NONE; CLIP_NEGATIVE max(c, 0);
+ * SATURATE clip(c, 0, 1); NORMALIZE over all pixels and channels of the call,
+ * c - min(c) where min(c) < 0, then divided by its maximum where that is > 0
+ * (two reductions more; the gradient needs the workspace too, of the same
+ * size, and four more launches).  Gradients: max(c, 0) and clip pass where
+ * 0 <= c (<= 1); a full min / max reduction shares its gradient evenly among
+ * the elements equal to it, as TensorFlow and PyTorch do.  The plain
+ * gft_image_loss(_grad) are the GFT_TONEMAP_NONE case. */
+#define GFT_TONEMAP_NONE 0
+#define GFT_TONEMAP_CLIP_NEGATIVE 1
+#define GFT_TONEMAP_SATURATE 2
+#define GFT_TONEMAP_NORMALIZE 3
+gft_status gft_image_loss_tonemap(const float* image, const float* target, const float background[3], int64_t pixels,
+                                  int32_t tonemap, float* loss, void* workspace, size_t workspace_bytes,
+                                  void* stream);
+gft_status gft_image_loss_tonemap_grad(const float* image, const float* target, const float background[3],
+                                       int64_t pixels, int32_t tonemap, const float* loss_grad, float* image_grad,
+                                       void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- Launch-configuration knobs (no counterpart in the reference) ----
  * Process-wide settings of how some kernels are launched, chosen per workload

@@ -74,6 +74,41 @@ def test_image_loss(fused):
     assert float(fused.image_loss(a, tgt, bkg)) == float(loss)
 
 
+@pytest.mark.parametrize('mode', ['NONE', 'CLIP_NEGATIVE', 'SATURATE', 'NORMALIZE'])
+@pytest.mark.parametrize('ties', [False, True])
+def test_image_loss_tonemap(fused, mode, ties):
+    """The loss with the renderer's tonemapping folded in against the FP64
+    oracle and against the tensor-op composition (pipeline.tonemap_tensor):
+    values below 0 and above 1, and (ties) repeated extrema and pixels exactly
+    at the clip points, where the gradient is shared / passed as autograd
+    does."""
+    from gft.pipeline import tonemap_tensor
+    from oracle import tonemap as TM
+    g = torch.Generator().manual_seed(8)
+    img0 = torch.rand((5, 27, 48, 4), generator=g) * 1.6 - 0.5
+    img0[..., 3] = img0[..., 3].abs()
+    if ties:
+        img0[0, 0, 0, :] = torch.tensor([3.0, -2.0, 0.0, 0.0])
+        img0[3, 5, 7, :] = torch.tensor([3.0, -2.0, 0.0, 0.0])   # same composite: tied max (r), tied min (g)
+        img0[1, 2, 3, :] = torch.tensor([0.0, 0.5, 0.0, 0.0])    # composite r = 0, g = 1: the clip points
+    img0 = img0.cuda()
+    tgt = torch.rand((5, 27, 48, 3), generator=g).cuda()
+    bkg_host = np.array([0.0, 0.5, 1.0], np.float32)
+    bkg = torch.from_numpy(bkg_host).cuda()
+    a = img0.clone().requires_grad_(True)
+    loss = fused.image_loss(a, tgt, bkg_host, tonemap=mode)
+    (loss * 3.0).backward()
+    b = img0.clone().requires_grad_(True)
+    ref = torch.mean((tonemap_tensor(b[..., :3] + bkg * torch.exp(-b[..., 3:]), mode) - tgt) ** 2)
+    (ref * 3.0).backward()
+    l64, g64 = TM.image_loss(_np(img0), _np(tgt), bkg_host, mode)
+    assert abs(float(loss) - l64) <= 1e-5 * abs(l64)
+    assert abs(float(loss) - float(ref)) <= 1e-6 * abs(float(ref))
+    assert rel_l2(_np(a.grad), 3.0 * g64) <= 1e-5
+    assert rel_l2(_np(a.grad), _np(b.grad)) <= 1e-6
+    assert float(fused.image_loss(a, tgt, bkg_host, tonemap=mode)) == float(loss)
+
+
 def test_fused_argument_errors(fused):
     from gft import _lib
     with pytest.raises(_lib.GftInvalidArgument):
@@ -83,3 +118,6 @@ def test_fused_argument_errors(fused):
                             torch.zeros((4, 4, 4, 3), device='cuda'), 0.5, 1.0)
     with pytest.raises(_lib.GftInvalidArgument):
         fused.image_loss(torch.zeros((2, 3, 4), device='cuda'), torch.zeros((2, 3, 4), device='cuda'), [0, 0, 0])
+    with pytest.raises(_lib.GftInvalidArgument):
+        fused.image_loss(torch.zeros((2, 3, 4), device='cuda'), torch.zeros((2, 3, 3), device='cuda'), [0, 0, 0],
+                         tonemap='GAMMA')

@@ -213,6 +213,25 @@ def test_misaligned_pointers_are_rejected(lib):
     assert st == lib.ERR_INVALID_ARGUMENT and b'aligned' in L.gft_last_error()
 
 
+def test_tonemap_and_deterministic_arguments(lib):
+    """Argument checks of the tonemapped image loss and the deterministic
+    advection workspace, rejected before any launch."""
+    L = lib.load()
+    buf = np.zeros(4096, np.float32)
+    al = buf.ctypes.data + (-buf.ctypes.data) % 256
+    bkg = np.zeros(3, np.float32).ctypes.data_as(ctypes.c_void_p)
+    st = L.gft_image_loss_tonemap(al, al, bkg, 16, 4, al, al, 1 << 20, None)
+    assert st == lib.ERR_INVALID_ARGUMENT and b'tonemap' in L.gft_last_error()
+    st = L.gft_image_loss_tonemap_grad(al, al, bkg, 16, 3, al, al, None, 0, None)
+    assert st == lib.ERR_WORKSPACE
+    assert L.gft_image_loss_workspace_size(16) >= 4 * (4 + 5)
+    shape = lib.i64([1, 16, 20, 12, 1])
+    base = L.gft_advect_grad_workspace_size(shape, 2)
+    assert L.gft_advect_grad_workspace_size_mode(shape, 2, 0) == base
+    assert L.gft_advect_grad_workspace_size_mode(shape, 2, 0x400) > base
+    assert L.gft_advect_grad_workspace_size_mode(shape, 2, 0x400 | 1) >= 16 * 20 * 12 * (6 * 4 + 3 * 4 + 2 * 4)
+
+
 def test_workspace_sizes(lib):
     L = lib.load()
     s = lib.i64([2, 16, 20, 12, 2])

@@ -189,3 +189,41 @@ def test_step_oracle_forward_is_the_render_composition():
                             sc['depth_step'], cut_alpha=False)
     ref = np.concatenate(imgs, 0)
     assert np.max(np.abs(parts['img'] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize('mode', ['NONE', 'CLIP_NEGATIVE', 'SATURATE', 'NORMALIZE'])
+@pytest.mark.parametrize('shift', [0.0, -0.8])
+def test_tonemapped_image_loss_fd(mode, shift):
+    """The image loss through the renderer's tonemapping: gradient against
+    central differences (random values, no ties or kinks within EPS)."""
+    from oracle import tonemap as TM
+    rng = np.random.default_rng(71)
+    img = rng.random((3, 5, 7, 4)) * 1.6 - 0.3
+    img[..., :3] += shift
+    tgt = rng.random((3, 5, 7, 3))
+    bkg = np.array([0.0, 0.5, 1.0])
+    d = rng.standard_normal(img.shape)
+    _, g = TM.image_loss(img, tgt, bkg, mode)
+    fd = _fd(lambda x: TM.image_loss(x, tgt, bkg, mode)[0], img, d)
+    assert abs(np.sum(g * d) - fd) <= 1e-6 * max(abs(fd), 1e-12)
+
+
+@pytest.mark.parametrize('mode', ['CLIP_NEGATIVE', 'SATURATE', 'NORMALIZE'])
+def test_tonemap_ties_and_kinks_follow_tensor_autograd(mode):
+    """At ties of the min / max and at the clip points the oracle's gradient
+    is the one tensor autograd gives (even split among tied extrema; the
+    clip passes at its end points), in float64."""
+    import torch
+    from gft.pipeline import tonemap_tensor
+    from oracle import tonemap as TM
+    rng = np.random.default_rng(72)
+    c = rng.random((4, 6, 3)) * 2.0 - 0.5
+    c[0, 0, 0] = c[1, 2, 1] = c.max() + 0.25    # two maxima
+    c[2, 3, 2] = c[3, 1, 0] = c.min() - 0.25    # two minima
+    c[1, 1, :] = [0.0, 1.0, 0.5]                # the clip points
+    g = rng.standard_normal(c.shape)
+    t = torch.tensor(c, dtype=torch.float64, requires_grad=True)
+    y = tonemap_tensor(t, mode)
+    y.backward(torch.tensor(g))
+    assert np.allclose(y.detach().numpy(), TM.tonemap(c, mode), rtol=0, atol=1e-15)
+    assert np.allclose(t.grad.numpy(), TM.tonemap_grad(c, g, mode), rtol=1e-12, atol=1e-15)
