@@ -415,7 +415,8 @@ __global__ void __launch_bounds__(AD_THREADS)
                   const unsigned int* __restrict__ cnt2, float* __restrict__ gd_sc, unsigned int* __restrict__ cnt3,
                   float* __restrict__ glut, bool first, const unsigned long long* __restrict__ iacc_in,
                   const float* __restrict__ iscale_in, unsigned long long* __restrict__ iacc_out,
-                  const float* __restrict__ iscale_out) {
+                  const float* __restrict__ iscale_out, float* __restrict__ gvx, float* __restrict__ gvy,
+                  float* __restrict__ gvz) {
     const int64_t nv = voxels(dm), t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = t0 < nv;  // lanes past the end stay for the merged scatter
     const int64_t t = in ? t0 : nv - 1;
@@ -463,15 +464,32 @@ __global__ void __launch_bounds__(AD_THREADS)
         sz += gf.v[i] * ddz.v[i];
     }
     float* gl = glut + t;  // three planes (x, y, z components) of nv floats
-    if (first) {           // the slice's first lookup-gradient term: written, not added
-        gl[0] = sx;
-        gl[nv] = sy;
-        gl[2 * nv] = sz;
-    } else {
-        gl[0] += sx;
-        gl[nv] += sy;
-        gl[2 * nv] += sz;
+    if (!first) {
+        sx += gl[0];
+        sy += gl[nv];
+        sz += gl[2 * nv];
     }
+    if (gvx != nullptr) {
+        // the last slice: the velocity gradient directly.  g_centred = -dt
+        // g_lut, and the adjoint of the face average gives each of the cell's
+        // two faces per axis half of it.  Every face receives at most two
+        // additions into the zeroed gradient, whose sum does not depend on
+        // their order.
+        const float h = -0.5f * dt;
+        const int64_t rx = ((int64_t)z * dm.y + y) * (dm.x + 1) + x;
+        const int64_t ry = ((int64_t)z * (dm.y + 1) + y) * dm.x + x;
+        const float ax = h * sx, ay = h * sy, az = h * sz;
+        atomicAdd(gvx + rx, ax);
+        atomicAdd(gvx + rx + 1, ax);
+        atomicAdd(gvy + ry, ay);
+        atomicAdd(gvy + ry + dm.x, ay);
+        atomicAdd(gvz + t, az);
+        atomicAdd(gvz + t + (int64_t)dm.x * dm.y, az);
+        return;
+    }
+    gl[0] = sx;  // the slice's lookup-gradient terms, added to the earlier slices'
+    gl[nv] = sy;
+    gl[2 * nv] = sz;
 }
 
 // Stage D: density gradient = direct term + (normalised) forward-lookup scatter.
@@ -501,7 +519,8 @@ __global__ void k_adv_bwd_density(float* __restrict__ gd, const float* __restric
     store<C>(gd, t, vadd(loadf<C>(gd, t), sc));
 }
 
-// Velocity gradient: g_centred = -dt * g_lut, then the adjoint of the face
+// Velocity gradient of the deterministic adjoint (the float adjoint adds it in
+// its last kernel): g_centred = -dt * g_lut, then the adjoint of the face
 // average (each face receives half of both adjacent cells).  glut holds the
 // lookup gradient as three planes (x, y, z components) of voxels(dm) floats.
 __global__ void k_adv_bwd_velocity(const float* __restrict__ glut, Dims dm, float dt, float* __restrict__ gvx,
@@ -612,7 +631,8 @@ static bool adv_bwd_det(const AdvectArgs& a, bool forward_ready, const float* dy
             k_adv_det_scale<<<1, 1, 0, s>>>(maxbits + 1, (double)nv, scale + 1);
             k_adv_bwd_fwd<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
                                                                    gdir, nullptr, cnt2, nullptr, cnt3, glut, false,
-                                                                   acc2, scale, acc3, scale + 1);
+                                                                   acc2, scale, acc3, scale + 1, nullptr, nullptr,
+                                                                   nullptr);
             n += 6;
         } else {
             if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
@@ -621,7 +641,7 @@ static bool adv_bwd_det(const AdvectArgs& a, bool forward_ready, const float* dy
             k_adv_bwd_fwd<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
                                                                    a.clamp == CLAMP_NEGATIVE, dyb, nullptr, nullptr,
                                                                    nullptr, cnt3, glut, b == 0, nullptr, nullptr,
-                                                                   acc3, scale + 1);
+                                                                   acc3, scale + 1, nullptr, nullptr, nullptr);
             n += 3;
         }
         k_adv_bwd_density<C, COUNT, true><<<blocks, T, 0, s>>>(gdb, nullptr, cnt3, nv, acc3, scale + 1);
@@ -652,9 +672,17 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
     unsigned int* cnt2 = PACK ? nullptr : reinterpret_cast<unsigned int*>(glut + (size_t)nv * 3);
     unsigned int* cnt3 = PACK ? nullptr : cnt2 + nv;
     // glut: slice 0's first kernel writes every voxel's lookup gradient, the
-    // later kernels and slices add to it (no zeroing pass)
+    // later kernels and slices add to it (no zeroing pass); the last slice's
+    // final kernel adds its terms into the velocity faces instead
+    const size_t nfx = (size_t)(a.d.x + 1) * a.d.y * a.d.z, nfy = (size_t)a.d.x * (a.d.y + 1) * a.d.z,
+                 nfz = (size_t)a.d.x * a.d.y * (a.d.z + 1);
+    if (!cuda_ok(cudaMemsetAsync(gvx, 0, sizeof(float) * nfx, s), "zero velocity gradient") ||
+        !cuda_ok(cudaMemsetAsync(gvy, 0, sizeof(float) * nfy, s), "zero velocity gradient") ||
+        !cuda_ok(cudaMemsetAsync(gvz, 0, sizeof(float) * nfz, s), "zero velocity gradient"))
+        return false;
     const float* dens = reinterpret_cast<const float*>(a.density);
     for (int b = 0; b < a.N; ++b) {
+        const bool last = b == a.N - 1;
         const float* db = dens + (size_t)b * vc;
         const float* dyb = dy + (size_t)b * vc;
         float* gdb = gd + (size_t)b * vc;
@@ -672,22 +700,20 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
                                                               nullptr, nullptr);
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
                                                                      gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut, false,
-                                                             nullptr, nullptr, nullptr, nullptr);
+                                                             nullptr, nullptr, nullptr, nullptr,
+                                                             last ? gvx : nullptr, gvy, gvz);
         } else {
             if (!cuda_ok(cudaMemsetAsync(gdb, 0, sizeof(float) * vc, s), "zero gradient")) return false;
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, true,
                                                                      a.clamp == CLAMP_NEGATIVE, dyb, nullptr,
                                                                      nullptr, gd_sc, cnt3, glut, b == 0, nullptr,
-                                                             nullptr, nullptr, nullptr);
+                                                             nullptr, nullptr, nullptr, last ? gvx : nullptr, gvy,
+                                                             gvz);
         }
         k_adv_bwd_density<C, COUNT><<<blocks, T, 0, s>>>(gdb, gd_sc, cnt3, nv, nullptr, nullptr);
         if (!launched(a.order == 2 ? (forward_ready ? 3 : 4) : 2, "advect gradient launch")) return false;
     }
-    const int64_t nstag = (int64_t)(a.d.x + 1) * a.d.y * a.d.z + (int64_t)a.d.x * (a.d.y + 1) * a.d.z +
-                          (int64_t)a.d.x * a.d.y * (a.d.z + 1);
-    k_adv_bwd_velocity<<<(unsigned)((nstag + T - 1) / T), T, 0, s>>>(glut, a.d, a.dt, gvx,
-                                                                                                 gvy, gvz);
-    return launched(1, "velocity gradient launch");
+    return true;
 }
 
 template <int C, int BM>

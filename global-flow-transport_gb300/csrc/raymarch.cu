@@ -422,12 +422,12 @@ __device__ __forceinline__ unsigned zero_weight_mask(float fx, float fy, float f
 // accumulate into one gradient) and skips corners with no weight.  Zero-weight
 // contributions are skipped; the ceil corner is floor + 1 (the reference's
 // ceil(p) equals floor(p) only where the ceil weight is 0).
-// iacc != nullptr (deterministic adjoint): the corner sums go, scaled by the
+// DET (deterministic adjoint): the corner sums go, scaled by the
 // power of two iscale and rounded to integers, into int64 accumulators
 // (MODE 2: one per brick cell of the pair; MODE 0/1: C per cell of the batch
 // slice) instead of the float reductions; integer addition is associative, so
 // the sums do not depend on the order in which the warps add them.
-template <int C, int BM, int MODE, int L>
+template <int C, int BM, int MODE, int L, bool DET = false>
 __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
                                              bool act, float px, float py, float pz, Vec<C> val,
                                              unsigned long long* __restrict__ iacc = nullptr, float iscale = 0.f) {
@@ -467,14 +467,19 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
             for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? w[k] : w[k] * val.v[c];
     }
     if constexpr (MODE == 2) {
-        // Weight sums: a member's 8 sums are its own weights (members never
-        // accumulate), so the head pulls them as they are; zero weights add 0.
-        nz = 0xffu;
+        // Weight sums: the head pulls each member's three fractions (not its
+        // eight weights: shuffles are the scarcer issue slots) and adds the
+        // member's corner weights; corners no member weights are skipped, as
+        // in the adjoint that these sums normalise.
         for (int r = 1; r <= rounds; ++r) {
+            const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
+                        mz = __shfl_down_sync(0xffffffffu, wz, r);
+            if (r <= n) {
+                nz |= zero_weight_mask(mx, my, mz);
+                float w[8];
+                corner_weights(mx, my, mz, w);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const float t = __shfl_down_sync(0xffffffffu, acc[k][0], r);
-                if (r <= n) acc[k][0] += t;
+                for (int k = 0; k < 8; ++k) acc[k][0] += w[k];
             }
         }
     } else {
@@ -535,7 +540,7 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
         Vec<C> a;
 #pragma unroll
         for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];
-        if (iacc != nullptr) {
+        if constexpr (DET) {
             if constexpr (MODE == 2) {
                 atomicAdd(iacc + bi, (unsigned long long)__float2ll_rn(a.v[0] * iscale));
             } else {
@@ -579,7 +584,7 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 // full.  (Non-finite adjoints are not propagated through skipped samples.)
 // Every lane stays in the loop to its warp's last step (scatter_step is
 // warp-collective); lanes without a sample at a step pass act = false.
-template <int C, typename S, int BM, int MODE, int L>
+template <int C, typename S, int BM, int MODE, int L, bool DET>
 __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, Dims din, int blend_mode,
                                                       const float* __restrict__ out, const float* __restrict__ dout,
                                                       float* __restrict__ grad, const float* __restrict__ cnt,
@@ -590,8 +595,8 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
     const bool live = ray_pixel(tab, r);
     const int p = r.p, x = r.x, y = r.y, W = r.W, H = r.H, D = r.D;
     unsigned long long* idst =
-        iacc == nullptr ? nullptr
-        : MODE == 2     ? iacc + (size_t)(tab.pair_base + p) * brick_cells(din)
+        !DET        ? nullptr
+        : MODE == 2 ? iacc + (size_t)(tab.pair_base + p) * brick_cells(din)
                         : iacc + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     float3 farp, step, nearp;
     ray_far_step(tab.cam[p], x, y, W, H, D, farp, step, nearp);
@@ -657,14 +662,14 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             }
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
-        scatter_step<C, BM, MODE, L>(dst, count, din, on, px, py, pz, val, idst, iscale);
+        scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);
     }
 }
 
 // At least 6 resident blocks per SM: the tile loop would otherwise take 90
 // registers (5 blocks); with the bound it stays at the 80 of one tile per
 // block, without spills.
-template <int C, typename S, int BM, int MODE, int L>
+template <int C, typename S, int BM, int MODE, int L, bool DET = false>
 __global__ void __launch_bounds__(RM_BX* RM_BY, 6)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
@@ -672,10 +677,10 @@ __global__ void __launch_bounds__(RM_BX* RM_BY, 6)
                        const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
     // integer accumulation: MODE 2 with the host's weight scale, the adjoint
     // with the scale its bound kernel wrote
-    const float iscale = iacc == nullptr ? 0.f : MODE == 2 ? wscale : *iscale_ptr;
+    const float iscale = !DET ? 0.f : MODE == 2 ? wscale : *iscale_ptr;
     const int tiles = tab.tile0[tab.n];
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
-        raymarch_scatter_tile<C, S, BM, MODE, L>(in, din, blend_mode, out, dout, grad, cnt, iacc, iscale, st, tab,
+        raymarch_scatter_tile<C, S, BM, MODE, L, DET>(in, din, blend_mode, out, dout, grad, cnt, iacc, iscale, st, tab,
                                                  tile);
 }
 
@@ -727,12 +732,20 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
 template <int C, typename S, int BM, int L>
 static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
                            const float* dout, float* grad, const float* cnt, const PairTable& t) {
-    if (exact)
+    if (a.det) {
+        if (exact)
+            k_raymarch_scatter<C, S, BM, 0, L, true><<<grid, block, 0, s>>>(
+                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
+        else
+            k_raymarch_scatter<C, S, BM, 1, L, true><<<grid, block, 0, s>>>(
+                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
+    } else if (exact) {
         k_raymarch_scatter<C, S, BM, 0, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
-    else
+                                                                     cnt, nullptr, nullptr, 0.f, a.store, t);
+    } else {
         k_raymarch_scatter<C, S, BM, 1, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
+                                                                     cnt, nullptr, nullptr, 0.f, a.store, t);
+    }
 }
 
 template <int C, typename S, int BM>
@@ -757,8 +770,12 @@ static void bwd_dispatch_bm(bool exact, dim3 grid, dim3 block, cudaStream_t s, c
 template <int BM>
 static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, float* cnt,
                              unsigned long long* wacc, float wscale, const PairTable& t) {
-    k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(
-        nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, wacc, nullptr, wscale, RaymarchArgs::Store{}, t);
+    if (wacc != nullptr)
+        k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT, true><<<grid, block, 0, s>>>(
+            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, wacc, nullptr, wscale, RaymarchArgs::Store{}, t);
+    else
+        k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(
+            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, 0.f, RaymarchArgs::Store{}, t);
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel), 16
