@@ -272,14 +272,16 @@ def test_captured_step_bit_reproducible(ops, storage):
     with ops.deterministic():
         s = RenderAdvectStep('tiny', torch.device('cuda', 0), storage_dtype=storage)
         s.setup_static(s.make_inputs())
-        loss_e, grads_e = s.run_static()
-        grads_e = [g.clone() for g in grads_e]
         s.capture(warmup=3)
-    runs = []
-    for _ in range(RUNS):
-        loss, grads = s.replay()
+        runs = []
+        for _ in range(RUNS):
+            loss, grads = s.replay()
+            torch.cuda.synchronize()
+            runs.append([loss.clone()] + [g.clone() for g in grads])
+        # the same step run eagerly (outside the graph) gives the same bits
+        loss_e, grads_e = s.step(s.s_d, s.s_vx, s.s_vy, s.s_vz, s.s_t)
         torch.cuda.synchronize()
-        runs.append([loss.clone()] + [g.clone() for g in grads])
     assert _all_equal(runs)
+    assert torch.equal(runs[0][0], loss_e.detach())
     for a, b in zip(runs[0][1:], grads_e):
         assert torch.equal(a, b)
