@@ -319,6 +319,17 @@ size_t gft_raymarch_grid_transform_samples_size(const int64_t input_shape[5], in
     return align256(raymarch_store_bytes(pairs, (int)input_shape[4], (int)input_shape[0], dims_of(input_shape)));
 }
 
+size_t gft_raymarch_grid_transform_samples_min_size(const int64_t input_shape[5], int32_t num_cameras,
+                                                    const int32_t output_shape[3], int32_t separate_camera_batch) {
+    std::string why;
+    if (!grid_shape_ok(input_shape, why) || !channels_ok(input_shape[4]) || output_shape == nullptr ||
+        output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1 || num_cameras < 1)
+        return 0;
+    std::vector<Pair> pairs((size_t)input_shape[0] * (separate_camera_batch ? (size_t)num_cameras : 1));
+    set_uniform_images(pairs, output_shape[0], output_shape[1], output_shape[2]);
+    return align256(raymarch_store_min_bytes(pairs, (int)input_shape[0], dims_of(input_shape)));
+}
+
 static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
                                     const float* matrix_m, int32_t num_m, const float* matrix_v,
                                     const float* matrix_p, const float* frustum, int32_t num_cameras,
@@ -361,14 +372,14 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
     if (samples != nullptr) {
-        if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
+        if (samples_bytes < raymarch_store_min_bytes(pairs, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
     }
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
         (st = check_aligned({output}, vec_bytes(a.C, 0))) != GFT_OK || (st = check_workspace_aligned(samples)) != GFT_OK)
         return st;
     if (samples != nullptr) {
-        a.store = raymarch_store_layout(samples, pairs, a.C, a.N, a.din);
+        a.store = raymarch_store_layout(samples, samples_bytes, pairs, a.C, a.N, a.din);
         if (!launch_raymarch_occupancy(a, as_stream(stream))) return GFT_ERR_CUDA;
     }
     if (!launch_raymarch_fwd(a, pairs, output, as_stream(stream))) return GFT_ERR_CUDA;
@@ -492,9 +503,9 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     a.n_slots = (int)pairs.size();
     a.det = det;
     if (samples != nullptr) {
-        if (samples_bytes < raymarch_store_bytes(pairs, a.C, a.N, a.din))
+        if (samples_bytes < raymarch_store_min_bytes(pairs, a.N, a.din))
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
-        a.store = raymarch_store_layout(const_cast<float*>(samples), pairs, a.C, a.N, a.din);
+        a.store = raymarch_store_layout(const_cast<float*>(samples), samples_bytes, pairs, a.C, a.N, a.din);
     }
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
         (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||

@@ -99,8 +99,12 @@ struct RaymarchArgs {
     // Sample store (LINEAR only): the forward writes the samples it blends, the
     // adjoint reads them instead of re-sampling (store.samples != nullptr).
     struct Store {
-        float* samples = nullptr;     // cells of C floats, sample_index
-        uint32_t* words = nullptr;    // per pair, tile, step and warp: the lanes that stored a sample
+        float* samples = nullptr;     // the pool: cells of C floats
+        uint32_t capacity = 0;        // cells of the pool
+        unsigned long long* count = nullptr;  // pool cells handed out (in chunks)
+        uint32_t* words = nullptr;    // per pair, tile, step and warp: the lanes with a non-zero sample
+        uint32_t* first = nullptr;    // per pair, tile, step and warp: the step's first pool cell, or
+                                      // 0xffffffff where the pool was full
         uint8_t* occ = nullptr;       // per input slice and 4^3-voxel block: 0 = no non-zero voxel in
                                       // the block grown by one voxel at its upper faces
         int nbx = 0, nby = 0, nbz = 0;
@@ -115,8 +119,12 @@ struct RaymarchArgs {
 size_t raymarch_det_bytes(int N, int C, Dims din, size_t pairs);
 // Bytes of the sample store of these pairs (samples, ballot words,
 // occupancy map of the N input slices), and its parts at `base`.
+// a store whose pool holds every sample the launch could store, and the part
+// before the pool (a store of that size keeps no samples)
 size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din);
-RaymarchArgs::Store raymarch_store_layout(void* base, const std::vector<Pair>& pairs, int C, int N, Dims din);
+size_t raymarch_store_min_bytes(const std::vector<Pair>& pairs, int N, Dims din);
+RaymarchArgs::Store raymarch_store_layout(void* base, size_t bytes, const std::vector<Pair>& pairs, int C, int N,
+                                          Dims din);
 // Fills a.store.occ from the input (before the storing forward).
 bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s);
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);

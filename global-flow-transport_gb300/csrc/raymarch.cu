@@ -130,9 +130,23 @@ static unsigned set_ray_tiles(PairTable& t, int64_t* cells = nullptr) {
 // 4^3-voxel block without a non-zero voxel (grown by one voxel at its upper
 // faces, so that it holds every corner of a sample with its base cell in the
 // block) is exactly zero, and the forward neither fetches nor stores it; per
-// warp and step a ballot word records which lanes stored one, and the adjoint
-// reads a sample where its bit is set and uses zero elsewhere.
+// warp and step a ballot word records which lanes have a non-zero sample, and
+// the adjoint uses zero where a lane's bit is clear.
+//
+// The samples go into a pool that warps fill in chunks: a warp takes
+// STORE_CHUNK cells from the store's counter when its current chunk cannot
+// hold a step's samples, writes them at consecutive cells (in lane order) and
+// records the step's first cell beside its ballot word.  A pool smaller than
+// every sample the launch could store is allowed: once a chunk request goes
+// past the pool's end the warp records STORE_OVERFLOW for its remaining steps
+// of the tile, and the adjoint re-samples the grid there.
+//
+// Layout: [counter (one uint64), 256 bytes][ballot words][first cells][occupancy
+// maps][pool]: the words and first cells hold one uint32 per pair, pixel tile,
+// step and warp.
 constexpr int OCC_SHIFT = 2;  // 4^3-voxel occupancy blocks
+constexpr uint32_t STORE_CHUNK = 256;
+constexpr uint32_t STORE_OVERFLOW = 0xffffffffu;
 
 static int64_t store_cells(const std::vector<Pair>& pairs) {
     int64_t f = 0;
@@ -145,37 +159,65 @@ static Dims occ_dims(Dims d) {
 }
 static size_t align256u(size_t n) { return (n + 255) & ~size_t(255); }
 
-size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din) {
+// bytes before the pool
+static size_t store_meta_bytes(const std::vector<Pair>& pairs, int N, Dims din) {
     const int64_t cells = store_cells(pairs);
-    return align256u(sizeof(float) * cells * C) + align256u(sizeof(uint32_t) * (cells / 32)) +
-           align256u((size_t)voxels(occ_dims(din)) * N);
+    return 256 + 2 * align256u(sizeof(uint32_t) * (cells / 32)) + align256u((size_t)voxels(occ_dims(din)) * N);
+}
+size_t raymarch_store_min_bytes(const std::vector<Pair>& pairs, int N, Dims din) {
+    return store_meta_bytes(pairs, N, din);
+}
+// Pool cells that hold every sample the launch could store: a warp abandons a
+// chunk only when a step's samples (at most 32) do not fit its rest, so each
+// abandoned chunk holds at least STORE_CHUNK - 31 samples, and each warp's
+// last chunk of a tile may be mostly empty.
+static int64_t store_pool_full_cells(const std::vector<Pair>& pairs) {
+    int64_t f = 0;
+    for (const Pair& p : pairs) {
+        const int64_t tiles = ray_tiles(p.W, p.H), cells = tiles * p.D * (RM_BX * RM_BY);
+        f += (cells * STORE_CHUNK + (STORE_CHUNK - 32)) / (STORE_CHUNK - 31) +
+             tiles * (RM_BX * RM_BY / 32) * STORE_CHUNK;
+    }
+    return f;
+}
+size_t raymarch_store_bytes(const std::vector<Pair>& pairs, int C, int N, Dims din) {
+    return store_meta_bytes(pairs, N, din) + align256u(sizeof(float) * store_pool_full_cells(pairs) * C);
 }
 
-RaymarchArgs::Store raymarch_store_layout(void* base, const std::vector<Pair>& pairs, int C, int N, Dims din) {
+RaymarchArgs::Store raymarch_store_layout(void* base, size_t bytes, const std::vector<Pair>& pairs, int C, int N,
+                                          Dims din) {
     RaymarchArgs::Store st;
     const int64_t cells = store_cells(pairs);
     char* p = static_cast<char*>(base);
-    st.samples = reinterpret_cast<float*>(p);
-    p += align256u(sizeof(float) * cells * C);
+    st.count = reinterpret_cast<unsigned long long*>(p);
+    p += 256;
     st.words = reinterpret_cast<uint32_t*>(p);
+    p += align256u(sizeof(uint32_t) * (cells / 32));
+    st.first = reinterpret_cast<uint32_t*>(p);
     p += align256u(sizeof(uint32_t) * (cells / 32));
     st.occ = reinterpret_cast<uint8_t*>(p);
     const Dims od = occ_dims(din);
     st.nbx = od.x;
     st.nby = od.y;
     st.nbz = od.z;
+    p += align256u((size_t)voxels(od) * N);
+    st.samples = reinterpret_cast<float*>(p);
+    const size_t meta = store_meta_bytes(pairs, N, din);
+    const uint64_t cap = bytes > meta ? (uint64_t)((bytes - meta) / (sizeof(float) * (size_t)C)) : 0;
+    st.capacity = (uint32_t)std::min<uint64_t>(cap, STORE_OVERFLOW - 1);
     return st;
 }
 
-// Cell index of this lane's step i in the sample store, and of its warp's
-// ballot word (a pair's cells and words start at smp0 and smp0 / 32).
-__device__ __forceinline__ int64_t sample_index(const PairTable& tab, int tile, int p, int D, int i) {
-    const int tid = threadIdx.y * RM_BX + threadIdx.x;
-    return tab.smp0[p] + ((int64_t)(tile - tab.tile0[p]) * D + i) * (RM_BX * RM_BY) + tid;
-}
+// Index of this lane's warp's ballot word (and first cell) for step i (a
+// pair's words start at smp0 / 32).
 __device__ __forceinline__ int64_t sample_word_index(const PairTable& tab, int tile, int p, int D, int i) {
     const int tid = threadIdx.y * RM_BX + threadIdx.x;
     return (tab.smp0[p] >> 5) + ((int64_t)(tile - tab.tile0[p]) * D + i) * (RM_BX * RM_BY / 32) + (tid >> 5);
+}
+
+// Rank of this lane among the set bits of a warp's ballot word.
+__device__ __forceinline__ uint32_t lane_rank(unsigned word, unsigned lane) {
+    return (uint32_t)__popc(word & ((1u << lane) - 1u));
 }
 
 // Occupancy of one input slice per block: a non-zero voxel marks the blocks
@@ -246,9 +288,12 @@ static void occ_launch(const RaymarchArgs& a, cudaStream_t s) {
 bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s) {
     const Dims od{a.store.nbx, a.store.nby, a.store.nbz};
     if (!cuda_ok(cudaMemsetAsync(a.store.occ, 0, (size_t)voxels(od) * a.N, s), "zero occupancy")) return false;
-    // ballot words of steps no warp marches stay 0, so the store is fully defined
-    const size_t words = reinterpret_cast<const char*>(a.store.occ) - reinterpret_cast<const char*>(a.store.words);
-    if (!cuda_ok(cudaMemsetAsync(a.store.words, 0, words, s), "zero sample words")) return false;
+    // ballot words of steps no warp marches stay 0, so the store is fully
+    // defined; the pool counter starts at 0
+    const size_t words = reinterpret_cast<const char*>(a.store.first) - reinterpret_cast<const char*>(a.store.words);
+    if (!cuda_ok(cudaMemsetAsync(a.store.words, 0, words, s), "zero sample words") ||
+        !cuda_ok(cudaMemsetAsync(a.store.count, 0, sizeof(unsigned long long), s), "zero sample counter"))
+        return false;
     const bool brick = a.layout == LAYOUT_BRICK;
     if (a.dtype == 0) {
         if (a.C == 4) brick ? occ_launch<4, float, LAYOUT_BRICK>(a, s) : occ_launch<4, float, LAYOUT_FLAT>(a, s);
@@ -324,28 +369,54 @@ __device__ __forceinline__ void raymarch_fwd_tile(const S* __restrict__ in, Dims
         i1 = -1;
     }
     const uint8_t* occ = storing ? st.occ + (size_t)tab.in_batch[p] * st.nbx * st.nby * st.nbz : nullptr;
+    const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;
+    // the warp's current pool chunk [cur, end) (uniform across the warp);
+    // full: a chunk request went past the pool's end
+    uint32_t cur = 0, end = 0;
+    bool full = false;
     for (int i = w0; i <= w1; ++i) {
-        bool stored = false;
+        bool nonzero = false;
+        Vec<C> smp = vzero<C>();
         if (i >= i0 && i <= i1) {
             const float3 pos = ray_sample(nearp, step, i);
-            Vec<C> smp;
             if constexpr (LIN) {
                 const float qx = pos.x - 0.5f, qy = pos.y - 0.5f, qz = pos.z - 0.5f;
                 const bool empty = storing && sample_empty<BM>(din, qx, qy, qz, occ, st.nbx, st.nby);
-                smp = empty ? vzero<C>() : fetch_linear<C, S, BM, L>(g, din, qx, qy, qz);
-                if (storing && !empty) {
-                    store_stream<C>(st.samples, sample_index(tab, r.tile, p, D, i), smp);
-                    stored = true;
-                }
+                if (!empty) smp = fetch_linear<C, S, BM, L>(g, din, qx, qy, qz);
+                nonzero = storing && !empty;
             } else {
                 smp = fetch<C, S, BM, true>(filter, g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
             }
             acc = blend<C>(blend_mode, acc, smp);
         }
         if (storing) {
-            const unsigned word = __ballot_sync(0xffffffffu, stored);
-            if ((threadIdx.x & 31u) == 0 && (threadIdx.y & 3u) == 0)
-                st.words[sample_word_index(tab, r.tile, p, D, i)] = word;
+            const unsigned word = __ballot_sync(0xffffffffu, nonzero);
+            uint32_t first = STORE_OVERFLOW;
+            if (word != 0u && !full) {
+                const uint32_t n = (uint32_t)__popc(word);
+                if (end - cur < n) {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(st.count, (unsigned long long)STORE_CHUNK);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (base + STORE_CHUNK <= (unsigned long long)st.capacity) {
+                        cur = (uint32_t)base;
+                        end = cur + STORE_CHUNK;
+                    } else {
+                        full = true;
+                    }
+                }
+                if (!full) {
+                    first = cur;
+                    cur += n;
+                }
+            }
+            if (nonzero && first != STORE_OVERFLOW)
+                store_stream<C>(st.samples, (int64_t)(first + lane_rank(word, lane)), smp);
+            if (lane == 0) {
+                const int64_t w = sample_word_index(tab, r.tile, p, D, i);
+                st.words[w] = word;
+                st.first[w] = first;
+            }
         }
     }
     if (!live) return;
@@ -641,7 +712,8 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
     // 480x270x192; capping registers at 64 or 72 spilled and was slower too).
     // Stored samples: step k reads the forward's step i = D - 1 - k: zero
     // outside the forward's range or where the warp's ballot word for that
-    // step has this lane's bit clear, else the stored sample.  (Words are only
+    // step has this lane's bit clear, else the stored sample (re-sampled where
+    // the forward found the pool full).  (Words are only
     // read for steps inside the lane's own forward range, which the forward's
     // warp wrote; a warp's words of consecutive steps share a cache line.)
     const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;
@@ -652,14 +724,23 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
         const float px = pos.x - 0.5f, py = pos.y - 0.5f, pz = pos.z - 0.5f;
         Vec<C> val = vfill<C>(1.f);
         if (MODE != 2 && on) {
-            Vec<C> smp;
+            Vec<C> smp = vzero<C>();
+            bool resample = !use_store;
             if (use_store) {
                 const int i = D - 1 - k;
-                const uint32_t word = i >= s_lo && i <= s_hi ? __ldg(st.words + sample_word_index(tab, r.tile, p, D, i)) : 0u;
-                smp = (word >> lane) & 1u ? load_stream<C>(st.samples, sample_index(tab, r.tile, p, D, i)) : vzero<C>();
-            } else {
-                smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
+                if (i >= s_lo && i <= s_hi) {
+                    const int64_t w = sample_word_index(tab, r.tile, p, D, i);
+                    const uint32_t word = __ldg(st.words + w);
+                    if ((word >> lane) & 1u) {
+                        const uint32_t first = __ldg(st.first + w);
+                        if (first != STORE_OVERFLOW)
+                            smp = load_stream<C>(st.samples, (int64_t)(first + lane_rank(word, lane)));
+                        else
+                            resample = true;  // the pool was full: not stored
+                    }
+                }
             }
+            if (resample) smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
         scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);

@@ -51,6 +51,7 @@ _SIGS = {
     'gft_raymarch_grid_transform_store': (_I32, [_P, _I32, _I64P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                                  _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
     'gft_raymarch_grid_transform_samples_size': (_SZ, [_I64P, _I32, _I32P, _I32]),
+    'gft_raymarch_grid_transform_samples_min_size': (_SZ, [_I64P, _I32, _I32P, _I32]),
     'gft_raymarch_grid_transform_grad_stored': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                                        _I32, _I32, _I32, _I32, _I32, _P, _SZ, _P, _P, _SZ, _P]),
     'gft_raymarch_grid_transform_grad_workspace_size': (_SZ, [_I64P, _I32, _I32, _I32]),

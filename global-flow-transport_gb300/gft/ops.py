@@ -22,7 +22,8 @@ COORD = {'TRANSFORM_LINDEPTH': 0, 'TRANSFORM_LINDEPTH_REVERSE': 1, 'TRANSFORM': 
 GRAD = {'REFERENCE': 0, 'EXACT': 1}
 CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
 
-_state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True, 'deterministic': False}
+_state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True, 'sample_pool': 0.25,
+          'deterministic': False}
 DETERMINISTIC = 0x400  # GFT_GRAD_DETERMINISTIC
 
 
@@ -212,31 +213,45 @@ def _grid5(x, grid):
     return (x.shape[0],) + tuple(int(v) for v in grid) + (x.shape[-1],), _dtype_code(x) | LAYOUT_BRICK
 
 
-def set_raymarch_sample_store(enabled):
+def set_raymarch_sample_store(enabled, pool_fraction=None):
     """The differentiable raymarch stores the samples its forward blends and
-    its backward reads them instead of re-sampling the grid (default on; one
-    float per channel, depth sample and pixel of each camera, about 2 GB at
-    5 views of 480x270 with 192 samples and 4 channels, held from the forward
-    to the backward)."""
+    its backward reads them instead of re-sampling the grid (default on).  The
+    store holds the samples that can be non-zero, in a pool sized at
+    ``pool_fraction`` (default 0.25) of every sample the cameras could store;
+    samples beyond it are re-sampled by the backward.  The store lives from
+    the forward to the backward."""
     _state['sample_store'] = bool(enabled)
+    if pool_fraction is not None:
+        f = float(pool_fraction)
+        if not 0.0 <= f <= 1.0:
+            raise ValueError('pool_fraction must lie in [0, 1]')
+        _state['sample_pool'] = f
+
 
 
 def stored_sample_count(samples, shape5, nv, out_shape, separate=True):
-    """Samples a storing raymarch forward wrote into ``samples`` (the set bits
-    of its per-warp ballot words, which follow the 256-byte aligned sample
-    cells: per camera, 8x16-pixel tile, depth sample and lane)."""
+    """Samples with a non-zero ballot bit in a store a forward filled (stored,
+    or re-sampled by the backward where the pool was full)."""
     D, H, W = out_shape
     pairs = shape5[0] * (nv if separate else 1)
     cells = pairs * ((W + 7) // 8) * ((H + 15) // 16) * D * 128
-    off = (cells * shape5[4] * 4 + 255) // 256 * 256
-    words = samples.view(torch.uint8)[off:off + cells // 8].cpu().numpy()
+    words = samples.view(torch.uint8)[256:256 + cells // 8].cpu().numpy()  # after the pool counter
     return int(np.unpackbits(words).sum())
 
 
-def _samples_buffer(shape5, nv, out_shape, separate, device):
-    n = _lib.load().gft_raymarch_grid_transform_samples_size(_lib.i64(shape5), nv, _lib.i32(out_shape),
-                                                               int(separate))
-    return _workspace(n, device)
+def sample_pool_cells(samples):
+    """Pool cells the forward's warps took (in chunks of 256; chunk requests
+    past the pool's end included)."""
+    return int(samples.view(torch.uint8)[:8].view(torch.int64).item())
+
+
+def _samples_buffer(shape5, nv, out_shape, separate, device, pool_fraction=None):
+    lib = _lib.load()
+    args = (_lib.i64(shape5), nv, _lib.i32(out_shape), int(separate))
+    full = lib.gft_raymarch_grid_transform_samples_size(*args)
+    meta = lib.gft_raymarch_grid_transform_samples_min_size(*args)
+    f = _state['sample_pool'] if pool_fraction is None else float(pool_fraction)
+    return _workspace(meta + int((full - meta) * f) // 256 * 256, device)
 
 
 def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=None, samples=None):

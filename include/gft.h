@@ -121,16 +121,25 @@ gft_status gft_raymarch_grid_transform_grad(
     int32_t grad_mode, float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
 /* Sample store (no counterpart in the reference, whose gradient re-samples the
  * grid): gft_raymarch_grid_transform_store is gft_raymarch_grid_transform
- * (LINEAR interpolation) that also writes every ray sample it blends, within
- * each ray's clipped step range, into `samples` (an internal layout of
- * gft_raymarch_grid_transform_samples_size bytes: per camera, per 8x16-pixel
- * tile, per depth sample, 128 x C floats).  gft_raymarch_grid_transform_grad_stored
+ * (LINEAR interpolation) that also writes the ray samples it blends that can
+ * be non-zero, within each ray's clipped step range, into `samples` (an
+ * internal layout: per camera, 8x16-pixel tile, depth sample and warp a
+ * ballot word and a pool offset, occupancy maps of the input, then a pool of
+ * C-float cells that warps fill in chunks).  gft_raymarch_grid_transform_grad_stored
  * is gft_raymarch_grid_transform_grad reading those samples instead of
- * re-sampling the input; input, geometry and output_shape must be those of
- * the store call, with the input unchanged in between.  The adjoint then uses
- * the samples at the forward's positions (marched front to back), which
- * differ from the re-sampled back-to-front positions by float rounding only. */
+ * re-sampling the input; input, geometry, output_shape and samples_bytes must
+ * be those of the store call, with the input unchanged in between.  The
+ * adjoint then uses the samples at the forward's positions, which differ from
+ * re-sampled ones by float rounding only.
+ * samples_bytes may be anything from gft_raymarch_grid_transform_samples_min_size
+ * (no pool) to gft_raymarch_grid_transform_samples_size (a pool for every
+ * sample the launch could store): samples that do not fit the pool are not
+ * stored and the adjoint re-samples the grid for them, with the same result
+ * up to rounding.  Typical plumes store a few percent of the full bound. */
 size_t gft_raymarch_grid_transform_samples_size(
+    const int64_t input_shape[5], int32_t num_cameras, const int32_t output_shape[3],
+    int32_t separate_camera_batch);
+size_t gft_raymarch_grid_transform_samples_min_size(
     const int64_t input_shape[5], int32_t num_cameras, const int32_t output_shape[3],
     int32_t separate_camera_batch);
 gft_status gft_raymarch_grid_transform_store(

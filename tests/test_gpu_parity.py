@@ -235,6 +235,46 @@ def test_raymarch_sample_store_sparse_grid(ops, boundary, mode):
     assert counts[1] == 0 if boundary != 'WRAP' else counts[1] < counts[0]
 
 
+@pytest.mark.parametrize('fraction', [0.0, 0.01, 1.0])
+@pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
+def test_raymarch_sample_store_pool_sizes(ops, fraction, mode):
+    """A sample pool too small for the launch (none, about one chunk) or as
+    large as every sample: the forward output is bit-identical, the samples
+    that did not fit are re-sampled by the adjoint (gradient equal to the
+    re-sampling one up to rounding), and the warps stop taking chunks at the
+    pool's end."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 35) * 0.4
+    dy = cuda(np.random.default_rng(36).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+    grads, outs = [], []
+    for store, frac in ((False, None), (True, fraction)):
+        ops.set_raymarch_sample_store(store, pool_fraction=frac)
+        try:
+            xt = cuda(x).requires_grad_(True)
+            with ops.grad_mode(mode):
+                y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11))
+                y.backward(dy)
+        finally:
+            ops.set_raymarch_sample_store(True, pool_fraction=0.25)
+        grads.append(np_(xt.grad))
+        outs.append(np_(y))
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(grads[1], grads[0]) <= 1e-5
+    shape5 = (1, 10, 14, 12, 4)
+    smp = ops._samples_buffer(shape5, 3, (13, 9, 11), True, 'cuda', pool_fraction=fraction)
+    ops._raymarch_fwd(cuda(x), M, V, P, F, (13, 9, 11), 1, 0, 0, True, samples=smp)
+    n = ops.stored_sample_count(smp, shape5, 3, (13, 9, 11))
+    lib = ops._lib.load()
+    args = (ops._lib.i64(shape5), 3, ops._lib.i32((13, 9, 11)), 1)
+    cap = (smp.numel() - lib.gft_raymarch_grid_transform_samples_min_size(*args)) // 16
+    taken = ops.sample_pool_cells(smp)
+    assert n > 0
+    if fraction == 1.0:
+        assert n <= taken <= cap  # everything fit
+    else:
+        assert cap < n and taken >= cap - 256  # the pool ran full
+
+
 def test_raymarch_sample_store_many_pairs(ops):
     """More (batch, camera) pairs than one launch table holds (2 x 9 = 18):
     the store offsets continue across the tables, and each batch slice skips

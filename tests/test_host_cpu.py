@@ -119,15 +119,21 @@ def test_argument_errors_without_a_gpu(lib):
     st = L.gft_raymarch_grid_transform(ctypes.c_void_p(1), 0, huge, p, 1, p, p, f, 1, out, 1, 0, 0, 1,
                                        ctypes.c_void_p(1), None)
     assert st == lib.ERR_INVALID_ARGUMENT and b'2^32' in L.gft_last_error()
-    # sample store: LINEAR only, a large enough store, a store pointer
-    # one 8x16-pixel tile x 4 steps x 128 lanes of 4 floats, a ballot word per
-    # warp and step, a 2x2x2 occupancy map (256-byte aligned parts)
-    assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == 4 * 128 * 4 * 4 + 256 + 256
+    # sample store: LINEAR only, a large enough store, a store pointer.
+    # Before the pool: the pool counter, a ballot word and a pool offset per
+    # warp and step, a 2x2x2 occupancy map (256-byte aligned parts); the full
+    # pool: one 8x16-pixel tile x 4 steps x 128 lanes, plus the chunks' slack
+    # (abandoned chunks hold >= 225 of 256 cells; a last chunk per warp), of 4 floats
+    meta = 256 + 256 + 256 + 256
+    cells = 4 * 128
+    pool = -(-cells * 256 // 225) + 4 * 256
+    assert L.gft_raymarch_grid_transform_samples_min_size(shape4, 1, out, 1) == meta
+    assert L.gft_raymarch_grid_transform_samples_size(shape4, 1, out, 1) == meta + -(-pool * 16 // 256) * 256
     st = L.gft_raymarch_grid_transform_store(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 0, 0, 0, 1,
                                              ctypes.c_void_p(1), ctypes.c_void_p(1), 1 << 20, None)
     assert st == lib.ERR_INVALID_ARGUMENT and b'LINEAR' in L.gft_last_error()
     st = L.gft_raymarch_grid_transform_store(ctypes.c_void_p(1), 0, shape4, p, 1, p, p, f, 1, out, 1, 0, 0, 1,
-                                             ctypes.c_void_p(1), ctypes.c_void_p(1), 64, None)
+                                             ctypes.c_void_p(1), ctypes.c_void_p(1), meta - 256, None)
     assert st == lib.ERR_WORKSPACE
     st = L.gft_raymarch_grid_transform_grad_stored(ctypes.c_void_p(1), 0, shape4, ctypes.c_void_p(1),
                                                    ctypes.c_void_p(1), p, 1, p, p, f, 1, out, 1, 0, 0, 1, 1, None, 0,
