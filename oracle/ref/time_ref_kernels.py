@@ -204,6 +204,13 @@ def main():
     a_bwd_our = lambda: ops._advect_bwd(d0, step.s_vx.detach(), step.s_vy.detach(), step.s_vz.detach(),
                                         dyv[0], 1.0, 2, 1, 1, ops.GRAD['REFERENCE'])
     res['advect_bwd'] = (timed(adv_bwd_ref), timed(a_bwd_our))
+    # as the step runs it: the adjoint reads the semi-Lagrangian grid the
+    # forward left in the shared workspace (GFT_GRAD_FORWARD_READY)
+    ws_adv = ops._advect_grad_workspace(d0.shape, 2, dev)
+    ops._advect_fwd(d0, step.s_vx.detach(), step.s_vy.detach(), step.s_vz.detach(), 1.0, 2, 1, 1, ws=ws_adv)
+    a_bwd_ready = lambda: ops._advect_bwd(d0, step.s_vx.detach(), step.s_vy.detach(), step.s_vz.detach(),
+                                          dyv[0], 1.0, 2, 1, 1, ops.GRAD['REFERENCE'] | ops.FORWARD_READY, ws=ws_adv)
+    res['advect_bwd_forward_ready'] = timed(a_bwd_ready)
 
     ops_rows = [k for k, v in res.items() if isinstance(v, tuple)]
 
@@ -218,7 +225,8 @@ def main():
            'raymarch_bwd_relL2_vs_reference': res['raymarch_bwd_relL2'],
            'raymarch_bwd_relL2_vs_reference_image_loss_adjoint': res['raymarch_bwd_loss_grad_relL2'],
            'raymarch_bwd_relL2_own_one_ulp_matrix_change': res['raymarch_bwd_one_ulp_matrix_relL2'],
-           'shadow_sample_relL2_vs_reference': res['shadow_sample_relL2']}
+           'shadow_sample_relL2_vs_reference': res['shadow_sample_relL2'],
+           'advect_bwd_ours_forward_ready_ms': res['advect_bwd_forward_ready']}
     s = json.dumps(out)
     print(s)
     if args.out:
