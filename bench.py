@@ -211,8 +211,8 @@ def alg_bytes(step, storage_bytes):
 # the dominant kernel, from one ncu capture of
 #   python bench.py --kernel-only raymarch_scatter --config <c> --storage <s>
 # (summaries in profiles/raymarch_scatter_<c>.md): cfg5 BF16, MODE 1 launch,
-# 3.35 GB read + 2.24 GB written.
-SCATTER_TRAFFIC = {('cfg5', 'bf16'): 5.59e9}
+# 3.34 GB read + 2.24 GB written.
+SCATTER_TRAFFIC = {('cfg5', 'bf16'): 5.58e9}
 
 
 # ------------------------------------------------------------------ our arm
