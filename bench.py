@@ -444,15 +444,19 @@ def other_config(config, args, dev, timed):
     from gft.pipeline import RenderAdvectStep
     res = {}
     inputs = None
+    from gft import autotune
     for name, dt in (('f32', None), ('bf16', torch.bfloat16)):
-        st = RenderAdvectStep(config, dev, storage_dtype=dt, mode='batched')
-        inputs = inputs or st.make_inputs()
-        st.setup_static(inputs)
-        st.capture(warmup=3)
-        for _ in range(3):
-            st.replay()
-        t = timed(st.replay, 30)
-        res[name] = {'ms_per_step': float(np.mean(t)), 'value': 1000.0 / float(np.mean(t)), 'unit': 'iters/s'}
+        # this workload's own launch configuration; the headline's is restored after
+        with autotune.knob_settings(autotune.knobs()):
+            st = RenderAdvectStep(config, dev, storage_dtype=dt, mode='batched', autotune=not args.no_autotune)
+            inputs = inputs or st.make_inputs()
+            st.setup_static(inputs)
+            st.capture(warmup=3)
+            for _ in range(3):
+                st.replay()
+            t = timed(st.replay, 30)
+        res[name] = {'ms_per_step': float(np.mean(t)), 'value': 1000.0 / float(np.mean(t)), 'unit': 'iters/s',
+                     'knobs': st.knobs, 'candidates_ms': st.tune_log or None}
         del st
         torch.cuda.empty_cache()
     res['workload'] = workload_config(config, 'f32|bf16', args.grad_mode)['workload']
@@ -599,17 +603,21 @@ def uneven_batch(dev, timed, storage=None, frames=64, views=8):
         inputs = st.make_inputs(seed=4000)
         st.setup_static(inputs)
         torch.cuda.reset_peak_memory_stats(dev)
-        st.capture(warmup=3)
-        for _ in range(2):
-            st.replay()
-        t = float(np.median(timed(st.replay, 5)))
+        from gft import autotune
+        tune_log = {}
+        with autotune.knob_settings(autotune.knobs()):  # this workload's own knobs, the headline's restored after
+            st.capture(warmup=3, autotune=True, tune_log=tune_log)
+            for _ in range(2):
+                st.replay()
+            t = float(np.median(timed(st.replay, 5)))
         nviews = len(st.shapes)
         res = {'workload': '%d frames x (1 + %d) views of 64-256 px, density %s, %d samples, shadow + BEER_LAMBERT, '
                            'fwd+bwd to every frame density, one CUDA graph' % (frames, views,
                                                                                'x'.join(map(str, st.shape)),
                                                                                st.shapes[0][0]),
                'ms_per_iteration': t, 'iters_per_s': 1000.0 / t, 'renders_per_s': nviews * 1000.0 / t,
-               'views': nviews, 'pixels': st.pixels, 'peak_hbm_bytes': int(torch.cuda.max_memory_allocated(dev))}
+               'views': nviews, 'pixels': st.pixels, 'peak_hbm_bytes': int(torch.cuda.max_memory_allocated(dev)),
+               'autotune': {'knobs': getattr(st, 'knobs', None), 'candidates_ms': tune_log}}
         # raymarch alone: one views op vs one call per view
         with torch.no_grad():
             x = (torch.from_numpy(inputs['d']).to(dev).repeat(1, 1, 1, 1, 4) * 0.02).contiguous()

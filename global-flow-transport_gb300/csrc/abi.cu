@@ -1360,20 +1360,22 @@ gft_status gft_raymarch_check(const void* input, int32_t input_dtype, const int6
 }
 
 gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
-                             const int64_t shape[5], float ambient, float scale, int32_t output_layout, float* output,
+                             const int64_t shape[5], float ambient, float scale, int32_t output_layout, void* output,
                              void* stream) {
     std::string why;
     if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    const bool bf16 = (output_layout & ~GFT_LAYOUT_BRICK) == GFT_DTYPE_BF16;
+    if (bf16) output_layout &= GFT_LAYOUT_BRICK;
     if (!layout_ok(output_layout)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid layout");
     if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
     if (!density || !transmittance || !light_color || !output)
         return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
     gft_status st;
     if ((st = check_aligned({density, transmittance, light_color}, 4)) != GFT_OK ||
-        (st = check_aligned({output}, 16)) != GFT_OK)
+        (st = check_aligned({output}, bf16 ? 8 : 16)) != GFT_OK)
         return st;
     if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], dims_of(shape), ambient, scale,
-                              output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, output, as_stream(stream)))
+                              output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, bf16, output, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }

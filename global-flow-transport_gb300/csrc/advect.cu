@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(AD_THREADS, C == 1 ? 4 : 1)
     }
     if (in) {
         store<C>(gd, t, vscale(gcorr, 0.5f));
-        store<C>(gdir, t, g);
+        if (gdir != nullptr) store<C>(gdir, t, g);  // only the NEGATIVE clamp changes g
     }
     scatter_merged<C, BM, COUNT, DET>(gfwd_sc, cnt2, dm, in, bx, by, bz, gback, iacc, DET ? *iscale : 0.f);
     if (!in) return;
@@ -624,13 +624,15 @@ static bool adv_bwd_det(const AdvectArgs& a, bool forward_ready, const float* dy
             // back-lookup scatter of -0.5 g_corr: |sum| <= 0.5 max|dy| * voxels
             k_adv_det_absmax<<<rb, 256, 0, s>>>(dyb, (int64_t)vc, maxbits);
             k_adv_det_scale<<<1, 1, 0, s>>>(maxbits, 0.5 * (double)nv, scale);
+            const bool neg = a.clamp == CLAMP_NEGATIVE;
+            const float* gd_dir = neg ? gdir : dyb;
             k_adv_bwd_back<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
-                                                                    dyb, gdb, nullptr, cnt2, gdir, glut, b == 0,
-                                                                    acc2, scale);
-            k_adv_det_gfmax<C, COUNT><<<rb, 256, 0, s>>>(gdir, acc2, scale, cnt2, nv, maxbits + 1);
+                                                                    dyb, gdb, nullptr, cnt2, neg ? gdir : nullptr,
+                                                                    glut, b == 0, acc2, scale);
+            k_adv_det_gfmax<C, COUNT><<<rb, 256, 0, s>>>(gd_dir, acc2, scale, cnt2, nv, maxbits + 1);
             k_adv_det_scale<<<1, 1, 0, s>>>(maxbits + 1, (double)nv, scale + 1);
             k_adv_bwd_fwd<C, BM, COUNT, true><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
-                                                                   gdir, nullptr, cnt2, nullptr, cnt3, glut, false,
+                                                                   gd_dir, nullptr, cnt2, nullptr, cnt3, glut, false,
                                                                    acc2, scale, acc3, scale + 1, nullptr, nullptr,
                                                                    nullptr);
             n += 6;
@@ -695,11 +697,15 @@ static bool adv_bwd_impl(const AdvectArgs& a, bool forward_ready, const float* d
                 return false;
             if (!forward_ready)  // else fwd holds this slice's semi-Lagrangian grid already
                 k_adv_sl<C, float, BM><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, fwd);
+            // the fwd adjoint's direct term is the output gradient itself
+            // unless the NEGATIVE clamp zeroes parts of it
+            const bool neg = a.clamp == CLAMP_NEGATIVE;
             k_adv_bwd_back<C, BM, COUNT><<<blocks, T, 0, s>>>(db, fwd, a.d, a.vx, a.vy, a.vz, a.dt, a.clamp,
-                                                                      dyb, gdb, gfwd_sc, cnt2, gdir, glut, b == 0,
-                                                              nullptr, nullptr);
+                                                                      dyb, gdb, gfwd_sc, cnt2, neg ? gdir : nullptr,
+                                                                      glut, b == 0, nullptr, nullptr);
             k_adv_bwd_fwd<C, BM, COUNT><<<blocks, T, 0, s>>>(db, a.d, a.vx, a.vy, a.vz, a.dt, false, false,
-                                                                     gdir, gfwd_sc, cnt2, gd_sc, cnt3, glut, false,
+                                                                     neg ? gdir : dyb, gfwd_sc, cnt2, gd_sc, cnt3,
+                                                                     glut, false,
                                                              nullptr, nullptr, nullptr, nullptr,
                                                              last ? gvx : nullptr, gvy, gvz);
         } else {

@@ -15,6 +15,7 @@
 // Elementwise products and sums use __fmul_rn / __fadd_rn so that they round
 // exactly like the separate tensor ops they replace (no FMA contraction).
 #include <algorithm>
+#include <type_traits>
 
 #include "gft_internal.h"
 
@@ -114,10 +115,22 @@ bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, f
 // density, tr [N, V] (V voxels per batch slice, rows), color [V, 3] shared by
 // all slices; out [N, cells, 4] in layout L (rows, or the raymarch's bricks).
 // One batch slice per blockIdx.y.
-template <int L>
+template <typename T>
+__device__ __forceinline__ void store_cell(T* out, int64_t o, float r, float g, float b, float a) {
+    if constexpr (std::is_same<T, float>::value) {
+        reinterpret_cast<float4*>(out)[o] = make_float4(r, g, b, a);
+    } else {
+        __nv_bfloat162 h[2] = {__floats2bfloat162_rn(r, g), __floats2bfloat162_rn(b, a)};
+        reinterpret_cast<uint2*>(out)[o] = *reinterpret_cast<const uint2*>(h);
+    }
+}
+
+// T: the output's storage type (float, or bf16 rounded to nearest even as a
+// separate conversion would round the fp32 result).
+template <int L, typename T>
 __global__ void __launch_bounds__(CP_THREADS)
     k_light_compose(const float* __restrict__ dens, const float* __restrict__ tr, const float* __restrict__ color,
-                    Dims d, float ambient, float scale, float* __restrict__ out) {
+                    Dims d, float ambient, float scale, T* __restrict__ out) {
     const int64_t nvox = voxels(d), b = blockIdx.y;
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = b * nvox + v;
@@ -134,7 +147,25 @@ __global__ void __launch_bounds__(CP_THREADS)
             unflat32((uint32_t)v, d, x, y, z);
             o = b * brick_cells(d) + brick_index(x, y, z, d);
         }
-        reinterpret_cast<float4*>(out)[o] = make_float4(r[0], r[1], r[2], __fmul_rn(dv, scale));
+        const float a = __fmul_rn(dv, scale);
+        store_cell<T>(out, o, r[0], r[1], r[2], a);
+        if constexpr (L == LAYOUT_BRICK) {
+            // the bricks of an odd-sized axis end in a padding cell: the cell
+            // at the last index writes zeros there (the sample store's
+            // occupancy map reads whole bricks)
+            int x, y, z;
+            unflat32((uint32_t)v, d, x, y, z);
+            const int px = (x == d.x - 1 && (d.x & 1)) ? 1 : 0, py = (y == d.y - 1 && (d.y & 1)) ? 1 : 0,
+                      pz = (z == d.z - 1 && (d.z & 1)) ? 1 : 0;
+            if (px | py | pz) {
+                const int64_t base = b * brick_cells(d);
+                for (int k = 1; k < 8; ++k) {
+                    const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
+                    if ((sx && !px) || (sy && !py) || (sz && !pz)) continue;
+                    store_cell<T>(out, base + brick_index(x + sx, y + sy, z + sz, d), 0.f, 0.f, 0.f, 0.f);
+                }
+            }
+        }
     }
 }
 
@@ -169,13 +200,22 @@ __global__ void __launch_bounds__(CP_THREADS)
     }
 }
 
-bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
-                          float scale, int layout, float* out, cudaStream_t st) {
+template <typename T>
+static void light_compose_t(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
+                            float scale, int layout, void* out, cudaStream_t st) {
     const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
     if (layout == LAYOUT_BRICK)
-        k_light_compose<LAYOUT_BRICK><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, out);
+        k_light_compose<LAYOUT_BRICK, T><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, (T*)out);
     else
-        k_light_compose<LAYOUT_FLAT><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, out);
+        k_light_compose<LAYOUT_FLAT, T><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, (T*)out);
+}
+
+bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
+                          float scale, int layout, bool bf16, void* out, cudaStream_t st) {
+    if (bf16)
+        light_compose_t<__nv_bfloat16>(dens, tr, color, N, d, ambient, scale, layout, out, st);
+    else
+        light_compose_t<float>(dens, tr, color, N, d, ambient, scale, layout, out, st);
     return launched(1, "light compose launch");
 }
 

@@ -194,7 +194,7 @@ bool launch_advect_bwd(const AdvectArgs& a, bool exact, bool forward_ready, cons
 bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st);
 bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st);
 bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
-                          float scale, int layout, float* out, cudaStream_t st);
+                          float scale, int layout, bool bf16, void* out, cudaStream_t st);
 bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
                                float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st);
 int image_loss_blocks(int64_t npix);

@@ -48,33 +48,93 @@ def transmittance(x):
     return _Transmittance.apply(x)
 
 
+def _compose(d, tr, color, ambient, scale, brick, bf16=False):
+    lib = _lib.load()
+    dt = torch.bfloat16 if bf16 else torch.float32
+    if brick:
+        out = torch.empty((d.shape[0], ops.brick_cells(d.shape[1:4]), 4), dtype=dt, device=d.device)
+    else:
+        out = torch.empty(tuple(d.shape[:4]) + (4,), dtype=dt, device=d.device)
+    layout = (ops.LAYOUT_BRICK if brick else 0) | (1 if bf16 else 0)  # | GFT_DTYPE_BF16
+    with torch.cuda.device(d.device):
+        _lib.check(lib.gft_light_compose(_p(d), _p(tr), _p(color), _shape(d), float(ambient), float(scale),
+                                         layout, _p(out), _stream(d.device)), 'LightCompose')
+    return out
+
+
+def _compose_grad(d, tr, color, ambient, scale, brick, g):
+    lib = _lib.load()
+    g = g.contiguous()
+    gd = torch.empty_like(d)
+    gt = torch.empty_like(tr)
+    layout = ops.LAYOUT_BRICK if brick else 0
+    with torch.cuda.device(d.device):
+        _lib.check(lib.gft_light_compose_grad(_p(d), _p(tr), _p(color), _shape(d), float(ambient), float(scale),
+                                              layout, _p(g), _p(gd), _p(gt), _stream(d.device)), 'LightComposeGrad')
+    return gd, gt
+
+
+class _ComposeRaymarch(torch.autograd.Function):
+    """light_compose(brick=True) followed by the bricked raymarch, as one
+    autograd op: the composition writes the raymarch input directly in its
+    storage type (bf16 or fp32), and the raymarch's fp32 gradient reaches the
+    composition's adjoint without being rounded to the storage type."""
+
+    @staticmethod
+    def forward(ctx, d, tr, color, ambient, scale, grid, M, V, P, F, out_shape, boundary, blend, storage_dtype):
+        xs = _compose(d, tr, color, ambient, scale, True, storage_dtype == torch.bfloat16)
+        need = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        y, samples = ops._raymarch_forward_ctx(ctx, xs, need, M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary,
+                                               blend, True, grid)
+        ctx.save_for_backward(d, tr, color, xs, y, samples)
+        ctx.k = (float(ambient), float(scale))
+        ctx.args = (M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary, blend, True, grid)
+        ctx.mark_non_differentiable(xs)
+        return y, xs
+
+    @staticmethod
+    def backward(ctx, dy, _dxs):
+        d, tr, color, xs, y, samples = ctx.saved_tensors
+        g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
+        gd, gt = _compose_grad(d, tr, color, ctx.k[0], ctx.k[1], True, g)
+        return (gd, gt) + (None,) * 12
+
+
+def render_bricked(density, transmittance, light_color, ambient, scale, matrix_m, matrix_v, matrix_p,
+                   frustum_params, output_shape, boundary='BORDER', blending_mode='BEER_LAMBERT', storage_dtype=None):
+    """raymarch_grid_transform_bricked(light_compose(density, transmittance,
+    light_color, ambient, scale, brick=True), density's grid, ...) in one
+    autograd op; with storage_dtype=torch.bfloat16 the composition writes the
+    raymarch input in bf16 directly.  Returns (images [1, V, H, W, 4], the
+    raymarch input as stored: [1, brick_cells, 4], no gradient)."""
+    d = _cuda(density, 'density')
+    tr = _cuda(transmittance, 'transmittance')
+    color = _cuda(light_color, 'light_color')
+    if d.dim() != 5 or d.shape[4] != 1 or tuple(tr.shape) != tuple(d.shape):
+        raise _lib.GftInvalidArgument('density and transmittance must both be [N, D, H, W, 1]')
+    if color.numel() != int(np.prod(d.shape[1:4])) * 3 or color.shape[-1] != 3:
+        raise _lib.GftInvalidArgument('light_color must be [D, H, W, 3]')
+    if storage_dtype not in (None, torch.float32, torch.bfloat16):
+        raise _lib.GftInvalidArgument('storage_dtype must be float32 or bfloat16')
+    grid = tuple(int(v) for v in d.shape[1:4])
+    return _ComposeRaymarch.apply(d, tr, color.detach(), ambient, scale, grid, matrix_m, matrix_v, matrix_p,
+                                  frustum_params, ops._shape3(output_shape), ops._enum(ops.BOUNDARY, boundary, 'boundary'),
+                                  ops._enum(ops.BLEND, blending_mode, 'blending_mode'), storage_dtype)
+
+
 class _LightCompose(torch.autograd.Function):
     @staticmethod
     def forward(ctx, d, tr, color, ambient, scale, brick):
-        lib = _lib.load()
-        if brick:
-            out = torch.empty((d.shape[0], ops.brick_cells(d.shape[1:4]), 4), dtype=torch.float32, device=d.device)
-        else:
-            out = torch.empty(tuple(d.shape[:4]) + (4,), dtype=torch.float32, device=d.device)
-        layout = ops.LAYOUT_BRICK if brick else 0
-        with torch.cuda.device(d.device):
-            _lib.check(lib.gft_light_compose(_p(d), _p(tr), _p(color), _shape(d), float(ambient), float(scale),
-                                             layout, _p(out), _stream(d.device)), 'LightCompose')
+        out = _compose(d, tr, color, ambient, scale, brick)
         ctx.save_for_backward(d, tr, color)
-        ctx.k = (float(ambient), float(scale), layout)
+        ctx.k = (float(ambient), float(scale), bool(brick))
         return out
 
     @staticmethod
     def backward(ctx, g):
         d, tr, color = ctx.saved_tensors
-        ambient, scale, layout = ctx.k
-        lib = _lib.load()
-        g = g.contiguous()
-        gd = torch.empty_like(d)
-        gt = torch.empty_like(tr)
-        with torch.cuda.device(d.device):
-            _lib.check(lib.gft_light_compose_grad(_p(d), _p(tr), _p(color), _shape(d), ambient, scale, layout,
-                                                  _p(g), _p(gd), _p(gt), _stream(d.device)), 'LightComposeGrad')
+        ambient, scale, brick = ctx.k
+        gd, gt = _compose_grad(d, tr, color, ambient, scale, brick, g)
         return gd, gt, None, None, None, None
 
 

@@ -435,26 +435,46 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
     return grad
 
 
+def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, boundary, blend, separate, grid):
+    """Forward of a differentiable raymarch of the storage-typed input xs:
+    starts the reference normalisation's weight pass (cached, prefetched or on
+    a side stream) into ctx.weights and returns (output, sample store)."""
+    shape5 = _grid5(xs, grid)[0]
+    ctx.weights = None
+    if need_grad and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR'] and not _state['deterministic']:
+        cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
+        if cached is not None:
+            ctx.weights = (cached, None)
+        elif _state['side_weights']:
+            key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
+            ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
+                                                                                out_shape, boundary, separate)
+    samples = None
+    if need_grad and interp == FILTER['LINEAR'] and _state['sample_store']:
+        samples = _samples_buffer(shape5, _mats(V)[1], out_shape, separate, xs.device)
+    y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=grid, samples=samples)
+    return y, samples
+
+
+def _raymarch_backward_ctx(ctx, xs, y, samples, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, grid):
+    """The fp32 input gradient of a raymarch run by _raymarch_forward_ctx."""
+    ws = None
+    if ctx.weights is not None:
+        ws, ev = ctx.weights
+        if ev is not None:
+            torch.cuda.current_stream(xs.device).wait_event(ev)
+    g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
+                      _scatter_gmode(), weights=ws, grid=grid, samples=samples)
+    ctx.weights = None
+    return g
+
+
 class _Raymarch(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, blend, separate, storage_dtype, grid=None):
         xs = _storage(x, storage_dtype)
-        shape5 = _grid5(xs, grid)[0]
-        ctx.weights = None
-        if (ctx.needs_input_grad[0] and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']
-                and not _state['deterministic']):
-            cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
-            if cached is not None:
-                ctx.weights = (cached, None)
-            elif _state['side_weights']:
-                key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
-                ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
-                                                                                    out_shape, boundary, separate)
-        samples = None
-        if ctx.needs_input_grad[0] and interp == FILTER['LINEAR'] and _state['sample_store']:
-            samples = _samples_buffer(shape5, _mats(V)[1], out_shape, separate, xs.device)
-        y = _raymarch_fwd(xs, M, V, P, F, out_shape, interp, boundary, blend, separate, grid=grid,
-                          samples=samples)
+        y, samples = _raymarch_forward_ctx(ctx, xs, ctx.needs_input_grad[0], M, V, P, F, out_shape, interp,
+                                           boundary, blend, separate, grid)
         # a saved tensor, so that checkpointing drops and recomputes it
         ctx.save_for_backward(xs, y, samples)
         ctx.args = (M, V, P, F, out_shape, interp, boundary, blend, separate, grid)
@@ -464,15 +484,7 @@ class _Raymarch(torch.autograd.Function):
     @staticmethod
     def backward(ctx, dy):
         xs, y, samples = ctx.saved_tensors
-        M, V, P, F, out_shape, interp, boundary, blend, separate, grid = ctx.args
-        ws = None
-        if ctx.weights is not None:
-            ws, ev = ctx.weights
-            if ev is not None:
-                torch.cuda.current_stream(xs.device).wait_event(ev)
-        g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                          _scatter_gmode(), weights=ws, grid=grid, samples=samples)
-        ctx.weights = None
+        g = _raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
         return (g.to(ctx.in_dtype),) + (None,) * 11
 
 

@@ -145,19 +145,16 @@ class RenderAdvectStep:
         if self.mode == 'plain':
             light = d * (self.shadow(d) * self.falloff_col + self.ambient)
             data = torch.cat([light, d], dim=-1) * self.depth_step
-        else:
-            # the raymarch input in the brick layout (written directly by the light composition)
-            data = fused.light_compose(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step,
-                                       brick=True)
-        if self.mode == 'plain':
             imgs = [ops.raymarch_grid_transform(data, self.M, self.V[i:i + 1], self.P[i:i + 1], self.F[i:i + 1],
                                                 self.res) for i in range(len(self.V))]
             img = torch.cat(imgs, dim=1)
         else:
-            img = ops.raymarch_grid_transform_bricked(data, self.shape, self.M, self.V, self.P, self.F, self.res,
-                                                      storage_dtype=self.storage_dtype)
+            # the light composition writes the raymarch input directly, in the
+            # brick layout and the storage type
+            img, xs = fused.render_bricked(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step,
+                                           self.M, self.V, self.P, self.F, self.res,
+                                           storage_dtype=self.storage_dtype)
             if self.fp64_check:
-                xs = data.detach() if self.storage_dtype is None else data.detach().to(self.storage_dtype)
                 ops.raymarch_check(xs, self.M, self.V, self.P, self.F, self.res, img.detach(), self.check_strides[1],
                                    grid_shape=self.shape, out=self.check_buf[2:4])
         return img.squeeze(0)  # [V,H,W,4]
@@ -250,6 +247,7 @@ class UnevenBatchStep:
     def __init__(self, frames=64, views=8, shape=(96, 170, 96), samples=128, device='cuda', storage_dtype=None,
                  clip_cameras=True, seed=4000, shadow=(128, 128, 128), mips=3, sizes=(64, 256)):
         self.dev = torch.device(device)
+        self.knobs = None
         self.frames = int(frames)
         self.shape = tuple(shape)
         self.storage_dtype = storage_dtype
@@ -320,7 +318,13 @@ class UnevenBatchStep:
         self.s_d = torch.from_numpy(inputs['d']).to(self.dev).requires_grad_(True)
         self.s_t = torch.from_numpy(inputs['target']).to(self.dev)
 
-    def capture(self, warmup=3):
+    def capture(self, warmup=3, autotune=False, tune_log=None):
+        """Captures step() into one CUDA graph (after tuning the
+        launch-configuration knobs on it, with autotune; the chosen values
+        stay set and are kept in self.knobs)."""
+        if autotune:
+            from . import autotune as _at
+            self.knobs = _at.tune(lambda: self.step(self.s_d, self.s_t), key=_at.step_key(self), log=tune_log)
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):

@@ -382,11 +382,13 @@ gft_status gft_transmittance_grad(const float* output, const float* output_grad,
  * [D, H, W, 3] shared by the batch; output [N, D, H, W, 4] =
  * concat(density * (transmittance * light_color + ambient), density) * scale,
  * in NDHWC rows (output_layout 0) or in the raymarch's brick layout
- * (output_layout GFT_LAYOUT_BRICK); the gradient reads output_grad in that
- * layout. */
+ * (output_layout GFT_LAYOUT_BRICK); the gradient reads output_grad (fp32) in
+ * that layout.  output_layout | GFT_DTYPE_BF16: the output is stored in bf16
+ * (the fp32 result rounded to nearest even), ready as a BF16-storage raymarch
+ * input; output_grad stays fp32. */
 gft_status gft_light_compose(const float* density, const float* transmittance, const float* light_color,
                              const int64_t shape[5], float ambient, float scale, int32_t output_layout,
-                             float* output, void* stream);
+                             void* output, void* stream);
 gft_status gft_light_compose_grad(const float* density, const float* transmittance, const float* light_color,
                                   const int64_t shape[5], float ambient, float scale, int32_t output_layout,
                                   const float* output_grad, float* density_grad, float* transmittance_grad,

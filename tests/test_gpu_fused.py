@@ -109,6 +109,37 @@ def test_image_loss_tonemap(fused, mode, ties):
     assert float(fused.image_loss(a, tgt, bkg_host, tonemap=mode)) == float(loss)
 
 
+@pytest.mark.parametrize('storage', [None, torch.bfloat16])
+def test_render_bricked_equals_compose_then_raymarch(fused, storage):
+    """The fused composition + bricked raymarch (the composition writing the
+    raymarch input in its storage type) against light_compose(brick=True)
+    followed by raymarch_grid_transform_bricked with the same storage type:
+    identical input bits and images, gradients equal up to summation order."""
+    from gft import ops
+    from scene_utils import scene
+    g = torch.Generator().manual_seed(9)
+    D, H, W = 9, 13, 11
+    _, _, M, V, P, F = scene((D, H, W), 3, (13, 9, 11))
+    d0 = (torch.rand((1, D, H, W, 1), generator=g) * 0.3).cuda()
+    t0 = torch.rand((1, D, H, W, 1), generator=g).cuda()
+    col = torch.rand((1, D, H, W, 3), generator=g).cuda()
+    dy = torch.randn((1, 3, 9, 11, 4), generator=g).cuda()
+    d1, t1 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    img, xs = fused.render_bricked(d1, t1, col, 0.64, 0.37, M, V, P, F, (13, 9, 11), storage_dtype=storage)
+    img.backward(dy)
+    d2, t2 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+    data = fused.light_compose(d2, t2, col, 0.64, 0.37, brick=True)
+    ref = ops.raymarch_grid_transform_bricked(data, (D, H, W), M, V, P, F, (13, 9, 11), storage_dtype=storage)
+    ref.backward(dy)
+    want = data.detach() if storage is None else data.detach().to(storage)
+    assert xs.dtype == want.dtype
+    # the bricks of odd-sized grids carry padding cells that nothing writes
+    assert torch.equal(ops.from_bricks(xs.float(), (D, H, W)), ops.from_bricks(want.float(), (D, H, W)))
+    assert torch.equal(img, ref)
+    assert rel_l2(_np(d1.grad), _np(d2.grad)) <= 1e-6
+    assert rel_l2(_np(t1.grad), _np(t2.grad)) <= 1e-6
+
+
 def test_fused_argument_errors(fused):
     from gft import _lib
     with pytest.raises(_lib.GftInvalidArgument):
