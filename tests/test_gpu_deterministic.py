@@ -226,9 +226,11 @@ def test_advect_deterministic(ops, order, clamp, boundary, mode, C):
 
 
 def test_advect_deterministic_reuses_forward_intermediate(ops):
-    """MacCormack on one fp32 slice reads the forward's semi-Lagrangian grid
-    from the (deterministic-size) workspace; switching the mode on between
-    forward and backward recomputes it instead."""
+    """The deterministic MacCormack adjoint reading the forward's
+    semi-Lagrangian grid from a deterministic-size workspace
+    (GFT_GRAD_FORWARD_READY) equals the one recomputing it, bit for bit; the
+    autograd op recomputes it (also when the mode is switched on between
+    forward and backward)."""
     from gft import synthetic as syn
     shape = (10, 12, 9)
     d = cuda(syn.plume_density(shape, 133))
@@ -236,6 +238,13 @@ def test_advect_deterministic_reuses_forward_intermediate(ops):
     dy = cuda(np.random.default_rng(135).standard_normal((1,) + shape + (1,)).astype(np.float32))
     ref = ops._advect_bwd(d, vx, vy, vz, dy, 1.0, 2, ops.CLAMP['MC_SMOOTH'], ops.BOUNDARY['CLAMP'],
                           ops.GRAD['REFERENCE'] | ops.DETERMINISTIC)
+    gm = ops.GRAD['REFERENCE'] | ops.DETERMINISTIC
+    ws = ops._advect_grad_workspace(d.shape, 2, d.device, gm)
+    ops._advect_fwd(d, vx, vy, vz, 1.0, 2, ops.CLAMP['MC_SMOOTH'], ops.BOUNDARY['CLAMP'], ws=ws)
+    ready = ops._advect_bwd(d, vx, vy, vz, dy, 1.0, 2, ops.CLAMP['MC_SMOOTH'], ops.BOUNDARY['CLAMP'],
+                            gm | ops.FORWARD_READY, ws=ws)
+    for a, b in zip(ready, ref):
+        assert torch.equal(a, b)
     for switch_late in (False, True):
         ts = [t.clone().requires_grad_(True) for t in (d, vx, vy, vz)]
         with ops.deterministic(not switch_late):
