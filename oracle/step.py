@@ -12,7 +12,7 @@ oracle's ops:
     light  = d * (trv * falloff * colour + ambient)              lighting.py:23-147
     data   = concat(light, d) * depth_step                       renderer.py:420-437
     img    = RaymarchGridTransform(data, cameras)                renderer.py:555-568
-    loss   = mean((img.rgb + bkg * exp(-img.a) - target)^2)      renderer.py:626-640
+    loss   = mean((tone(img.rgb + bkg * exp(-img.a)) - target)^2) renderer.py:626-640
 
 The backward follows how the reference differentiates it: the raymarch and
 lookup gradient ops (reference-normalised unless ``exact``) and, for both
@@ -26,7 +26,8 @@ against finite differences.
 ``scene`` is a dict of plain arrays: M [1,16]; V, P [V,16]; F [V,6]; res
 (D, H, W) of the camera frusta; depth_step; Vs, Ps, Fs of the light; shadow_res;
 shadow_step; mips; falloff_col [D,H,W,3]; ambient; bkg [3]; order; clamp;
-boundary (of the advection lookups).
+boundary (of the advection lookups); optionally tonemap (one of
+oracle/tonemap.py MODES; NONE by default).
 """
 import numpy as np
 
@@ -35,6 +36,7 @@ from . import blend as B
 from . import raymarch as RM
 from . import resample as R
 from . import sampling as S
+from . import tonemap as TM
 from . import transforms as T
 
 
@@ -60,6 +62,11 @@ def forward(sc, d_prev, vx, vy, vz, target):
                           B.BEER_LAMBERT)[0]                                             # [V,H,W,4]
     bkg = np.asarray(sc['bkg'], np.float64)
     ea = np.exp(-img[..., 3:])
+    tm = sc.get('tonemap', 'NONE')
+    if tm != 'NONE':  # the renderer's tonemapping before the loss (renderer.py:528-541, :639-640)
+        loss, g_img = TM.image_loss(img, target, bkg, tm)
+        parts = dict(d=d, sh=sh, tr=tr, trv=trv, light=light, data=data, img=img, g_img=g_img)
+        return loss, parts
     r = img[..., :3] + bkg * ea - np.asarray(target, np.float64)
     loss = float(np.mean(r * r))
     parts = dict(d=d, sh=sh, tr=tr, trv=trv, light=light, data=data, img=img, ea=ea, r=r)
@@ -71,12 +78,16 @@ def backward(sc, d_prev, vx, vy, vz, parts, exact=False, shadow_grad='inverse', 
     dict that receives the intermediate gradients (g_img, g_data, g_trv,
     g_tr, g_sh, g_d of the advected density)."""
     p = parts
-    img, r, ea = p['img'], p['r'], p['ea']
-    n = r.size
-    bkg = np.asarray(sc['bkg'], np.float64)
-    g_img = np.zeros_like(img)
-    g_img[..., :3] = 2.0 * r / n
-    g_img[..., 3] = -np.sum(2.0 * r / n * bkg, axis=-1) * ea[..., 0]
+    img = p['img']
+    if 'g_img' in p:
+        g_img = p['g_img']
+    else:
+        r, ea = p['r'], p['ea']
+        n = r.size
+        bkg = np.asarray(sc['bkg'], np.float64)
+        g_img = np.zeros_like(img)
+        g_img[..., :3] = 2.0 * r / n
+        g_img[..., 3] = -np.sum(2.0 * r / n * bkg, axis=-1) * ea[..., 0]
     g_data = RM.raymarch_bwd(p['data'][None], img[None], g_img[None], sc['M'], sc['V'], sc['P'], sc['F'], sc['res'],
                              S.BORDER, B.BEER_LAMBERT, exact=exact)[0]                   # [D,H,W,4]
     g_data = g_data * sc['depth_step']

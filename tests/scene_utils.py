@@ -50,4 +50,4 @@ def step_scene(step):
                 Fs=np.asarray(step.Fs), shadow_res=tuple(step.shadow_res), shadow_step=step.shadow_step,
                 mips=int(step.rs.num_mips), falloff_col=fc, ambient=float(step.ambient),
                 bkg=np.asarray(step.bkg_host, np.float64), order=int(step.order), clamp=step.clamp,
-                boundary=S.CLAMP)
+                boundary=S.CLAMP, tonemap=getattr(step, 'tonemap', 'NONE'))

@@ -102,6 +102,33 @@ def test_bf16_storage_step_vs_fp64(gpu, order):
         assert e <= 1e-2, '%s gradient rel-L2 %.3g' % (name, e)
 
 
+@pytest.mark.parametrize('tonemap', ['CLIP_NEGATIVE', 'SATURATE', 'NORMALIZE'])
+def test_tonemapped_step_vs_fp64(gpu, tonemap):
+    """The captured step with the renderer's tonemapping folded into its loss
+    against the FP64 step oracle with the same tonemapping (FP32 tolerances,
+    outside the advection adjoint's discontinuities)."""
+    import tie_masks as TM
+    from scene_utils import step_scene
+    from gft.pipeline import RenderAdvectStep
+    from oracle import step as OS
+    st = RenderAdvectStep('tiny', gpu, tonemap=tonemap)
+    inp = st.make_inputs()
+    st.setup_static(inp)
+    st.capture(warmup=3)
+    loss, grads = st.replay()
+    torch.cuda.synchronize()
+    d0 = inp['d_prev'][0].astype(np.float64)
+    vel = [inp[k].astype(np.float64) for k in ('vx', 'vy', 'vz')]
+    ref_loss, _, ref_grads = OS.step(step_scene(st), d0, *vel, inp['target'])
+    assert abs(float(loss) - ref_loss) <= 1e-5 * abs(ref_loss)
+    dmask, vmask = TM.advect_masks(d0, *vel, order=st.order, clamp=st.clamp, reference=True)
+    masks = (dmask,) + TM.face_masks(vmask)
+    for name, g, r, m in zip(('density', 'vel_x', 'vel_y', 'vel_z'), grads, ref_grads, masks):
+        mm = np.broadcast_to(m.reshape(m.shape + (1,) * (r.ndim - m.ndim)), r.shape)
+        e = rel_l2(np.where(mm, 0.0, _np(g).reshape(r.shape)), np.where(mm, 0.0, r))
+        assert e <= 1e-4, '%s gradient rel-L2 %.3g' % (name, e)
+
+
 def test_checkpointed_chain_gradients(gpu):
     from gft.chain import TransportChain
     from gft.pipeline import RenderAdvectStep

@@ -227,3 +227,34 @@ def test_tonemap_ties_and_kinks_follow_tensor_autograd(mode):
     y.backward(torch.tensor(g))
     assert np.allclose(y.detach().numpy(), TM.tonemap(c, mode), rtol=0, atol=1e-15)
     assert np.allclose(t.grad.numpy(), TM.tonemap_grad(c, g, mode), rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize('mode', ['SATURATE', 'NORMALIZE'])
+def test_step_oracle_tonemapped_loss_fd(mode):
+    """The step oracle with the tonemapped loss is the true gradient of its
+    forward (set-up of test_step_oracle_gradient_fd, MacCormack without the
+    clamp)."""
+    from gft import synthetic as syn
+    from gft.pipeline import RenderAdvectStep
+    from oracle import step as OS
+    from scene_utils import step_scene
+    st = RenderAdvectStep('tiny', 'cpu', order=2, tonemap=mode)
+    sc = step_scene(st)
+    assert sc['tonemap'] == mode
+    sc['mips'] = 0
+    sc['clamp'] = 'NONE'
+    rng = np.random.default_rng(74)
+    d = syn.plume_density(st.shape, 7)[0].astype(np.float64) * 8 + 0.05 + 0.01 * rng.random(st.shape + (1,))
+    vel = [v[0].astype(np.float64) for v in syn.curl_velocity(st.shape, 8)]
+    tgt = rng.random((len(st.cams), st.res[1], st.res[2], 3)) * 0.3
+    _, _, grads = OS.step(sc, d, *vel, tgt, exact=True, shadow_grad='adjoint')
+    xs = [d] + vel
+    for k in range(4):
+        u = rng.standard_normal(xs[k].shape)
+
+        def loss(e):
+            a = [x.copy() for x in xs]
+            a[k] = a[k] + e * u
+            return OS.forward(sc, *a, tgt)[0]
+        fd = (loss(EPS) - loss(-EPS)) / (2 * EPS)
+        assert abs(fd - np.sum(grads[k] * u)) <= 1e-4 * abs(fd), (k, fd, np.sum(grads[k] * u))
