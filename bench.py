@@ -4,7 +4,7 @@ Workload (default ``cfg5``, the largest configuration, with BF16 storage and
 FP32 arithmetic): plume density 256x455x256 advected one MacCormack step
 (MC_SMOOTH, CLAMP) by a staggered curl-noise velocity field, spot light with a
 256x196x196 shadow frustum (4 mip levels, inverse-resampling gradients), 5
-perspective views of 960x540 with 256 depth samples, fused Beer-Lambert
+perspective portrait views of 540x960 (width x height) with 256 depth samples, fused Beer-Lambert
 raymarch, L2 image loss against seeded target renders; one step = forward +
 backward to the previous density and all three velocity components, replayed
 from one CUDA graph.  Synthetic seeded data stand in for ScalarFlow.
@@ -156,9 +156,10 @@ def workload_config(config, storage, grad_mode):
     from gft.pipeline import CONFIGS
     c = CONFIGS[config]
     D, H, W = c['grid']
-    Wi, Hi = c['image']
+    Hi, Wi = c['image']  # rows, columns (the pipeline's order)
     return {'workload': '%s: density %dx%dx%d (%s storage, fp32 arithmetic), MacCormack advect (MC_SMOOTH, CLAMP), '
-                        'spot-light shadow %s (%d mips), %d views %dx%d x%d samples, L2 image loss, fwd+bwd'
+                        'spot-light shadow %s (%d mips), %d views %dx%d (width x height) x%d samples, L2 image loss, '
+                        'fwd+bwd'
                         % (config, D, H, W, storage, 'x'.join(map(str, c['shadow'])), c['mips'], c['views'], Wi, Hi,
                            c['samples']),
             'config': config, 'storage': storage, 'grad_mode': grad_mode,
@@ -434,7 +435,51 @@ def extras(args, step, dev, timed, storage, inputs, ms):
             out['cpu_baseline'] = cpu_step.time_step(budget_s=args.cpu_budget, workers=1, config=args.config)
         except Exception as e:  # the baseline is reported, not required
             out['cpu_baseline'] = {'error': repr(e)}
+        out['fp64_subblock'] = fp64_subblock(step, dev, storage)
     return out
+
+
+def fp64_subblock(step, dev, storage, size=32):
+    """The headline step's raymarch (its own input: the light composition of
+    the advected density, stored as the step stores it) against the FP64
+    oracle on a size^3 block inside the plume: rel-L2 of the images over the
+    pixels whose rays reach the block and of the density gradient inside it,
+    for the adjoint of the step's image loss.  The oracle marches the
+    unrounded FP32 input, so BF16 storage rounding is part of the error.
+    (The oracle here is the checker, run on the host.)"""
+    import numpy as np
+    import torch
+    from gft import fused, ops
+    from oracle import subblock as SB
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
+        light = d * (step.shadow(d) * step.falloff_col + step.ambient)
+        data = (torch.cat([light, d], dim=-1) * step.depth_step).contiguous()
+    x = data.clone().requires_grad_(True)
+    y = ops.raymarch_grid_transform(x, step.M, step.V, step.P, step.F, step.res, storage_dtype=storage)
+    yl = y.detach().clone().requires_grad_(True)
+    fused.image_loss(yl[0], step.s_t, step.bkg_host).backward()
+    dy = yl.grad.contiguous()
+    (gx,) = torch.autograd.grad(y, x, dy)
+    D, H, W = step.shape
+    block = (D // 2 - size // 2, max(0, int(0.2 * H) - size // 2), W // 2 - size // 2)
+    x64 = data.double().cpu().numpy()
+    y_ref, g_ref, rows, cols = SB.raymarch_block(x64, step.M, step.V, step.P, step.F, step.res,
+                                                 dy.double().cpu().numpy(), block, size)
+    yg = y.detach().double().cpu().numpy()
+    gg = gx.detach().double().cpu().numpy()
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    img = max(rel(yg[0, c][rows[c], cols[c]], y_ref[0, c][rows[c], cols[c]]) for c in range(len(step.V)))
+    box = (0, slice(block[0], block[0] + size), slice(block[1], block[1] + size), slice(block[2], block[2] + size))
+    return {'image_rel_l2_max_over_views': img, 'density_grad_rel_l2': rel(gg[box], g_ref[box]),
+            'block': {'zyx': list(block), 'size': size}, 'storage': 'bf16' if storage is not None else 'f32',
+            'grad_mode': ops.get_grad_mode(), 'seconds': time.perf_counter() - t0,
+            'what': 'raymarch of the step vs the FP64 oracle on the rays reaching a block in the plume; '
+                    'adjoint of the step\'s image loss'}
 
 
 def other_config(config, args, dev, timed):

@@ -40,13 +40,13 @@ class RenderSettings:
 
 
 CONFIGS = {
-    # multi-view frame: 5 views 480x270, 192 samples, 3 mips, spot light + shadow volume
+    # multi-view frame: 5 views of 480x270 (height x width), 192 samples, 3 mips, spot light + shadow volume
     'cfg2': dict(grid=(128, 227, 128), views=5, image=(480, 270), samples=192, mips=3,
                  shadow=(256, 196, 196), seed=2000),
     # 64^3 single-view case for quick runs / CPU timing
     'cfg1': dict(grid=(64, 64, 64), views=1, image=(128, 128), samples=64, mips=3,
                  shadow=(64, 64, 64), seed=1000),
-    # stress grid 256x455x256, 5 views 960x540, 256 samples (one frame)
+    # stress grid 256x455x256, 5 views of 960x540 (height x width), 256 samples (one frame)
     'cfg5': dict(grid=(256, 455, 256), views=5, image=(960, 540), samples=256, mips=4,
                  shadow=(256, 196, 196), seed=5000),
     # tiny case for tests

@@ -156,32 +156,6 @@ def _box(b):
     return (slice(z0, z0 + BLOCK), slice(y0, y0 + BLOCK), slice(x0, x0 + BLOCK))
 
 
-def _pixel_windows(sc, b, margin_vox=2.0, margin_px=2):
-    """Per camera, the (rows, cols) slices of the pixels whose rays can reach
-    the block: the bounding rectangle of the projected block corners, the
-    block widened by ``margin_vox`` voxels (a sample reaches voxels within one
-    cell of its position) and the rectangle by ``margin_px`` pixels."""
-    from oracle import transforms as T
-    z0, y0, x0 = b
-    lo = np.array([x0, y0, z0], np.float64) - margin_vox
-    hi = lo + BLOCK + 2 * margin_vox
-    corners = np.array([[(hi if (k >> a) & 1 else lo)[a] for a in range(3)] for k in range(8)])
-    D, H, W = sc['res']
-    rows, cols = [], []
-    for c in range(len(sc['V'])):
-        cam = T.CameraXform(sc['M'][0], sc['V'][c], sc['P'][c], sc['F'][c])
-        ndc = T.os_to_ndc(cam, corners)
-        px = (ndc[:, 0] + 1.0) * W / 2.0 - 0.5
-        py = (ndc[:, 1] + 1.0) * H / 2.0 - 0.5
-        c0 = int(max(0, np.floor(px.min()) - margin_px))
-        c1 = int(min(W, np.ceil(px.max()) + margin_px + 1))
-        r0 = int(max(0, np.floor(py.min()) - margin_px))
-        r1 = int(min(H, np.ceil(py.max()) + margin_px + 1))
-        rows.append(slice(r0, max(r0, r1)))
-        cols.append(slice(c0, max(c0, c1)))
-    return rows, cols
-
-
 def _raymarch_input(sc, d):
     return (np.concatenate([d * 0.7, d * 0.5, d * 0.3, d], axis=-1) * sc['depth_step']).astype(np.float32)
 
@@ -211,15 +185,8 @@ def _raymarch_gpu(cfg, gpu, storage, mode, adjoint):
 
 
 def _raymarch_oracle(sc, x, dy_full, b, exact):
-    from oracle import raymarch as RM
-    rows, cols = _pixel_windows(sc, b)
-    x64 = x.astype(np.float64)
-    y = RM.raymarch_fwd(x64, sc['M'], sc['V'], sc['P'], sc['F'], sc['res'], rows=rows, cols=cols)
-    dy = np.zeros_like(y)
-    for c in range(len(sc['V'])):
-        dy[0, c][rows[c], cols[c]] = dy_full[0, c][rows[c], cols[c]]
-    g = RM.raymarch_bwd(x64, y, dy, sc['M'], sc['V'], sc['P'], sc['F'], sc['res'], exact=exact, rows=rows, cols=cols)
-    return y, g, rows, cols
+    from oracle import subblock as SB
+    return SB.raymarch_block(x, sc['M'], sc['V'], sc['P'], sc['F'], sc['res'], dy_full, b, BLOCK, exact)
 
 
 @pytest.mark.parametrize('storage', ['f32', 'bf16'])
