@@ -1080,13 +1080,9 @@ class _Advect(torch.autograd.Function):
         # MacCormack on one fp32 slice: run the forward in the gradient's
         # workspace and keep it, so that the backward reads the intermediate
         # semi-Lagrangian grid instead of recomputing it
-        # (not in the deterministic mode, whose adjoint recomputes the grid: a
-        # step captured while the autograd graph of an eager deterministic
-        # step with that workspace was still alive failed to capture)
         ws = None
-        if (any(ctx.needs_input_grad[:4]) and order == 2 and ds.shape[0] == 1 and ds is d
-                and d.dtype == torch.float32 and not _state['deterministic']):
-            ws = _advect_grad_workspace(d.shape, order, d.device)
+        if any(ctx.needs_input_grad[:4]) and order == 2 and ds.shape[0] == 1 and ds is d and d.dtype == torch.float32:
+            ws = _advect_grad_workspace(d.shape, order, d.device, _scatter_gmode())
         y = _advect_fwd(ds, vx, vy, vz, dt, order, clamp, boundary, ws=ws)
         # the workspace is a saved tensor, so that checkpointing drops and recomputes it
         ctx.save_for_backward(d, vx, vy, vz, ws)

@@ -39,6 +39,16 @@ class RenderSettings:
         self.blend_mode = 'BEER_LAMBERT'
 
 
+def _fresh_leaves(*ts):
+    """New leaf tensors on the same storage (the graph's static inputs keep
+    their memory).  A leaf's gradient accumulator records the stream of its
+    first use and lives as long as any autograd graph through the leaf; if
+    an eager step on the default stream still holds one, a capture of the
+    step on another stream would wait on the default stream, which CUDA
+    refuses during capture."""
+    return tuple(t.detach().requires_grad_(t.requires_grad) for t in ts)
+
+
 CONFIGS = {
     # multi-view frame: 5 views of 480x270 (height x width), 192 samples, 3 mips, spot light + shadow volume
     'cfg2': dict(grid=(128, 227, 128), views=5, image=(480, 270), samples=192, mips=3,
@@ -200,6 +210,7 @@ class RenderAdvectStep:
     def capture(self, warmup=3):
         """Captures step() on the static inputs into one CUDA graph (after
         tuning the launch-configuration knobs on them, with autotune)."""
+        self.s_d, self.s_vx, self.s_vy, self.s_vz = _fresh_leaves(self.s_d, self.s_vx, self.s_vy, self.s_vz)
         args = (self.s_d, self.s_vx, self.s_vy, self.s_vz, self.s_t)
         if self.autotune:
             from . import autotune as _at
@@ -322,6 +333,7 @@ class UnevenBatchStep:
         """Captures step() into one CUDA graph (after tuning the
         launch-configuration knobs on it, with autotune; the chosen values
         stay set and are kept in self.knobs)."""
+        (self.s_d,) = _fresh_leaves(self.s_d)
         if autotune:
             from . import autotune as _at
             self.knobs = _at.tune(lambda: self.step(self.s_d, self.s_t), key=_at.step_key(self), log=tune_log)

@@ -228,9 +228,9 @@ def test_advect_deterministic(ops, order, clamp, boundary, mode, C):
 def test_advect_deterministic_reuses_forward_intermediate(ops):
     """The deterministic MacCormack adjoint reading the forward's
     semi-Lagrangian grid from a deterministic-size workspace
-    (GFT_GRAD_FORWARD_READY) equals the one recomputing it, bit for bit; the
-    autograd op recomputes it (also when the mode is switched on between
-    forward and backward)."""
+    (GFT_GRAD_FORWARD_READY) equals the one recomputing it, bit for bit, as
+    does the autograd op (which reads it, or recomputes it when the mode is
+    switched on between forward and backward)."""
     from gft import synthetic as syn
     shape = (10, 12, 9)
     d = cuda(syn.plume_density(shape, 133))

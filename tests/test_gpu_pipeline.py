@@ -37,6 +37,23 @@ def test_graph_replay_equals_eager(gpu):
         assert rel_l2(_np(a), b) <= 1e-4
 
 
+def test_capture_while_an_eager_step_is_alive(gpu):
+    """Capturing the step while the autograd graph of an eager step through
+    the same static inputs is still referenced (the static inputs become
+    fresh leaves on the same memory)."""
+    from gft.pipeline import RenderAdvectStep
+    s = RenderAdvectStep('tiny', gpu)
+    d_before = s.setup_static(s.make_inputs())[0]
+    loss_e, grads_e = s.run_static()
+    s.capture(warmup=3)
+    assert s.s_d.data_ptr() == d_before.data_ptr()
+    loss_g, grads_g = s.replay()
+    torch.cuda.synchronize()
+    assert abs(float(loss_g) - float(loss_e)) <= 1e-5 * abs(float(loss_e))
+    for a, b in zip(grads_g, grads_e):
+        assert rel_l2(_np(a), _np(b)) <= 1e-4
+
+
 def test_streamed_steps_equal_single_steps(gpu):
     """StreamedSteps (inputs copied while the previous step runs, losses read
     one step late) gives each step the loss and gradients of running that
