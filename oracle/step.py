@@ -121,3 +121,17 @@ def step(sc, d_prev, vx, vy, vz, target, exact=False, shadow_grad='inverse'):
     """(loss, img [V,H,W,4], (g_d_prev, g_vx, g_vy, g_vz))."""
     loss, parts = forward(sc, d_prev, vx, vy, vz, target)
     return loss, parts['img'], backward(sc, d_prev, vx, vy, vz, parts, exact, shadow_grad)
+
+
+def scene_of(step):
+    """The scene dict of a render + advect step object that carries the
+    step's plain arrays as attributes (gft.pipeline.RenderAdvectStep: M, V,
+    P, F, res, depth_step, Vs, Ps, Fs, shadow_res, shadow_step, rs.num_mips,
+    falloff_col, ambient, bkg_host, order, clamp, tonemap)."""
+    fc = step.falloff_col.detach().cpu().numpy()[0].astype(np.float64)
+    return dict(M=np.asarray(step.M), V=np.asarray(step.V), P=np.asarray(step.P), F=np.asarray(step.F),
+                res=tuple(step.res), depth_step=step.depth_step, Vs=np.asarray(step.Vs), Ps=np.asarray(step.Ps),
+                Fs=np.asarray(step.Fs), shadow_res=tuple(step.shadow_res), shadow_step=step.shadow_step,
+                mips=int(step.rs.num_mips), falloff_col=fc, ambient=float(step.ambient),
+                bkg=np.asarray(step.bkg_host, np.float64), order=int(step.order), clamp=step.clamp,
+                boundary=S.CLAMP, tonemap=getattr(step, 'tonemap', 'NONE'))

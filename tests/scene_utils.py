@@ -43,11 +43,5 @@ def rel_l2(a, b):
 def step_scene(step):
     """The plain-array scene of a gft.pipeline.RenderAdvectStep for the FP64
     step oracle (oracle/step.py)."""
-    from oracle import sampling as S
-    fc = step.falloff_col.detach().cpu().numpy()[0].astype(np.float64)
-    return dict(M=np.asarray(step.M), V=np.asarray(step.V), P=np.asarray(step.P), F=np.asarray(step.F),
-                res=tuple(step.res), depth_step=step.depth_step, Vs=np.asarray(step.Vs), Ps=np.asarray(step.Ps),
-                Fs=np.asarray(step.Fs), shadow_res=tuple(step.shadow_res), shadow_step=step.shadow_step,
-                mips=int(step.rs.num_mips), falloff_col=fc, ambient=float(step.ambient),
-                bkg=np.asarray(step.bkg_host, np.float64), order=int(step.order), clamp=step.clamp,
-                boundary=S.CLAMP, tonemap=getattr(step, 'tonemap', 'NONE'))
+    from oracle import step as OS
+    return OS.scene_of(step)
