@@ -28,7 +28,7 @@ bool cuda_ok(cudaError_t e, const char* what) {
 static std::atomic<unsigned long long> g_launches{0};
 
 // launch-configuration knobs, defaults as documented in gft.h
-static std::atomic<int> g_knobs[GFT_KNOB_COUNT] = {{0}, {256}, {256}, {8}};
+static std::atomic<int> g_knobs[GFT_KNOB_COUNT] = {{0}, {256}, {256}, {8}, {0}};
 int knob_value(int k) { return (k >= 0 && k < GFT_KNOB_COUNT) ? g_knobs[k].load(std::memory_order_relaxed) : 0; }
 int sm_count() {
     int dev = 0, sms = 0;
@@ -39,6 +39,11 @@ int sm_count() {
 unsigned raymarch_blocks(int tiles) {
     const int k = knob_value(GFT_KNOB_RAYMARCH_BLOCKS_PER_SM);
     if (k <= 0) return (unsigned)std::max(tiles, 1);
+    return (unsigned)std::max(1, std::min(tiles, k * sm_count()));
+}
+unsigned weights_blocks(int tiles) {
+    const int k = knob_value(GFT_KNOB_WEIGHTS_BLOCKS_PER_SM);
+    if (k <= 0) return raymarch_blocks(tiles);
     return (unsigned)std::max(1, std::min(tiles, k * sm_count()));
 }
 
@@ -262,7 +267,8 @@ unsigned long long gft_launch_count(void) { return g_launches.load(std::memory_o
 gft_status gft_set_knob(int32_t knob, int32_t value) {
     bool ok = false;
     switch (knob) {
-        case GFT_KNOB_RAYMARCH_BLOCKS_PER_SM: ok = value >= 0 && value <= 32; break;
+        case GFT_KNOB_RAYMARCH_BLOCKS_PER_SM:
+        case GFT_KNOB_WEIGHTS_BLOCKS_PER_SM: ok = value >= 0 && value <= 32; break;
         case GFT_KNOB_ADVECT_THREADS:
         case GFT_KNOB_RESAMPLE_THREADS: ok = value == 64 || value == 128 || value == 256; break;
         case GFT_KNOB_SCAN_SEGMENTS: ok = value == 4 || value == 8 || value == 16; break;

@@ -78,6 +78,8 @@ int sm_count();  // SMs of the current device
 // Blocks of a raymarch launch over `tiles` pixel tiles under
 // GFT_KNOB_RAYMARCH_BLOCKS_PER_SM.
 unsigned raymarch_blocks(int tiles);
+// ... of the weight pass (GFT_KNOB_WEIGHTS_BLOCKS_PER_SM; 0: raymarch_blocks)
+unsigned weights_blocks(int tiles);
 
 // error helpers
 void set_error(const std::string& msg);

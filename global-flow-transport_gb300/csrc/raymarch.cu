@@ -1031,7 +1031,7 @@ static bool raymarch_weights_impl(const RaymarchArgs& a, const std::vector<Pair>
     }
     const dim3 block(RM_BX, RM_BY, 1);
     for (PairTable& t : make_tables(pairs)) {
-        const dim3 grid(raymarch_blocks((int)set_ray_tiles(t)));
+        const dim3 grid(weights_blocks((int)set_ray_tiles(t)));
         switch (a.boundary) {
             case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, s, a, ws_cnt, L.wacc, wscale, t); break;
             case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, s, a, ws_cnt, L.wacc, wscale, t); break;

@@ -3,7 +3,9 @@
 The knobs change only how kernels are launched -- the raymarch kernels' grid
 (one block per pixel tile, or a persistent grid of a few blocks per SM, which
 bounds how many tiles are in flight and so the set of gradient lines the
-adjoint's reductions keep in L2), the block size of the advection and
+adjoint's reductions keep in L2), the grid of the gradient's weight pass
+alone (which runs ahead on a side stream beside the forward kernels; a small
+persistent grid leaves them room), the block size of the advection and
 SampleGridTransform kernels, and the segment count of the transmittance scans
 -- never what they compute.  ``tune`` times a step for every candidate of
 every knob with CUDA events on the current stream (a coordinate search: each
@@ -30,6 +32,7 @@ KNOBS = {
     'advect_threads': (1, (256, 128, 64), 256),
     'resample_threads': (2, (256, 128, 64), 256),
     'scan_segments': (3, (8, 4, 16), 8),
+    'weights_blocks_per_sm': (4, (0, 1, 2, 4), 0),
 }
 
 _cache = {}

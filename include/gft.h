@@ -441,12 +441,20 @@ gft_status gft_image_loss_tonemap_grad(const float* image, const float* target, 
  *                                    256 (default)
  *   GFT_KNOB_SCAN_SEGMENTS           depth segments per column of the
  *                                    transmittance scans: 4, 8 (default) or 16
+ *   GFT_KNOB_WEIGHTS_BLOCKS_PER_SM   the grid of the reference-normalised
+ *                                    gradient's weight pass alone: 0
+ *                                    (default) as the other raymarch
+ *                                    kernels, 1-32 a persistent grid of that
+ *                                    many blocks per SM (a small grid leaves
+ *                                    room for the kernels it overlaps when it
+ *                                    runs ahead on another stream)
  * gft_set_knob returns GFT_ERR_INVALID_ARGUMENT for an unknown knob or value. */
 #define GFT_KNOB_RAYMARCH_BLOCKS_PER_SM 0
 #define GFT_KNOB_ADVECT_THREADS 1
 #define GFT_KNOB_RESAMPLE_THREADS 2
 #define GFT_KNOB_SCAN_SEGMENTS 3
-#define GFT_KNOB_COUNT 4
+#define GFT_KNOB_WEIGHTS_BLOCKS_PER_SM 4
+#define GFT_KNOB_COUNT 5
 gft_status gft_set_knob(int32_t knob, int32_t value);
 int32_t gft_get_knob(int32_t knob);
 

@@ -57,7 +57,8 @@ def test_persistent_raymarch_grid_equals_one_block_per_tile(gpu, mode):
         assert rel_l2(_np(g), _np(g0)) <= 1e-6, v
 
 
-@pytest.mark.parametrize('name', ['advect_threads', 'resample_threads', 'scan_segments', 'raymarch_blocks_per_sm'])
+@pytest.mark.parametrize('name', ['advect_threads', 'resample_threads', 'scan_segments', 'raymarch_blocks_per_sm',
+                                  'weights_blocks_per_sm'])
 def test_step_results_equal_for_every_knob_value(gpu, name):
     from gft import autotune
     from gft.pipeline import RenderAdvectStep
