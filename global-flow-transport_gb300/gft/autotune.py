@@ -32,7 +32,7 @@ KNOBS = {
     'advect_threads': (1, (256, 128, 64), 256),
     'resample_threads': (2, (256, 128, 64), 256),
     'scan_segments': (3, (8, 4, 16), 8),
-    'weights_blocks_per_sm': (4, (0, 1, 2, 4), 0),
+    'weights_blocks_per_sm': (4, (0, 2, 4, 6, 8), 0),
 }
 
 _cache = {}
