@@ -237,7 +237,12 @@ def bench_ours(args):
     inputs = step.make_inputs(frame=rank)
     step.setup_static(inputs)
     tune_log = {}
-    if not args.no_autotune:
+    if args.knobs:
+        # fixed launch-configuration knobs (e.g. for a profiler run of the tuned step)
+        from gft import autotune
+        autotune.apply({k: int(v) for k, v in (kv.split('=') for kv in args.knobs.split(','))})
+        step.knobs = autotune.knobs()
+    elif not args.no_autotune:
         # launch-configuration knobs timed on this workload before the capture
         from gft import autotune
         statics = (step.s_d, step.s_vx, step.s_vy, step.s_vz, step.s_t)
@@ -883,6 +888,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-chain5', action='store_true', help='skip the long transport chain on the headline grid')
     ap.add_argument('--no-autotune', action='store_true', help='default launch configuration (no tuning)')
+    ap.add_argument('--knobs', default=None, metavar='NAME=V,...',
+                    help='fixed launch-configuration knobs instead of tuning (gft.autotune.KNOBS names)')
     ap.add_argument('--chain-frames', type=int, default=120)
     ap.add_argument('--cpu-budget', type=float, default=20.0)
     ap.add_argument('--ref-budget', type=float, default=240.0,
