@@ -90,11 +90,14 @@ class _ComposeRaymarch(torch.autograd.Function):
         ctx.k = (float(ambient), float(scale))
         ctx.args = (M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary, blend, True, grid)
         ctx.mark_non_differentiable(xs)
+        ctx.set_materialize_grads(False)  # no zero-filled gradient for the stored input
         return y, xs
 
     @staticmethod
     def backward(ctx, dy, _dxs):
         d, tr, color, xs, y, samples = ctx.saved_tensors
+        if dy is None:
+            dy = torch.zeros_like(y)
         g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
         gd, gt = _compose_grad(d, tr, color, ctx.k[0], ctx.k[1], True, g)
         return (gd, gt) + (None,) * 12
