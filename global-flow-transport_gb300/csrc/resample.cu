@@ -8,6 +8,8 @@
 // per-camera transforms travel in the launch parameters.
 #include <algorithm>
 
+#include <cmath>
+
 #include "gft_internal.h"
 
 namespace gft {
@@ -426,9 +428,11 @@ __device__ __forceinline__ float4 sample_pos(const CamX& c, int cm, float3 idx, 
 // One kernel per coordinate mode (the transform and its LOD are inlined for
 // that mode only).  The transform sampler reads nothing under WRAP, as the
 // reference's (zeros for any coordinate mode).
+// lod: the sample's LOD is computed (mip modes, unless the host proved it
+// zero for every sample of the launch, reverse_lod_zero).
 template <int C, typename S, int BM, int CM>
 __global__ void __launch_bounds__(RS_THREADS)
-    k_sample_transform(Dims dout, int filter, int mip_mode, float bias, float cco, const MipSet ms,
+    k_sample_transform(Dims dout, int filter, int mip_mode, bool lod, float bias, float cco, const MipSet ms,
                        float* __restrict__ out, const __grid_constant__ PairTable tab) {
     const int64_t nv = voxels(dout);
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(RS_THREADS)
         const float3 din = make_float3((float)ms.dims[0].x, (float)ms.dims[0].y, (float)ms.dims[0].z);
         const float3 dinv = make_float3(1.f / (float)dout.x, 1.f / (float)dout.y, 1.f / (float)dout.z);
         const float4 pos = sample_pos_cm<CM>(tab.cam[p], make_float3(x + 0.5f, y + 0.5f, z + 0.5f), din, dinv,
-                                             mip_mode != MIP_NONE,
+                                             lod,
                                              BM == BM_BORDER && filter == F_LINEAR && cco == 0.5f, ms.occ,
                                              ms.occ_dims);
         if ((filter == F_LINEAR || filter == F_NEAREST) && !(pos.w < 0.f))
@@ -450,12 +454,105 @@ __global__ void __launch_bounds__(RS_THREADS)
     store<C>(out, (int64_t)tab.out_slot[p] * nv + v, r);
 }
 
+// The reverse modes (volume -> frustum grid) sample the frustum grid at
+// each volume voxel with the LOD of one voxel step measured in frustum cells
+// (the largest squared step length qm; LOD = max(0, log2(qm) / 2)).  Each
+// component of the map is scale * N / D + const with N and D affine in the
+// voxel position, so its derivative along axis k is scale * (N_k D - N D_k)
+// / D^2, whose numerator is affine: over a box its magnitude is at most the
+// largest |numerator| at the box's corners over the smallest D^2 there (D
+// keeping one sign).  The positions of the voxels and of their steps,
+// [0.5, n + 0.5] per axis, are cut into 8^3 boxes; a step along k is at most
+// the largest of these bounds per component.  If the squared length so
+// bounded stays below 0.98 (the rest absorbs the float rounding of the
+// kernel's differences) for every axis and pair, every sample's LOD is 0
+// and the kernel need not compute it: the result is the same.
+static bool reverse_lod_zero(const CamX& c, int cm, Dims vol, Dims frus) {
+    if (cm != CM_LINDEPTH_REVERSE && cm != CM_TRANSFORM_REVERSE) return false;
+    const float4 rows[4] = {c.r.r0, c.r.r1, c.r.r2, c.r.r3};
+    double X[4], Y[4], Z[4], Wc[4];
+    double* dst[4] = {X, Y, Z, Wc};
+    for (int i = 0; i < 4; ++i) {
+        dst[i][0] = rows[i].x, dst[i][1] = rows[i].y, dst[i][2] = rows[i].z, dst[i][3] = rows[i].w;
+    }
+    struct Comp {
+        double scale, n[4], d[4];
+    } comp[3];
+    comp[0].scale = 0.5 * frus.x;
+    comp[1].scale = 0.5 * frus.y;
+    for (int j = 0; j < 4; ++j) {
+        comp[0].n[j] = X[j], comp[0].d[j] = Wc[j];
+        comp[1].n[j] = Y[j], comp[1].d[j] = Wc[j];
+    }
+    if (cm == CM_LINDEPTH_REVERSE) {
+        // idx.z = -(z + near) / (far - near) * dims.z with z = -p23 w / (clip_z + p22 w)
+        const double range = (double)c.far_ - (double)c.near_;
+        if (!(std::fabs(range) > 0.0)) return false;
+        comp[2].scale = (double)frus.z / std::fabs(range);
+        for (int j = 0; j < 4; ++j) {
+            comp[2].n[j] = (double)c.p23 * Wc[j];
+            comp[2].d[j] = Z[j] + (double)c.p22 * Wc[j];
+        }
+    } else {
+        comp[2].scale = 0.5 * frus.z;
+        for (int j = 0; j < 4; ++j) comp[2].n[j] = Z[j], comp[2].d[j] = Wc[j];
+    }
+    constexpr int S = 8;
+    const double n3[3] = {(double)vol.x, (double)vol.y, (double)vol.z};
+    double bound[3][3] = {};  // [axis][component]
+    for (int bz = 0; bz < S; ++bz)
+        for (int by = 0; by < S; ++by)
+            for (int bx = 0; bx < S; ++bx) {
+                const int bi[3] = {bx, by, bz};
+                double lo[3], hi[3];
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = 0.5 + n3[a] * bi[a] / S;
+                    hi[a] = 0.5 + n3[a] * (bi[a] + 1) / S;
+                }
+                for (int i = 0; i < 3; ++i) {
+                    const Comp& f = comp[i];
+                    double nv[8], dv[8], dmin = INFINITY;
+                    int sign = 0;
+                    for (int corner = 0; corner < 8; ++corner) {
+                        double n = f.n[3], d = f.d[3];
+                        for (int a = 0; a < 3; ++a) {
+                            const double v = (corner >> a) & 1 ? hi[a] : lo[a];
+                            n += f.n[a] * v;
+                            d += f.d[a] * v;
+                        }
+                        const int sd = d > 0.0 ? 1 : (d < 0.0 ? -1 : 0);
+                        if (sd == 0 || (sign != 0 && sd != sign)) return false;
+                        sign = sd;
+                        nv[corner] = n;
+                        dv[corner] = d;
+                        dmin = std::min(dmin, std::fabs(d));
+                    }
+                    for (int k = 0; k < 3; ++k) {
+                        double num = 0.0;
+                        for (int corner = 0; corner < 8; ++corner)
+                            num = std::max(num, std::fabs(f.n[k] * dv[corner] - nv[corner] * f.d[k]));
+                        bound[k][i] = std::max(bound[k][i], f.scale * num / (dmin * dmin));
+                    }
+                }
+            }
+    double qm = 0.0;
+    for (int k = 0; k < 3; ++k)
+        qm = std::max(qm, bound[k][0] * bound[k][0] + bound[k][1] * bound[k][1] + bound[k][2] * bound[k][2]);
+    return qm < 0.98;
+}
+
 template <int C, typename S, int BM>
 static void st_fwd_cm(int cm, dim3 blocks, int T, cudaStream_t s, const SampleArgs& a, const MipSet& ms, float* out,
                       const PairTable& t) {
+    bool lod = a.mip_mode != MIP_NONE;
+    if (lod) {
+        bool zero = true;
+        for (int k = 0; k < t.n && zero; ++k) zero = reverse_lod_zero(t.cam[k], cm, a.dout, a.din);
+        lod = !zero;
+    }
 #define GFT_ST(CMV)                                                                                             \
-    k_sample_transform<C, S, BM, CMV><<<blocks, T, 0, s>>>(a.dout, a.filter, a.mip_mode, a.mip_bias, a.cco, ms, \
-                                                           out, t)
+    k_sample_transform<C, S, BM, CMV><<<blocks, T, 0, s>>>(a.dout, a.filter, a.mip_mode, lod, a.mip_bias, a.cco, \
+                                                           ms, out, t)
     switch (cm) {
         case CM_LINDEPTH: GFT_ST(CM_LINDEPTH); break;
         case CM_TRANSFORM: GFT_ST(CM_TRANSFORM); break;
@@ -473,7 +570,8 @@ static void st_fwd(int bm, dim3 blocks, int T, cudaStream_t s, const SampleArgs&
         case BM_CLAMP: st_fwd_cm<C, S, BM_CLAMP>(a.coord_mode, blocks, T, s, a, ms, out, t); break;
         default:
             k_sample_transform<C, S, BM_WRAP, CM_LINDEPTH><<<blocks, T, 0, s>>>(a.dout, a.filter, a.mip_mode,
-                                                                                a.mip_bias, a.cco, ms, out, t);
+                                                                                a.mip_mode != MIP_NONE, a.mip_bias,
+                                                                                a.cco, ms, out, t);
             break;
     }
 }
