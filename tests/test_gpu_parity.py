@@ -450,6 +450,34 @@ def test_sample_transform_sparse_volume(ops, cm, filt, boundary, mip, N):
         assert rel_l2(np_(y), ref) <= FWD_TOL
 
 
+@pytest.mark.parametrize('cm', ['TRANSFORM_LINDEPTH_REVERSE', 'TRANSFORM_REVERSE'])
+@pytest.mark.parametrize('frustum', ['coarse', 'fine'])
+def test_sample_transform_reverse_lod_bound(ops, cm, frustum):
+    """Frustum -> volume with mips and no bias: where every voxel step spans
+    less than one frustum cell (a coarse frustum) the LOD is 0 for every
+    sample and the launch may skip it; where some steps span more (a fine
+    frustum) it must be computed.  Both match the oracle over the whole
+    output, and the oracle's LOD range confirms which case each one is."""
+    from oracle import resample as R
+    from oracle import transforms as OT
+    shape = (24, 28, 24)
+    res = (8, 8, 8) if frustum == 'coarse' else (48, 56, 56)
+    _, _, M, V, P, F = scene(shape, 2, res)
+    ocm = OT.LINDEPTH_REVERSE if cm == 'TRANSFORM_LINDEPTH_REVERSE' else OT.TRANSFORM_REVERSE
+    x = small_grid(res, 1, 36)
+    y = ops.sample_grid_transform(cuda(x), M, V, P, F, shape, 'LINEAR', 'BORDER', 'LINEAR', 2, 0.0, cm)
+    ref = R.sample_grid_transform(x, M, V, P, F, shape, 1, 0, 2, 2, 0.0, ocm)
+    idx = np.stack(np.meshgrid(*[np.arange(n) + 0.5 for n in shape], indexing='ij'), -1)[..., ::-1]
+    lods = [OT.sample_positions(OT.CameraXform(M[0], V[c], P[c], F[c]), ocm, idx, np.array(res[::-1]),
+                                np.array(shape[::-1]), True)[..., 3].max() for c in range(2)]
+    if frustum == 'coarse':
+        assert max(lods) == 0.0
+    else:
+        assert max(lods) > 0.5
+    assert np.abs(ref).max() > 0
+    assert rel_l2(np_(y), ref) <= FWD_TOL
+
+
 @pytest.mark.parametrize('cm', CMS)
 @pytest.mark.parametrize('boundary', BOUNDS)
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
