@@ -827,12 +827,15 @@ def kernel_only(args):
         'raymarch_weights': lambda: ops._raymarch_weights((1,) + tuple(grid) + (4,), data.device, step.M, step.V,
                                                           step.P, step.F, step.res, 0, True),
     }
-    if args.kernel_only == 'raymarch_scatter':
+    if args.kernel_only in ('raymarch_scatter', 'raymarch_scatter_projected'):
+        from gft import fused
         ws = ops._raymarch_weights((1,) + tuple(grid) + (4,), data.device, step.M, step.V, step.P, step.F, step.res,
                                    0, True)
-        fns['raymarch_scatter'] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
-                                                            0, 0, True, ops.GRAD['REFERENCE'], weights=ws,
-                                                            grid=grid, samples=smp)
+        proj = (fused.compose_projection(step.light[1], step.ambient, step.depth_step)
+                if args.kernel_only == 'raymarch_scatter_projected' else None)
+        fns[args.kernel_only] = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1,
+                                                          0, 0, True, ops.GRAD['REFERENCE'], weights=ws,
+                                                          grid=grid, samples=smp, projection=proj)
     fn = fns[args.kernel_only]
     for _ in range(args.repeat):
         fn()
@@ -896,8 +899,8 @@ def main():
                     help='reference arm: seconds of whole FP64 iterations to run (at least one)')
     ap.add_argument('--save-clocks', default=None, metavar='CSV', help='write every clock sample to this file')
     ap.add_argument('--kernel-only', default=None,
-                    choices=['raymarch_fwd', 'raymarch_bwd', 'raymarch_weights', 'raymarch_scatter', 'advect_fwd',
-                             'advect_bwd', 'shadow_fwd'],
+                    choices=['raymarch_fwd', 'raymarch_bwd', 'raymarch_weights', 'raymarch_scatter',
+                             'raymarch_scatter_projected', 'advect_fwd', 'advect_bwd', 'shadow_fwd'],
                     help='run one op of the workload --repeat times (profiling)')
     ap.add_argument('--repeat', type=int, default=3)
     args = ap.parse_args()

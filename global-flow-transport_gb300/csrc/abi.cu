@@ -423,7 +423,7 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
                                      int32_t interpolation, int32_t boundary, int32_t blending_mode,
                                      int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
                                      size_t samples_bytes, float* input_grad, void* workspace,
-                                     size_t workspace_bytes, void* stream);
+                                     size_t workspace_bytes, void* stream, const float* projection = nullptr);
 
 gft_status gft_raymarch_grid_transform_grad(const void* input, int32_t input_dtype, const int64_t input_shape[5],
                                             const float* output, const float* output_grad, const float* matrix_m,
@@ -451,6 +451,20 @@ gft_status gft_raymarch_grid_transform_grad_stored(
                               workspace_bytes, stream);
 }
 
+gft_status gft_raymarch_grid_transform_grad_projected(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5], const float* output,
+    const float* output_grad, const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3], int32_t interpolation,
+    int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
+    size_t samples_bytes, const float projection[8], float* input_grad, void* workspace, size_t workspace_bytes,
+    void* stream) {
+    if (projection == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "projection is NULL");
+    return raymarch_grad_impl(input, input_dtype, input_shape, output, output_grad, matrix_m, num_m, matrix_v,
+                              matrix_p, frustum, num_cameras, output_shape, interpolation, boundary, blending_mode,
+                              separate_camera_batch, grad_mode, samples, samples_bytes, input_grad, workspace,
+                              workspace_bytes, stream, projection);
+}
+
 static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, const int64_t input_shape[5],
                                      const float* output, const float* output_grad, const float* matrix_m,
                                      int32_t num_m, const float* matrix_v, const float* matrix_p,
@@ -458,7 +472,7 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
                                      int32_t interpolation, int32_t boundary, int32_t blending_mode,
                                      int32_t separate_camera_batch, int32_t grad_mode, const float* samples,
                                      size_t samples_bytes, float* input_grad, void* workspace,
-                                     size_t workspace_bytes, void* stream) {
+                                     size_t workspace_bytes, void* stream, const float* projection) {
     std::string why;
     if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
@@ -482,6 +496,11 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_DETERMINISTIC computes its own weight sums");
     if (det && !det_blend_ok(blending_mode, input_shape[4]))
         return fail(GFT_ERR_UNIMPLEMENTED, "deterministic gradient: BEER_LAMBERT or ADDITIVE blending only");
+    if (projection != nullptr) {
+        if (input_shape[4] != 4) return fail(GFT_ERR_INVALID_ARGUMENT, "projected gradient: 4 channels only");
+        if (layout != LAYOUT_BRICK) return fail(GFT_ERR_INVALID_ARGUMENT, "projected gradient: brick layout only");
+        if (det) return fail(GFT_ERR_UNIMPLEMENTED, "projected gradient: not with GFT_GRAD_DETERMINISTIC");
+    }
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
@@ -513,8 +532,16 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
         a.store = raymarch_store_layout(const_cast<float*>(samples), samples_bytes, pairs, a.C, a.N, a.din);
     }
+    if (projection != nullptr) {
+        a.project = true;
+        for (int c = 0; c < 4; ++c) {
+            a.proj.a[c] = projection[c];
+            a.proj.b[c] = projection[4 + c];
+        }
+    }
     if ((st = check_aligned({input}, vec_bytes(a.C, input_dtype))) != GFT_OK ||
-        (st = check_aligned({output, output_grad, input_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
+        (st = check_aligned({output, output_grad}, vec_bytes(a.C, 0))) != GFT_OK ||
+        (st = check_aligned({input_grad}, vec_bytes(a.project ? 2 : a.C, 0))) != GFT_OK ||
         (st = check_workspace_aligned(samples)) != GFT_OK || (st = check_workspace_aligned(workspace)) != GFT_OK)
         return st;
     float* cnt = need > 0 ? reinterpret_cast<float*>(workspace) : nullptr;
@@ -1380,8 +1407,61 @@ gft_status gft_light_compose(const float* density, const float* transmittance, c
     if ((st = check_aligned({density, transmittance, light_color}, 4)) != GFT_OK ||
         (st = check_aligned({output}, bf16 ? 8 : 16)) != GFT_OK)
         return st;
-    if (!launch_light_compose(density, transmittance, light_color, (int)shape[0], dims_of(shape), ambient, scale,
-                              output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, bf16, output, as_stream(stream)))
+    if (!launch_light_compose(density, transmittance, light_color, nullptr, (int)shape[0], dims_of(shape), ambient,
+                              scale, output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, bf16, output, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose_factored(const float* density, const float* transmittance, const float* falloff,
+                                      const float light_rgb[3], const int64_t shape[5], float ambient, float scale,
+                                      int32_t output_layout, void* output, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    const bool bf16 = (output_layout & ~GFT_LAYOUT_BRICK) == GFT_DTYPE_BF16;
+    if (bf16) output_layout &= GFT_LAYOUT_BRICK;
+    if (!layout_ok(output_layout)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid layout");
+    if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
+    if (!density || !transmittance || !falloff || !light_rgb || !output)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({density, transmittance, falloff}, 4)) != GFT_OK ||
+        (st = check_aligned({output}, bf16 ? 8 : 16)) != GFT_OK)
+        return st;
+    if (!launch_light_compose(density, transmittance, falloff, light_rgb, (int)shape[0], dims_of(shape), ambient,
+                              scale, output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, bf16, output, as_stream(stream)))
+        return GFT_ERR_CUDA;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose_projection(const float light_rgb[3], float ambient, float scale, float projection[8]) {
+    if (light_rgb == nullptr || projection == nullptr) return fail(GFT_ERR_INVALID_ARGUMENT, "pointer is NULL");
+    for (int c = 0; c < 3; ++c) {
+        projection[c] = scale * light_rgb[c];
+        projection[4 + c] = scale * ambient;
+    }
+    projection[3] = 0.f;
+    projection[7] = scale;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose_factored_grad(const float* density, const float* transmittance, const float* falloff,
+                                           const int64_t shape[5], int32_t output_layout,
+                                           const float* projected_grad, float* density_grad,
+                                           float* transmittance_grad, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (!layout_ok(output_layout)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid layout");
+    if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
+    if (!density || !transmittance || !falloff || !projected_grad || !density_grad || !transmittance_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({density, transmittance, falloff, density_grad, transmittance_grad}, 4)) != GFT_OK ||
+        (st = check_aligned({projected_grad}, 8)) != GFT_OK)
+        return st;
+    if (!launch_light_compose_factored_grad(density, transmittance, falloff, projected_grad, (int)shape[0],
+                                            dims_of(shape), output_layout ? LAYOUT_BRICK : LAYOUT_FLAT, density_grad,
+                                            transmittance_grad, as_stream(stream)))
         return GFT_ERR_CUDA;
     return GFT_OK;
 }

@@ -127,18 +127,26 @@ __device__ __forceinline__ void store_cell(T* out, int64_t o, float r, float g, 
 
 // T: the output's storage type (float, or bf16 rounded to nearest even as a
 // separate conversion would round the fp32 result).
-template <int L, typename T>
+// FACT (a factored light): color[v, c] = falloff[v] * rgb[c], formed here by
+// the same single rounded product as a precomputed colour grid.
+struct Rgb {
+    float c[3];
+};
+
+template <int L, typename T, bool FACT>
 __global__ void __launch_bounds__(CP_THREADS)
     k_light_compose(const float* __restrict__ dens, const float* __restrict__ tr, const float* __restrict__ color,
-                    Dims d, float ambient, float scale, T* __restrict__ out) {
+                    const Rgb rgb, Dims d, float ambient, float scale, T* __restrict__ out) {
     const int64_t nvox = voxels(d), b = blockIdx.y;
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = b * nvox + v;
         const float dv = dens[i], t = tr[i];
+        const float fv = FACT ? color[v] : 0.f;
         float r[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float lc = __fmul_rn(dv, __fadd_rn(__fmul_rn(t, color[v * 3 + c]), ambient));
+            const float col = FACT ? __fmul_rn(fv, rgb.c[c]) : color[v * 3 + c];
+            const float lc = __fmul_rn(dv, __fadd_rn(__fmul_rn(t, col), ambient));
             r[c] = __fmul_rn(lc, scale);
         }
         int64_t o = i;
@@ -200,23 +208,68 @@ __global__ void __launch_bounds__(CP_THREADS)
     }
 }
 
-template <typename T>
-static void light_compose_t(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
-                            float scale, int layout, void* out, cudaStream_t st) {
-    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
-    if (layout == LAYOUT_BRICK)
-        k_light_compose<LAYOUT_BRICK, T><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, (T*)out);
-    else
-        k_light_compose<LAYOUT_FLAT, T><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, d, ambient, scale, (T*)out);
+// The adjoint of the factored composition from the raymarch gradient
+// projected onto (P, Q) = (scale rgb . g_rgb, scale (ambient sum(g_rgb) + g_a))
+// per cell: g_d = Q + t f P, g_t = d f P (the colour's per-voxel factor f
+// leaves the sums over samples).
+template <int L>
+__global__ void __launch_bounds__(CP_THREADS)
+    k_light_compose_factored_grad(const float* __restrict__ dens, const float* __restrict__ tr,
+                                  const float* __restrict__ fall, const float* __restrict__ g2, Dims d,
+                                  float* __restrict__ gd, float* __restrict__ gt) {
+    const int64_t nvox = voxels(d), b = blockIdx.y;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b * nvox + v;
+        int64_t o = i;
+        if constexpr (L == LAYOUT_BRICK) {
+            int x, y, z;
+            unflat32((uint32_t)v, d, x, y, z);
+            o = b * brick_cells(d) + brick_index(x, y, z, d);
+        }
+        const float2 pq = reinterpret_cast<const float2*>(g2)[o];
+        const float fp = __fmul_rn(fall[v], pq.x);
+        gd[i] = __fadd_rn(pq.y, __fmul_rn(tr[i], fp));
+        gt[i] = __fmul_rn(dens[i], fp);
+    }
 }
 
-bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
-                          float scale, int layout, bool bf16, void* out, cudaStream_t st) {
-    if (bf16)
-        light_compose_t<__nv_bfloat16>(dens, tr, color, N, d, ambient, scale, layout, out, st);
+template <typename T, bool FACT>
+static void light_compose_t(const float* dens, const float* tr, const float* color, const Rgb& rgb, int N, Dims d,
+                            float ambient, float scale, int layout, void* out, cudaStream_t st) {
+    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
+    if (layout == LAYOUT_BRICK)
+        k_light_compose<LAYOUT_BRICK, T, FACT><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, rgb, d, ambient, scale,
+                                                                            (T*)out);
     else
-        light_compose_t<float>(dens, tr, color, N, d, ambient, scale, layout, out, st);
+        k_light_compose<LAYOUT_FLAT, T, FACT><<<grid, CP_THREADS, 0, st>>>(dens, tr, color, rgb, d, ambient, scale,
+                                                                           (T*)out);
+}
+
+bool launch_light_compose(const float* dens, const float* tr, const float* color, const float* rgb3, int N, Dims d,
+                          float ambient, float scale, int layout, bool bf16, void* out, cudaStream_t st) {
+    Rgb rgb = {{0.f, 0.f, 0.f}};
+    if (rgb3 != nullptr) rgb = Rgb{{rgb3[0], rgb3[1], rgb3[2]}};
+    if (rgb3 != nullptr) {
+        if (bf16)
+            light_compose_t<__nv_bfloat16, true>(dens, tr, color, rgb, N, d, ambient, scale, layout, out, st);
+        else
+            light_compose_t<float, true>(dens, tr, color, rgb, N, d, ambient, scale, layout, out, st);
+    } else if (bf16) {
+        light_compose_t<__nv_bfloat16, false>(dens, tr, color, rgb, N, d, ambient, scale, layout, out, st);
+    } else {
+        light_compose_t<float, false>(dens, tr, color, rgb, N, d, ambient, scale, layout, out, st);
+    }
     return launched(1, "light compose launch");
+}
+
+bool launch_light_compose_factored_grad(const float* dens, const float* tr, const float* fall, const float* g2,
+                                        int N, Dims d, int layout, float* gd, float* gt, cudaStream_t st) {
+    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
+    if (layout == LAYOUT_BRICK)
+        k_light_compose_factored_grad<LAYOUT_BRICK><<<grid, CP_THREADS, 0, st>>>(dens, tr, fall, g2, d, gd, gt);
+    else
+        k_light_compose_factored_grad<LAYOUT_FLAT><<<grid, CP_THREADS, 0, st>>>(dens, tr, fall, g2, d, gd, gt);
+    return launched(1, "light compose gradient launch");
 }
 
 bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,

@@ -89,6 +89,11 @@ bool cuda_ok(cudaError_t e, const char* what);
 bool launched(int n, const char* what);
 
 // launchers ------------------------------------------------------------------
+// Two projections of a 4-channel gradient: (a . g, b . g).
+struct ChanProj {
+    float a[4], b[4];
+};
+
 struct RaymarchArgs {
     const void* input;
     int dtype;
@@ -116,6 +121,10 @@ struct RaymarchArgs {
     bool det = false;
     unsigned long long* det_acc = nullptr;  // set by launch_raymarch_bwd
     const float* det_scale = nullptr;
+    // Projected adjoint (C == 4, brick layout, float path): the gradient
+    // holds (proj.a . g, proj.b . g) per cell instead of the 4 channels of g.
+    bool project = false;
+    ChanProj proj = {};
 };
 // Workspace bytes of the deterministic adjoint for `pairs` (batch, camera) pairs.
 size_t raymarch_det_bytes(int N, int C, Dims din, size_t pairs);
@@ -195,8 +204,13 @@ bool launch_advect_bwd(const AdvectArgs& a, bool exact, bool forward_ready, cons
 // pipeline fusions (compose.cu)
 bool launch_transmittance(const float* s, int N, Dims d, float* out, cudaStream_t st);
 bool launch_transmittance_grad(const float* tr, const float* g, int N, Dims d, float* gs, cudaStream_t st);
-bool launch_light_compose(const float* dens, const float* tr, const float* color, int N, Dims d, float ambient,
-                          float scale, int layout, bool bf16, void* out, cudaStream_t st);
+// rgb3 != nullptr: color is the per-voxel falloff [V] of a factored light
+// (colour = falloff x rgb3), else the colour grid [V, 3].
+bool launch_light_compose(const float* dens, const float* tr, const float* color, const float* rgb3, int N, Dims d,
+                          float ambient, float scale, int layout, bool bf16, void* out, cudaStream_t st);
+// g2: the projected raymarch gradient (P, Q) per cell of layout `layout`.
+bool launch_light_compose_factored_grad(const float* dens, const float* tr, const float* fall, const float* g2,
+                                        int N, Dims d, int layout, float* gd, float* gt, cudaStream_t st);
 bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
                                float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st);
 int image_loss_blocks(int64_t npix);

@@ -655,12 +655,22 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 // full.  (Non-finite adjoints are not propagated through skipped samples.)
 // Every lane stays in the loop to its warp's last step (scatter_step is
 // warp-collective); lanes without a sample at a step pass act = false.
-template <int C, typename S, int BM, int MODE, int L, bool DET>
+//
+// PROJ (C == 4, float path): each sample's 4-channel adjoint is projected
+// onto two channels, (pj.a . g, pj.b . g), before its corner reduction, and
+// the gradient holds those two per cell.  A caller whose next adjoint is
+// linear in the four channels with coefficients of the form
+// (per-voxel factor) x (constant) -- the light composition -- needs only the
+// two sums, and the reductions move half the bytes.
+template <int C, typename S, int BM, int MODE, int L, bool DET, bool PROJ>
 __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, Dims din, int blend_mode,
                                                       const float* __restrict__ out, const float* __restrict__ dout,
                                                       float* __restrict__ grad, const float* __restrict__ cnt,
                                                       unsigned long long* __restrict__ iacc, float iscale,
-                                                      const RaymarchArgs::Store& st, const PairTable& tab, int tile) {
+                                                      const RaymarchArgs::Store& st, const PairTable& tab, int tile,
+                                                      const ChanProj& pj) {
+    static_assert(!PROJ || (C == 4 && MODE != 2 && !DET), "projection: 4-channel float adjoint only");
+    constexpr int CA = PROJ ? 2 : C;  // channels of the accumulated gradient
     RayPix r;
     r.tile = tile;
     const bool live = ray_pixel(tab, r);
@@ -683,7 +693,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
         }
     const S* g = in + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
     float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * brick_cells(din)
-                           : grad + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
+                           : grad + (size_t)tab.in_batch[p] * slice_cells<L>(din) * CA;
     const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * brick_cells(din) : nullptr;
     Vec<C> acc = vzero<C>(), go = vzero<C>();
     if (MODE != 2 && live) {
@@ -743,26 +753,33 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             if (resample) smp = fetch_linear<C, S, BM, L>(g, din, px, py, pz);
             val = blend_grad<C>(blend_mode, MODE == 0, go, smp, acc);
         }
-        scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);
+        if constexpr (PROJ) {
+            Vec<2> pv;
+            pv.v[0] = pj.a[0] * val.v[0] + pj.a[1] * val.v[1] + pj.a[2] * val.v[2] + pj.a[3] * val.v[3];
+            pv.v[1] = pj.b[0] * val.v[0] + pj.b[1] * val.v[1] + pj.b[2] * val.v[2] + pj.b[3] * val.v[3];
+            scatter_step<2, BM, MODE, L, false>(dst, count, din, on, px, py, pz, pv);
+        } else {
+            scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);
+        }
     }
 }
 
 // At least 6 resident blocks per SM: the tile loop would otherwise take 90
 // registers (5 blocks); with the bound it stays at the 80 of one tile per
 // block, without spills.
-template <int C, typename S, int BM, int MODE, int L, bool DET = false>
+template <int C, typename S, int BM, int MODE, int L, bool DET = false, bool PROJ = false>
 __global__ void __launch_bounds__(RM_BX* RM_BY, 6)
     k_raymarch_scatter(const S* __restrict__ in, Dims din, int blend_mode, const float* __restrict__ out,
                        const float* __restrict__ dout, float* __restrict__ grad, const float* __restrict__ cnt,
                        unsigned long long* __restrict__ iacc, const float* __restrict__ iscale_ptr, float wscale,
-                       const RaymarchArgs::Store st, const __grid_constant__ PairTable tab) {
+                       const RaymarchArgs::Store st, const __grid_constant__ PairTable tab, const ChanProj pj) {
     // integer accumulation: MODE 2 with the host's weight scale, the adjoint
     // with the scale its bound kernel wrote
     const float iscale = !DET ? 0.f : MODE == 2 ? wscale : *iscale_ptr;
     const int tiles = tab.tile0[tab.n];
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
-        raymarch_scatter_tile<C, S, BM, MODE, L, DET>(in, din, blend_mode, out, dout, grad, cnt, iacc, iscale, st, tab,
-                                                 tile);
+        raymarch_scatter_tile<C, S, BM, MODE, L, DET, PROJ>(in, din, blend_mode, out, dout, grad, cnt, iacc, iscale,
+                                                             st, tab, tile, pj);
 }
 
 template <int C, typename S, int BM>
@@ -813,19 +830,31 @@ bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, 
 template <int C, typename S, int BM, int L>
 static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, const RaymarchArgs& a, const float* out,
                            const float* dout, float* grad, const float* cnt, const PairTable& t) {
+    const ChanProj pj = a.proj;
+    if constexpr (C == 4 && L == LAYOUT_BRICK) {
+        if (a.project) {  // the ABI admits it for the float path only
+            if (exact)
+                k_raymarch_scatter<C, S, BM, 0, L, false, true><<<grid, block, 0, s>>>(
+                    (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, nullptr, nullptr, 0.f, a.store, t, pj);
+            else
+                k_raymarch_scatter<C, S, BM, 1, L, false, true><<<grid, block, 0, s>>>(
+                    (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, nullptr, nullptr, 0.f, a.store, t, pj);
+            return;
+        }
+    }
     if (a.det) {
         if (exact)
             k_raymarch_scatter<C, S, BM, 0, L, true><<<grid, block, 0, s>>>(
-                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
+                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t, pj);
         else
             k_raymarch_scatter<C, S, BM, 1, L, true><<<grid, block, 0, s>>>(
-                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t);
+                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t, pj);
     } else if (exact) {
         k_raymarch_scatter<C, S, BM, 0, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, nullptr, nullptr, 0.f, a.store, t);
+                                                                     cnt, nullptr, nullptr, 0.f, a.store, t, pj);
     } else {
         k_raymarch_scatter<C, S, BM, 1, L><<<grid, block, 0, s>>>((const S*)a.input, a.din, a.blend, out, dout, grad,
-                                                                     cnt, nullptr, nullptr, 0.f, a.store, t);
+                                                                     cnt, nullptr, nullptr, 0.f, a.store, t, pj);
     }
 }
 
@@ -853,10 +882,12 @@ static void weights_dispatch(dim3 grid, dim3 block, cudaStream_t s, const Raymar
                              unsigned long long* wacc, float wscale, const PairTable& t) {
     if (wacc != nullptr)
         k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT, true><<<grid, block, 0, s>>>(
-            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, wacc, nullptr, wscale, RaymarchArgs::Store{}, t);
+            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, wacc, nullptr, wscale, RaymarchArgs::Store{}, t,
+            ChanProj{});
     else
         k_raymarch_scatter<1, float, BM, 2, LAYOUT_FLAT><<<grid, block, 0, s>>>(
-            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, 0.f, RaymarchArgs::Store{}, t);
+            nullptr, a.din, a.blend, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, 0.f, RaymarchArgs::Store{}, t,
+            ChanProj{});
 }
 
 // Weight sums -> their reciprocals (0 where no sample reached the voxel), 16
@@ -1064,7 +1095,7 @@ bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pair
                          cudaStream_t s) {
     RaymarchArgs a = a_in;
     const int64_t cells = a.layout == LAYOUT_BRICK ? brick_cells(a.din) : voxels(a.din);
-    const int64_t n = cells * a.C * a.N;
+    const int64_t n = cells * (a.project ? 2 : a.C) * a.N;
     if (!a.det) {
         if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * n, s), "zero gradient")) return false;
         if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;

@@ -54,6 +54,9 @@ _SIGS = {
     'gft_raymarch_grid_transform_samples_min_size': (_SZ, [_I64P, _I32, _I32P, _I32]),
     'gft_raymarch_grid_transform_grad_stored': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                                        _I32, _I32, _I32, _I32, _I32, _P, _SZ, _P, _P, _SZ, _P]),
+    'gft_raymarch_grid_transform_grad_projected': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32,
+                                                          _I32P, _I32, _I32, _I32, _I32, _I32, _P, _SZ, _P, _P, _P,
+                                                          _SZ, _P]),
     'gft_raymarch_grid_transform_grad_workspace_size': (_SZ, [_I64P, _I32, _I32, _I32]),
     'gft_raymarch_grid_transform_grad': (_I32, [_P, _I32, _I64P, _P, _P, _P, _I32, _P, _P, _P, _I32, _I32P,
                                                 _I32, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
@@ -63,6 +66,9 @@ _SIGS = {
     'gft_transmittance_grad': (_I32, [_P, _P, _I64P, _P, _P]),
     'gft_light_compose': (_I32, [_P, _P, _P, _I64P, _F, _F, _I32, _P, _P]),
     'gft_light_compose_grad': (_I32, [_P, _P, _P, _I64P, _F, _F, _I32, _P, _P, _P, _P]),
+    'gft_light_compose_factored': (_I32, [_P, _P, _P, _P, _I64P, _F, _F, _I32, _P, _P]),
+    'gft_light_compose_projection': (_I32, [_P, _F, _F, _P]),
+    'gft_light_compose_factored_grad': (_I32, [_P, _P, _P, _I64P, _I32, _P, _P, _P, _P]),
     'gft_image_loss_workspace_size': (_SZ, [ctypes.c_int64]),
     'gft_image_loss': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _SZ, _P]),
     'gft_image_loss_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),

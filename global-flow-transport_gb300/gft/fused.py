@@ -74,20 +74,65 @@ def _compose_grad(d, tr, color, ambient, scale, brick, g):
     return gd, gt
 
 
+def _compose_factored(d, tr, fall, rgb, ambient, scale, bf16):
+    lib = _lib.load()
+    dt = torch.bfloat16 if bf16 else torch.float32
+    out = torch.empty((d.shape[0], ops.brick_cells(d.shape[1:4]), 4), dtype=dt, device=d.device)
+    layout = ops.LAYOUT_BRICK | (1 if bf16 else 0)  # | GFT_DTYPE_BF16
+    with torch.cuda.device(d.device):
+        _lib.check(lib.gft_light_compose_factored(_p(d), _p(tr), _p(fall), _p(rgb), _shape(d), float(ambient),
+                                                  float(scale), layout, _p(out), _stream(d.device)),
+                   'LightComposeFactored')
+    return out
+
+
+def compose_projection(rgb, ambient, scale):
+    """The 8 floats projecting a 4-channel raymarch gradient onto the two sums
+    the factored composition's adjoint reads (gft_light_compose_projection)."""
+    lib = _lib.load()
+    rgb = np.ascontiguousarray(np.asarray(rgb, dtype=np.float32).reshape(3))
+    proj = np.zeros(8, np.float32)
+    _lib.check(lib.gft_light_compose_projection(_p(rgb), float(ambient), float(scale), _p(proj)), 'ComposeProjection')
+    return proj
+
+
+def _compose_factored_grad(d, tr, fall, g2):
+    lib = _lib.load()
+    g2 = g2.contiguous()
+    gd = torch.empty_like(d)
+    gt = torch.empty_like(tr)
+    with torch.cuda.device(d.device):
+        _lib.check(lib.gft_light_compose_factored_grad(_p(d), _p(tr), _p(fall), _shape(d), ops.LAYOUT_BRICK, _p(g2),
+                                                       _p(gd), _p(gt), _stream(d.device)), 'LightComposeFactoredGrad')
+    return gd, gt
+
+
 class _ComposeRaymarch(torch.autograd.Function):
     """light_compose(brick=True) followed by the bricked raymarch, as one
     autograd op: the composition writes the raymarch input directly in its
     storage type (bf16 or fp32), and the raymarch's fp32 gradient reaches the
-    composition's adjoint without being rounded to the storage type."""
+    composition's adjoint without being rounded to the storage type.
+
+    With a factored light (rgb not None: color is the per-voxel falloff, the
+    light colour falloff x rgb) the raymarch adjoint accumulates only the two
+    projections of its 4-channel gradient that the composition's adjoint
+    reads (gft_raymarch_grid_transform_grad_projected): half the reduction
+    bytes.  The deterministic adjoint forms the 4 channels and projects them
+    afterwards."""
 
     @staticmethod
-    def forward(ctx, d, tr, color, ambient, scale, grid, M, V, P, F, out_shape, boundary, blend, storage_dtype):
-        xs = _compose(d, tr, color, ambient, scale, True, storage_dtype == torch.bfloat16)
+    def forward(ctx, d, tr, color, rgb, ambient, scale, grid, M, V, P, F, out_shape, boundary, blend, storage_dtype):
+        bf16 = storage_dtype == torch.bfloat16
+        if rgb is None:
+            xs = _compose(d, tr, color, ambient, scale, True, bf16)
+        else:
+            xs = _compose_factored(d, tr, color, rgb, ambient, scale, bf16)
         need = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
         y, samples = ops._raymarch_forward_ctx(ctx, xs, need, M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary,
                                                blend, True, grid)
         ctx.save_for_backward(d, tr, color, xs, y, samples)
         ctx.k = (float(ambient), float(scale))
+        ctx.rgb = rgb
         ctx.args = (M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary, blend, True, grid)
         ctx.mark_non_differentiable(xs)
         ctx.set_materialize_grads(False)  # no zero-filled gradient for the stored input
@@ -98,9 +143,20 @@ class _ComposeRaymarch(torch.autograd.Function):
         d, tr, color, xs, y, samples = ctx.saved_tensors
         if dy is None:
             dy = torch.zeros_like(y)
-        g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
-        gd, gt = _compose_grad(d, tr, color, ctx.k[0], ctx.k[1], True, g)
-        return (gd, gt) + (None,) * 12
+        if ctx.rgb is None:
+            g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
+            gd, gt = _compose_grad(d, tr, color, ctx.k[0], ctx.k[1], True, g)
+        else:
+            proj = compose_projection(ctx.rgb, *ctx.k)
+            if ops._state['deterministic']:
+                g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
+                a, b = [float(v) for v in proj[:4]], [float(v) for v in proj[4:]]  # host scalars: capturable
+                g2 = torch.stack([g[..., 0] * a[0] + g[..., 1] * a[1] + g[..., 2] * a[2] + g[..., 3] * a[3],
+                                  g[..., 0] * b[0] + g[..., 1] * b[1] + g[..., 2] * b[2] + g[..., 3] * b[3]], -1)
+            else:
+                g2 = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args, projection=proj)
+            gd, gt = _compose_factored_grad(d, tr, color, g2)
+        return (gd, gt) + (None,) * 13
 
 
 def render_bricked(density, transmittance, light_color, ambient, scale, matrix_m, matrix_v, matrix_p,
@@ -108,19 +164,36 @@ def render_bricked(density, transmittance, light_color, ambient, scale, matrix_m
     """raymarch_grid_transform_bricked(light_compose(density, transmittance,
     light_color, ambient, scale, brick=True), density's grid, ...) in one
     autograd op; with storage_dtype=torch.bfloat16 the composition writes the
-    raymarch input in bf16 directly.  Returns (images [1, V, H, W, 4], the
-    raymarch input as stored: [1, brick_cells, 4], no gradient)."""
+    raymarch input in bf16 directly.  light_color: a [D, H, W, 3] colour grid,
+    or a factored light (falloff [D, H, W, 1], rgb of 3 host floats) whose
+    colour is falloff * rgb (a point or spot light; the adjoint then
+    accumulates two channels instead of four).  Returns (images
+    [1, V, H, W, 4], the raymarch input as stored: [1, brick_cells, 4], no
+    gradient)."""
     d = _cuda(density, 'density')
     tr = _cuda(transmittance, 'transmittance')
-    color = _cuda(light_color, 'light_color')
     if d.dim() != 5 or d.shape[4] != 1 or tuple(tr.shape) != tuple(d.shape):
         raise _lib.GftInvalidArgument('density and transmittance must both be [N, D, H, W, 1]')
-    if color.numel() != int(np.prod(d.shape[1:4])) * 3 or color.shape[-1] != 3:
-        raise _lib.GftInvalidArgument('light_color must be [D, H, W, 3]')
+    nvox = int(np.prod(d.shape[1:4]))
+    if isinstance(light_color, (tuple, list)):
+        if len(light_color) != 2:
+            raise _lib.GftInvalidArgument('a factored light is (falloff [D, H, W, 1], rgb [3])')
+        color = _cuda(light_color[0], 'falloff')
+        rgb = light_color[1]
+        if isinstance(rgb, torch.Tensor):
+            rgb = rgb.detach().cpu().numpy()
+        rgb = np.ascontiguousarray(np.asarray(rgb, dtype=np.float32).reshape(3))
+        if color.numel() != nvox or color.shape[-1] != 1:
+            raise _lib.GftInvalidArgument('falloff must be [D, H, W, 1]')
+    else:
+        color = _cuda(light_color, 'light_color')
+        rgb = None
+        if color.numel() != nvox * 3 or color.shape[-1] != 3:
+            raise _lib.GftInvalidArgument('light_color must be [D, H, W, 3]')
     if storage_dtype not in (None, torch.float32, torch.bfloat16):
         raise _lib.GftInvalidArgument('storage_dtype must be float32 or bfloat16')
     grid = tuple(int(v) for v in d.shape[1:4])
-    return _ComposeRaymarch.apply(d, tr, color.detach(), ambient, scale, grid, matrix_m, matrix_v, matrix_p,
+    return _ComposeRaymarch.apply(d, tr, color.detach(), rgb, ambient, scale, grid, matrix_m, matrix_v, matrix_p,
                                   frustum_params, ops._shape3(output_shape), ops._enum(ops.BOUNDARY, boundary, 'boundary'),
                                   ops._enum(ops.BLEND, blending_mode, 'blending_mode'), storage_dtype)
 

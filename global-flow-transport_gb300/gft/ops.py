@@ -404,7 +404,9 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
 
 
 def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None,
-                  grid=None, samples=None):
+                  grid=None, samples=None, projection=None):
+    """projection (8 host floats, bricked 4-channel x): the gradient
+    accumulated projected onto two channels, [N, cells, 2]."""
     lib = _lib.load()
     Mh, nm = _mats(M)
     Vh, nv = _mats(V)
@@ -412,7 +414,8 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
     Fh, _ = _frustum(F)
     shape5, code = _grid5(x, grid)
     shape = _lib.i64(shape5)
-    grad = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+    gshape = x.shape if projection is None else tuple(x.shape[:-1]) + (2,)
+    grad = torch.empty(gshape, dtype=torch.float32, device=x.device)
     if weights is not None and gmode == GRAD['REFERENCE']:
         ws = weights
         gmode = gmode | WEIGHTS_READY
@@ -420,7 +423,14 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
         ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode),
                         x.device)
     with torch.cuda.device(x.device):
-        if samples is None:
+        if projection is not None:
+            proj = np.ascontiguousarray(np.asarray(projection, dtype=np.float32).reshape(8))
+            st = lib.gft_raymarch_grid_transform_grad_projected(
+                _p(x), code, shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv, _lib.i32(out_shape),
+                interp, boundary, blend, int(separate), gmode, _p(samples) if samples is not None else None,
+                samples.numel() if samples is not None else 0, _p(proj), _p(grad), _p(ws), ws.numel(),
+                _stream(x.device))
+        elif samples is None:
             st = lib.gft_raymarch_grid_transform_grad(_p(x), code, shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
                                                       _p(Ph), _p(Fh), nv, _lib.i32(out_shape), interp, boundary,
                                                       blend, int(separate), gmode, _p(grad), _p(ws), ws.numel(),
@@ -456,15 +466,17 @@ def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, bou
     return y, samples
 
 
-def _raymarch_backward_ctx(ctx, xs, y, samples, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, grid):
-    """The fp32 input gradient of a raymarch run by _raymarch_forward_ctx."""
+def _raymarch_backward_ctx(ctx, xs, y, samples, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, grid,
+                           projection=None):
+    """The fp32 input gradient of a raymarch run by _raymarch_forward_ctx
+    (projected onto two channels with ``projection``)."""
     ws = None
     if ctx.weights is not None:
         ws, ev = ctx.weights
         if ev is not None:
             torch.cuda.current_stream(xs.device).wait_event(ev)
     g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                      _scatter_gmode(), weights=ws, grid=grid, samples=samples)
+                      _scatter_gmode(), weights=ws, grid=grid, samples=samples, projection=projection)
     ctx.weights = None
     return g
 

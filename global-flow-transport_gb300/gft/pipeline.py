@@ -101,6 +101,8 @@ class RenderAdvectStep:
         fall = self.spot.falloff(_Holder(self.gt), self.dev)  # [D,H,W,1]
         col = torch.tensor(self.spot.c * np.float32(self.spot.i), dtype=torch.float32, device=self.dev)
         self.falloff_col = (fall * col)[None].contiguous()  # [1,D,H,W,3]
+        # the same light factored (falloff x colour) for the fused render
+        self.light = (fall.contiguous(), col.cpu().numpy())
         self.bkg_host = np.array([0.0, 0.5, 1.0], dtype=np.float32)
         self.bkg = torch.from_numpy(self.bkg_host).to(self.dev)
         self.graph = None
@@ -161,7 +163,7 @@ class RenderAdvectStep:
         else:
             # the light composition writes the raymarch input directly, in the
             # brick layout and the storage type
-            img, xs = fused.render_bricked(d, self.shadow(d), self.falloff_col, self.ambient, self.depth_step,
+            img, xs = fused.render_bricked(d, self.shadow(d), self.light, self.ambient, self.depth_step,
                                            self.M, self.V, self.P, self.F, self.res,
                                            storage_dtype=self.storage_dtype)
             if self.fp64_check:

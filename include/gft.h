@@ -156,6 +156,25 @@ gft_status gft_raymarch_grid_transform_grad_stored(
     int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
     int32_t grad_mode, const float* samples, size_t samples_bytes, float* input_grad,
     void* workspace, size_t workspace_bytes, void* stream);
+/* gft_raymarch_grid_transform_grad_projected: gft_raymarch_grid_transform_grad_stored
+ * (samples may be NULL: the grid is re-sampled, as gft_raymarch_grid_transform_grad)
+ * whose gradient is accumulated already projected onto two channels:
+ * input_grad [N, cells, 2] holds (projection[0..3] . g, projection[4..7] . g)
+ * per cell for the 4-channel gradient g of the plain call.  Each sample's
+ * 4-channel adjoint is projected before its trilinear reduction, so the
+ * reductions move half the bytes; the result equals the projection of the
+ * plain gradient up to float rounding.  4 channels, GFT_LAYOUT_BRICK,
+ * GFT_GRAD_REFERENCE or GFT_GRAD_EXACT (with GFT_GRAD_WEIGHTS_READY as
+ * usual), not GFT_GRAD_DETERMINISTIC; the same workspace.  No counterpart in
+ * the reference. */
+gft_status gft_raymarch_grid_transform_grad_projected(
+    const void* input, int32_t input_dtype, const int64_t input_shape[5],
+    const float* output, const float* output_grad,
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t interpolation, int32_t boundary, int32_t blending_mode, int32_t separate_camera_batch,
+    int32_t grad_mode, const float* samples, size_t samples_bytes, const float projection[8],
+    float* input_grad, void* workspace, size_t workspace_bytes, void* stream);
 /* The geometry-only first pass of the GFT_GRAD_REFERENCE raymarch gradient:
  * per (batch, camera) pair the reciprocals of the per-voxel sums of the
  * trilinear weights of all ray samples (the reference's float sampleCounter,
@@ -393,6 +412,29 @@ gft_status gft_light_compose_grad(const float* density, const float* transmittan
                                   const int64_t shape[5], float ambient, float scale, int32_t output_layout,
                                   const float* output_grad, float* density_grad, float* transmittance_grad,
                                   void* stream);
+/* A light whose colour is a per-voxel falloff times a constant colour (a
+ * point or spot light: falloff x color x intensity, phitest/render/lighting.py:49-70,
+ * the shadow map multiplied in at :144-147): gft_light_compose_factored is gft_light_compose
+ * with light_color[v, c] = falloff[v] * light_rgb[c] (falloff [D, H, W, 1],
+ * light_rgb 3 host floats), formed by the same rounded product as a
+ * precomputed colour grid, so the output is identical.  Its adjoint needs
+ * only two sums of the raymarch gradient g per cell:
+ * (P, Q) = (scale rgb . g_rgb, scale (ambient (g_r + g_g + g_b) + g_density)),
+ * i.e. the projection that gft_light_compose_projection writes (8 floats, for
+ * gft_raymarch_grid_transform_grad_projected); then
+ * density_grad = Q + transmittance * falloff * P and
+ * transmittance_grad = density * falloff * P.  projected_grad [N, cells, 2]
+ * fp32 in output_layout (rows or bricks).  No counterpart in the reference,
+ * which forms the 4-channel gradient and differentiates the composition by
+ * tensor ops. */
+gft_status gft_light_compose_factored(const float* density, const float* transmittance, const float* falloff,
+                                      const float light_rgb[3], const int64_t shape[5], float ambient, float scale,
+                                      int32_t output_layout, void* output, void* stream);
+gft_status gft_light_compose_projection(const float light_rgb[3], float ambient, float scale, float projection[8]);
+gft_status gft_light_compose_factored_grad(const float* density, const float* transmittance, const float* falloff,
+                                           const int64_t shape[5], int32_t output_layout,
+                                           const float* projected_grad, float* density_grad,
+                                           float* transmittance_grad, void* stream);
 /* gft_image_loss: image [pixels, 4] (rgb + density), target [pixels, 3],
  * background = 3 host floats; *loss (device) = mean over pixels and rgb of
  * (rgb + background * exp(-density) - target)^2, summed in a fixed order.

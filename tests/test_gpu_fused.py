@@ -140,6 +140,79 @@ def test_render_bricked_equals_compose_then_raymarch(fused, storage):
     assert rel_l2(_np(t1.grad), _np(t2.grad)) <= 1e-6
 
 
+@pytest.mark.parametrize('storage', [None, torch.bfloat16])
+@pytest.mark.parametrize('gmode', ['REFERENCE', 'EXACT', 'DETERMINISTIC'])
+@pytest.mark.parametrize('store', [True, False])
+def test_render_bricked_factored_light(fused, storage, gmode, store):
+    """A factored light (falloff [D, H, W, 1] x rgb): the composition forms
+    falloff * rgb by the same rounded product as a precomputed colour grid, so
+    the raymarch input and images equal those of the colour grid bit for bit;
+    the adjoint accumulates the two projections of the raymarch gradient that
+    the composition's adjoint reads (the deterministic adjoint: projected after
+    its integer sums), and the density and transmittance gradients equal the
+    colour grid's up to summation order."""
+    from gft import ops
+    from scene_utils import scene
+    g = torch.Generator().manual_seed(19)
+    D, H, W = 9, 13, 11
+    _, _, M, V, P, F = scene((D, H, W), 3, (13, 9, 11))
+    d0 = (torch.rand((1, D, H, W, 1), generator=g) * 0.3).cuda()
+    t0 = torch.rand((1, D, H, W, 1), generator=g).cuda()
+    fall = torch.rand((D, H, W, 1), generator=g).cuda()
+    rgb = np.array([0.9, 0.7, 1.3], np.float32)
+    col = (fall * torch.from_numpy(rgb).cuda())[None].contiguous()
+    dy = torch.randn((1, 3, 9, 11, 4), generator=g).cuda()
+    saved = ops.get_grad_mode(), ops._state['deterministic'], ops._state['sample_store']
+    try:
+        ops.set_grad_mode('EXACT' if gmode == 'EXACT' else 'REFERENCE')
+        ops.set_deterministic(gmode == 'DETERMINISTIC')
+        ops.set_raymarch_sample_store(store)
+        res = []
+        for light in ((fall, rgb), col):
+            d1, t1 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
+            img, xs = fused.render_bricked(d1, t1, light, 0.64, 0.37, M, V, P, F, (13, 9, 11),
+                                           storage_dtype=storage)
+            img.backward(dy)
+            res.append((img.detach(), ops.from_bricks(xs.float(), (D, H, W)), d1.grad, t1.grad))
+    finally:
+        ops.set_grad_mode(saved[0])
+        ops.set_deterministic(saved[1])
+        ops.set_raymarch_sample_store(saved[2])
+    (i1, x1, gd1, gt1), (i2, x2, gd2, gt2) = res
+    assert torch.equal(x1, x2)
+    assert torch.equal(i1, i2)
+    assert np.abs(_np(gd2)).max() > 0 and np.abs(_np(gt2)).max() > 0
+    assert rel_l2(_np(gd1), _np(gd2)) <= 1e-6
+    assert rel_l2(_np(gt1), _np(gt2)) <= 1e-6
+
+
+@pytest.mark.parametrize('gmode', ['REFERENCE', 'EXACT'])
+def test_raymarch_grad_projected(fused, gmode):
+    """gft_raymarch_grid_transform_grad_projected against the projection of the
+    plain 4-channel gradient (bricked input, both grad modes)."""
+    from gft import ops
+    from scene_utils import scene
+    g = torch.Generator().manual_seed(21)
+    D, H, W = 10, 14, 12
+    _, _, M, V, P, F = scene((D, H, W), 2, (12, 10, 9))
+    x = (torch.rand((1, D, H, W, 4), generator=g) * 0.3).cuda()
+    xb = ops.to_bricks(x)
+    y = ops.raymarch_grid_transform_bricked(xb, (D, H, W), M, V, P, F, (12, 10, 9)).detach().contiguous()
+    dy = torch.randn(y.shape, generator=g).cuda()
+    proj = np.array([0.3, -1.2, 0.7, 0.0, 0.5, 0.5, 0.5, 1.1], np.float32)
+    gm = ops.GRAD[gmode]
+    args = (xb, y, dy, M, V, P, F, (12, 10, 9), ops.FILTER['LINEAR'], ops.BOUNDARY['BORDER'],
+            ops.BLEND['BEER_LAMBERT'], True, gm)
+    g4 = ops._raymarch_bwd(*args, grid=(D, H, W))
+    g2 = ops._raymarch_bwd(*args, grid=(D, H, W), projection=proj)
+    assert tuple(g2.shape) == tuple(xb.shape[:-1]) + (2,)
+    pm = torch.from_numpy(proj.reshape(2, 4)).cuda()
+    ref = torch.stack([(g4 * pm[0]).sum(-1), (g4 * pm[1]).sum(-1)], -1)
+    a, b = _np(ops.from_bricks(g2, (D, H, W))), _np(ops.from_bricks(ref, (D, H, W)))
+    assert np.abs(b).max() > 0
+    assert rel_l2(a, b) <= 1e-6
+
+
 def test_fused_argument_errors(fused):
     from gft import _lib
     with pytest.raises(_lib.GftInvalidArgument):

@@ -238,6 +238,43 @@ def test_tonemap_and_deterministic_arguments(lib):
     assert L.gft_advect_grad_workspace_size_mode(shape, 2, 0x400 | 1) >= 16 * 20 * 12 * (6 * 4 + 3 * 4 + 2 * 4)
 
 
+def test_projected_gradient_and_factored_light_arguments(lib):
+    """The projected raymarch adjoint takes 4-channel bricked inputs on the
+    float path only; the composition's projection is (scale rgb, 0, scale
+    ambient x3, scale); checks happen before any launch."""
+    L = lib.load()
+    eye = np.eye(4, dtype=np.float32).reshape(-1)
+    fr = np.array([1, 3, -1, 1, 1, -1], dtype=np.float32)
+    p = eye.ctypes.data_as(ctypes.c_void_p)
+    f = fr.ctypes.data_as(ctypes.c_void_p)
+    out = lib.i32([4, 4, 4])
+    proj = np.zeros(8, np.float32)
+    pj = proj.ctypes.data_as(ctypes.c_void_p)
+    one = ctypes.c_void_p(1)
+    brick = 0x10
+
+    def grad(shape, code, mode, projection):
+        return L.gft_raymarch_grid_transform_grad_projected(one, code, lib.i64(shape), one, one, p, 1, p, p, f, 1,
+                                                            out, 1, 0, 0, 1, mode, None, 0, projection, one, None,
+                                                            0, None)
+    assert grad([1, 8, 8, 8, 4], brick, 1, None) == lib.ERR_INVALID_ARGUMENT
+    assert b'projection' in L.gft_last_error()
+    assert grad([1, 8, 8, 8, 2], brick, 1, pj) == lib.ERR_INVALID_ARGUMENT
+    assert b'4 channels' in L.gft_last_error()
+    assert grad([1, 8, 8, 8, 4], 0, 1, pj) == lib.ERR_INVALID_ARGUMENT
+    assert b'brick' in L.gft_last_error()
+    assert grad([1, 8, 8, 8, 4], brick, 0x400 | 1, pj) == lib.ERR_UNIMPLEMENTED
+    rgb = np.array([0.5, 2.0, -1.0], np.float32)
+    assert L.gft_light_compose_projection(rgb.ctypes.data_as(ctypes.c_void_p), 0.25, 4.0, pj) == lib.OK
+    assert proj.tolist() == [2.0, 8.0, -4.0, 0.0, 1.0, 1.0, 1.0, 4.0]
+    assert L.gft_light_compose_projection(None, 0.25, 4.0, pj) == lib.ERR_INVALID_ARGUMENT
+    shape = lib.i64([1, 4, 4, 4, 1])
+    assert L.gft_light_compose_factored(one, one, one, None, shape, 0.5, 1.0, brick, one, None) == \
+        lib.ERR_INVALID_ARGUMENT
+    assert L.gft_light_compose_factored_grad(one, one, one, shape, 7, one, one, one, None) == \
+        lib.ERR_INVALID_ARGUMENT
+
+
 def test_workspace_sizes(lib):
     L = lib.load()
     s = lib.i64([2, 16, 20, 12, 2])
