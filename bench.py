@@ -210,10 +210,10 @@ def alg_bytes(step, storage_bytes):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # the dominant kernel, from one ncu capture of
-#   python bench.py --kernel-only raymarch_scatter --config <c> --storage <s>
-# (summaries in profiles/raymarch_scatter_<c>.md): cfg5 BF16, MODE 1 launch,
-# 3.34 GB read + 2.24 GB written.
-SCATTER_TRAFFIC = {('cfg5', 'bf16'): 5.58e9}
+#   python bench.py --kernel-only raymarch_scatter_projected --config <c> --storage <s>
+# (summaries in profiles/raymarch_scatter_<c>.md): cfg5 BF16, the projected
+# MODE 1 launch, 2.17 GB read + 1.10 GB written.
+SCATTER_TRAFFIC = {('cfg5', 'bf16'): 3.27e9}
 
 
 # ------------------------------------------------------------------ our arm
@@ -711,14 +711,17 @@ def kernel_roofline(step, dev, timed, storage=None):
     adjoint's scatter pass (k_raymarch_scatter, one launch for all views) as
     the step runs it: reading the samples the forward stored, with its
     per-camera weight sums precomputed (GFT_GRAD_WEIGHTS_READY: a gradient
-    memset plus the scatter launch).  ``alg_bytes`` is the render-backward
-    formula (N*4*s + 2*P*4*4 + 2*N*4*4: the grid read once, image and adjoint,
-    gradient read-modify-write); ``impl_bytes`` adds what this implementation
-    moves on top of it (the stored samples it reads instead of re-gathering,
-    the per-camera reciprocal weight sums)."""
+    memset plus the scatter launch), accumulating the two projections of the
+    4-channel gradient that the light composition's adjoint reads.
+    ``alg_bytes`` is the render-backward formula (N*4*s + 2*P*4*4 + 2*N*4*4:
+    the grid read once, image and adjoint, 4-channel gradient
+    read-modify-write); ``impl_bytes`` is what this implementation moves (the
+    stored samples it reads instead of re-gathering, image and adjoint, the
+    per-camera reciprocal weight sums, the 2-channel gradient
+    read-modify-write).  The 4-channel scatter is timed beside it."""
     import numpy as np
     import torch
-    from gft import ops
+    from gft import fused, ops
     peak, src = _peaks()
     with torch.no_grad():
         d = step.advect(step.s_d, step.s_vx, step.s_vy, step.s_vz)
@@ -743,15 +746,19 @@ def kernel_roofline(step, dev, timed, storage=None):
                                       ops.GRAD[m], grid=grid, samples=smp)
     weights = lambda: ops._raymarch_weights(shape5, data.device, step.M, step.V, step.P, step.F, step.res, 0, True)
     ws = weights()
+    proj = fused.compose_projection(step.light[1], step.ambient, step.depth_step)
     scatter = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
-                                        ops.GRAD['REFERENCE'], weights=ws, grid=grid, samples=smp)
+                                        ops.GRAD['REFERENCE'], weights=ws, grid=grid, samples=smp, projection=proj)
+    scatter4 = lambda: ops._raymarch_bwd(data, y, dy, step.M, step.V, step.P, step.F, step.res, 1, 0, 0, True,
+                                         ops.GRAD['REFERENCE'], weights=ws, grid=grid, samples=smp)
     for _ in range(2):
-        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter()
+        fwd(), bwd('REFERENCE'), bwd('EXACT'), weights(), scatter(), scatter4()
     tf = float(np.median(timed(fwd, 7)))
     tb_ref = float(np.median(timed(lambda: bwd('REFERENCE'), 7)))
     tb_ex = float(np.median(timed(lambda: bwd('EXACT'), 7)))
     tw = float(np.median(timed(weights, 7)))
     ts = float(np.median(timed(scatter, 7)))
+    ts4 = float(np.median(timed(scatter4, 7)))
     nvox = int(np.prod(step.shape))
     s = 2 if storage is not None else 4
     C = 4
@@ -761,13 +768,18 @@ def kernel_roofline(step, dev, timed, storage=None):
     stored = n_stored * C * 4
     alg_fwd = nvox * C * s + pix * C * 4
     alg_bwd = nvox * C * s + 2 * pix * C * 4 + 2 * nvox * C * 4
-    impl_scatter = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
+    impl_scatter = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * 2 * 4
+    impl_scatter4 = stored + 2 * pix * C * 4 + V * nvox * 4 + 2 * nvox * C * 4
     kern = {
         'raymarch_fwd': {'ms': tf, 'alg_bytes': alg_fwd, 'GBps': alg_fwd / tf / 1e6,
                          'impl_bytes': alg_fwd + stored, 'samples_per_s': samples / tf * 1e3},
         'raymarch_bwd_scatter': {'ms': ts, 'alg_bytes': alg_bwd, 'GBps': alg_bwd / ts / 1e6,
                                  'impl_bytes': impl_scatter, 'samples_per_s': samples / ts * 1e3,
-                                 'what': 'reference normalisation, weights ready, stored samples'},
+                                 'what': 'reference normalisation, weights ready, stored samples, gradient '
+                                         'projected onto the light composition\'s two sums (as the step)'},
+        'raymarch_bwd_scatter_4ch': {'ms': ts4, 'alg_bytes': alg_bwd, 'GBps': alg_bwd / ts4 / 1e6,
+                                     'impl_bytes': impl_scatter4, 'samples_per_s': samples / ts4 * 1e3,
+                                     'what': 'the same pass accumulating the 4-channel gradient'},
         'raymarch_samples_stored': n_stored,
         'raymarch_samples_stored_bytes': stored,
         'raymarch_bwd_weights': {'ms': tw, 'impl_bytes': 2 * V * nvox * 4, 'samples_per_s': samples / tw * 1e3,
@@ -787,7 +799,8 @@ def kernel_roofline(step, dev, timed, storage=None):
                          'traffic_source': ('ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch'
                                             if traffic else None),
                          'note': 'alg_bytes = the render-backward formula; the pass is bound by the L1/L2 path of '
-                                 'its merged trilinear gradient reductions and by latency, not by HBM'},
+                                 'its merged trilinear gradient reductions and by latency, not by HBM; it '
+                                 'accumulates two projected channels (impl_bytes), as the step does'},
             'kernels': kern}
 
 

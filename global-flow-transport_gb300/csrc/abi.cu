@@ -28,7 +28,7 @@ bool cuda_ok(cudaError_t e, const char* what) {
 static std::atomic<unsigned long long> g_launches{0};
 
 // launch-configuration knobs, defaults as documented in gft.h
-static std::atomic<int> g_knobs[GFT_KNOB_COUNT] = {{0}, {256}, {256}, {8}, {0}};
+static std::atomic<int> g_knobs[GFT_KNOB_COUNT] = {{0}, {256}, {256}, {8}, {0}, {0}};
 int knob_value(int k) { return (k >= 0 && k < GFT_KNOB_COUNT) ? g_knobs[k].load(std::memory_order_relaxed) : 0; }
 int sm_count() {
     int dev = 0, sms = 0;
@@ -272,9 +272,13 @@ gft_status gft_set_knob(int32_t knob, int32_t value) {
         case GFT_KNOB_ADVECT_THREADS:
         case GFT_KNOB_RESAMPLE_THREADS: ok = value == 64 || value == 128 || value == 256; break;
         case GFT_KNOB_SCAN_SEGMENTS: ok = value == 4 || value == 8 || value == 16; break;
+        case GFT_KNOB_WEIGHTS_PIPELINE: ok = value == 0 || value == 1; break;
         default: return fail(GFT_ERR_INVALID_ARGUMENT, "unknown knob");
     }
     if (!ok) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid knob value");
+    // the side stream is made now, outside any stream capture, where a device
+    // is present (else at the first gradient call that uses it)
+    if (knob == GFT_KNOB_WEIGHTS_PIPELINE && value == 1 && !prepare_side_stream()) (void)cudaGetLastError();
     g_knobs[knob].store(value, std::memory_order_relaxed);
     return GFT_OK;
 }

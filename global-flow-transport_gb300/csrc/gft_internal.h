@@ -80,6 +80,9 @@ int sm_count();  // SMs of the current device
 unsigned raymarch_blocks(int tiles);
 // ... of the weight pass (GFT_KNOB_WEIGHTS_BLOCKS_PER_SM; 0: raymarch_blocks)
 unsigned weights_blocks(int tiles);
+// Creates the library's side stream of the current device (the pipelined
+// weight pass) ahead of any stream capture.
+bool prepare_side_stream();
 
 // error helpers
 void set_error(const std::string& msg);

@@ -7,6 +7,8 @@
 // tile so that the 32 rays of a warp gather from neighbouring voxels.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <mutex>
 
 #include "gft_internal.h"
 
@@ -1090,6 +1092,108 @@ static void det_absmax_grid(const RaymarchArgs& a, unsigned int* out, cudaStream
                                                                                       out);
 }
 
+// ---- weight pass beside the scatter (GFT_KNOB_WEIGHTS_PIPELINE) ---------------------
+// The reference-normalised adjoint needs each camera's weight sums before its
+// scatter.  The weight pass is bound by instruction issue, the scatter by its
+// L2 reductions, so they share the SMs well: the weight sums of camera k + 1
+// are computed on a side stream while camera k scatters.  The side stream and
+// its events belong to the library (one set per device); the side stream
+// forks from and joins the caller's stream through events, which a CUDA-graph
+// capture records as dependencies.
+constexpr int PIPE_MAX_PAIRS = 64;
+namespace {
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[PIPE_MAX_PAIRS + 1] = {};
+};
+std::mutex g_side_mu;
+SideStream g_side[64];
+}  // namespace
+
+static SideStream* side_stream() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_side_mu);
+    SideStream& ss = g_side[dev];
+    if (ss.st == nullptr) {
+        cudaStream_t st = nullptr;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "side stream")) return nullptr;
+        for (int i = 0; i <= PIPE_MAX_PAIRS; ++i)
+            if (!cuda_ok(cudaEventCreateWithFlags(&ss.ev[i], cudaEventDisableTiming), "side stream event"))
+                return nullptr;
+        ss.st = st;
+    }
+    return &ss;
+}
+
+bool prepare_side_stream() { return side_stream() != nullptr; }
+
+// Pair k of a table as a one-pair table: same camera, image, output pixels
+// and sample-store offset, its tiles numbered from 0.
+static PairTable single_pair(const PairTable& t, int k) {
+    PairTable u;
+    std::memset(&u, 0, sizeof(u));
+    u.cam[0] = t.cam[k];
+    u.in_batch[0] = t.in_batch[k];
+    u.out_slot[0] = t.out_slot[k];
+    u.rw[0] = t.rw[k];
+    u.rh[0] = t.rh[k];
+    u.rd[0] = t.rd[k];
+    u.pix0[0] = t.pix0[k];
+    u.smp0[0] = t.smp0[k];
+    u.tile0[0] = 0;
+    u.tile0[1] = t.tile0[k + 1] - t.tile0[k];
+    u.pair_base = t.pair_base + k;
+    u.n = 1;
+    return u;
+}
+
+static bool raymarch_bwd_pipelined(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
+                                   const float* dout, float* grad, float* ws_cnt, SideStream& ss, cudaStream_t s) {
+    const int64_t cells = brick_cells(a.din);
+    const dim3 block(RM_BX, RM_BY, 1);
+    std::vector<PairTable> singles;
+    int64_t smp_cells = 0;
+    for (PairTable& t : make_tables(pairs)) {
+        set_ray_tiles(t, &smp_cells);
+        for (int k = 0; k < t.n; ++k) singles.push_back(single_pair(t, k));
+    }
+    if (!cuda_ok(cudaEventRecord(ss.ev[0], s), "fork") || !cuda_ok(cudaStreamWaitEvent(ss.st, ss.ev[0], 0), "fork") ||
+        !cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * cells * pairs.size(), ss.st), "zero weights"))
+        return false;
+    for (size_t k = 0; k < singles.size(); ++k) {
+        const PairTable& u = singles[k];
+        const dim3 grid(weights_blocks(u.tile0[1]));
+        switch (a.boundary) {
+            case BM_BORDER: weights_dispatch<BM_BORDER>(grid, block, ss.st, a, ws_cnt, nullptr, 0.f, u); break;
+            case BM_CLAMP: weights_dispatch<BM_CLAMP>(grid, block, ss.st, a, ws_cnt, nullptr, 0.f, u); break;
+            default: weights_dispatch<BM_WRAP>(grid, block, ss.st, a, ws_cnt, nullptr, 0.f, u); break;
+        }
+        const int64_t n4 = cells / 4;  // cells is a multiple of 8
+        const int64_t want = (n4 + 255) / 256;
+        k_invert_weights<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * 8)), 256, 0,
+                           ss.st>>>(reinterpret_cast<float4*>(ws_cnt + (size_t)u.pair_base * cells), n4);
+        if (!launched(2, "raymarch weight launch") || !cuda_ok(cudaEventRecord(ss.ev[1 + k], ss.st), "weights event"))
+            return false;
+    }
+    for (size_t k = 0; k < singles.size(); ++k) {
+        const PairTable& u = singles[k];
+        if (!cuda_ok(cudaStreamWaitEvent(s, ss.ev[1 + k], 0), "join")) return false;
+        const dim3 grid(raymarch_blocks(u.tile0[1]));
+        if (a.dtype == 0) {
+            if (a.C == 4) bwd_dispatch_bm<4, float>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+            else if (a.C == 2) bwd_dispatch_bm<2, float>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+            else bwd_dispatch_bm<1, float>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+        } else {
+            if (a.C == 4) bwd_dispatch_bm<4, __nv_bfloat16>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+            else if (a.C == 2) bwd_dispatch_bm<2, __nv_bfloat16>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+            else bwd_dispatch_bm<1, __nv_bfloat16>(false, grid, block, s, a, out, dout, grad, ws_cnt, u);
+        }
+        if (!launched(1, "raymarch backward launch")) return false;
+    }
+    return true;
+}
+
 bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pairs, const float* out,
                          const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,
                          cudaStream_t s) {
@@ -1098,6 +1202,12 @@ bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pair
     const int64_t n = cells * (a.project ? 2 : a.C) * a.N;
     if (!a.det) {
         if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * n, s), "zero gradient")) return false;
+        if (!exact && !weights_ready && knob_value(GFT_KNOB_WEIGHTS_PIPELINE) == 1 &&
+            pairs.size() <= (size_t)PIPE_MAX_PAIRS) {
+            SideStream* ss = side_stream();
+            if (ss == nullptr) return false;
+            return raymarch_bwd_pipelined(a, pairs, out, dout, grad, ws_cnt, *ss, s);
+        }
         if (!exact && !weights_ready && !launch_raymarch_weights(a, pairs, ws_cnt, s)) return false;
     } else {
         // integer sums into gacc, then converted into grad

@@ -5,7 +5,9 @@ The knobs change only how kernels are launched -- the raymarch kernels' grid
 bounds how many tiles are in flight and so the set of gradient lines the
 adjoint's reductions keep in L2), the grid of the gradient's weight pass
 alone (which runs ahead on a side stream beside the forward kernels; a small
-persistent grid leaves them room), the block size of the advection and
+persistent grid leaves them room), whether the weight pass instead runs
+camera by camera beside the adjoint's scatter (the library's side stream),
+the block size of the advection and
 SampleGridTransform kernels, and the segment count of the transmittance scans
 -- never what they compute.  ``tune`` times a step for every candidate of
 every knob with CUDA events on the current stream (a coordinate search: each
@@ -28,6 +30,7 @@ from . import _lib
 
 # name -> (knob id of gft.h, candidates, default)
 KNOBS = {
+    'weights_pipeline': (5, (0, 1), 0),
     'raymarch_blocks_per_sm': (0, (0, 2, 3, 4, 6), 0),
     'advect_threads': (1, (256, 128, 64), 256),
     'resample_threads': (2, (256, 128, 64), 256),

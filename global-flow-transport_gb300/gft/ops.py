@@ -20,6 +20,7 @@ MIP = {'NONE': 0, 'NEAREST': 1, 'LINEAR': 2}
 BLEND = {'BEER_LAMBERT': 0, 'BEER_LAMBERT_EXCLUSIVE': 1, 'ALPHA': 2, 'ALPHA_ADDITIVE': 3, 'ADDITIVE': 4}
 COORD = {'TRANSFORM_LINDEPTH': 0, 'TRANSFORM_LINDEPTH_REVERSE': 1, 'TRANSFORM': 3, 'TRANSFORM_REVERSE': 4}
 GRAD = {'REFERENCE': 0, 'EXACT': 1}
+KNOB_WEIGHTS_PIPELINE = 5  # GFT_KNOB_WEIGHTS_PIPELINE
 CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
 
 _state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True, 'sample_pool': 0.25,
@@ -392,6 +393,8 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
     captured too (they join the side stream)."""
     if _state['deterministic']:
         return  # the deterministic gradient computes its own (integer) weight sums
+    if _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) == 1:
+        return  # the gradient call computes them, beside its scatter
     dev = _cuda_device(device)
     out_shape = _shape3(output_shape)
     b = _enum(BOUNDARY, boundary, 'boundary')
@@ -455,7 +458,9 @@ def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, bou
         cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
         if cached is not None:
             ctx.weights = (cached, None)
-        elif _state['side_weights']:
+        elif _state['side_weights'] and _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) != 1:
+            # (with the pipeline knob the gradient call computes the weight
+            # sums itself, beside its scatter)
             key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
             ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
                                                                                 out_shape, boundary, separate)

@@ -490,13 +490,27 @@ gft_status gft_image_loss_tonemap_grad(const float* image, const float* target, 
  *                                    many blocks per SM (a small grid leaves
  *                                    room for the kernels it overlaps when it
  *                                    runs ahead on another stream)
+ *   GFT_KNOB_WEIGHTS_PIPELINE        0 (default) or 1: a GFT_GRAD_REFERENCE
+ *                                    raymarch gradient whose weight sums are
+ *                                    not ready (no GFT_GRAD_WEIGHTS_READY,
+ *                                    not deterministic, at most 64 pairs)
+ *                                    computes them camera by camera on a
+ *                                    side stream the library owns (created
+ *                                    when the knob is set to 1), each
+ *                                    camera's weight pass running beside the
+ *                                    previous camera's scatter, which then
+ *                                    runs camera by camera; the side stream
+ *                                    forks from and joins the call's stream
+ *                                    through events, so a CUDA-graph capture
+ *                                    records it
  * gft_set_knob returns GFT_ERR_INVALID_ARGUMENT for an unknown knob or value. */
 #define GFT_KNOB_RAYMARCH_BLOCKS_PER_SM 0
 #define GFT_KNOB_ADVECT_THREADS 1
 #define GFT_KNOB_RESAMPLE_THREADS 2
 #define GFT_KNOB_SCAN_SEGMENTS 3
 #define GFT_KNOB_WEIGHTS_BLOCKS_PER_SM 4
-#define GFT_KNOB_COUNT 5
+#define GFT_KNOB_WEIGHTS_PIPELINE 5
+#define GFT_KNOB_COUNT 6
 gft_status gft_set_knob(int32_t knob, int32_t value);
 int32_t gft_get_knob(int32_t knob);
 

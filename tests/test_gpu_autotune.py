@@ -58,7 +58,7 @@ def test_persistent_raymarch_grid_equals_one_block_per_tile(gpu, mode):
 
 
 @pytest.mark.parametrize('name', ['advect_threads', 'resample_threads', 'scan_segments', 'raymarch_blocks_per_sm',
-                                  'weights_blocks_per_sm'])
+                                  'weights_blocks_per_sm', 'weights_pipeline'])
 def test_step_results_equal_for_every_knob_value(gpu, name):
     from gft import autotune
     from gft.pipeline import RenderAdvectStep
@@ -73,6 +73,60 @@ def test_step_results_equal_for_every_knob_value(gpu, name):
         assert abs(float(loss.detach()) - l0) <= 1e-6 * abs(l0), (name, v)
         for a, b in zip(grads, g0):
             assert rel_l2(_np(a), b) <= 1e-5, (name, v)
+
+
+@pytest.mark.parametrize('project', [False, True])
+def test_pipelined_weight_pass_gradient(gpu, project):
+    """GFT_KNOB_WEIGHTS_PIPELINE: the reference-normalised gradient with each
+    camera's weight sums computed on the library's side stream beside the
+    previous camera's scatter equals the one-pass gradient (5 views, stored
+    samples; 4 channels, or projected onto two)."""
+    from gft import autotune, ops
+    shape, res = (24, 30, 20), (40, 135, 240)
+    _, _, M, V, P, F = scene(shape, 5, res)
+    x = torch.from_numpy(small_grid(shape, 4, 11) * 0.3).cuda()
+    xb = ops.to_bricks(x)
+    shape5 = (1,) + shape + (4,)
+    smp = ops._samples_buffer(shape5, 5, res, True, gpu)
+    y = ops._raymarch_fwd(xb, M, V, P, F, res, 1, 0, 0, True, grid=shape, samples=smp)
+    dy = torch.randn(y.shape, device='cuda', generator=torch.Generator('cuda').manual_seed(5)) * 1e-3
+    proj = np.array([0.3, -1.2, 0.7, 0.0, 0.5, 0.5, 0.5, 1.1], np.float32) if project else None
+    bwd = lambda: ops._raymarch_bwd(xb, y, dy, M, V, P, F, res, 1, 0, 0, True, ops.GRAD['REFERENCE'], grid=shape,
+                                    samples=smp, projection=proj)
+    with autotune.knob_settings({'weights_pipeline': 0}):
+        g0 = bwd()
+    with autotune.knob_settings({'weights_pipeline': 1}):
+        g1 = bwd()
+        torch.cuda.synchronize()
+        # twice in a row on the same side stream and events
+        g2 = bwd()
+    torch.cuda.synchronize()
+    assert np.abs(_np(g0)).max() > 0
+    assert rel_l2(_np(g1), _np(g0)) <= 1e-6
+    assert rel_l2(_np(g2), _np(g0)) <= 1e-6
+
+
+def test_pipelined_weight_pass_in_a_captured_step(gpu):
+    """The side stream forks from and joins the capturing stream: a step
+    captured with the pipeline knob replays to the eager default step's loss
+    and gradients."""
+    from gft import autotune
+    from gft.pipeline import RenderAdvectStep
+    st = RenderAdvectStep('cfg1', gpu)
+    st.setup_static(st.make_inputs())
+    with autotune.knob_settings(autotune.defaults()):
+        l0, g0 = st.run_static()
+        l0, g0 = float(l0.detach()), [_np(g) for g in g0]
+    with autotune.knob_settings({'weights_pipeline': 1}):
+        cap = RenderAdvectStep('cfg1', gpu)
+        cap.setup_static(cap.make_inputs())
+        cap.capture(warmup=2)
+        for _ in range(2):
+            loss, grads = cap.replay()
+        torch.cuda.synchronize()
+    assert abs(float(loss.detach()) - l0) <= 1e-6 * abs(l0)
+    for a, b in zip(grads, g0):
+        assert rel_l2(_np(a), b) <= 1e-5
 
 
 def test_tuner_picks_a_candidate_and_caches_it(gpu):
