@@ -117,6 +117,9 @@ struct RaymarchArgs {
                                       // 0xffffffff where the pool was full
         uint8_t* occ = nullptr;       // per input slice and 4^3-voxel block: 0 = no non-zero voxel in
                                       // the block grown by one voxel at its upper faces
+        uint8_t* dist = nullptr;      // per slice and block: Chebyshev distance (in blocks, capped) to the
+                                      // nearest occupied block; 0 = occupied
+        uint8_t* dist_tmp = nullptr;  // scratch of the distance passes
         int nbx = 0, nby = 0, nbz = 0;
     } store;
     // Deterministic adjoint (GFT_GRAD_DETERMINISTIC): integer accumulation in

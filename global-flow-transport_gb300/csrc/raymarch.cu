@@ -144,8 +144,9 @@ static unsigned set_ray_tiles(PairTable& t, int64_t* cells = nullptr) {
 // of the tile, and the adjoint re-samples the grid there.
 //
 // Layout: [counter (one uint64), 256 bytes][ballot words][first cells][occupancy
-// maps][pool]: the words and first cells hold one uint32 per pair, pixel tile,
-// step and warp.
+// maps][empty-space distance maps][their scratch][pool]: the words and first
+// cells hold one uint32 per pair, pixel tile, step and warp; the maps one byte
+// per input slice and block.
 constexpr int OCC_SHIFT = 2;  // 4^3-voxel occupancy blocks
 constexpr uint32_t STORE_CHUNK = 256;
 constexpr uint32_t STORE_OVERFLOW = 0xffffffffu;
@@ -164,7 +165,7 @@ static size_t align256u(size_t n) { return (n + 255) & ~size_t(255); }
 // bytes before the pool
 static size_t store_meta_bytes(const std::vector<Pair>& pairs, int N, Dims din) {
     const int64_t cells = store_cells(pairs);
-    return 256 + 2 * align256u(sizeof(uint32_t) * (cells / 32)) + align256u((size_t)voxels(occ_dims(din)) * N);
+    return 256 + 2 * align256u(sizeof(uint32_t) * (cells / 32)) + 3 * align256u((size_t)voxels(occ_dims(din)) * N);
 }
 size_t raymarch_store_min_bytes(const std::vector<Pair>& pairs, int N, Dims din) {
     return store_meta_bytes(pairs, N, din);
@@ -202,6 +203,10 @@ RaymarchArgs::Store raymarch_store_layout(void* base, size_t bytes, const std::v
     st.nbx = od.x;
     st.nby = od.y;
     st.nbz = od.z;
+    p += align256u((size_t)voxels(od) * N);
+    st.dist = reinterpret_cast<uint8_t*>(p);
+    p += align256u((size_t)voxels(od) * N);
+    st.dist_tmp = reinterpret_cast<uint8_t*>(p);
     p += align256u((size_t)voxels(od) * N);
     st.samples = reinterpret_cast<float*>(p);
     const size_t meta = store_meta_bytes(pairs, N, din);
@@ -287,6 +292,36 @@ static void occ_launch(const RaymarchArgs& a, cudaStream_t s) {
     }
 }
 
+// Empty-space distance of each block: the Chebyshev distance, in blocks, to
+// the nearest block the occupancy map marks (capped at DIST_CAP), so that the
+// storing forward can step over samples that are all zero.  Three 1D passes:
+// along x the distance to the nearest marked block of the row; along y and z
+// the smallest max(|offset|, previous distance) over the offsets up to the cap
+// -- the min-max composition is exactly the Chebyshev distance.  Blocks
+// outside the map are never looked up (positions are clamped to the grid).
+constexpr int DIST_CAP = 7;
+template <int AXIS>
+__global__ void k_empty_distance(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, Dims od) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= voxels(od)) return;
+    const size_t base = (size_t)blockIdx.y * voxels(od);
+    int x, y, z;
+    unflat32(v, od, x, y, z);
+    const int c = AXIS == 0 ? x : AXIS == 1 ? y : z;
+    const int n = AXIS == 0 ? od.x : AXIS == 1 ? od.y : od.z;
+    const int64_t stride = AXIS == 0 ? 1 : AXIS == 1 ? od.x : (int64_t)od.x * od.y;
+    const uint8_t* row = src + base + v - (int64_t)c * stride;
+    int best = DIST_CAP;
+    for (int o = -(DIST_CAP - 1); o <= DIST_CAP - 1; ++o) {
+        const int k = c + o;
+        if (k < 0 || k >= n) continue;
+        const int val = row[(int64_t)k * stride];
+        const int dd = AXIS == 0 ? (val != 0 ? abs(o) : DIST_CAP) : max(abs(o), (int)val);
+        best = min(best, dd);
+    }
+    dst[base + v] = (uint8_t)best;
+}
+
 bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s) {
     const Dims od{a.store.nbx, a.store.nby, a.store.nbz};
     if (!cuda_ok(cudaMemsetAsync(a.store.occ, 0, (size_t)voxels(od) * a.N, s), "zero occupancy")) return false;
@@ -306,30 +341,39 @@ bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s) {
         else if (a.C == 2) brick ? occ_launch<2, __nv_bfloat16, LAYOUT_BRICK>(a, s) : occ_launch<2, __nv_bfloat16, LAYOUT_FLAT>(a, s);
         else brick ? occ_launch<1, __nv_bfloat16, LAYOUT_BRICK>(a, s) : occ_launch<1, __nv_bfloat16, LAYOUT_FLAT>(a, s);
     }
-    return launched(1, "raymarch occupancy launch");
+    if (!launched(1, "raymarch occupancy launch")) return false;
+    // occupancy -> distance along x (dist) -> y (dist_tmp) -> z (dist, the
+    // map the forward reads)
+    const dim3 grid((unsigned)((voxels(od) + 255) / 256), (unsigned)a.N);
+    k_empty_distance<0><<<grid, 256, 0, s>>>(a.store.occ, a.store.dist, od);
+    k_empty_distance<1><<<grid, 256, 0, s>>>(a.store.dist, a.store.dist_tmp, od);
+    k_empty_distance<2><<<grid, 256, 0, s>>>(a.store.dist_tmp, a.store.dist, od);
+    return launched(3, "raymarch empty-distance launch");
 }
 
-// True where the sample at p is exactly zero by the occupancy map, without a
-// fetch: its corners that the boundary mode reads lie in the grown region of
-// one block without a non-zero voxel.  BORDER and CLAMP: the block of the base
+// The sample at p is exactly zero by the occupancy map, without a fetch, where
+// its corners that the boundary mode reads lie in the grown region of one
+// block without a non-zero voxel.  BORDER and CLAMP: the block of the base
 // cell clamped to the grid (corners outside read 0 resp. the clamped border
 // voxels, which that block holds); WRAP: interior base cells only (all 8
-// corners inside).  Non-finite positions are fetched.
+// corners inside).  Non-finite positions are fetched.  sample_distance
+// returns that block's empty-space distance (>= 1: the sample is zero), or 0
+// where the sample must be fetched.
 template <int BM>
-__device__ __forceinline__ bool sample_empty(Dims d, float px, float py, float pz, const uint8_t* __restrict__ occ,
-                                             int nbx, int nby) {
-    if (!(fabsf(px) <= 3.0e9f && fabsf(py) <= 3.0e9f && fabsf(pz) <= 3.0e9f)) return false;
+__device__ __forceinline__ int sample_distance(Dims d, float px, float py, float pz, const uint8_t* __restrict__ dist,
+                                               int nbx, int nby) {
+    if (!(fabsf(px) <= 3.0e9f && fabsf(py) <= 3.0e9f && fabsf(pz) <= 3.0e9f)) return 0;
     int x0 = (int)floorf(px), y0 = (int)floorf(py), z0 = (int)floorf(pz);
     if constexpr (BM == BM_WRAP) {
         if (!((unsigned)x0 < (unsigned)(d.x - 1) && (unsigned)y0 < (unsigned)(d.y - 1) &&
               (unsigned)z0 < (unsigned)(d.z - 1)))
-            return false;
+            return 0;
     } else {
         x0 = min(max(x0, 0), d.x - 1);
         y0 = min(max(y0, 0), d.y - 1);
         z0 = min(max(z0, 0), d.z - 1);
     }
-    return __ldg(occ + ((uint32_t)(z0 >> OCC_SHIFT) * nby + (uint32_t)(y0 >> OCC_SHIFT)) * nbx + (x0 >> OCC_SHIFT)) == 0;
+    return __ldg(dist + ((uint32_t)(z0 >> OCC_SHIFT) * nby + (uint32_t)(y0 >> OCC_SHIFT)) * nbx + (x0 >> OCC_SHIFT));
 }
 
 template <int C, typename S, int BM, bool LIN, int L>
@@ -370,29 +414,57 @@ __device__ __forceinline__ void raymarch_fwd_tile(const S* __restrict__ in, Dims
         i0 = D;
         i1 = -1;
     }
-    const uint8_t* occ = storing ? st.occ + (size_t)tab.in_batch[p] * st.nbx * st.nby * st.nbz : nullptr;
+    const uint8_t* dist = storing ? st.dist + (size_t)tab.in_batch[p] * st.nbx * st.nby * st.nbz : nullptr;
     const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;
+    // Empty-space skipping: where every sample of a warp step is zero, the
+    // warp steps over the samples its lanes' distance maps prove zero too.  A
+    // lane at q in a block at distance d reaches only blocks within d - 1 of
+    // it (all empty) while it moves at most 4d - 6 voxels along each axis
+    // (floor and the block shift add 1 and 3; 0.01 of slack covers the
+    // rounding of the positions, which ray_sample computes directly from the
+    // step index, so the samples processed are the same).  Zero samples leave
+    // the blend unchanged exactly where the ray is clipped: the same
+    // condition.  Lanes past their range do not limit the skip; lanes before
+    // it limit it by their current position.
+    const bool skipping = storing && BM == BM_BORDER && (C == 1 || blend_mode != BL_BEER_LAMBERT_EXCLUSIVE);
+    const float smax = fmaxf(fabsf(step.x), fmaxf(fabsf(step.y), fabsf(step.z)));
+    const float inv_smax = smax > 1e-6f ? 1.f / smax : 0.f;
     // the warp's current pool chunk [cur, end) (uniform across the warp);
     // full: a chunk request went past the pool's end
     uint32_t cur = 0, end = 0;
     bool full = false;
-    for (int i = w0; i <= w1; ++i) {
+    for (int i = w0; i <= w1;) {
         bool nonzero = false;
+        int dcur = 0;  // this lane's empty-space distance at step i
         Vec<C> smp = vzero<C>();
         if (i >= i0 && i <= i1) {
             const float3 pos = ray_sample(nearp, step, i);
             if constexpr (LIN) {
                 const float qx = pos.x - 0.5f, qy = pos.y - 0.5f, qz = pos.z - 0.5f;
-                const bool empty = storing && sample_empty<BM>(din, qx, qy, qz, occ, st.nbx, st.nby);
+                if (storing) dcur = sample_distance<BM>(din, qx, qy, qz, dist, st.nbx, st.nby);
+                const bool empty = dcur != 0;
                 if (!empty) smp = fetch_linear<C, S, BM, L>(g, din, qx, qy, qz);
                 nonzero = storing && !empty;
             } else {
                 smp = fetch<C, S, BM, true>(filter, g, din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f);
             }
             acc = blend<C>(blend_mode, acc, smp);
+        } else if (skipping && live && i < i0) {
+            const float3 pos = ray_sample(nearp, step, i);
+            dcur = sample_distance<BM>(din, pos.x - 0.5f, pos.y - 0.5f, pos.z - 0.5f, dist, st.nbx, st.nby);
         }
+        int adv = 1;
         if (storing) {
             const unsigned word = __ballot_sync(0xffffffffu, nonzero);
+            if (skipping && word == 0u) {
+                unsigned m = 0xffffffffu;
+                if (live && i <= i1) {
+                    const float lim = 4.f * (float)dcur - 6.01f;
+                    m = lim > 0.f ? (unsigned)fminf(lim * inv_smax, 1e6f) : 0u;
+                }
+                m = __reduce_min_sync(0xffffffffu, m);
+                adv = 1 + (int)min(m, (unsigned)(w1 - i));
+            }
             uint32_t first = STORE_OVERFLOW;
             if (word != 0u && !full) {
                 const uint32_t n = (uint32_t)__popc(word);
@@ -414,12 +486,13 @@ __device__ __forceinline__ void raymarch_fwd_tile(const S* __restrict__ in, Dims
             }
             if (nonzero && first != STORE_OVERFLOW)
                 store_stream<C>(st.samples, (int64_t)(first + lane_rank(word, lane)), smp);
-            if (lane == 0) {
+            if (lane == 0 && word != 0u) {  // the words start zeroed
                 const int64_t w = sample_word_index(tab, r.tile, p, D, i);
                 st.words[w] = word;
                 st.first[w] = first;
             }
         }
+        i += adv;
     }
     if (!live) return;
     store<C>(out, tab.pix0[p] + (int64_t)y * W + x, acc);

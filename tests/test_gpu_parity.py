@@ -235,6 +235,44 @@ def test_raymarch_sample_store_sparse_grid(ops, boundary, mode):
     assert counts[1] == 0 if boundary != 'WRAP' else counts[1] < counts[0]
 
 
+@pytest.mark.parametrize('C', [1, 4])
+@pytest.mark.parametrize('blend', BLENDS)
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+@pytest.mark.parametrize('negative', [False, True])
+def test_raymarch_empty_space_skipping(ops, C, blend, boundary, negative):
+    """A 48x56x40 grid that is zero outside two small boxes, rays of 96
+    samples: the storing forward steps over runs of samples its empty-space
+    distance map proves zero (the positions come from the step index, so the
+    samples it processes are the same); its images equal the plain forward's
+    bit for bit, for every blend mode (also with negative values, where a zero
+    sample still leaves the blend unchanged), and the gradient from the stored
+    samples equals the re-sampling one."""
+    shape, res = (48, 56, 40), (96, 40, 44)
+    _, _, M, V, P, F = scene(shape, 3, res)
+    x = np.zeros((1,) + shape + (C,), np.float32)
+    x[:, 20:28, 24:33, 15:24] = small_grid((8, 9, 9), C, 41, positive=not negative)[0] * 0.4
+    x[:, 40:44, 5:9, 30:35] = small_grid((4, 4, 5), C, 42, positive=not negative)[0] * 0.4
+    dy = cuda(np.random.default_rng(43).standard_normal((1, 3) + res[1:] + (C,)).astype(np.float32))
+    grads, outs = [], []
+    for store in (False, True):
+        ops.set_raymarch_sample_store(store)
+        try:
+            xt = cuda(x).requires_grad_(True)
+            y = ops.raymarch_grid_transform(xt, M, V, P, F, res, 'LINEAR', boundary, blend)
+            y.backward(dy)
+        finally:
+            ops.set_raymarch_sample_store(True)
+        grads.append(np_(xt.grad))
+        outs.append(np_(y))
+    assert np.abs(outs[0]).max() > 0
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(grads[1], grads[0]) <= 1e-5
+    smp = ops._samples_buffer(x.shape, 3, res, True, 'cuda')
+    ops._raymarch_fwd(cuda(x), M, V, P, F, res, 1, BOUNDS.index(boundary), ops.BLEND[blend], True, samples=smp)
+    n = ops.stored_sample_count(smp, x.shape, 3, res)
+    assert 0 < n < 3 * 40 * 44 * 96 // 4
+
+
 @pytest.mark.parametrize('fraction', [0.0, 0.01, 1.0])
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
 def test_raymarch_sample_store_pool_sizes(ops, fraction, mode):

@@ -121,10 +121,11 @@ def test_argument_errors_without_a_gpu(lib):
     assert st == lib.ERR_INVALID_ARGUMENT and b'2^32' in L.gft_last_error()
     # sample store: LINEAR only, a large enough store, a store pointer.
     # Before the pool: the pool counter, a ballot word and a pool offset per
-    # warp and step, a 2x2x2 occupancy map (256-byte aligned parts); the full
-    # pool: one 8x16-pixel tile x 4 steps x 128 lanes, plus the chunks' slack
-    # (abandoned chunks hold >= 225 of 256 cells; a last chunk per warp), of 4 floats
-    meta = 256 + 256 + 256 + 256
+    # warp and step, a 2x2x2 occupancy map, its empty-space distance map and
+    # the distance passes' scratch (256-byte aligned parts); the full pool: one
+    # 8x16-pixel tile x 4 steps x 128 lanes, plus the chunks' slack (abandoned
+    # chunks hold >= 225 of 256 cells; a last chunk per warp), of 4 floats
+    meta = 256 + 256 + 256 + 3 * 256
     cells = 4 * 128
     pool = -(-cells * 256 // 225) + 4 * 256
     assert L.gft_raymarch_grid_transform_samples_min_size(shape4, 1, out, 1) == meta
