@@ -157,7 +157,8 @@ def workload_config(config, storage, grad_mode):
     c = CONFIGS[config]
     D, H, W = c['grid']
     Hi, Wi = c['image']  # rows, columns (the pipeline's order)
-    return {'workload': '%s: density %dx%dx%d (%s storage, fp32 arithmetic), MacCormack advect (MC_SMOOTH, CLAMP), '
+    return {'workload': '%s: density %dx%dx%d (raymarch input in %s storage, fp32 arithmetic), MacCormack advect '
+                        '(MC_SMOOTH, CLAMP), '
                         'spot-light shadow %s (%d mips), %d views %dx%d (width x height) x%d samples, L2 image loss, '
                         'fwd+bwd'
                         % (config, D, H, W, storage, 'x'.join(map(str, c['shadow'])), c['mips'], c['views'], Wi, Hi,

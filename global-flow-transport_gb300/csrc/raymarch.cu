@@ -603,7 +603,9 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
     // zero weight adds +0 to a finite sum; corners that no member reaches with
     // a non-zero weight are not reduced (nz).  (MODE 2: the value is 1.)
     float acc[8][C];
-    unsigned nz = zero_weight_mask(wx, wy, wz);
+    // (MODE 2 adds weights, which are finite: a zero one adds +0 and needs no
+    // mask)
+    unsigned nz = MODE == 2 ? 0xffu : zero_weight_mask(wx, wy, wz);
     {
         float w[8];
         corner_weights(wx, wy, wz, w);
@@ -615,13 +617,12 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
     if constexpr (MODE == 2) {
         // Weight sums: the head pulls each member's three fractions (not its
         // eight weights: shuffles are the scarcer issue slots) and adds the
-        // member's corner weights; corners no member weights are skipped, as
-        // in the adjoint that these sums normalise.
+        // member's corner weights.  Corners no member weights receive +0,
+        // which leaves the sums unchanged (the adjoint skips them).
         for (int r = 1; r <= rounds; ++r) {
             const float mx = __shfl_down_sync(0xffffffffu, wx, r), my = __shfl_down_sync(0xffffffffu, wy, r),
                         mz = __shfl_down_sync(0xffffffffu, wz, r);
             if (r <= n) {
-                nz |= zero_weight_mask(mx, my, mz);
                 float w[8];
                 corner_weights(mx, my, mz, w);
 #pragma unroll
@@ -647,6 +648,69 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
         }
     }
     if (!head) return;
+    if constexpr (BM == BM_BORDER) {
+        // BORDER: the corners are base + (0|1) per axis without a remap.  In
+        // the bricks the +1 neighbour along x is the next cell of the brick
+        // (even x0) or cell 0 of the next brick, 7 cells on (odd x0); along y
+        // 2 cells or a brick row minus 2, along z 4 cells or a brick slab
+        // minus 4.  In 32-bit arithmetic this holds for the base -1 too (its
+        // index wraps below 0 and its neighbour lands on cell 0).  Corners
+        // outside the grid (base -1, or base + 1 = dims) are left out through
+        // a mask of the eight corners.
+        const uint32_t bx = (uint32_t)(d.x + 1) / 2, bxy = bx * ((uint32_t)(d.y + 1) / 2);
+        const uint32_t bbase = (uint32_t)(x0 >> 1) * 8u + (uint32_t)(x0 & 1) + (uint32_t)(y0 >> 1) * bx * 8u +
+                               ((uint32_t)(y0 & 1) << 1) + (uint32_t)(z0 >> 1) * bxy * 8u + ((uint32_t)(z0 & 1) << 2);
+        const uint32_t box = (x0 & 1) ? 7u : 1u, boy = (y0 & 1) ? bx * 8u - 2u : 2u,
+                       boz = (z0 & 1) ? bxy * 8u - 4u : 4u;
+        uint32_t cbase = bbase, cox = box, coy = boy, coz = boz;
+        if constexpr (L == LAYOUT_FLAT) {
+            cbase = (uint32_t)x0 + (uint32_t)y0 * (uint32_t)d.x + (uint32_t)z0 * (uint32_t)d.x * (uint32_t)d.y;
+            cox = 1u;
+            coy = (uint32_t)d.x;
+            coz = (uint32_t)d.x * (uint32_t)d.y;
+        }
+        unsigned mask = nz;
+        if (x0 < 0) mask &= 0xaau;
+        if (x0 + 1 >= d.x) mask &= 0x55u;
+        if (y0 < 0) mask &= 0xccu;
+        if (y0 + 1 >= d.y) mask &= 0x33u;
+        if (z0 < 0) mask &= 0xf0u;
+        if (z0 + 1 >= d.z) mask &= 0x0fu;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int sx = k & 1, sy = (k >> 1) & 1, sz = (k >> 2) & 1;
+            if (!((mask >> k) & 1u)) continue;
+            const uint32_t bi = bbase + (sx ? box : 0u) + (sy ? boy : 0u) + (sz ? boz : 0u);
+            const uint32_t ci = L == LAYOUT_FLAT ? cbase + (sx ? cox : 0u) + (sy ? coy : 0u) + (sz ? coz : 0u) : bi;
+            Vec<C> a;
+#pragma unroll
+            for (int c = 0; c < C; ++c) a.v[c] = acc[k][c];
+            if constexpr (DET) {
+                if constexpr (MODE == 2) {
+                    atomicAdd(iacc + bi, (unsigned long long)__float2ll_rn(a.v[0] * iscale));
+                } else {
+                    float inv = 1.f;
+                    if constexpr (MODE == 1) inv = __ldg(cnt + bi);
+                    if (inv > 0.f) {
+#pragma unroll
+                        for (int c = 0; c < C; ++c)
+                            atomicAdd(iacc + (uint64_t)ci * C + c,
+                                      (unsigned long long)__float2ll_rn(a.v[c] * inv * iscale));
+                    }
+                }
+                continue;
+            }
+            if constexpr (MODE == 1) {
+                const float inv = __ldg(cnt + bi);
+                if (inv > 0.f) atomic_add<C>(grad, ci, vscale(a, inv));
+            } else if constexpr (MODE == 2) {
+                atomic_add<C>(grad, bi, a);
+            } else {
+                atomic_add<C>(grad, ci, a);
+            }
+        }
+        return;
+    }
     int xs[2] = {x0, x0 + 1}, ys[2] = {y0, y0 + 1}, zs[2] = {z0, z0 + 1};
     bool vx[2] = {true, true}, vy[2] = {true, true}, vz[2] = {true, true};
 #pragma unroll

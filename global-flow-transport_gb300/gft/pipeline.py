@@ -66,9 +66,18 @@ CONFIGS = {
 
 
 class RenderAdvectStep:
+    """One render + advect iteration (see the module docstring).  storage_dtype
+    (torch.bfloat16) stores the raymarch input in bf16; advect_storage_dtype
+    does the same for the advection's input density (default fp32: the
+    advection's gathers are latency-bound, so bf16 saves little there, and an
+    fp32 input lets the adjoint reuse the forward's intermediate grid and
+    differentiate at the fp32 density)."""
+
     def __init__(self, config='cfg2', device='cuda', storage_dtype=None, mode='batched', order=None,
-                 fp64_check=False, check_strides=(7, 257), autotune=False, tonemap='NONE'):
+                 fp64_check=False, check_strides=(7, 257), autotune=False, tonemap='NONE',
+                 advect_storage_dtype=None):
         self.config_name = config if isinstance(config, str) else None
+        self.advect_storage_dtype = advect_storage_dtype
         # tonemapping of the composited images before the loss (renderer.py:639-640)
         self.tonemap = str(tonemap).upper()
         cfg = dict(CONFIGS[config] if isinstance(config, str) else config)
@@ -134,7 +143,7 @@ class RenderAdvectStep:
         if self.mode == 'plain':
             return advect_composed(d_prev, vx, vy, vz, dt=1.0, order=self.order, clamp=self.clamp, boundary='CLAMP')
         return ops.advect(d_prev, vx, vy, vz, dt=1.0, order=self.order, clamp=self.clamp, boundary='CLAMP',
-                          storage_dtype=self.storage_dtype)
+                          storage_dtype=self.advect_storage_dtype)
 
     def shadow(self, d):
         from phitest.render.renderer import _InverseSampleGrad
@@ -373,7 +382,8 @@ class StreamedSteps:
     def __init__(self, step, example, warmup=3):
         self.dev = step.dev
         self.slots = [step, RenderAdvectStep(step.config_name or step.cfg, step.dev, storage_dtype=step.storage_dtype,
-                                             mode=step.mode, order=step.order)]
+                                             mode=step.mode, order=step.order,
+                                             advect_storage_dtype=step.advect_storage_dtype)]
         for st in self.slots:
             st.setup_static(example)
             st.capture(warmup=warmup)
