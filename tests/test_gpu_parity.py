@@ -273,6 +273,39 @@ def test_raymarch_empty_space_skipping(ops, C, blend, boundary, negative):
     assert 0 < n < 3 * 40 * 44 * 96 // 4
 
 
+def test_raymarch_empty_space_distance_map(ops):
+    """The distance map the storing forward builds next to the occupancy map
+    (4^3-voxel blocks, one byte each, per input slice): the Chebyshev distance
+    in blocks to the nearest occupied block, capped at 7, equal to a direct
+    computation from the occupancy map the store holds."""
+    shape, res = (52, 60, 44), (40, 30, 32)
+    _, _, M, V, P, F = scene(shape, 2, res)
+    x = np.zeros((2,) + shape + (4,), np.float32)
+    x[0, 20:24, 30:35, 10:14] = 0.5
+    x[0, 45:48, 2:5, 40:44] = 0.3
+    x[1, 5:9, 50:55, 20:30] = 0.2
+    M2 = np.stack([M[0], M[0]])
+    smp = ops._samples_buffer(x.shape, 2, res, True, 'cuda')
+    ops._raymarch_fwd(cuda(x), M2, V, P, F, res, 1, 0, 0, True, samples=smp)
+    torch.cuda.synchronize()
+    D, H, W = res
+    cells = 2 * 2 * ((W + 7) // 8) * ((H + 15) // 16) * D * 128  # 2 slices x 2 views
+    words = -(-4 * (cells // 32) // 256) * 256
+    nb = tuple(-(-n // 4) for n in shape)
+    nvox = int(np.prod(nb))
+    part = -(-nvox * 2 // 256) * 256
+    raw = smp.view(torch.uint8).cpu().numpy()
+    occ = raw[256 + 2 * words:][:nvox * 2].reshape((2,) + nb)
+    dist = raw[256 + 2 * words + part:][:nvox * 2].reshape((2,) + nb)
+    assert occ.any() and not occ.all()
+    for n in range(2):
+        z, y, xx = np.nonzero(occ[n])
+        grid = np.stack(np.meshgrid(*[np.arange(k) for k in nb], indexing='ij'), -1)
+        pts = np.stack([z, y, xx], -1)
+        cheb = np.abs(grid[..., None, :] - pts[None, None, None]).max(-1).min(-1)
+        assert np.array_equal(dist[n], np.minimum(cheb, 7).astype(np.uint8))
+
+
 @pytest.mark.parametrize('fraction', [0.0, 0.01, 1.0])
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
 def test_raymarch_sample_store_pool_sizes(ops, fraction, mode):
