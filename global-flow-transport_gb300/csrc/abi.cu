@@ -401,7 +401,7 @@ static gft_status raymarch_fwd_impl(const void* input, int32_t input_dtype, cons
 // integer accumulators of the deterministic adjoint.
 static size_t raymarch_grad_ws(const int64_t* input_shape, size_t pairs, int32_t grad_mode) {
     const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
-    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC);
+    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC | GFT_GRAD_CAMERA_SUMS);
     if (det) return raymarch_det_bytes((int)input_shape[0], (int)input_shape[4], dims_of(input_shape), pairs);
     if (grad_mode == GFT_GRAD_EXACT) return 0;
     return align256(sizeof(float) * (size_t)brick_cells(dims_of(input_shape)) * pairs);
@@ -489,8 +489,9 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
         return fail(GFT_ERR_INVALID_ARGUMENT, "invalid blend mode");
     const bool weights_ready = (grad_mode & GFT_GRAD_WEIGHTS_READY) != 0;
     const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    const bool camera_sums = (grad_mode & GFT_GRAD_CAMERA_SUMS) != 0;
     const int32_t ws_mode = grad_mode;
-    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC);
+    grad_mode &= ~(GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC | GFT_GRAD_CAMERA_SUMS);
     const int layout = (input_dtype & GFT_LAYOUT_BRICK) ? LAYOUT_BRICK : LAYOUT_FLAT;
     input_dtype &= ~GFT_LAYOUT_BRICK;
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
@@ -505,6 +506,9 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
         if (layout != LAYOUT_BRICK) return fail(GFT_ERR_INVALID_ARGUMENT, "projected gradient: brick layout only");
         if (det) return fail(GFT_ERR_UNIMPLEMENTED, "projected gradient: not with GFT_GRAD_DETERMINISTIC");
     }
+    if (camera_sums && (projection == nullptr || grad_mode != GFT_GRAD_REFERENCE || weights_ready))
+        return fail(GFT_ERR_INVALID_ARGUMENT,
+                    "GFT_GRAD_CAMERA_SUMS: projected GFT_GRAD_REFERENCE gradient without GFT_GRAD_WEIGHTS_READY");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
@@ -536,6 +540,7 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
             return fail(GFT_ERR_WORKSPACE, "raymarch sample store too small");
         a.store = raymarch_store_layout(const_cast<float*>(samples), samples_bytes, pairs, a.C, a.N, a.din);
     }
+    a.camera_sums = camera_sums;
     if (projection != nullptr) {
         a.project = true;
         for (int c = 0; c < 4; ++c) {
@@ -1446,6 +1451,29 @@ gft_status gft_light_compose_projection(const float light_rgb[3], float ambient,
     }
     projection[3] = 0.f;
     projection[7] = scale;
+    return GFT_OK;
+}
+
+gft_status gft_light_compose_factored_grad_cameras(const float* density, const float* transmittance,
+                                                   const float* falloff, const int64_t shape[5], int32_t num_cameras,
+                                                   const float* camera_sums, const float* weight_sums,
+                                                   float* density_grad, float* transmittance_grad, void* stream) {
+    std::string why;
+    if (!single_channel_grid(shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
+    if (num_cameras < 1) return fail(GFT_ERR_INVALID_ARGUMENT, "num_cameras must be positive");
+    if (voxels(dims_of(shape)) >= MAX_SLICE_CELLS) return fail(GFT_ERR_INVALID_ARGUMENT, "grid slice too large");
+    if (!density || !transmittance || !falloff || !camera_sums || !weight_sums || !density_grad ||
+        !transmittance_grad)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "tensor pointer is NULL");
+    gft_status st;
+    if ((st = check_aligned({density, transmittance, falloff, weight_sums, density_grad, transmittance_grad}, 4)) !=
+            GFT_OK ||
+        (st = check_aligned({camera_sums}, 8)) != GFT_OK)
+        return st;
+    if (!launch_light_compose_factored_grad_cameras(density, transmittance, falloff, camera_sums, weight_sums,
+                                                    num_cameras, (int)shape[0], dims_of(shape), density_grad,
+                                                    transmittance_grad, as_stream(stream)))
+        return GFT_ERR_CUDA;
     return GFT_OK;
 }
 

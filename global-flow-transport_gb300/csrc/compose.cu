@@ -233,6 +233,44 @@ __global__ void __launch_bounds__(CP_THREADS)
     }
 }
 
+// From per-camera sums: P, Q = sum over the slice's cameras of the camera's
+// value sums divided by its weight sums (where positive), in camera order;
+// then as above.  Brick layout.
+__global__ void __launch_bounds__(CP_THREADS)
+    k_light_compose_factored_grad_cameras(const float* __restrict__ dens, const float* __restrict__ tr,
+                                          const float* __restrict__ fall, const float* __restrict__ g2,
+                                          const float* __restrict__ wsum, int ncam, Dims d, float* __restrict__ gd,
+                                          float* __restrict__ gt) {
+    const int64_t nvox = voxels(d), b = blockIdx.y, cells = brick_cells(d);
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b * nvox + v;
+        int x, y, z;
+        unflat32((uint32_t)v, d, x, y, z);
+        const int64_t o = brick_index(x, y, z, d);
+        float P = 0.f, Q = 0.f;
+        for (int c = 0; c < ncam; ++c) {
+            const int64_t pc = (b * ncam + c) * cells + o;
+            const float w = __ldcs(wsum + pc);
+            if (w > 0.f) {
+                const float2 s = __ldcs(reinterpret_cast<const float2*>(g2) + pc);
+                P += s.x / w;
+                Q += s.y / w;
+            }
+        }
+        const float fp = __fmul_rn(fall[v], P);
+        gd[i] = __fadd_rn(Q, __fmul_rn(tr[i], fp));
+        gt[i] = __fmul_rn(dens[i], fp);
+    }
+}
+
+bool launch_light_compose_factored_grad_cameras(const float* dens, const float* tr, const float* fall,
+                                                const float* g2, const float* wsum, int ncam, int N, Dims d,
+                                                float* gd, float* gt, cudaStream_t st) {
+    const dim3 grid(grid_for(voxels(d), CP_THREADS), N);
+    k_light_compose_factored_grad_cameras<<<grid, CP_THREADS, 0, st>>>(dens, tr, fall, g2, wsum, ncam, d, gd, gt);
+    return launched(1, "light compose gradient launch");
+}
+
 template <typename T, bool FACT>
 static void light_compose_t(const float* dens, const float* tr, const float* color, const Rgb& rgb, int N, Dims d,
                             float ambient, float scale, int layout, void* out, cudaStream_t st) {

@@ -131,6 +131,10 @@ struct RaymarchArgs {
     // holds (proj.a . g, proj.b . g) per cell instead of the 4 channels of g.
     bool project = false;
     ChanProj proj = {};
+    // With project, GFT_GRAD_REFERENCE: per pair the unnormalised projected
+    // sums (the gradient, [pairs][cells][2]) and the weight sums (the
+    // workspace) from one pass; the caller divides.
+    bool camera_sums = false;
 };
 // Workspace bytes of the deterministic adjoint for `pairs` (batch, camera) pairs.
 size_t raymarch_det_bytes(int N, int C, Dims din, size_t pairs);
@@ -217,6 +221,11 @@ bool launch_light_compose(const float* dens, const float* tr, const float* color
 // g2: the projected raymarch gradient (P, Q) per cell of layout `layout`.
 bool launch_light_compose_factored_grad(const float* dens, const float* tr, const float* fall, const float* g2,
                                         int N, Dims d, int layout, float* gd, float* gt, cudaStream_t st);
+// From per-camera sums (ncam pairs per batch slice): g2 [N*ncam][cells][2],
+// wsum [N*ncam][cells], brick layout.
+bool launch_light_compose_factored_grad_cameras(const float* dens, const float* tr, const float* fall,
+                                                const float* g2, const float* wsum, int ncam, int N, Dims d,
+                                                float* gd, float* gt, cudaStream_t st);
 bool launch_light_compose_grad(const float* dens, const float* tr, const float* color, const float* g, int N, Dims d,
                                float ambient, float scale, int layout, float* gd, float* gt, cudaStream_t st);
 int image_loss_blocks(int64_t npix);

@@ -573,10 +573,16 @@ __device__ __forceinline__ unsigned zero_weight_mask(float fx, float fy, float f
 // (MODE 2: one per brick cell of the pair; MODE 0/1: C per cell of the batch
 // slice) instead of the float reductions; integer addition is associative, so
 // the sums do not depend on the order in which the warps add them.
+// MODE 3 (per-camera sums, the reference normalisation in one pass): the
+// corner sums of the values go into the pair's own gradient, unscaled, and
+// the corner sums of the weights into the pair's weight sums (wsum), from the
+// same merge rounds; the caller divides per voxel afterwards.
 template <int C, int BM, int MODE, int L, bool DET = false>
 __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const float* __restrict__ cnt, Dims d,
                                              bool act, float px, float py, float pz, Vec<C> val,
-                                             unsigned long long* __restrict__ iacc = nullptr, float iscale = 0.f) {
+                                             unsigned long long* __restrict__ iacc = nullptr, float iscale = 0.f,
+                                             float* __restrict__ wsum = nullptr) {
+    static_assert(MODE != 3 || !DET, "per-camera sums: float path only");
     const unsigned lane = (threadIdx.y * RM_BX + threadIdx.x) & 31u;  // blockDim.x == RM_BX
     if constexpr (BM == BM_BORDER) {
         if constexpr (MODE != 0)
@@ -603,6 +609,7 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
     // zero weight adds +0 to a finite sum; corners that no member reaches with
     // a non-zero weight are not reduced (nz).  (MODE 2: the value is 1.)
     float acc[8][C];
+    float accw[8];  // MODE 3: the weights' corner sums
     // (MODE 2 adds weights, which are finite: a zero one adds +0 and needs no
     // mask)
     unsigned nz = MODE == 2 ? 0xffu : zero_weight_mask(wx, wy, wz);
@@ -610,9 +617,11 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
         float w[8];
         corner_weights(wx, wy, wz, w);
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < 8; ++k) {
 #pragma unroll
             for (int c = 0; c < C; ++c) acc[k][c] = MODE == 2 ? w[k] : w[k] * val.v[c];
+            if constexpr (MODE == 3) accw[k] = w[k];
+        }
     }
     if constexpr (MODE == 2) {
         // Weight sums: the head pulls each member's three fractions (not its
@@ -641,9 +650,11 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
                 float w[8];
                 corner_weights(mx, my, mz, w);
 #pragma unroll
-                for (int k = 0; k < 8; ++k)
+                for (int k = 0; k < 8; ++k) {
 #pragma unroll
                     for (int c = 0; c < C; ++c) acc[k][c] = fmaf(w[k], mv[c], acc[k][c]);
+                    if constexpr (MODE == 3) accw[k] += w[k];
+                }
             }
         }
     }
@@ -705,6 +716,9 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
                 if (inv > 0.f) atomic_add<C>(grad, ci, vscale(a, inv));
             } else if constexpr (MODE == 2) {
                 atomic_add<C>(grad, bi, a);
+            } else if constexpr (MODE == 3) {
+                atomic_add<C>(grad, ci, a);
+                atomicAdd(wsum + bi, accw[k]);
             } else {
                 atomic_add<C>(grad, ci, a);
             }
@@ -769,6 +783,9 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
             if (inv > 0.f) atomic_add<C>(grad, ci, vscale(a, inv));
         } else if constexpr (MODE == 2) {
             atomic_add<C>(grad, bi, a);
+        } else if constexpr (MODE == 3) {
+            atomic_add<C>(grad, ci, a);
+            atomicAdd(wsum + bi, accw[k]);
         } else {
             atomic_add<C>(grad, ci, a);
         }
@@ -809,6 +826,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
                                                       const RaymarchArgs::Store& st, const PairTable& tab, int tile,
                                                       const ChanProj& pj) {
     static_assert(!PROJ || (C == 4 && MODE != 2 && !DET), "projection: 4-channel float adjoint only");
+    static_assert(MODE != 3 || PROJ, "per-camera sums: projected adjoint only");
     constexpr int CA = PROJ ? 2 : C;  // channels of the accumulated gradient
     RayPix r;
     r.tile = tile;
@@ -831,9 +849,12 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             s_hi = -1;
         }
     const S* g = in + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
-    float* dst = MODE == 2 ? grad + (size_t)(tab.pair_base + p) * brick_cells(din)
-                           : grad + (size_t)tab.in_batch[p] * slice_cells<L>(din) * CA;
+    float* dst = MODE == 2   ? grad + (size_t)(tab.pair_base + p) * brick_cells(din)
+                 : MODE == 3 ? grad + (size_t)(tab.pair_base + p) * slice_cells<L>(din) * CA
+                             : grad + (size_t)tab.in_batch[p] * slice_cells<L>(din) * CA;
     const float* count = MODE == 1 ? cnt + (size_t)(tab.pair_base + p) * brick_cells(din) : nullptr;
+    // MODE 3: the pair's weight sums (the workspace, written by this pass)
+    float* wdst = MODE == 3 ? const_cast<float*>(cnt) + (size_t)(tab.pair_base + p) * brick_cells(din) : nullptr;
     Vec<C> acc = vzero<C>(), go = vzero<C>();
     if (MODE != 2 && live) {
         const int64_t pix = tab.pix0[p] + (int64_t)y * W + x;
@@ -896,7 +917,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             Vec<2> pv;
             pv.v[0] = pj.a[0] * val.v[0] + pj.a[1] * val.v[1] + pj.a[2] * val.v[2] + pj.a[3] * val.v[3];
             pv.v[1] = pj.b[0] * val.v[0] + pj.b[1] * val.v[1] + pj.b[2] * val.v[2] + pj.b[3] * val.v[3];
-            scatter_step<2, BM, MODE, L, false>(dst, count, din, on, px, py, pz, pv);
+            scatter_step<2, BM, MODE, L, false>(dst, count, din, on, px, py, pz, pv, nullptr, 0.f, wdst);
         } else {
             scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);
         }
@@ -971,6 +992,11 @@ static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, co
                            const float* dout, float* grad, const float* cnt, const PairTable& t) {
     const ChanProj pj = a.proj;
     if constexpr (C == 4 && L == LAYOUT_BRICK) {
+        if (a.project && a.camera_sums) {  // reference normalisation by per-camera sums
+            k_raymarch_scatter<C, S, BM, 3, L, false, true><<<grid, block, 0, s>>>(
+                (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, nullptr, nullptr, 0.f, a.store, t, pj);
+            return;
+        }
         if (a.project) {  // the ABI admits it for the float path only
             if (exact)
                 k_raymarch_scatter<C, S, BM, 0, L, false, true><<<grid, block, 0, s>>>(
@@ -1337,6 +1363,23 @@ bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pair
     RaymarchArgs a = a_in;
     const int64_t cells = a.layout == LAYOUT_BRICK ? brick_cells(a.din) : voxels(a.din);
     const int64_t n = cells * (a.project ? 2 : a.C) * a.N;
+    if (a.camera_sums) {
+        // per pair: the projected value sums and the weight sums, both
+        // accumulated from zero by one pass
+        const size_t pn = (size_t)cells * 2 * pairs.size(), wn = (size_t)brick_cells(a.din) * pairs.size();
+        if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * pn, s), "zero gradient") ||
+            !cuda_ok(cudaMemsetAsync(ws_cnt, 0, sizeof(float) * wn, s), "zero weight sums"))
+            return false;
+        const dim3 block(RM_BX, RM_BY, 1);
+        int64_t smp_cells = 0;
+        for (PairTable& t : make_tables(pairs)) {
+            const dim3 grid(raymarch_blocks((int)set_ray_tiles(t, &smp_cells)));
+            if (a.dtype == 0) bwd_dispatch_bm<4, float>(false, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            else bwd_dispatch_bm<4, __nv_bfloat16>(false, grid, block, s, a, out, dout, grad, ws_cnt, t);
+            if (!launched(1, "raymarch backward launch")) return false;
+        }
+        return true;
+    }
     if (!a.det) {
         if (!cuda_ok(cudaMemsetAsync(grad, 0, sizeof(float) * n, s), "zero gradient")) return false;
         if (!exact && !weights_ready && knob_value(GFT_KNOB_WEIGHTS_PIPELINE) == 1 &&

@@ -69,6 +69,7 @@ _SIGS = {
     'gft_light_compose_factored': (_I32, [_P, _P, _P, _P, _I64P, _F, _F, _I32, _P, _P]),
     'gft_light_compose_projection': (_I32, [_P, _F, _F, _P]),
     'gft_light_compose_factored_grad': (_I32, [_P, _P, _P, _I64P, _I32, _P, _P, _P, _P]),
+    'gft_light_compose_factored_grad_cameras': (_I32, [_P, _P, _P, _I64P, _I32, _P, _P, _P, _P, _P]),
     'gft_image_loss_workspace_size': (_SZ, [ctypes.c_int64]),
     'gft_image_loss': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _SZ, _P]),
     'gft_image_loss_grad': (_I32, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),

@@ -96,6 +96,17 @@ def compose_projection(rgb, ambient, scale):
     return proj
 
 
+def _compose_factored_grad_cameras(d, tr, fall, ncam, g2p, wsum):
+    lib = _lib.load()
+    gd = torch.empty_like(d)
+    gt = torch.empty_like(tr)
+    with torch.cuda.device(d.device):
+        _lib.check(lib.gft_light_compose_factored_grad_cameras(_p(d), _p(tr), _p(fall), _shape(d), int(ncam), _p(g2p),
+                                                               _p(wsum), _p(gd), _p(gt), _stream(d.device)),
+                   'LightComposeFactoredGradCameras')
+    return gd, gt
+
+
 def _compose_factored_grad(d, tr, fall, g2):
     lib = _lib.load()
     g2 = g2.contiguous()
@@ -128,8 +139,11 @@ class _ComposeRaymarch(torch.autograd.Function):
         else:
             xs = _compose_factored(d, tr, color, rgb, ambient, scale, bf16)
         need = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        # a factored light's reference-normalised adjoint sums the weights in
+        # its own pass: no weight pass ahead
+        ctx.camera_sums = rgb is not None and ops.camera_sums_active()
         y, samples = ops._raymarch_forward_ctx(ctx, xs, need, M, V, P, F, out_shape, ops.FILTER['LINEAR'], boundary,
-                                               blend, True, grid)
+                                               blend, True, grid, weights_pass=not ctx.camera_sums)
         ctx.save_for_backward(d, tr, color, xs, y, samples)
         ctx.k = (float(ambient), float(scale))
         ctx.rgb = rgb
@@ -148,6 +162,12 @@ class _ComposeRaymarch(torch.autograd.Function):
             gd, gt = _compose_grad(d, tr, color, ctx.k[0], ctx.k[1], True, g)
         else:
             proj = compose_projection(ctx.rgb, *ctx.k)
+            if ctx.camera_sums and ops.camera_sums_active():
+                g2p, wsum = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args, projection=proj,
+                                                       camera_sums=True)
+                ncam = g2p.shape[0] // d.shape[0]
+                gd, gt = _compose_factored_grad_cameras(d, tr, color, ncam, g2p, wsum)
+                return (gd, gt) + (None,) * 13
             if ops._state['deterministic']:
                 g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
                 a, b = [float(v) for v in proj[:4]], [float(v) for v in proj[4:]]  # host scalars: capturable

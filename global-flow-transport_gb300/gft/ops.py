@@ -24,8 +24,27 @@ KNOB_WEIGHTS_PIPELINE = 5  # GFT_KNOB_WEIGHTS_PIPELINE
 CLAMP = {'NONE': 0, 'MC_SMOOTH': 1, 'NEGATIVE': 2}
 
 _state = {'grad_mode': 'REFERENCE', 'side_weights': True, 'sample_store': True, 'sample_pool': 0.25,
-          'deterministic': False}
+          'deterministic': False, 'camera_sums': False}
 DETERMINISTIC = 0x400  # GFT_GRAD_DETERMINISTIC
+CAMERA_SUMS = 0x800  # GFT_GRAD_CAMERA_SUMS
+
+
+def set_raymarch_camera_sums(enabled):
+    """The reference-normalised adjoint of the fused render with a factored
+    light (gft.fused.render_bricked) in one pass: per camera the projected
+    value sums and the weight sums from the same walk over the samples, the
+    division per voxel afterwards (gft.h GFT_GRAD_CAMERA_SUMS), instead of a
+    separate weight pass before a normalised scatter.  Off by default: the
+    one-pass scatter does both reductions and is slower than the weight pass
+    running beside the forward kernels plus the normalised scatter (cfg5
+    step 9.00 against 8.61 ms)."""
+    _state['camera_sums'] = bool(enabled)
+
+
+def camera_sums_active():
+    """Whether a fused render's reference-normalised adjoint uses per-camera
+    sums now (then no weight pass runs ahead of it)."""
+    return _state['camera_sums'] and _state['grad_mode'] == 'REFERENCE' and not _state['deterministic']
 
 
 def set_deterministic(enabled):
@@ -383,18 +402,22 @@ def _cuda_device(device):
 
 
 def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
-                              boundary='BORDER', separate_camera_batch=True, device=None):
+                              boundary='BORDER', separate_camera_batch=True, device=None, for_camera_sums=False):
     """Starts the first, geometry-only pass of the reference-normalised
     raymarch gradient (the per-camera weight sums) on a side stream now, so
     that it overlaps whatever the caller runs before the raymarch.  The next
     differentiable raymarch_grid_transform with the same input shape, device
     and geometry takes it over; until then it holds one float per voxel and
     camera.  Under CUDA-graph capture that raymarch and its backward must be
-    captured too (they join the side stream)."""
+    captured too (they join the side stream).  for_camera_sums: the raymarch
+    is a fused render with a factored light, whose adjoint sums the weights
+    itself while camera_sums_active(); nothing is started then."""
     if _state['deterministic']:
         return  # the deterministic gradient computes its own (integer) weight sums
     if _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) == 1:
         return  # the gradient call computes them, beside its scatter
+    if for_camera_sums and camera_sums_active():
+        return  # the fused render's adjoint sums the weights itself
     dev = _cuda_device(device)
     out_shape = _shape3(output_shape)
     b = _enum(BOUNDARY, boundary, 'boundary')
@@ -407,9 +430,12 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
 
 
 def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None,
-                  grid=None, samples=None, projection=None):
+                  grid=None, samples=None, projection=None, camera_sums=False):
     """projection (8 host floats, bricked 4-channel x): the gradient
-    accumulated projected onto two channels, [N, cells, 2]."""
+    accumulated projected onto two channels, [N, cells, 2].  camera_sums
+    (with projection, REFERENCE): per pair the unnormalised projected sums
+    [pairs, cells, 2] and the workspace holding the pairs' weight sums, as
+    (sums, workspace)."""
     lib = _lib.load()
     Mh, nm = _mats(M)
     Vh, nv = _mats(V)
@@ -418,6 +444,9 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
     shape5, code = _grid5(x, grid)
     shape = _lib.i64(shape5)
     gshape = x.shape if projection is None else tuple(x.shape[:-1]) + (2,)
+    if camera_sums:
+        gshape = (shape5[0] * (nv if separate else 1),) + tuple(x.shape[1:-1]) + (2,)
+        weights = None
     grad = torch.empty(gshape, dtype=torch.float32, device=x.device)
     if weights is not None and gmode == GRAD['REFERENCE']:
         ws = weights
@@ -430,9 +459,9 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
             proj = np.ascontiguousarray(np.asarray(projection, dtype=np.float32).reshape(8))
             st = lib.gft_raymarch_grid_transform_grad_projected(
                 _p(x), code, shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv, _lib.i32(out_shape),
-                interp, boundary, blend, int(separate), gmode, _p(samples) if samples is not None else None,
-                samples.numel() if samples is not None else 0, _p(proj), _p(grad), _p(ws), ws.numel(),
-                _stream(x.device))
+                interp, boundary, blend, int(separate), gmode | (CAMERA_SUMS if camera_sums else 0),
+                _p(samples) if samples is not None else None, samples.numel() if samples is not None else 0,
+                _p(proj), _p(grad), _p(ws), ws.numel(), _stream(x.device))
         elif samples is None:
             st = lib.gft_raymarch_grid_transform_grad(_p(x), code, shape, _p(y), _p(dy), _p(Mh), nm, _p(Vh),
                                                       _p(Ph), _p(Fh), nv, _lib.i32(out_shape), interp, boundary,
@@ -445,16 +474,19 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
                                                              samples.numel(), _p(grad), _p(ws), ws.numel(),
                                                              _stream(x.device))
     _lib.check(st, 'RaymarchGridTransformGrad')
-    return grad
+    return (grad, ws) if camera_sums else grad
 
 
-def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, boundary, blend, separate, grid):
+def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, boundary, blend, separate, grid,
+                          weights_pass=True):
     """Forward of a differentiable raymarch of the storage-typed input xs:
     starts the reference normalisation's weight pass (cached, prefetched or on
-    a side stream) into ctx.weights and returns (output, sample store)."""
+    a side stream; not with weights_pass False, for an adjoint that sums the
+    weights itself) into ctx.weights and returns (output, sample store)."""
     shape5 = _grid5(xs, grid)[0]
     ctx.weights = None
-    if need_grad and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR'] and not _state['deterministic']:
+    if (need_grad and weights_pass and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR'] and
+            not _state['deterministic']):
         cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
         if cached is not None:
             ctx.weights = (cached, None)
@@ -472,16 +504,18 @@ def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, bou
 
 
 def _raymarch_backward_ctx(ctx, xs, y, samples, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, grid,
-                           projection=None):
+                           projection=None, camera_sums=False):
     """The fp32 input gradient of a raymarch run by _raymarch_forward_ctx
-    (projected onto two channels with ``projection``)."""
+    (projected onto two channels with ``projection``; per-camera sums and
+    weight sums with ``camera_sums``)."""
     ws = None
     if ctx.weights is not None:
         ws, ev = ctx.weights
         if ev is not None:
             torch.cuda.current_stream(xs.device).wait_event(ev)
     g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
-                      _scatter_gmode(), weights=ws, grid=grid, samples=samples, projection=projection)
+                      _scatter_gmode(), weights=ws, grid=grid, samples=samples, projection=projection,
+                      camera_sums=camera_sums)
     ctx.weights = None
     return g
 

@@ -194,7 +194,7 @@ class RenderAdvectStep:
         if self.mode != 'plain' and torch.is_grad_enabled() and ops.get_grad_mode() == 'REFERENCE':
             # the raymarch gradient's geometry-only weight pass overlaps advection and shadow
             ops.prefetch_raymarch_weights(tuple(d_prev.shape[:4]) + (4,), self.M, self.V, self.P, self.F, self.res,
-                                          device=d_prev.device)
+                                          device=d_prev.device, for_camera_sums=True)
         d = self.advect(d_prev, vx, vy, vz)
         img = self.render(d)
         if self.mode != 'plain':

@@ -167,6 +167,19 @@ gft_status gft_raymarch_grid_transform_grad_stored(
  * GFT_GRAD_REFERENCE or GFT_GRAD_EXACT (with GFT_GRAD_WEIGHTS_READY as
  * usual), not GFT_GRAD_DETERMINISTIC; the same workspace.  No counterpart in
  * the reference. */
+/* OR'ed into grad_mode of gft_raymarch_grid_transform_grad_projected with
+ * GFT_GRAD_REFERENCE (not GFT_GRAD_WEIGHTS_READY): the reference
+ * normalisation in one pass.  input_grad [pairs, cells, 2] receives, per
+ * (batch, camera) pair, the projected corner sums unnormalised, and the
+ * first pairs x cells floats of the workspace the pair's per-voxel sums of
+ * the trilinear weights (both in the brick layout, cells =
+ * ceil(D/2)*ceil(H/2)*ceil(W/2)*8); the caller divides each pair's sums by
+ * its weight sums where those are positive and adds the pairs
+ * (gft_light_compose_factored_grad_cameras does so).  The reference
+ * divides each camera's gradient by that camera's sample weights
+ * (raymarch_grid.cu.cc:519-568) after a separate counting pass; here both
+ * sums come from the same walk over the samples. */
+#define GFT_GRAD_CAMERA_SUMS 0x800
 gft_status gft_raymarch_grid_transform_grad_projected(
     const void* input, int32_t input_dtype, const int64_t input_shape[5],
     const float* output, const float* output_grad,
@@ -435,6 +448,15 @@ gft_status gft_light_compose_factored_grad(const float* density, const float* tr
                                            const int64_t shape[5], int32_t output_layout,
                                            const float* projected_grad, float* density_grad,
                                            float* transmittance_grad, void* stream);
+/* The same adjoint from per-camera sums (GFT_GRAD_CAMERA_SUMS): for batch
+ * slice b, (P, Q) = sum over its num_cameras pairs c = b * num_cameras + k of
+ * camera_sums[c] / weight_sums[c] where weight_sums[c] > 0; camera_sums
+ * [N * num_cameras, cells, 2] and weight_sums [N * num_cameras, cells] in the
+ * brick layout. */
+gft_status gft_light_compose_factored_grad_cameras(const float* density, const float* transmittance,
+                                                   const float* falloff, const int64_t shape[5], int32_t num_cameras,
+                                                   const float* camera_sums, const float* weight_sums,
+                                                   float* density_grad, float* transmittance_grad, void* stream);
 /* gft_image_loss: image [pixels, 4] (rgb + density), target [pixels, 3],
  * background = 3 host floats; *loss (device) = mean over pixels and rgb of
  * (rgb + background * exp(-density) - target)^2, summed in a fixed order.

@@ -141,16 +141,18 @@ def test_render_bricked_equals_compose_then_raymarch(fused, storage):
 
 
 @pytest.mark.parametrize('storage', [None, torch.bfloat16])
-@pytest.mark.parametrize('gmode', ['REFERENCE', 'EXACT', 'DETERMINISTIC'])
+@pytest.mark.parametrize('gmode', ['REFERENCE', 'REFERENCE_CAMERA_SUMS', 'EXACT', 'DETERMINISTIC'])
 @pytest.mark.parametrize('store', [True, False])
 def test_render_bricked_factored_light(fused, storage, gmode, store):
     """A factored light (falloff [D, H, W, 1] x rgb): the composition forms
     falloff * rgb by the same rounded product as a precomputed colour grid, so
     the raymarch input and images equal those of the colour grid bit for bit;
     the adjoint accumulates the two projections of the raymarch gradient that
-    the composition's adjoint reads (the deterministic adjoint: projected after
-    its integer sums), and the density and transmittance gradients equal the
-    colour grid's up to summation order."""
+    the composition's adjoint reads (REFERENCE: the weight pass ahead and a
+    normalised scatter, or per-camera value and weight sums from one pass,
+    divided per voxel; the deterministic adjoint: projected after its integer
+    sums), and the density and transmittance gradients equal the colour
+    grid's up to summation order."""
     from gft import ops
     from scene_utils import scene
     g = torch.Generator().manual_seed(19)
@@ -162,11 +164,12 @@ def test_render_bricked_factored_light(fused, storage, gmode, store):
     rgb = np.array([0.9, 0.7, 1.3], np.float32)
     col = (fall * torch.from_numpy(rgb).cuda())[None].contiguous()
     dy = torch.randn((1, 3, 9, 11, 4), generator=g).cuda()
-    saved = ops.get_grad_mode(), ops._state['deterministic'], ops._state['sample_store']
+    saved = ops.get_grad_mode(), ops._state['deterministic'], ops._state['sample_store'], ops._state['camera_sums']
     try:
         ops.set_grad_mode('EXACT' if gmode == 'EXACT' else 'REFERENCE')
         ops.set_deterministic(gmode == 'DETERMINISTIC')
         ops.set_raymarch_sample_store(store)
+        ops.set_raymarch_camera_sums(gmode == 'REFERENCE_CAMERA_SUMS')
         res = []
         for light in ((fall, rgb), col):
             d1, t1 = d0.clone().requires_grad_(True), t0.clone().requires_grad_(True)
@@ -178,6 +181,7 @@ def test_render_bricked_factored_light(fused, storage, gmode, store):
         ops.set_grad_mode(saved[0])
         ops.set_deterministic(saved[1])
         ops.set_raymarch_sample_store(saved[2])
+        ops.set_raymarch_camera_sums(saved[3])
     (i1, x1, gd1, gt1), (i2, x2, gd2, gt2) = res
     assert torch.equal(x1, x2)
     assert torch.equal(i1, i2)

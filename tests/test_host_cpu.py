@@ -265,6 +265,14 @@ def test_projected_gradient_and_factored_light_arguments(lib):
     assert grad([1, 8, 8, 8, 4], 0, 1, pj) == lib.ERR_INVALID_ARGUMENT
     assert b'brick' in L.gft_last_error()
     assert grad([1, 8, 8, 8, 4], brick, 0x400 | 1, pj) == lib.ERR_UNIMPLEMENTED
+    # per-camera sums: projected GFT_GRAD_REFERENCE without GFT_GRAD_WEIGHTS_READY only
+    assert grad([1, 8, 8, 8, 4], brick, 0x800 | 1, pj) == lib.ERR_INVALID_ARGUMENT
+    assert b'CAMERA_SUMS' in L.gft_last_error()
+    assert grad([1, 8, 8, 8, 4], brick, 0x800 | 0x100, pj) == lib.ERR_INVALID_ARGUMENT
+    assert L.gft_raymarch_grid_transform_grad(one, brick, lib.i64([1, 8, 8, 8, 4]), one, one, p, 1, p, p, f, 1, out,
+                                              1, 0, 0, 1, 0x800, one, None, 0, None) == lib.ERR_INVALID_ARGUMENT
+    assert L.gft_light_compose_factored_grad_cameras(one, one, one, lib.i64([1, 4, 4, 4, 1]), 0, one, one, one,
+                                                     one, None) == lib.ERR_INVALID_ARGUMENT
     rgb = np.array([0.5, 2.0, -1.0], np.float32)
     assert L.gft_light_compose_projection(rgb.ctypes.data_as(ctypes.c_void_p), 0.25, 4.0, pj) == lib.OK
     assert proj.tolist() == [2.0, 8.0, -4.0, 0.0, 1.0, 1.0, 1.0, 4.0]
