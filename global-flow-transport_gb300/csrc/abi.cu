@@ -504,11 +504,11 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     if (projection != nullptr) {
         if (input_shape[4] != 4) return fail(GFT_ERR_INVALID_ARGUMENT, "projected gradient: 4 channels only");
         if (layout != LAYOUT_BRICK) return fail(GFT_ERR_INVALID_ARGUMENT, "projected gradient: brick layout only");
-        if (det) return fail(GFT_ERR_UNIMPLEMENTED, "projected gradient: not with GFT_GRAD_DETERMINISTIC");
     }
-    if (camera_sums && (projection == nullptr || grad_mode != GFT_GRAD_REFERENCE || weights_ready))
+    if (camera_sums && (projection == nullptr || grad_mode != GFT_GRAD_REFERENCE || weights_ready || det))
         return fail(GFT_ERR_INVALID_ARGUMENT,
-                    "GFT_GRAD_CAMERA_SUMS: projected GFT_GRAD_REFERENCE gradient without GFT_GRAD_WEIGHTS_READY");
+                    "GFT_GRAD_CAMERA_SUMS: projected GFT_GRAD_REFERENCE gradient without GFT_GRAD_WEIGHTS_READY "
+                    "or GFT_GRAD_DETERMINISTIC");
     gft_status st = check_cameras(matrix_m, num_m, input_shape[0], matrix_v, matrix_p, frustum, num_cameras,
                                   separate_camera_batch);
     if (st != GFT_OK) return st;

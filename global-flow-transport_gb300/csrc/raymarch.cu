@@ -825,7 +825,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
                                                       unsigned long long* __restrict__ iacc, float iscale,
                                                       const RaymarchArgs::Store& st, const PairTable& tab, int tile,
                                                       const ChanProj& pj) {
-    static_assert(!PROJ || (C == 4 && MODE != 2 && !DET), "projection: 4-channel float adjoint only");
+    static_assert(!PROJ || (C == 4 && MODE != 2 && !(DET && MODE == 3)), "projection: 4-channel adjoint only");
     static_assert(MODE != 3 || PROJ, "per-camera sums: projected adjoint only");
     constexpr int CA = PROJ ? 2 : C;  // channels of the accumulated gradient
     RayPix r;
@@ -835,7 +835,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
     unsigned long long* idst =
         !DET        ? nullptr
         : MODE == 2 ? iacc + (size_t)(tab.pair_base + p) * brick_cells(din)
-                        : iacc + (size_t)tab.in_batch[p] * slice_cells<L>(din) * C;
+                        : iacc + (size_t)tab.in_batch[p] * slice_cells<L>(din) * CA;
     float3 farp, step, nearp;
     ray_far_step(tab.cam[p], x, y, W, H, D, farp, step, nearp);
     // With a sample store: the forward's own clip range (front-to-back steps
@@ -917,7 +917,7 @@ __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, 
             Vec<2> pv;
             pv.v[0] = pj.a[0] * val.v[0] + pj.a[1] * val.v[1] + pj.a[2] * val.v[2] + pj.a[3] * val.v[3];
             pv.v[1] = pj.b[0] * val.v[0] + pj.b[1] * val.v[1] + pj.b[2] * val.v[2] + pj.b[3] * val.v[3];
-            scatter_step<2, BM, MODE, L, false>(dst, count, din, on, px, py, pz, pv, nullptr, 0.f, wdst);
+            scatter_step<2, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, pv, idst, iscale, wdst);
         } else {
             scatter_step<C, BM, MODE, L, DET>(dst, count, din, on, px, py, pz, val, idst, iscale);
         }
@@ -997,7 +997,18 @@ static void bwd_dispatch_l(bool exact, dim3 grid, dim3 block, cudaStream_t s, co
                 (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, nullptr, nullptr, 0.f, a.store, t, pj);
             return;
         }
-        if (a.project) {  // the ABI admits it for the float path only
+        if (a.project && a.det) {
+            if (exact)
+                k_raymarch_scatter<C, S, BM, 0, L, true, true><<<grid, block, 0, s>>>(
+                    (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t,
+                    pj);
+            else
+                k_raymarch_scatter<C, S, BM, 1, L, true, true><<<grid, block, 0, s>>>(
+                    (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, a.det_acc, a.det_scale, 0.f, a.store, t,
+                    pj);
+            return;
+        }
+        if (a.project) {
             if (exact)
                 k_raymarch_scatter<C, S, BM, 0, L, false, true><<<grid, block, 0, s>>>(
                     (const S*)a.input, a.din, a.blend, out, dout, grad, cnt, nullptr, nullptr, 0.f, a.store, t, pj);
@@ -1156,11 +1167,16 @@ __global__ void k_det_absmax_grid(const S* __restrict__ in, Dims d, int N, unsig
 }
 // bounds: [0] max|dy| bits, [1] max|x| bits; wmax: the largest integer weight
 // sum (EXACT); scale <- 2^(61 - ceil(log2 bound)), NaN for a non-finite bound
+// pfac: the accumulated values are projections sum_c p_c v_c of the channels
+// (1 when they are the channels), at most pfac = max sum_c |p_c| times the
+// channels' bound.
 __global__ void k_det_scale(const unsigned int* __restrict__ bounds, const unsigned long long* __restrict__ wmax,
-                            float wscale, int C, int D, int blend, int pairs, bool exact, float* __restrict__ scale) {
+                            float wscale, int C, int D, int blend, int pairs, bool exact, float pfac,
+                            float* __restrict__ scale) {
     const double dy = (double)__uint_as_float(bounds[0]), x = (double)__uint_as_float(bounds[1]);
     double b = dy;
     if (C > 1 && blend == BL_BEER_LAMBERT) b = dy * (1.0 + (double)(C - 1) * D * x);
+    b *= (double)pfac;
     double f = (double)pairs;
     if (exact) f *= (double)(*wmax) / (double)wscale;
     const double t = b * f;
@@ -1413,8 +1429,17 @@ bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pair
             else if (a.C == 2) brick ? det_absmax_grid<2, __nv_bfloat16, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<2, __nv_bfloat16, LAYOUT_FLAT>(a, L.bounds + 1, s);
             else brick ? det_absmax_grid<1, __nv_bfloat16, LAYOUT_BRICK>(a, L.bounds + 1, s) : det_absmax_grid<1, __nv_bfloat16, LAYOUT_FLAT>(a, L.bounds + 1, s);
         }
+        float pfac = 1.f;
+        if (a.project) {
+            float sa = 0.f, sb = 0.f;
+            for (int c = 0; c < 4; ++c) {
+                sa += std::fabs(a.proj.a[c]);
+                sb += std::fabs(a.proj.b[c]);
+            }
+            pfac = std::max(sa, sb);
+        }
         k_det_scale<<<1, 1, 0, s>>>(L.bounds, L.wmax, det_weight_scale(pairs, a), a.C, dmax, a.blend, (int)pairs.size(),
-                                    exact, L.scale);
+                                    exact, pfac, L.scale);
         if (!launched(3, "deterministic bound launch")) return false;
         a.det_acc = L.gacc;
         a.det_scale = L.scale;

@@ -128,8 +128,8 @@ class _ComposeRaymarch(torch.autograd.Function):
     light colour falloff x rgb) the raymarch adjoint accumulates only the two
     projections of its 4-channel gradient that the composition's adjoint
     reads (gft_raymarch_grid_transform_grad_projected): half the reduction
-    bytes.  The deterministic adjoint forms the 4 channels and projects them
-    afterwards."""
+    bytes (the deterministic adjoint: two integer sums per cell instead of
+    four)."""
 
     @staticmethod
     def forward(ctx, d, tr, color, rgb, ambient, scale, grid, M, V, P, F, out_shape, boundary, blend, storage_dtype):
@@ -168,13 +168,7 @@ class _ComposeRaymarch(torch.autograd.Function):
                 ncam = g2p.shape[0] // d.shape[0]
                 gd, gt = _compose_factored_grad_cameras(d, tr, color, ncam, g2p, wsum)
                 return (gd, gt) + (None,) * 13
-            if ops._state['deterministic']:
-                g = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args)
-                a, b = [float(v) for v in proj[:4]], [float(v) for v in proj[4:]]  # host scalars: capturable
-                g2 = torch.stack([g[..., 0] * a[0] + g[..., 1] * a[1] + g[..., 2] * a[2] + g[..., 3] * a[3],
-                                  g[..., 0] * b[0] + g[..., 1] * b[1] + g[..., 2] * b[2] + g[..., 3] * b[3]], -1)
-            else:
-                g2 = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args, projection=proj)
+            g2 = ops._raymarch_backward_ctx(ctx, xs, y, samples, dy, *ctx.args, projection=proj)
             gd, gt = _compose_factored_grad(d, tr, color, g2)
         return (gd, gt) + (None,) * 13
 

@@ -165,8 +165,10 @@ gft_status gft_raymarch_grid_transform_grad_stored(
  * reductions move half the bytes; the result equals the projection of the
  * plain gradient up to float rounding.  4 channels, GFT_LAYOUT_BRICK,
  * GFT_GRAD_REFERENCE or GFT_GRAD_EXACT (with GFT_GRAD_WEIGHTS_READY as
- * usual), not GFT_GRAD_DETERMINISTIC; the same workspace.  No counterpart in
- * the reference. */
+ * usual), also GFT_GRAD_DETERMINISTIC (two int64 sums per cell; the bound
+ * of the fixed point scales by the larger of sum |projection[0..3]| and
+ * sum |projection[4..7]|); the same workspace.  No counterpart in the
+ * reference. */
 /* OR'ed into grad_mode of gft_raymarch_grid_transform_grad_projected with
  * GFT_GRAD_REFERENCE (not GFT_GRAD_WEIGHTS_READY): the reference
  * normalisation in one pass.  input_grad [pairs, cells, 2] receives, per

@@ -191,9 +191,11 @@ def test_render_bricked_factored_light(fused, storage, gmode, store):
 
 
 @pytest.mark.parametrize('gmode', ['REFERENCE', 'EXACT'])
-def test_raymarch_grad_projected(fused, gmode):
+@pytest.mark.parametrize('det', [False, True])
+def test_raymarch_grad_projected(fused, gmode, det):
     """gft_raymarch_grid_transform_grad_projected against the projection of the
-    plain 4-channel gradient (bricked input, both grad modes)."""
+    plain 4-channel gradient (bricked input, both grad modes; deterministic:
+    two int64 sums per cell, bit-identical from run to run)."""
     from gft import ops
     from scene_utils import scene
     g = torch.Generator().manual_seed(21)
@@ -206,9 +208,12 @@ def test_raymarch_grad_projected(fused, gmode):
     proj = np.array([0.3, -1.2, 0.7, 0.0, 0.5, 0.5, 0.5, 1.1], np.float32)
     gm = ops.GRAD[gmode]
     args = (xb, y, dy, M, V, P, F, (12, 10, 9), ops.FILTER['LINEAR'], ops.BOUNDARY['BORDER'],
-            ops.BLEND['BEER_LAMBERT'], True, gm)
-    g4 = ops._raymarch_bwd(*args, grid=(D, H, W))
-    g2 = ops._raymarch_bwd(*args, grid=(D, H, W), projection=proj)
+            ops.BLEND['BEER_LAMBERT'], True)
+    g4 = ops._raymarch_bwd(*args, gm, grid=(D, H, W))
+    gp = gm | (ops.DETERMINISTIC if det else 0)
+    g2 = ops._raymarch_bwd(*args, gp, grid=(D, H, W), projection=proj)
+    if det:
+        assert torch.equal(g2, ops._raymarch_bwd(*args, gp, grid=(D, H, W), projection=proj))
     assert tuple(g2.shape) == tuple(xb.shape[:-1]) + (2,)
     pm = torch.from_numpy(proj.reshape(2, 4)).cuda()
     ref = torch.stack([(g4 * pm[0]).sum(-1), (g4 * pm[1]).sum(-1)], -1)

@@ -240,9 +240,9 @@ def test_tonemap_and_deterministic_arguments(lib):
 
 
 def test_projected_gradient_and_factored_light_arguments(lib):
-    """The projected raymarch adjoint takes 4-channel bricked inputs on the
-    float path only; the composition's projection is (scale rgb, 0, scale
-    ambient x3, scale); checks happen before any launch."""
+    """The projected raymarch adjoint takes 4-channel bricked inputs; the
+    composition's projection is (scale rgb, 0, scale ambient x3, scale);
+    checks happen before any launch."""
     L = lib.load()
     eye = np.eye(4, dtype=np.float32).reshape(-1)
     fr = np.array([1, 3, -1, 1, 1, -1], dtype=np.float32)
@@ -264,7 +264,8 @@ def test_projected_gradient_and_factored_light_arguments(lib):
     assert b'4 channels' in L.gft_last_error()
     assert grad([1, 8, 8, 8, 4], 0, 1, pj) == lib.ERR_INVALID_ARGUMENT
     assert b'brick' in L.gft_last_error()
-    assert grad([1, 8, 8, 8, 4], brick, 0x400 | 1, pj) == lib.ERR_UNIMPLEMENTED
+    # deterministic projected gradient: accepted (here it stops at the missing workspace)
+    assert grad([1, 8, 8, 8, 4], brick, 0x400 | 1, pj) == lib.ERR_WORKSPACE
     # per-camera sums: projected GFT_GRAD_REFERENCE without GFT_GRAD_WEIGHTS_READY only
     assert grad([1, 8, 8, 8, 4], brick, 0x800 | 1, pj) == lib.ERR_INVALID_ARGUMENT
     assert b'CAMERA_SUMS' in L.gft_last_error()
