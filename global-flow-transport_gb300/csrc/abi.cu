@@ -914,6 +914,8 @@ gft_status gft_sample_grid_transform(const void* input, int32_t input_dtype, con
                                      int32_t separate_camera_batch, float* output, void* workspace,
                                      size_t workspace_bytes, void* stream) {
     std::string why;
+    const bool dense = (interpolation & GFT_SAMPLE_DENSE) != 0;
+    interpolation &= ~GFT_SAMPLE_DENSE;
     if (!grid_shape_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (!channels_ok(input_shape[4])) return fail(GFT_ERR_UNIMPLEMENTED, "Only 1,2 and 4 Channel supported.");
     if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
@@ -944,7 +946,7 @@ gft_status gft_sample_grid_transform(const void* input, int32_t input_dtype, con
     // Occupancy (forward modes, whose input is a volume, often mostly empty;
     // BORDER / CLAMP with LINEAR or NEAREST filtering): samples reading only
     // zeros skip their LOD and fetches.
-    if (need > 0 && (coordinate_mode == 0 || coordinate_mode == 3) &&
+    if (need > 0 && !dense && (coordinate_mode == 0 || coordinate_mode == 3) &&
         (boundary == GFT_BOUNDARY_BORDER || boundary == GFT_BOUNDARY_CLAMP) &&
         (interpolation == GFT_FILTER_LINEAR || interpolation == GFT_FILTER_NEAREST)) {
         const Dims d = dims_of(input_shape);

@@ -868,13 +868,16 @@ def _sample_transform_bwd(in_shape, dy, M, V, P, F, interp, boundary, coord, cco
     return grad
 
 
+SAMPLE_DENSE = 0x100  # GFT_SAMPLE_DENSE
+
+
 class _SampleTransform(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco, separate,
-                storage_dtype):
+                storage_dtype, dense):
         xs = _storage(x, storage_dtype)
-        y = _sample_transform_fwd(xs, M, V, P, F, out_shape, interp, boundary, mip, num_mips, bias, coord, cco,
-                                  separate)
+        y = _sample_transform_fwd(xs, M, V, P, F, out_shape, interp | (SAMPLE_DENSE if dense else 0), boundary, mip,
+                                  num_mips, bias, coord, cco, separate)
         ctx.args = (tuple(x.shape), M, V, P, F, interp, boundary, mip, coord, cco, separate)
         ctx.in_dtype = x.dtype
         return y
@@ -887,14 +890,16 @@ class _SampleTransform(torch.autograd.Function):
             raise _lib.GftInvalidArgument('SampleGridTransformGrad: mipmapping must be NONE')
         g = _sample_transform_bwd(in_shape, _cuda(dy, 'output_grad'), M, V, P, F, interp, boundary, coord, cco,
                                   separate, GRAD[get_grad_mode()], dy.device)
-        return (g.to(ctx.in_dtype),) + (None,) * 14
+        return (g.to(ctx.in_dtype),) + (None,) * 15
 
 
 def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
                           interpolation='LINEAR', boundary='BORDER', mipmapping='NONE', num_mipmaps=0, mip_bias=0.0,
                           coordinate_mode='TRANSFORM_LINDEPTH', cell_center_offset=0.5, separate_camera_batch=True,
-                          storage_dtype=None):
-    """SampleGridTransform: [N,D,H,W,C] -> [N, V (or 1), Do, Ho, Wo, C]."""
+                          storage_dtype=None, dense_input=False):
+    """SampleGridTransform: [N,D,H,W,C] -> [N, V (or 1), Do, Ho, Wo, C].
+    dense_input: the input is known to be dense (e.g. a gradient), so no
+    occupancy map is built for it (gft.h GFT_SAMPLE_DENSE); same result."""
     x = _cuda(input, 'input', (torch.float32, torch.bfloat16))
     if x.dim() != 5 or x.shape[4] > 4:
         raise _lib.GftInvalidArgument('Invalid input shape (NDHWC): %s' % (tuple(x.shape),))
@@ -902,7 +907,7 @@ def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, o
                                   _enum(FILTER, interpolation, 'interpolation'), _enum(BOUNDARY, boundary, 'boundary'),
                                   _enum(MIP, mipmapping, 'mipmapping'), int(num_mipmaps), float(mip_bias),
                                   _enum(COORD, coordinate_mode, 'coordinate_mode'), float(cell_center_offset),
-                                  bool(separate_camera_batch), storage_dtype)
+                                  bool(separate_camera_batch), storage_dtype, bool(dense_input))
 
 
 def sample_grid_transform_grad(input, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,

@@ -49,7 +49,8 @@ class _InverseSampleGrad(torch.autograd.Function):
             dxv = _gops.sample_grid_transform(dy[i], m_views, V, P, F, in_shape[1:4], interpolation=r.filter_mode,
                                               boundary=r.boundary_mode, mipmapping=r.mip_mode,
                                               num_mipmaps=r.num_mips, mip_bias=r.mip_bias + r.gradient_mip_bias_add,
-                                              coordinate_mode=inv_cm, separate_camera_batch=False)  # V1DHWC
+                                              coordinate_mode=inv_cm, separate_camera_batch=False,
+                                              dense_input=True)  # V1DHWC (a gradient: dense)
             dx.append(torch.sum(dxv, dim=0) if views > 1 else dxv[0])  # 1DHWC (one view: the slice itself)
         dx = torch.cat(dx, dim=0) if batch > 1 else dx[0]
         return (dx,) + (None,) * 9

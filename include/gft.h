@@ -286,7 +286,12 @@ gft_status gft_raymarch_grid_transform_views_grad_weights(
 
 /* ---- SampleGridTransform (resample_grid.cc:23-61, :268-447; launcher resample_grid.cu.cc:289-438) ----
  * output [N, separate_camera_batch ? num_cameras : 1, Do, Ho, Wo, C] fp32.
- * The workspace holds the mip pyramid (empty without mips). */
+ * The workspace holds the mip pyramid (empty without mips) and, for the
+ * forward coordinate modes with mips, an occupancy map of the input that
+ * lets samples reading only zeros skip their LOD and fetches.
+ * interpolation | GFT_SAMPLE_DENSE: the input is known to be dense (e.g. a
+ * gradient), so the occupancy map is not built; the result is the same. */
+#define GFT_SAMPLE_DENSE 0x100
 size_t gft_sample_grid_transform_workspace_size(const int64_t input_shape[5], int32_t mipmapping, int32_t num_mipmaps);
 gft_status gft_sample_grid_transform(
     const void* input, int32_t input_dtype, const int64_t input_shape[5],

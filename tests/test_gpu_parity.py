@@ -549,6 +549,20 @@ def test_sample_transform_reverse_lod_bound(ops, cm, frustum):
     assert rel_l2(np_(y), ref) <= FWD_TOL
 
 
+@pytest.mark.parametrize('mip', ['NEAREST', 'LINEAR'])
+def test_sample_transform_dense_input_flag(ops, mip):
+    """dense_input (GFT_SAMPLE_DENSE) only leaves out the occupancy map: the
+    result is bit-identical, for a sparse volume too."""
+    shape, res = (96, 100, 96), (24, 30, 32)
+    _, _, M, V, P, F = scene(shape, 2, res)
+    x = np.zeros((1,) + shape + (1,), np.float32)
+    x[0, 40:64, 40:66, 40:64] = small_grid((24, 26, 24), 1, 37)[0]
+    outs = [ops.sample_grid_transform(cuda(x), M, V, P, F, res, 'LINEAR', 'BORDER', mip, 2, 0.3,
+                                      'TRANSFORM_LINDEPTH', dense_input=dense) for dense in (False, True)]
+    assert np.abs(np_(outs[0])).max() > 0
+    assert torch.equal(outs[0], outs[1])
+
+
 @pytest.mark.parametrize('cm', CMS)
 @pytest.mark.parametrize('boundary', BOUNDS)
 @pytest.mark.parametrize('mode', ['REFERENCE', 'EXACT'])
