@@ -23,12 +23,15 @@ constexpr int CLAMP_NONE = 0, CLAMP_MC_SMOOTH = 1, CLAMP_NEGATIVE = 2;
 // lut = -dt * centred velocity at voxel (x, y, z) (centered, data_structures.py:819-833)
 __device__ __forceinline__ float3 lut_at(const float* __restrict__ vx, const float* __restrict__ vy,
                                          const float* __restrict__ vz, Dims d, int x, int y, int z, float dt) {
-    const int64_t ix = ((int64_t)z * d.y + y) * (d.x + 1) + x;
-    const int64_t iy = ((int64_t)z * (d.y + 1) + y) * d.x + x;
-    const int64_t iz = ((int64_t)z * d.y + y) * d.x + x;
-    const float cx = (__ldg(vx + ix + 1) + __ldg(vx + ix)) * 0.5f;
-    const float cy = (__ldg(vy + iy + d.x) + __ldg(vy + iy)) * 0.5f;
-    const float cz = (__ldg(vz + iz + (int64_t)d.x * d.y) + __ldg(vz + iz)) * 0.5f;
+    // 32-bit indices: the launchers keep the staggered components of a slice
+    // below 2^32 values together (advect_size_ok)
+    const uint32_t ux = (uint32_t)x, uy = (uint32_t)y, uz = (uint32_t)z, dx = (uint32_t)d.x, dy = (uint32_t)d.y;
+    const uint32_t ix = (uz * dy + uy) * (dx + 1u) + ux;
+    const uint32_t iy = (uz * (dy + 1u) + uy) * dx + ux;
+    const uint32_t iz = (uz * dy + uy) * dx + ux;
+    const float cx = (__ldg(vx + ix + 1u) + __ldg(vx + ix)) * 0.5f;
+    const float cy = (__ldg(vy + iy + dx) + __ldg(vy + iy)) * 0.5f;
+    const float cz = (__ldg(vz + iz + dx * dy) + __ldg(vz + iz)) * 0.5f;
     return make_float3(cx * (-dt), cy * (-dt), cz * (-dt));
 }
 

@@ -23,8 +23,11 @@ struct Dims {
 };
 
 __host__ __device__ inline int64_t voxels(Dims d) { return (int64_t)d.x * d.y * d.z; }
+// Cell index in a grid slice, in 32-bit arithmetic: every launcher limits a
+// slice to fewer than 2^32 cells (MAX_SLICE_CELLS), so a cell inside the
+// slice gets its exact index (coordinates outside wrap and must not be read).
 __device__ __forceinline__ int64_t flat3(int x, int y, int z, Dims d) {
-    return ((int64_t)z * d.y + y) * d.x + x;
+    return (int64_t)(((uint32_t)z * (uint32_t)d.y + (uint32_t)y) * (uint32_t)d.x + (uint32_t)x);
 }
 
 // Cell (x, y, z) of a flat index v < 2^32 of a grid of dims d: two 32-bit
@@ -43,9 +46,11 @@ __device__ __forceinline__ void unflat32(uint32_t v, Dims d, int& x, int& y, int
 __host__ __device__ inline int64_t brick_cells(Dims d) {
     return (int64_t)((d.x + 1) / 2) * ((d.y + 1) / 2) * ((d.z + 1) / 2) * 8;
 }
+// (32-bit arithmetic, as flat3: brick_cells of a slice stays below 2^32.)
 __device__ __forceinline__ int64_t brick_index(int x, int y, int z, Dims d) {
-    const int64_t b = ((int64_t)(z >> 1) * ((d.y + 1) / 2) + (y >> 1)) * ((d.x + 1) / 2) + (x >> 1);
-    return b * 8 + ((z & 1) << 2 | (y & 1) << 1 | (x & 1));
+    const uint32_t b = ((uint32_t)(z >> 1) * (uint32_t)((d.y + 1) / 2) + (uint32_t)(y >> 1)) *
+                           (uint32_t)((d.x + 1) / 2) + (uint32_t)(x >> 1);
+    return (int64_t)(b * 8u + (uint32_t)((z & 1) << 2 | (y & 1) << 1 | (x & 1)));
 }
 
 // Cell layouts of a grid slice: rows (NDHWC) or 2x2x2-voxel bricks
