@@ -497,8 +497,6 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     if (!enum_in(grad_mode, 0, 1) || !enum_in(input_dtype, 0, 1)) return fail(GFT_ERR_INVALID_ARGUMENT, "invalid enum");
     if (weights_ready && grad_mode != GFT_GRAD_REFERENCE)
         return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_WEIGHTS_READY needs GFT_GRAD_REFERENCE");
-    if (det && weights_ready)
-        return fail(GFT_ERR_INVALID_ARGUMENT, "GFT_GRAD_DETERMINISTIC computes its own weight sums");
     if (det && !det_blend_ok(blending_mode, input_shape[4]))
         return fail(GFT_ERR_UNIMPLEMENTED, "deterministic gradient: BEER_LAMBERT or ADDITIVE blending only");
     if (projection != nullptr) {
@@ -560,12 +558,43 @@ static gft_status raymarch_grad_impl(const void* input, int32_t input_dtype, con
     return GFT_OK;
 }
 
+static gft_status raymarch_weights_impl_abi(const int64_t input_shape[5], const float* matrix_m, int32_t num_m,
+                                            const float* matrix_v, const float* matrix_p, const float* frustum,
+                                            int32_t num_cameras, const int32_t output_shape[3], int32_t boundary,
+                                            int32_t separate_camera_batch, int32_t grad_mode, void* workspace,
+                                            size_t workspace_bytes, void* stream);
+
 gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5], const float* matrix_m,
                                                     int32_t num_m, const float* matrix_v, const float* matrix_p,
                                                     const float* frustum, int32_t num_cameras,
                                                     const int32_t output_shape[3], int32_t boundary,
                                                     int32_t separate_camera_batch, void* workspace,
                                                     size_t workspace_bytes, void* stream) {
+    return raymarch_weights_impl_abi(input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras,
+                                     output_shape, boundary, separate_camera_batch, GFT_GRAD_REFERENCE, workspace,
+                                     workspace_bytes, stream);
+}
+
+gft_status gft_raymarch_grid_transform_grad_weights_mode(const int64_t input_shape[5], const float* matrix_m,
+                                                         int32_t num_m, const float* matrix_v,
+                                                         const float* matrix_p, const float* frustum,
+                                                         int32_t num_cameras, const int32_t output_shape[3],
+                                                         int32_t boundary, int32_t separate_camera_batch,
+                                                         int32_t grad_mode, void* workspace, size_t workspace_bytes,
+                                                         void* stream) {
+    return raymarch_weights_impl_abi(input_shape, matrix_m, num_m, matrix_v, matrix_p, frustum, num_cameras,
+                                     output_shape, boundary, separate_camera_batch, grad_mode, workspace,
+                                     workspace_bytes, stream);
+}
+
+static gft_status raymarch_weights_impl_abi(const int64_t input_shape[5], const float* matrix_m, int32_t num_m,
+                                            const float* matrix_v, const float* matrix_p, const float* frustum,
+                                            int32_t num_cameras, const int32_t output_shape[3], int32_t boundary,
+                                            int32_t separate_camera_batch, int32_t grad_mode, void* workspace,
+                                            size_t workspace_bytes, void* stream) {
+    const bool det = (grad_mode & GFT_GRAD_DETERMINISTIC) != 0;
+    if ((grad_mode & ~GFT_GRAD_DETERMINISTIC) != GFT_GRAD_REFERENCE)
+        return fail(GFT_ERR_INVALID_ARGUMENT, "weight sums: GFT_GRAD_REFERENCE (| GFT_GRAD_DETERMINISTIC) only");
     std::string why;
     if (!raymarch_grid_ok(input_shape, why)) return fail(GFT_ERR_INVALID_ARGUMENT, why);
     if (output_shape == nullptr || output_shape[0] < 1 || output_shape[1] < 1 || output_shape[2] < 1)
@@ -575,7 +604,7 @@ gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5]
                                   separate_camera_batch);
     if (st != GFT_OK) return st;
     const size_t need = gft_raymarch_grid_transform_grad_workspace_size(input_shape, num_cameras,
-                                                                        separate_camera_batch, GFT_GRAD_REFERENCE);
+                                                                        separate_camera_batch, grad_mode);
     if (workspace == nullptr || workspace_bytes < need)
         return fail(GFT_ERR_WORKSPACE, "raymarch gradient workspace too small");
     if ((st = check_workspace_aligned(workspace)) != GFT_OK) return st;
@@ -592,9 +621,9 @@ gft_status gft_raymarch_grid_transform_grad_weights(const int64_t input_shape[5]
                             separate_camera_batch != 0);
     set_uniform_images(pairs, a.D, a.H, a.W);
     a.n_slots = (int)pairs.size();
-    if (!launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream)))
-        return GFT_ERR_CUDA;
-    return GFT_OK;
+    const bool ok = det ? launch_raymarch_weights_det(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream))
+                        : launch_raymarch_weights(a, pairs, reinterpret_cast<float*>(workspace), as_stream(stream));
+    return ok ? GFT_OK : GFT_ERR_CUDA;
 }
 
 // ---------------------------------------------------------------- raymarch, cameras of different image sizes

@@ -151,6 +151,11 @@ bool launch_raymarch_occupancy(const RaymarchArgs& a, cudaStream_t s);
 bool launch_raymarch_fwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* out, cudaStream_t s);
 // Per-pair reciprocal weight sums of the reference-normalised adjoint (pass 1).
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s);
+// The deterministic adjoint's weight sums into its workspace layout (integer
+// sums, their largest value and the reciprocals), for a later gradient call
+// with GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC.
+bool launch_raymarch_weights_det(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt,
+                                 cudaStream_t s);
 // weights_ready: ws_cnt already holds the pass-1 reciprocals of the same geometry.
 bool launch_raymarch_bwd(const RaymarchArgs& a, const std::vector<Pair>& pairs, const float* out,
                          const float* dout, bool exact, bool weights_ready, float* grad, float* ws_cnt,

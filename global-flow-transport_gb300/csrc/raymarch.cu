@@ -1261,6 +1261,11 @@ static bool raymarch_weights_impl(const RaymarchArgs& a, const std::vector<Pair>
     return launched(1, "raymarch weight inversion launch");
 }
 
+bool launch_raymarch_weights_det(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt,
+                                cudaStream_t s) {
+    return raymarch_weights_impl(a, pairs, ws_cnt, true, s);
+}
+
 bool launch_raymarch_weights(const RaymarchArgs& a, const std::vector<Pair>& pairs, float* ws_cnt, cudaStream_t s) {
     return raymarch_weights_impl(a, pairs, ws_cnt, false, s);
 }
@@ -1411,7 +1416,9 @@ bool launch_raymarch_bwd(const RaymarchArgs& a_in, const std::vector<Pair>& pair
         if (!cuda_ok(cudaMemsetAsync(L.gacc, 0, sizeof(unsigned long long) * n, s), "zero gradient") ||
             !cuda_ok(cudaMemsetAsync(L.bounds, 0, 8, s), "zero bounds"))
             return false;
-        if (!raymarch_weights_impl(a, pairs, ws_cnt, true, s)) return false;
+        // (with the weights ready: integer sums, reciprocals and their largest
+        // sum from gft_raymarch_grid_transform_grad_weights_mode)
+        if (!weights_ready && !raymarch_weights_impl(a, pairs, ws_cnt, true, s)) return false;
         int64_t pix = 0;
         int dmax = a.D;
         for (const Pair& p : pairs) {

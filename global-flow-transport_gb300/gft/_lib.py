@@ -62,6 +62,8 @@ _SIGS = {
                                                 _I32, _I32, _I32, _I32, _I32, _P, _P, _SZ, _P]),
     'gft_raymarch_grid_transform_grad_weights': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32, _I32,
                                                         _P, _SZ, _P]),
+    'gft_raymarch_grid_transform_grad_weights_mode': (_I32, [_I64P, _P, _I32, _P, _P, _P, _I32, _I32P, _I32,
+                                                             _I32, _I32, _P, _SZ, _P]),
     'gft_transmittance': (_I32, [_P, _I64P, _P, _P]),
     'gft_transmittance_grad': (_I32, [_P, _P, _I64P, _P, _P]),
     'gft_light_compose': (_I32, [_P, _P, _P, _I64P, _F, _F, _I32, _P, _P]),

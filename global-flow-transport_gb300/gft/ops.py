@@ -304,9 +304,10 @@ def _raymarch_fwd(x, M, V, P, F, out_shape, interp, boundary, blend, separate, g
 WEIGHTS_READY = 0x100  # GFT_GRAD_WEIGHTS_READY
 
 
-def _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate):
+def _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate, det=False):
     """Pass 1 of the reference-normalised raymarch gradient (per-camera
-    reciprocal weight sums) for an input of ``x_shape`` into a new workspace,
+    reciprocal weight sums; det: the deterministic adjoint's integer sums in
+    its workspace layout) for an input of ``x_shape`` into a new workspace,
     on the current stream."""
     lib = _lib.load()
     Mh, nm = _mats(M)
@@ -314,12 +315,12 @@ def _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate
     Ph, _ = _mats(P)
     Fh, _ = _frustum(F)
     shape = _lib.i64(x_shape)
-    ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), GRAD['REFERENCE']),
-                    device)
+    gmode = GRAD['REFERENCE'] | (DETERMINISTIC if det else 0)
+    ws = _workspace(lib.gft_raymarch_grid_transform_grad_workspace_size(shape, nv, int(separate), gmode), device)
     with torch.cuda.device(device):
-        st = lib.gft_raymarch_grid_transform_grad_weights(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
-                                                          _lib.i32(out_shape), boundary, int(separate), _p(ws),
-                                                          ws.numel(), _stream(device))
+        st = lib.gft_raymarch_grid_transform_grad_weights_mode(shape, _p(Mh), nm, _p(Vh), _p(Ph), _p(Fh), nv,
+                                                               _lib.i32(out_shape), boundary, int(separate), gmode,
+                                                               _p(ws), ws.numel(), _stream(device))
     _lib.check(st, 'RaymarchGridTransformGrad weights')
     return ws
 
@@ -334,7 +335,7 @@ def _side_stream(dev):
     return s
 
 
-def _raymarch_weights_async(x_shape, device, M, V, P, F, out_shape, boundary, separate):
+def _raymarch_weights_async(x_shape, device, M, V, P, F, out_shape, boundary, separate, det=False):
     """Launches the geometry-only weight pass on a side stream forked from the
     current one, so that it overlaps the rest of the forward pass (the pass is
     bound by L2 reductions, the forward kernels by issue and L1); returns the
@@ -344,7 +345,7 @@ def _raymarch_weights_async(x_shape, device, M, V, P, F, out_shape, boundary, se
     side = _side_stream(device)
     side.wait_stream(cur)
     with torch.cuda.stream(side):
-        ws = _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate)
+        ws = _raymarch_weights(x_shape, device, M, V, P, F, out_shape, boundary, separate, det)
         ev = torch.cuda.Event()
         ev.record(side)
     return ws, ev
@@ -389,10 +390,10 @@ def _cached_weights(shape5, device, M, V, P, F, out_shape, boundary, separate):
     return ws
 
 
-def _weights_key(x_shape, M, V, P, F, out_shape, boundary, separate, device):
+def _weights_key(x_shape, M, V, P, F, out_shape, boundary, separate, device, det=False):
     return (tuple(int(v) for v in x_shape), _mats(M)[0].tobytes(), _mats(V)[0].tobytes(), _mats(P)[0].tobytes(),
             _frustum(F)[0].tobytes(), tuple(int(v) for v in out_shape), int(boundary), bool(separate),
-            _cuda_device(device).index)
+            _cuda_device(device).index, bool(det))
 
 
 def _cuda_device(device):
@@ -412,9 +413,8 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
     captured too (they join the side stream).  for_camera_sums: the raymarch
     is a fused render with a factored light, whose adjoint sums the weights
     itself while camera_sums_active(); nothing is started then."""
-    if _state['deterministic']:
-        return  # the deterministic gradient computes its own (integer) weight sums
-    if _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) == 1:
+    det = _state['deterministic']  # (then the integer sums of the deterministic adjoint)
+    if _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) == 1 and not det:
         return  # the gradient call computes them, beside its scatter
     if for_camera_sums and camera_sums_active():
         return  # the fused render's adjoint sums the weights itself
@@ -422,11 +422,11 @@ def prefetch_raymarch_weights(input_shape, matrix_m, matrix_v, matrix_p, frustum
     out_shape = _shape3(output_shape)
     b = _enum(BOUNDARY, boundary, 'boundary')
     key = _weights_key(input_shape, matrix_m, matrix_v, matrix_p, frustum_params, out_shape, b,
-                       separate_camera_batch, dev)
-    if _weight_cache['enabled'] and key in _weight_cache['entries']:
+                       separate_camera_batch, dev, det)
+    if not det and _weight_cache['enabled'] and key in _weight_cache['entries']:
         return
     _prefetched[key] = _raymarch_weights_async(tuple(input_shape), dev, matrix_m, matrix_v, matrix_p, frustum_params,
-                                               out_shape, b, bool(separate_camera_batch))
+                                               out_shape, b, bool(separate_camera_batch), det)
 
 
 def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, separate, gmode, weights=None,
@@ -448,7 +448,7 @@ def _raymarch_bwd(x, y, dy, M, V, P, F, out_shape, interp, boundary, blend, sepa
         gshape = (shape5[0] * (nv if separate else 1),) + tuple(x.shape[1:-1]) + (2,)
         weights = None
     grad = torch.empty(gshape, dtype=torch.float32, device=x.device)
-    if weights is not None and gmode == GRAD['REFERENCE']:
+    if weights is not None and (gmode & ~DETERMINISTIC) == GRAD['REFERENCE']:
         ws = weights
         gmode = gmode | WEIGHTS_READY
     else:
@@ -485,17 +485,19 @@ def _raymarch_forward_ctx(ctx, xs, need_grad, M, V, P, F, out_shape, interp, bou
     weights itself) into ctx.weights and returns (output, sample store)."""
     shape5 = _grid5(xs, grid)[0]
     ctx.weights = None
-    if (need_grad and weights_pass and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR'] and
-            not _state['deterministic']):
-        cached = _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
+    det = _state['deterministic']
+    if need_grad and weights_pass and get_grad_mode() == 'REFERENCE' and interp == FILTER['LINEAR']:
+        cached = None if det else _cached_weights(shape5, xs.device, M, V, P, F, out_shape, boundary, separate)
         if cached is not None:
             ctx.weights = (cached, None)
-        elif _state['side_weights'] and _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) != 1:
-            # (with the pipeline knob the gradient call computes the weight
-            # sums itself, beside its scatter)
-            key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device)
+        elif _state['side_weights'] and (det or _lib.load().gft_get_knob(KNOB_WEIGHTS_PIPELINE) != 1):
+            # (with the pipeline knob the float gradient call computes the
+            # weight sums itself, beside its scatter; the deterministic
+            # adjoint's integer sums also run ahead)
+            key = _weights_key(shape5, M, V, P, F, out_shape, boundary, separate, xs.device, det)
             ctx.weights = _prefetched.pop(key, None) or _raymarch_weights_async(shape5, xs.device, M, V, P, F,
-                                                                                out_shape, boundary, separate)
+                                                                                out_shape, boundary, separate, det)
+    ctx.weights_det = det
     samples = None
     if need_grad and interp == FILTER['LINEAR'] and _state['sample_store']:
         samples = _samples_buffer(shape5, _mats(V)[1], out_shape, separate, xs.device)
@@ -513,6 +515,8 @@ def _raymarch_backward_ctx(ctx, xs, y, samples, dy, M, V, P, F, out_shape, inter
         ws, ev = ctx.weights
         if ev is not None:
             torch.cuda.current_stream(xs.device).wait_event(ev)
+        if getattr(ctx, 'weights_det', False) != _state['deterministic']:
+            ws = None  # summed for the other mode: the gradient call sums its own
     g = _raymarch_bwd(xs, y, _cuda(dy, 'output_grad'), M, V, P, F, out_shape, interp, boundary, blend, separate,
                       _scatter_gmode(), weights=ws, grid=grid, samples=samples, projection=projection,
                       camera_sums=camera_sums)
@@ -588,7 +592,7 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
     return _raymarch_bwd(x, y.contiguous(), dy.contiguous(), matrix_m, matrix_v, matrix_p, frustum_params,
                          _shape3(output_shape), _enum(FILTER, interpolation, 'interpolation'),
                          _enum(BOUNDARY, boundary, 'boundary'), _enum(BLEND, blending_mode, 'blending_mode'),
-                         bool(separate_camera_batch), GRAD[get_grad_mode()])
+                         bool(separate_camera_batch), _scatter_gmode())
 
 
 # ------------------------------------------------------------------ raymarch, uneven camera batches

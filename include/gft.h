@@ -212,7 +212,9 @@ gft_status gft_raymarch_grid_transform_grad_projected(
  * sums computed on the GPU from maxima of the inputs; the result is then
  * converted to fp32.  Gradients are bit-identical from run to run and as
  * accurate as the float path or more.  Raymarch: BEER_LAMBERT or ADDITIVE
- * blending (any mode with C == 1), not with GFT_GRAD_WEIGHTS_READY; the
+ * blending (any mode with C == 1); with GFT_GRAD_WEIGHTS_READY the workspace
+ * must hold the weight sums of gft_raymarch_grid_transform_grad_weights_mode
+ * called with the flag (integer sums; the same input shape, C included); the
  * workspace size queries take the flag (larger workspaces; for the advection
  * gradient gft_advect_grad_workspace_size_mode).  Advection: both lookup
  * scatters; with GFT_GRAD_FORWARD_READY the workspace must be that size and
@@ -224,6 +226,16 @@ gft_status gft_raymarch_grid_transform_grad_weights(
     const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
     const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
     int32_t boundary, int32_t separate_camera_batch, void* workspace, size_t workspace_bytes, void* stream);
+/* The same with grad_mode GFT_GRAD_REFERENCE or GFT_GRAD_REFERENCE |
+ * GFT_GRAD_DETERMINISTIC (then the deterministic adjoint's integer weight
+ * sums, in its workspace layout, ahead of a gradient call with
+ * GFT_GRAD_WEIGHTS_READY | GFT_GRAD_DETERMINISTIC). */
+gft_status gft_raymarch_grid_transform_grad_weights_mode(
+    const int64_t input_shape[5],
+    const float* matrix_m, int32_t num_m, const float* matrix_v, const float* matrix_p,
+    const float* frustum, int32_t num_cameras, const int32_t output_shape[3],
+    int32_t boundary, int32_t separate_camera_batch, int32_t grad_mode, void* workspace, size_t workspace_bytes,
+    void* stream);
 
 /* ---- RaymarchGridTransform over cameras of different image sizes ----
  * No counterpart op in the reference, which takes one output_shape per call

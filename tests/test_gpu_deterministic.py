@@ -48,6 +48,29 @@ def _all_equal(runs):
 
 
 # ------------------------------------------------------------------ raymarch
+@pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
+def test_raymarch_deterministic_weights_ahead(ops, boundary):
+    """The deterministic adjoint's integer weight sums computed ahead on the
+    side stream during the forward (gft_raymarch_grid_transform_grad_weights_mode
+    + GFT_GRAD_WEIGHTS_READY) give the very gradient, bit for bit, of the
+    gradient call that sums them itself."""
+    _, _, M, V, P, F = scene((10, 14, 12), 3, (13, 9, 11))
+    x = small_grid((10, 14, 12), 4, 61) * 0.4
+    dy = cuda(np.random.default_rng(62).standard_normal((1, 3, 9, 11, 4)).astype(np.float32))
+    ops.set_raymarch_sample_store(False)  # both re-sample: the same samples
+    try:
+        with ops.deterministic(True), ops.grad_mode('REFERENCE'):
+            xt = cuda(x).requires_grad_(True)
+            y = ops.raymarch_grid_transform(xt, M, V, P, F, (13, 9, 11), 'LINEAR', boundary)
+            y.backward(dy)
+            g_inline = ops.raymarch_grid_transform_grad(cuda(x), y.detach(), dy, M, V, P, F, (13, 9, 11),
+                                                        'LINEAR', boundary)
+    finally:
+        ops.set_raymarch_sample_store(True)
+    assert np.abs(np_(g_inline)).max() > 0
+    assert torch.equal(xt.grad, g_inline)
+
+
 @pytest.mark.parametrize('C', [1, 4])
 @pytest.mark.parametrize('blend', ['BEER_LAMBERT', 'ADDITIVE'])
 @pytest.mark.parametrize('boundary', ['BORDER', 'CLAMP'])
