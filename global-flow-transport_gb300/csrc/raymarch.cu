@@ -812,12 +812,12 @@ __device__ __forceinline__ void scatter_step(float* __restrict__ grad, const flo
 // Every lane stays in the loop to its warp's last step (scatter_step is
 // warp-collective); lanes without a sample at a step pass act = false.
 //
-// PROJ (C == 4, float path): each sample's 4-channel adjoint is projected
-// onto two channels, (pj.a . g, pj.b . g), before its corner reduction, and
-// the gradient holds those two per cell.  A caller whose next adjoint is
-// linear in the four channels with coefficients of the form
-// (per-voxel factor) x (constant) -- the light composition -- needs only the
-// two sums, and the reductions move half the bytes.
+// PROJ (C == 4): each sample's 4-channel adjoint is projected onto two
+// channels, (pj.a . g, pj.b . g), before its corner reduction, and the
+// gradient holds those two per cell (DET: two integer sums per cell).  A
+// caller whose next adjoint is linear in the four channels with coefficients
+// of the form (per-voxel factor) x (constant) -- the light composition --
+// needs only the two sums, and the reductions move half the bytes.
 template <int C, typename S, int BM, int MODE, int L, bool DET, bool PROJ>
 __device__ __forceinline__ void raymarch_scatter_tile(const S* __restrict__ in, Dims din, int blend_mode,
                                                       const float* __restrict__ out, const float* __restrict__ dout,
