@@ -127,7 +127,7 @@ struct RaymarchArgs {
     bool det = false;
     unsigned long long* det_acc = nullptr;  // set by launch_raymarch_bwd
     const float* det_scale = nullptr;
-    // Projected adjoint (C == 4, brick layout, float path): the gradient
+    // Projected adjoint (C == 4, brick layout; float or deterministic): the gradient
     // holds (proj.a . g, proj.b . g) per cell instead of the 4 channels of g.
     bool project = false;
     ChanProj proj = {};
