@@ -350,10 +350,11 @@ __device__ __forceinline__ float packed_normalised(const float* __restrict__ buf
 // min/max), store the direct density term 0.5*g_corr, scatter the back-lookup
 // gradient -0.5*g_corr into the fwd adjoint and accumulate the lookup gradient
 // of the back lookup (whose lut is -lut).
-// Single channel: at most 64 registers (4 blocks of 256 per SM instead of 3,
-// 16 bytes spilled) for the latency of the two corner gathers.
+// Single channel: at most 51 registers (5 blocks of 256 per SM; 48 used, no
+// spills with the 32-bit cell indices) for the latency of the two corner
+// gathers.
 template <int C, int BM, int COUNT, bool DET = false>
-__global__ void __launch_bounds__(AD_THREADS, C == 1 ? 4 : 1)
+__global__ void __launch_bounds__(AD_THREADS, C == 1 ? 5 : 1)
     k_adv_bwd_back(const float* __restrict__ d, const float* __restrict__ fwd, Dims dm, const float* __restrict__ vx,
                    const float* __restrict__ vy, const float* __restrict__ vz, float dt, int clamp,
                    const float* __restrict__ dy, float* __restrict__ gd, float* __restrict__ gfwd_sc,
