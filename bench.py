@@ -356,29 +356,41 @@ def extras(args, step, dev, timed, storage, inputs, ms):
     hosts = [StreamedSteps.host_inputs(inputs), StreamedSteps.host_inputs(step.make_inputs(frame=1))]
     h2d = StreamedSteps.h2d_bytes(hosts[0])
     streamed = StreamedSteps(step, inputs, warmup=args.warmup)
-    k = min(max(6, args.steps // 2), 60)
+    # wall-clock over k steps per trial; three trials, the median one reported
+    # (a host hiccup inside one short trial would otherwise set the figure)
+    k = min(max(10, args.steps), 60)
+    trials = 3
     streamed.run([hosts[i % 2] for i in range(4)])
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses = streamed.run([hosts[i % 2] for i in range(k)])
-    e2e_ms = (time.perf_counter() - t0) * 1000.0 / k
+    trial_ms = []
+    for _ in range(trials):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = streamed.run([hosts[i % 2] for i in range(k)])
+        trial_ms.append((time.perf_counter() - t0) * 1000.0 / k)
+    e2e_ms = float(np.median(trial_ms))
     out['e2e'] = {'value': 1000.0 / e2e_ms, 'unit': 'iters/s', 'h2d_bytes_per_step': int(h2d),
-                  'd2h_bytes_per_step': 4, 'ms_per_step': e2e_ms, 'steps': k,
+                  'd2h_bytes_per_step': 4, 'ms_per_step': e2e_ms, 'steps': k, 'trials_ms_per_step': trial_ms,
                   'what': 'StreamedSteps: per-step H2D of pinned inputs overlapping the previous step, loss read '
-                          'back one step later', 'loss_last': losses[-1]}
+                          'back one step later; median of %d trials of %d steps' % (trials, k),
+                  'loss_last': losses[-1]}
 
     def serial_step(host):
         return streamed.run([host])[0]
 
     for i in range(2):
         serial_step(hosts[i % 2])
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(k):
-        serial_step(hosts[i % 2])
-    ser_ms = (time.perf_counter() - t0) * 1000.0 / k
+    ser_trials = []
+    for _ in range(trials):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(k):
+            serial_step(hosts[i % 2])
+        ser_trials.append((time.perf_counter() - t0) * 1000.0 / k)
+    ser_ms = float(np.median(ser_trials))
     out['e2e_serial'] = {'value': 1000.0 / ser_ms, 'unit': 'iters/s', 'ms_per_step': ser_ms,
-                         'what': 'one step at a time: copy inputs, replay, read the loss, wait'}
+                         'trials_ms_per_step': ser_trials,
+                         'what': 'one step at a time: copy inputs, replay, read the loss, wait; median of %d '
+                                 'trials of %d steps' % (trials, k)}
     del streamed
     torch.cuda.empty_cache()
 
